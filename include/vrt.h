@@ -1,0 +1,212 @@
+/*
+ * vrt.h - C ABI of the GB300 brickmap ray-traversal library (libvrt.so).
+ *
+ * The library replaces the storage-sync and traversal path of VoxelRT:
+ *   - the device-layout storage that GpuVoxelStorage::SyncBuffers(VoxelMap&)
+ *     (src/VoxelRT/GpuRenderer.cpp:45-167) and FlatVoxelStorage::SyncBuffers
+ *     (src/VoxelRT/CpuRenderer.cpp:33-61) build from the host VoxelMap;
+ *   - the mask re-derivation of UpdateOccupancy (src/VoxelRT/CpuRenderer.cpp:63-83,
+ *     src/VoxelRT/Shaders/UpdateOccupancy.comp:9-34);
+ *   - the traversal RayCast/GetStepPos (src/VoxelRT/CpuRenderer.cpp:135-224) and
+ *     its GLSL twin rayCast (src/VoxelRT/Shaders/VoxelTraversal.glsl:162-204),
+ *     driven per view as GpuRenderer::RenderFrame does (GpuRenderer.cpp:239-273);
+ *   - the edit path VoxelMap::RegionDispatchSIMD + brick GC
+ *     (src/VoxelRT/VoxelMap.h:222-263) and BrickSlotAllocator
+ *     (src/VoxelRT/BrickSlotAllocator.cpp:5-94).
+ *
+ * Conventions (all fixed by the reference's indexers, src/VoxelRT/VoxelMap.h:60-102):
+ *   - a brick is 8x8x8 u8 voxel ids, 0 = empty; voxel index x | z<<3 | y<<6;
+ *   - a sector is 4x4x4 bricks; brick index bx | bz<<2 | by<<4 is the bit in the
+ *     sector's 64-bit allocation mask;
+ *   - sector indices passed to the ABI use the reference's WorldSectorIndexer
+ *     packing (12-bit signed x, 12-bit signed z at bit 12, 8-bit signed y at bit
+ *     24); sectors outside the world's extent are ignored, as SyncBuffers skips
+ *     sectors outside its view (GpuRenderer.cpp:53-55, CpuRenderer.cpp:39-40).
+ *
+ * Errors are returned as vrt_status codes; nothing throws across the ABI.
+ * vrt_last_error() returns a thread-local message for the last failure.
+ *
+ * Every function taking a `stream` takes a cudaStream_t passed as void*
+ * (NULL = legacy default stream).  Functions with host buffers synchronise that
+ * stream before returning; *_device variants are asynchronous on it.
+ */
+#ifndef VRT_H_
+#define VRT_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VRT_ABI_VERSION 1
+
+typedef enum vrt_status {
+    VRT_OK = 0,
+    VRT_ERR_INVALID_ARG = 1,     /* bad pointer, size or descriptor */
+    VRT_ERR_OUT_OF_MEMORY = 2,   /* device or host allocation failed, or admission refused */
+    VRT_ERR_QUEUE_TIMEOUT = 3,   /* a bounded device or host wait gave up */
+    VRT_ERR_DEVICE = 4,          /* CUDA runtime error; see vrt_last_error() */
+    VRT_ERR_NO_DEVICE = 5,       /* no CUDA device */
+    VRT_ERR_SLOTS_EXHAUSTED = 6, /* brick pool full: BrickSlotAllocator.cpp:14-16 throws here */
+    VRT_ERR_NOT_FOUND = 7,
+    VRT_ERR_IO = 8,
+    VRT_ERR_FORMAT = 9           /* malformed stream or file */
+} vrt_status;
+
+/* ---- layout constants (VoxelMap.h:100-102) ---- */
+#define VRT_BRICK_DIM 8
+#define VRT_BRICK_BYTES 512
+#define VRT_SECTOR_DIM_BRICKS 4
+#define VRT_SECTOR_DIM 32
+/* Largest world: hit voxels are packed 11/10/11 bits (x | y<<11 | z<<21). */
+#define VRT_MAX_WORLD_X 2048
+#define VRT_MAX_WORLD_Y 1024
+#define VRT_MAX_WORLD_Z 2048
+
+#define VRT_DEFAULT_MAX_ITERS 128 /* CpuRenderer.cpp:185 */
+#define VRT_MISS_VOXEL 0xFFFFFFFFu
+#define VRT_MISS_FACE 0xFFu
+
+/* Ray in the frame of an integer world origin (CpuRenderer.cpp:172: origin is
+ * relative to worldOrigin; voxel = worldOrigin + floor(pos)). 32 bytes. */
+typedef struct vrt_ray {
+    float origin[3];
+    float dir[3];
+    uint32_t tag;      /* copied to vrt_hit.tag */
+    uint32_t reserved; /* must be 0 */
+} vrt_ray;
+
+/* Hit record, 16 bytes.
+ *   voxel    hit voxel in world coordinates packed x | y<<11 | z<<21, or VRT_MISS_VOXEL
+ *   face     axis*2 + (dir[axis] < 0), axis = X if sideX==t, else Y if sideY==t, else Z
+ *            (CpuRenderer.cpp:204-207); VRT_MISS_FACE on a miss
+ *   material voxel id (u8), 0 on a miss
+ *   steps    DDA iteration at which the ray left the active set (hit or out of
+ *            bounds); max_iters when the iteration cap ran out
+ *   t        hit distance min(sideX, sideY, sideZ) (CpuRenderer.cpp:204); +inf on a miss
+ *   tag      vrt_ray.tag, or the pixel index y*width+x for camera rays          */
+typedef struct vrt_hit {
+    uint32_t voxel;
+    uint8_t face;
+    uint8_t material;
+    uint16_t steps;
+    float t;
+    uint32_t tag;
+} vrt_hit;
+
+typedef struct vrt_cast_params {
+    int32_t world_origin[3]; /* FrameConstants::WorldOrigin (CpuRenderer.cpp:447) */
+    uint32_t max_iters;      /* 0 = VRT_DEFAULT_MAX_ITERS; at most 65535 */
+    uint32_t flags;          /* must be 0 */
+} vrt_cast_params;
+
+/* Pinhole camera in the reference's split form: integer world origin plus a
+ * fractional ray origin (GBuffer.h:79, CpuRenderer.cpp:447-448).  The ray of
+ * pixel (px, py), u = px + 0.5, v = py + 0.5, has unnormalised direction
+ * d0 + u*du + v*dv (each op rounded separately), normalised with an IEEE sqrt
+ * and divisions.  Build one with vrt_camera_look_at(). */
+typedef struct vrt_camera {
+    int32_t world_origin[3];
+    float origin[3];
+    float d0[3];
+    float du[3];
+    float dv[3];
+    uint32_t width;
+    uint32_t height;
+} vrt_camera;
+
+/* Marks records of rays that were never cast (shadow rays of missed pixels,
+ * bounces after a path ended). */
+#define VRT_NO_RAY 0xFFFFFFFFu
+
+/* Sphere edit (the brush of Brush.cpp:10-31 with an exact integer sphere):
+ * every voxel v with |v - center|^2 <= radius^2 (integer arithmetic) is set to
+ * `material` (0 carves).  mode VRT_EDIT_REPLACE only overwrites non-empty voxels
+ * (BrushAction::Replace, Brush.cpp:24-26).  Bricks are created for fills and
+ * every empty brick in the edit's brick bounding box is freed afterwards
+ * (VoxelMap.h:222-263).  Voxels outside the world are ignored. */
+typedef struct vrt_edit {
+    int32_t center[3];
+    uint32_t radius;
+    uint8_t material;
+    uint8_t mode;
+    uint16_t reserved; /* must be 0 */
+} vrt_edit;
+
+#define VRT_EDIT_FILL 0
+#define VRT_EDIT_REPLACE 1
+
+typedef struct vrt_world vrt_world;
+
+typedef struct vrt_world_desc {
+    uint32_t sectors_x, sectors_y, sectors_z; /* world extent in 32-voxel sectors */
+    uint32_t brick_capacity;                  /* initial brick-pool slots; 0 = 4096; grows on demand */
+    int32_t device;                           /* CUDA device ordinal */
+    uint32_t flags;                           /* VRT_WORLD_* */
+} vrt_world_desc;
+
+/* Pin the sector table and brick-mask array in L2 with a persisting
+ * access-policy window on streams passed to cast/render calls. */
+#define VRT_WORLD_L2_PERSIST 1u
+
+typedef struct vrt_world_stats {
+    uint32_t sectors_x, sectors_y, sectors_z;
+    uint32_t allocated_bricks;  /* FreeList::NumAllocated */
+    uint32_t brick_capacity;    /* slots in the device pool */
+    uint32_t free_ranges;       /* FreeList::FreeRanges.size() */
+    uint64_t device_bytes;      /* device memory held by the world */
+} vrt_world_stats;
+
+/* ---- library ---- */
+const char* vrt_last_error(void);
+uint32_t vrt_abi_version(void);
+int32_t vrt_sector_index(int32_t sx, int32_t sy, int32_t sz); /* WorldSectorIndexer::GetIndex */
+
+/* ---- world storage (GpuVoxelStorage, GpuRenderer.cpp:17-167) ---- */
+vrt_status vrt_world_create(const vrt_world_desc* desc, vrt_world** out);
+vrt_status vrt_world_destroy(vrt_world* world);
+vrt_status vrt_world_get_stats(const vrt_world* world, vrt_world_stats* out);
+
+/* Sync dirty bricks into device storage, as SyncBuffers(VoxelMap&) does for each
+ * DirtyLocs entry (GpuRenderer.cpp:52-166).  For sector i:
+ *   alloc_mask[i]  the sector's full allocation mask (0 deletes the sector);
+ *   dirty_mask[i]  bricks whose content is supplied (NULL = all of alloc_mask);
+ *   bricks         popcount(alloc_mask[i] & dirty_mask[i]) x 512 bytes per sector, in
+ *                  ascending bit order, sectors back to back (the cvox pack record
+ *                  shape, VoxelMap.cpp:234-242).
+ * Bricks that stay allocated but are not dirty keep their device content, even if
+ * their slots move.  Brick occupancy masks are re-derived on the device. */
+vrt_status vrt_world_sync_sectors(vrt_world* world, uint32_t n, const int32_t* sector_idx,
+                                  const uint64_t* alloc_mask, const uint64_t* dirty_mask,
+                                  const uint8_t* bricks, void* stream);
+
+/* Read one sector back: its allocation mask and popcount(mask) x 512 bytes. */
+vrt_status vrt_world_read_sector(vrt_world* world, int32_t sector_idx, uint64_t* alloc_mask,
+                                 uint8_t* bricks, size_t bricks_capacity, void* stream);
+
+/* ---- traversal ---- */
+/* Cast n explicit rays (host buffers): copies in, traverses, copies out. */
+vrt_status vrt_cast(vrt_world* world, const vrt_ray* rays, uint32_t n, const vrt_cast_params* params,
+                    vrt_hit* hits, void* stream);
+/* Same with device pointers; asynchronous on stream. */
+vrt_status vrt_cast_device(vrt_world* world, const vrt_ray* rays, uint32_t n,
+                           const vrt_cast_params* params, vrt_hit* hits, void* stream);
+
+/* Primary rays of one view, one launch (the per-view path, GpuRenderer.cpp:267-268).
+ * hits: width*height records in row-major pixel order (host buffer). */
+vrt_status vrt_render_view(vrt_world* world, const vrt_camera* cam, uint32_t max_iters,
+                           vrt_hit* hits, void* stream);
+vrt_status vrt_render_view_device(vrt_world* world, const vrt_camera* cam, uint32_t max_iters,
+                                  vrt_hit* hits, void* stream);
+
+/* Build a camera at `pos` looking at `target` (world voxel units), vertical field of
+ * view in degrees, for a width x height image; computed in double on the host. */
+vrt_status vrt_camera_look_at(const double pos[3], const double target[3], double vfov_deg,
+                              uint32_t width, uint32_t height, vrt_camera* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VRT_H_ */

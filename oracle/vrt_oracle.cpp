@@ -1,0 +1,639 @@
+// vrt_oracle.cpp - CPU oracle of the brickmap traversal path (test infrastructure).
+//
+// A scalar, per-ray restatement of the reference's CPU traversal.  Each function
+// names the reference lines it follows.  Build with -O2 -ffp-contract=off and no
+// -ffast-math: every float op is rounded on its own, in the source order of
+// src/VoxelRT/CpuRenderer.cpp:172-224, which is the order the device kernels use.
+//
+// Differences from the reference that are deliberate (all shared with the device):
+//   * the grid extent is the world's sector extent, not the fixed 2048x512x2048 view
+//     of CpuRenderer.cpp:13-16, and the bounds test is per axis (the x|z trick of
+//     CpuRenderer.cpp:114-117 needs a power-of-two XZ extent);
+//   * the ray start is clipped to the grid inset by one voxel, as the GLSL path does
+//     (VoxelTraversal.glsl:133-145, 164-167); tStart keeps the unclipped origin;
+//   * the hit voxel's material is read at worldOrigin + floor(pos) even when the
+//     iteration cap ran out (CpuRenderer.cpp:195 leaves relative coordinates in
+//     voxelPos in that case, a SIMD-lane artefact);
+//   * the step count mirrors GLSL hit.iters (VoxelTraversal.glsl:185,197).
+
+#include "vrt_oracle.h"
+
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <thread>
+#include <vector>
+
+namespace {
+
+constexpr uint32_t kSectorVoxels = 64 * 512;
+
+// FlatVoxelStorage keeps one dense 32 KiB block of voxels and 512 cell masks per
+// sector (CpuRenderer.cpp:20-31); here a block exists only for allocated sectors.
+struct SectorBlock {
+    uint8_t vox[kSectorVoxels];  // brick*512 + (x | z<<3 | y<<6)
+    uint64_t occ[64 * 8];        // brick*8 + cell
+};
+
+inline int popc64(uint64_t x) { return __builtin_popcountll(x); }
+inline int ctz64(uint64_t x) { return __builtin_ctzll(x); }
+
+// x86 minps/maxps: the second operand is returned unless the compare holds, so a
+// NaN in either operand yields the second one (SIMD_AVX512.h:123, SIMD_AVX2.h:129).
+inline float min_x86(float a, float b) { return a < b ? a : b; }
+inline float max_x86(float a, float b) { return a > b ? a : b; }
+
+// floor2i: round toward -inf, then convert; out of range and NaN give INT32_MIN
+// (the x86 "integer indefinite" value), SIMD_AVX512.h:109.
+inline int32_t floor2i(float x) {
+    float f = std::floor(x);
+    if (!(f >= -2147483648.0f && f < 2147483648.0f)) return INT32_MIN;
+    return (int32_t)f;
+}
+inline int32_t wadd(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
+inline int32_t wsub(int32_t a, int32_t b) { return (int32_t)((uint32_t)a - (uint32_t)b); }
+
+// WorldSectorIndexer::GetPos (VoxelMap.h:80-86): 12-bit signed x, z at 12, 8-bit y at 24.
+inline void decode_sector(int32_t idx, int32_t& x, int32_t& y, int32_t& z) {
+    uint32_t u = (uint32_t)idx;
+    x = (int32_t)(u << 20) >> 20;
+    z = (int32_t)(u << 8) >> 20;
+    y = (int32_t)u >> 24;
+}
+
+// UpdateOccupancy (CpuRenderer.cpp:63-83): 8 cells of 4^3 voxels; bit vx + vz*4 + vy*16;
+// cell index (cx | cz<<1 | cy<<2) as BrickMaskIndexer (CpuRenderer.cpp:18).
+void update_occupancy(const uint8_t* brick, uint64_t* cells) {
+    for (uint32_t cy = 0; cy < 8; cy += 4)
+        for (uint32_t cz = 0; cz < 8; cz += 4)
+            for (uint32_t cx = 0; cx < 8; cx += 4) {
+                uint64_t mask = 0;
+                for (uint32_t vy = 0; vy < 4; vy++)
+                    for (uint32_t vz = 0; vz < 4; vz++)
+                        for (uint32_t vx = 0; vx < 4; vx++) {
+                            uint32_t vi = (cx + vx) | (cz + vz) << 3 | (cy + vy) << 6;
+                            uint64_t occupied = brick[vi] != 0;
+                            mask |= occupied << (vx + vz * 4 + vy * 16);
+                        }
+                cells[(cx >> 2) | (cz >> 2) << 1 | (cy >> 2) << 2] = mask;
+            }
+}
+
+bool brick_is_empty(const uint8_t* brick) {
+    for (int i = 0; i < 512; i++)
+        if (brick[i]) return false;
+    return true;
+}
+
+template <typename F>
+void parallel_for(uint64_t n, int threads, F&& fn) {
+    if (threads <= 0) threads = (int)std::thread::hardware_concurrency();
+    if (threads <= 0) threads = 1;
+    const uint64_t chunk = 256;
+    uint64_t nchunks = (n + chunk - 1) / chunk;
+    if ((uint64_t)threads > nchunks) threads = (int)(nchunks ? nchunks : 1);
+    std::atomic<uint64_t> next{0};
+    auto worker = [&](int tid) {
+        for (;;) {
+            uint64_t c = next.fetch_add(1);
+            if (c >= nchunks) break;
+            uint64_t b = c * chunk, e = b + chunk < n ? b + chunk : n;
+            fn(tid, b, e);
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < threads; t++) pool.emplace_back(worker, t);
+    worker(0);
+    for (auto& th : pool) th.join();
+}
+
+struct Trace {
+    bool hit;
+    uint16_t steps;
+    uint8_t material;
+    int32_t vp[3];
+    float cur[3];   // final position (HitResult.Pos, CpuRenderer.cpp:212)
+    float side[3];  // final side distances
+    uint32_t step_calls;
+    uint32_t occ_fetches;
+};
+
+}  // namespace
+
+struct ora_world {
+    uint32_t sx, sy, sz;
+    std::vector<uint64_t> masks;
+    std::vector<std::unique_ptr<SectorBlock>> data;
+
+    uint32_t lin(int32_t x, int32_t y, int32_t z) const {
+        return (uint32_t)x + (uint32_t)z * sx + (uint32_t)y * sx * sz;
+    }
+    bool sector_in(int32_t x, int32_t y, int32_t z) const {
+        return (uint32_t)x < sx && (uint32_t)y < sy && (uint32_t)z < sz;
+    }
+    SectorBlock* block(uint32_t s) {
+        if (!data[s]) {
+            data[s].reset(new SectorBlock);
+            std::memset(data[s].get(), 0, sizeof(SectorBlock));
+        }
+        return data[s].get();
+    }
+    void clear_brick(uint32_t s, uint32_t b) {
+        if (!data[s]) return;
+        std::memset(&data[s]->vox[b * 512], 0, 512);
+        std::memset(&data[s]->occ[b * 8], 0, 64);
+    }
+};
+
+namespace {
+
+// GetStepPos (CpuRenderer.cpp:135-171) for one lane.  Returns true on a hit.
+inline bool get_step_pos(const ora_world& w, int32_t vp[3], const float dir[3], Trace& tr) {
+    uint32_t s = w.lin(vp[0] >> 5, vp[1] >> 5, vp[2] >> 5);
+    uint64_t m = w.masks[s];
+    uint32_t idx = ((vp[0] >> 3) & 3) | ((vp[2] >> 3) & 3) << 2 | ((vp[1] >> 3) & 3) << 4;
+    int32_t lod = 3;
+    tr.step_calls++;
+    if ((m >> idx) & 1) {
+        const SectorBlock* blk = w.data[s].get();
+        uint32_t brick = idx;
+        uint32_t cell = ((vp[0] >> 2) & 1) | ((vp[2] >> 2) & 1) << 1 | ((vp[1] >> 2) & 1) << 2;
+        m = blk->occ[brick * 8 + cell];
+        idx = (vp[0] & 3) | (vp[2] & 3) << 2 | (vp[1] & 3) << 4;
+        lod = 0;
+        tr.occ_fetches++;
+        if ((m >> idx) & 1) {
+            // GetVoxelMaterial (CpuRenderer.cpp:120-132): the raw voxel id.
+            uint32_t vi = (vp[0] & 7) | (vp[2] & 7) << 3 | (vp[1] & 7) << 6;
+            tr.material = blk->vox[brick * 512 + vi];
+            return true;
+        }
+    }
+    // level4: whole mask empty -> +2; level2: the 2^3 block holding idx empty -> +1.
+    uint32_t half = (uint32_t)(idx < 32 ? m : m >> 32);
+    if (m == 0)
+        lod += 2;
+    else if (((half >> (idx & 0xA)) & 0x00330033u) == 0)
+        lod += 1;
+    int32_t cm = (1 << lod) - 1;
+    for (int c = 0; c < 3; c++) vp[c] = dir[c] < 0.0f ? (vp[c] & ~cm) : (vp[c] | cm);
+    return false;
+}
+
+// RayCast (CpuRenderer.cpp:172-224) for one lane, with the GLSL entry clip.
+void trace_ray(const ora_world& w, const float o[3], const float d[3], const int32_t wo[3],
+               uint32_t max_iters, Trace& tr) {
+    tr.hit = false;
+    tr.material = 0;
+    tr.step_calls = 0;
+    tr.occ_fetches = 0;
+    float inv[3], ts[3];
+    for (int c = 0; c < 3; c++) inv[c] = 1.0f / d[c];
+    for (int c = 0; c < 3; c++) ts[c] = ((d[c] < 0.0f ? 0.0f : 1.0f) - o[c]) * inv[c];
+
+    const int32_t size[3] = {(int32_t)w.sx * 32, (int32_t)w.sy * 32, (int32_t)w.sz * 32};
+    // clipRayToAABB(origin, dir, 1 - wo, size - wo - 1), VoxelTraversal.glsl:133-145, 166.
+    float lo[3], hi[3];
+    for (int c = 0; c < 3; c++) {
+        float bmin = (float)(1 - wo[c]);
+        float bmax = ((float)size[c] - (float)wo[c]) - 1.0f;
+        float t1 = (bmin - o[c]) * inv[c];
+        float t2 = (bmax - o[c]) * inv[c];
+        lo[c] = min_x86(t1, t2);
+        hi[c] = max_x86(t1, t2);
+    }
+    float tmin = max_x86(lo[0], max_x86(lo[1], lo[2]));
+    float tmax = min_x86(hi[0], min_x86(hi[1], hi[2]));
+    float* cur = tr.cur;
+    if (tmin > 0.0f && tmin < tmax) {
+        for (int c = 0; c < 3; c++) cur[c] = o[c] + d[c] * tmin;
+    } else {
+        for (int c = 0; c < 3; c++) cur[c] = o[c];
+    }
+    float* side = tr.side;
+    side[0] = side[1] = side[2] = 0.0f;
+    int32_t* vp = tr.vp;
+
+    for (uint32_t i = 0; i < max_iters; i++) {
+        for (int c = 0; c < 3; c++) vp[c] = wadd(wo[c], floor2i(cur[c]));
+        // GetInboundMask (CpuRenderer.cpp:114-117), per axis.
+        if (!((uint32_t)vp[0] < (uint32_t)size[0] && (uint32_t)vp[1] < (uint32_t)size[1] &&
+              (uint32_t)vp[2] < (uint32_t)size[2])) {
+            tr.steps = (uint16_t)i;
+            return;
+        }
+        if (get_step_pos(w, vp, d, tr)) {
+            tr.hit = true;
+            tr.steps = (uint16_t)i;
+            return;
+        }
+        for (int c = 0; c < 3; c++) side[c] = ts[c] + (float)wsub(vp[c], wo[c]) * inv[c];
+        float t = min_x86(min_x86(side[0], side[1]), side[2]) + 0.001f;
+        for (int c = 0; c < 3; c++) cur[c] = o[c] + t * d[c];
+    }
+    tr.steps = (uint16_t)max_iters;
+}
+
+void fill_hit(const Trace& tr, const float d[3], uint32_t tag, vrt_hit& h) {
+    h.tag = tag;
+    h.steps = tr.steps;
+    if (!tr.hit) {
+        h.voxel = VRT_MISS_VOXEL;
+        h.face = VRT_MISS_FACE;
+        h.material = 0;
+        h.t = INFINITY;
+        return;
+    }
+    float t = min_x86(min_x86(tr.side[0], tr.side[1]), tr.side[2]);
+    uint32_t axis = tr.side[0] == t ? 0u : (tr.side[1] == t ? 1u : 2u);
+    h.t = t;
+    h.face = (uint8_t)(axis * 2 + (d[axis] < 0.0f ? 1 : 0));
+    h.material = tr.material;
+    h.voxel = (uint32_t)tr.vp[0] | (uint32_t)tr.vp[1] << 11 | (uint32_t)tr.vp[2] << 21;
+}
+
+void fill_no_ray(vrt_hit& h) {
+    h.voxel = VRT_MISS_VOXEL;
+    h.face = VRT_MISS_FACE;
+    h.material = 0;
+    h.steps = 0;
+    h.t = INFINITY;
+    h.tag = VRT_NO_RAY;
+}
+
+// HitResult.Normal (CpuRenderer.cpp:213-217): sideMaskX = sx==t, sideMaskY = sy==t,
+// sideMaskZ = neither; component = (sign bit of dir) ? +1 : -1.
+void hit_normal(const Trace& tr, const float d[3], float n[3]) {
+    float t = min_x86(min_x86(tr.side[0], tr.side[1]), tr.side[2]);
+    bool mx = tr.side[0] == t, my = tr.side[1] == t, mz = !mx && !my;
+    bool m[3] = {mx, my, mz};
+    for (int c = 0; c < 3; c++) n[c] = m[c] ? (std::signbit(d[c]) ? 1.0f : -1.0f) : 0.0f;
+}
+
+// origin = hit.Pos + hit.Normal * 0.01f (CpuRenderer.cpp:389)
+void offset_origin(const Trace& tr, const float n[3], float o[3]) {
+    for (int c = 0; c < 3; c++) o[c] = tr.cur[c] + n[c] * 0.01f;
+}
+
+void camera_ray(const vrt_camera& cam, uint32_t px, uint32_t py, float o[3], float d[3]) {
+    float u = (float)px + 0.5f, v = (float)py + 0.5f;
+    float x = (cam.d0[0] + u * cam.du[0]) + v * cam.dv[0];
+    float y = (cam.d0[1] + u * cam.du[1]) + v * cam.dv[1];
+    float z = (cam.d0[2] + u * cam.du[2]) + v * cam.dv[2];
+    float len = std::sqrt((x * x + y * y) + z * z);
+    d[0] = x / len;
+    d[1] = y / len;
+    d[2] = z / len;
+    for (int c = 0; c < 3; c++) o[c] = cam.origin[c];
+}
+
+// PCG32 (O'Neill, pcg-random.org: 64-bit LCG state, XSH-RR output).
+struct Pcg32 {
+    uint64_t state, inc;
+    Pcg32(uint64_t initstate, uint64_t initseq) {
+        state = 0;
+        inc = (initseq << 1) | 1u;
+        next();
+        state += initstate;
+        next();
+    }
+    uint32_t next() {
+        uint64_t old = state;
+        state = old * 6364136223846793005ULL + inc;
+        uint32_t xs = (uint32_t)(((old >> 18) ^ old) >> 27);
+        uint32_t rot = (uint32_t)(old >> 59);
+        return (xs >> rot) | (xs << ((32 - rot) & 31));
+    }
+    // uniform in [-1, 1) with 2^-23 spacing; every op exact
+    float next_signed() { return (float)(next() >> 8) * 0x1p-23f - 1.0f; }
+};
+
+constexpr uint64_t kBounceStream = 0x9E3779B97F4A7C15ULL;
+
+void bounce_dir(uint32_t pixel, uint32_t bounce, const float n[3], float out[3]) {
+    Pcg32 rng(pixel ^ bounce, kBounceStream);
+    for (int attempt = 0; attempt < 64; attempt++) {
+        float x = rng.next_signed(), y = rng.next_signed(), z = rng.next_signed();
+        float r2 = (x * x + y * y) + z * z;
+        if (!(r2 > 1e-6f && r2 <= 1.0f)) continue;
+        float r = std::sqrt(r2);
+        float dx = n[0] + x / r, dy = n[1] + y / r, dz = n[2] + z / r;
+        float l2 = (dx * dx + dy * dy) + dz * dz;
+        if (!(l2 > 1e-12f)) continue;
+        float l = std::sqrt(l2);
+        out[0] = dx / l;
+        out[1] = dy / l;
+        out[2] = dz / l;
+        return;
+    }
+    float l = std::sqrt((n[0] * n[0] + n[1] * n[1]) + n[2] * n[2]);
+    for (int c = 0; c < 3; c++) out[c] = n[c] / l;
+}
+
+uint32_t eff_iters(uint32_t max_iters) {
+    if (max_iters == 0) return VRT_DEFAULT_MAX_ITERS;
+    return max_iters > 65535 ? 65535 : max_iters;
+}
+
+struct StatAcc {
+    std::vector<ora_stats> per;
+    explicit StatAcc(int threads) {
+        int t = threads <= 0 ? (int)std::thread::hardware_concurrency() : threads;
+        per.assign(t > 0 ? t : 1, ora_stats{0, 0, 0, 0});
+    }
+    void add(int tid, const Trace& tr) {
+        ora_stats& s = per[tid];
+        s.rays++;
+        s.step_calls += tr.step_calls;
+        s.occ_fetches += tr.occ_fetches;
+        s.hits += tr.hit ? 1 : 0;
+    }
+    void store(ora_stats* out) const {
+        if (!out) return;
+        *out = ora_stats{0, 0, 0, 0};
+        for (auto& s : per) {
+            out->rays += s.rays;
+            out->step_calls += s.step_calls;
+            out->occ_fetches += s.occ_fetches;
+            out->hits += s.hits;
+        }
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+ora_world* ora_world_create(uint32_t sx, uint32_t sy, uint32_t sz) {
+    if (sx == 0 || sy == 0 || sz == 0 || sx * 32 > VRT_MAX_WORLD_X || sy * 32 > VRT_MAX_WORLD_Y ||
+        sz * 32 > VRT_MAX_WORLD_Z)
+        return nullptr;
+    ora_world* w = new ora_world;
+    w->sx = sx;
+    w->sy = sy;
+    w->sz = sz;
+    w->masks.assign((size_t)sx * sy * sz, 0);
+    w->data.resize((size_t)sx * sy * sz);
+    return w;
+}
+
+void ora_world_destroy(ora_world* w) { delete w; }
+
+// FlatVoxelStorage::SyncBuffers (CpuRenderer.cpp:33-61) for the record semantics of
+// vrt_world_sync_sectors: new mask, dirty bricks copied, occupancy re-derived.
+int ora_world_sync(ora_world* w, uint32_t n, const int32_t* sector_idx, const uint64_t* alloc_mask,
+                   const uint64_t* dirty_mask, const uint8_t* bricks) {
+    if (!w || (n && (!sector_idx || !alloc_mask))) return -1;
+    const uint8_t* p = bricks;
+    for (uint32_t i = 0; i < n; i++) {
+        uint64_t am = alloc_mask[i];
+        uint64_t dm = dirty_mask ? (dirty_mask[i] & am) : am;
+        int32_t x, y, z;
+        decode_sector(sector_idx[i], x, y, z);
+        if (dm && !p) return -1;
+        if (w->sector_in(x, y, z)) {
+            uint32_t s = w->lin(x, y, z);
+            uint64_t old = w->masks[s];
+            for (uint64_t r = old & ~am; r; r &= r - 1) w->clear_brick(s, ctz64(r));
+            if (am) {
+                SectorBlock* blk = w->block(s);
+                for (uint64_t r = am & ~old & ~dm; r; r &= r - 1) w->clear_brick(s, ctz64(r));
+                const uint8_t* q = p;
+                for (uint64_t r = dm; r; r &= r - 1) {
+                    uint32_t b = ctz64(r);
+                    std::memcpy(&blk->vox[b * 512], q, 512);
+                    update_occupancy(&blk->vox[b * 512], &blk->occ[b * 8]);
+                    q += 512;
+                }
+            } else {
+                w->data[s].reset();
+            }
+            w->masks[s] = am;
+        }
+        if (p) p += (size_t)popc64(dm) * 512;
+    }
+    return 0;
+}
+
+uint64_t ora_world_sector_mask(const ora_world* w, int32_t sector_idx) {
+    int32_t x, y, z;
+    decode_sector(sector_idx, x, y, z);
+    if (!w || !w->sector_in(x, y, z)) return 0;
+    return w->masks[w->lin(x, y, z)];
+}
+
+int ora_world_read_sector(const ora_world* w, int32_t sector_idx, uint64_t* mask, uint8_t* bricks) {
+    int32_t x, y, z;
+    decode_sector(sector_idx, x, y, z);
+    if (!w || !w->sector_in(x, y, z)) return -1;
+    uint32_t s = w->lin(x, y, z);
+    uint64_t m = w->masks[s];
+    if (mask) *mask = m;
+    if (bricks) {
+        for (uint64_t r = m; r; r &= r - 1) {
+            std::memcpy(bricks, &w->data[s]->vox[ctz64(r) * 512], 512);
+            bricks += 512;
+        }
+    }
+    return 0;
+}
+
+uint8_t ora_world_get_voxel(const ora_world* w, int32_t x, int32_t y, int32_t z) {
+    if (!w || !w->sector_in(x >> 5, y >> 5, z >> 5) || x < 0 || y < 0 || z < 0) return 0;
+    uint32_t s = w->lin(x >> 5, y >> 5, z >> 5);
+    uint32_t b = ((x >> 3) & 3) | ((z >> 3) & 3) << 2 | ((y >> 3) & 3) << 4;
+    if (!((w->masks[s] >> b) & 1)) return 0;
+    return w->data[s]->vox[b * 512 + ((x & 7) | (z & 7) << 3 | (y & 7) << 6)];
+}
+
+int ora_world_brick_occupancy(const ora_world* w, int32_t bx, int32_t by, int32_t bz, uint64_t out[8]) {
+    if (!w || bx < 0 || by < 0 || bz < 0 || !w->sector_in(bx >> 2, by >> 2, bz >> 2)) return -1;
+    uint32_t s = w->lin(bx >> 2, by >> 2, bz >> 2);
+    uint32_t b = (bx & 3) | (bz & 3) << 2 | (by & 3) << 4;
+    if (!((w->masks[s] >> b) & 1)) {
+        std::memset(out, 0, 64);
+        return 0;
+    }
+    std::memcpy(out, &w->data[s]->occ[b * 8], 64);
+    return 0;
+}
+
+uint64_t ora_world_allocated_bricks(const ora_world* w) {
+    uint64_t n = 0;
+    for (uint64_t m : w->masks) n += (uint64_t)popc64(m);
+    return n;
+}
+
+int ora_cast(const ora_world* w, const vrt_ray* rays, uint64_t n, const vrt_cast_params* params,
+             vrt_hit* hits, int threads, ora_stats* stats) {
+    if (!w || (n && (!rays || !hits)) || !params) return -1;
+    uint32_t iters = eff_iters(params->max_iters);
+    StatAcc acc(threads);
+    parallel_for(n, (int)acc.per.size(), [&](int tid, uint64_t b, uint64_t e) {
+        Trace tr;
+        for (uint64_t i = b; i < e; i++) {
+            trace_ray(*w, rays[i].origin, rays[i].dir, params->world_origin, iters, tr);
+            fill_hit(tr, rays[i].dir, rays[i].tag, hits[i]);
+            acc.add(tid, tr);
+        }
+    });
+    acc.store(stats);
+    return 0;
+}
+
+int ora_camera_rays(const vrt_camera* cam, vrt_ray* rays) {
+    if (!cam || !rays) return -1;
+    for (uint32_t py = 0; py < cam->height; py++)
+        for (uint32_t px = 0; px < cam->width; px++) {
+            vrt_ray& r = rays[(size_t)py * cam->width + px];
+            camera_ray(*cam, px, py, r.origin, r.dir);
+            r.tag = py * cam->width + px;
+            r.reserved = 0;
+        }
+    return 0;
+}
+
+int ora_render_view(const ora_world* w, const vrt_camera* cam, uint32_t max_iters, vrt_hit* hits,
+                    int threads, ora_stats* stats) {
+    if (!w || !cam || !hits) return -1;
+    uint32_t iters = eff_iters(max_iters);
+    uint64_t n = (uint64_t)cam->width * cam->height;
+    StatAcc acc(threads);
+    parallel_for(n, (int)acc.per.size(), [&](int tid, uint64_t b, uint64_t e) {
+        Trace tr;
+        float o[3], d[3];
+        for (uint64_t i = b; i < e; i++) {
+            camera_ray(*cam, (uint32_t)(i % cam->width), (uint32_t)(i / cam->width), o, d);
+            trace_ray(*w, o, d, cam->world_origin, iters, tr);
+            fill_hit(tr, d, (uint32_t)i, hits[i]);
+            acc.add(tid, tr);
+        }
+    });
+    acc.store(stats);
+    return 0;
+}
+
+int ora_render_view_shadow(const ora_world* w, const vrt_camera* cam, const float sun_dir[3],
+                           uint32_t max_iters, vrt_hit* primary, vrt_hit* shadow, int threads,
+                           ora_stats* stats) {
+    if (!w || !cam || !sun_dir || !primary || !shadow) return -1;
+    uint32_t iters = eff_iters(max_iters);
+    uint64_t n = (uint64_t)cam->width * cam->height;
+    StatAcc acc(threads);
+    parallel_for(n, (int)acc.per.size(), [&](int tid, uint64_t b, uint64_t e) {
+        Trace tr, ts;
+        float o[3], d[3], nrm[3], so[3];
+        for (uint64_t i = b; i < e; i++) {
+            camera_ray(*cam, (uint32_t)(i % cam->width), (uint32_t)(i / cam->width), o, d);
+            trace_ray(*w, o, d, cam->world_origin, iters, tr);
+            fill_hit(tr, d, (uint32_t)i, primary[i]);
+            acc.add(tid, tr);
+            if (!tr.hit) {
+                fill_no_ray(shadow[i]);
+                continue;
+            }
+            hit_normal(tr, d, nrm);
+            offset_origin(tr, nrm, so);
+            trace_ray(*w, so, sun_dir, cam->world_origin, iters, ts);
+            fill_hit(ts, sun_dir, (uint32_t)i, shadow[i]);
+            acc.add(tid, ts);
+        }
+    });
+    acc.store(stats);
+    return 0;
+}
+
+int ora_render_view_bounces(const ora_world* w, const vrt_camera* cam, uint32_t n_bounces,
+                            uint32_t max_iters, vrt_hit* hits, int threads, ora_stats* stats) {
+    if (!w || !cam || !hits) return -1;
+    uint32_t iters = eff_iters(max_iters);
+    uint64_t n = (uint64_t)cam->width * cam->height;
+    StatAcc acc(threads);
+    parallel_for(n, (int)acc.per.size(), [&](int tid, uint64_t b, uint64_t e) {
+        Trace tr;
+        float o[3], d[3], nrm[3];
+        for (uint64_t i = b; i < e; i++) {
+            camera_ray(*cam, (uint32_t)(i % cam->width), (uint32_t)(i / cam->width), o, d);
+            bool alive = true;
+            for (uint32_t k = 0; k <= n_bounces; k++) {
+                vrt_hit& h = hits[(uint64_t)k * n + i];
+                if (!alive) {
+                    fill_no_ray(h);
+                    continue;
+                }
+                if (k > 0) {
+                    hit_normal(tr, d, nrm);
+                    offset_origin(tr, nrm, o);
+                    bounce_dir((uint32_t)i, k, nrm, d);
+                }
+                trace_ray(*w, o, d, cam->world_origin, iters, tr);
+                fill_hit(tr, d, (uint32_t)i, h);
+                acc.add(tid, tr);
+                alive = tr.hit;
+            }
+        }
+    });
+    acc.store(stats);
+    return 0;
+}
+
+// VoxelMap::RegionDispatchSIMD + GC (VoxelMap.h:222-263) driving the sphere brush
+// (Brush.cpp:10-31) with an exact integer sphere test.
+int ora_world_edit(ora_world* w, const vrt_edit* edits, uint32_t n) {
+    if (!w || (n && !edits)) return -1;
+    const int32_t nbx = (int32_t)w->sx * 4, nby = (int32_t)w->sy * 4, nbz = (int32_t)w->sz * 4;
+    for (uint32_t k = 0; k < n; k++) {
+        const vrt_edit& e = edits[k];
+        const int64_t r = e.radius;
+        const int64_t r2 = r * r;
+        const bool create = e.material != 0;  // createEmpty = !isErasing (Brush.cpp:17)
+        int64_t lo[3], hi[3];
+        const int32_t nb[3] = {nbx, nby, nbz};
+        bool empty_range = false;
+        for (int c = 0; c < 3; c++) {
+            lo[c] = ((int64_t)e.center[c] - r) >> 3;
+            hi[c] = ((int64_t)e.center[c] + r) >> 3;
+            if (lo[c] < 0) lo[c] = 0;
+            if (hi[c] > nb[c] - 1) hi[c] = nb[c] - 1;
+            if (lo[c] > hi[c]) empty_range = true;
+        }
+        if (empty_range) continue;
+        for (int64_t by = lo[1]; by <= hi[1]; by++)
+            for (int64_t bz = lo[2]; bz <= hi[2]; bz++)
+                for (int64_t bx = lo[0]; bx <= hi[0]; bx++) {
+                    uint32_t s = w->lin((int32_t)bx >> 2, (int32_t)by >> 2, (int32_t)bz >> 2);
+                    uint32_t b = (uint32_t)((bx & 3) | (bz & 3) << 2 | (by & 3) << 4);
+                    bool allocated = (w->masks[s] >> b) & 1;
+                    if (!allocated && !create) continue;
+                    SectorBlock* blk = w->block(s);
+                    if (!allocated) {
+                        w->clear_brick(s, b);
+                        w->masks[s] |= 1ull << b;
+                    }
+                    uint8_t* brick = &blk->vox[b * 512];
+                    for (int vi = 0; vi < 512; vi++) {
+                        int64_t x = bx * 8 + (vi & 7), z = bz * 8 + ((vi >> 3) & 7), y = by * 8 + (vi >> 6);
+                        int64_t dx = x - e.center[0], dy = y - e.center[1], dz = z - e.center[2];
+                        if (dx * dx + dy * dy + dz * dz > r2) continue;
+                        if (e.mode == VRT_EDIT_REPLACE && brick[vi] == 0) continue;
+                        brick[vi] = e.material;
+                    }
+                    update_occupancy(brick, &blk->occ[b * 8]);
+                    if (brick_is_empty(brick)) {
+                        w->clear_brick(s, b);
+                        w->masks[s] &= ~(1ull << b);
+                    }
+                }
+        // drop blocks of sectors that became empty
+        for (int64_t sy = lo[1] >> 2; sy <= hi[1] >> 2; sy++)
+            for (int64_t sz = lo[2] >> 2; sz <= hi[2] >> 2; sz++)
+                for (int64_t sx = lo[0] >> 2; sx <= hi[0] >> 2; sx++) {
+                    uint32_t s = w->lin((int32_t)sx, (int32_t)sy, (int32_t)sz);
+                    if (w->masks[s] == 0) w->data[s].reset();
+                }
+    }
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,207 @@
+"""GB300 brickmap ray traversal: Python handle over libvrt.so.
+
+The library (C ABI in include/vrt.h) owns the device-resident brickmap and runs the
+sm_103a kernels; this module only converts numpy arrays and torch tensors into
+pointers.  It mirrors the reference's storage boundary:
+
+* ``World.sync_sectors`` is ``GpuVoxelStorage::SyncBuffers(VoxelMap&)``
+  (src/VoxelRT/GpuRenderer.cpp:45-167) fed with DirtyLocs-shaped records;
+* ``World.render_view`` is one ``GpuRenderer::RenderFrame`` traversal dispatch
+  (GpuRenderer.cpp:239-273) writing hit records;
+* ``World.cast`` traverses explicit rays.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .capi import (EDIT_DTYPE, HIT_DTYPE, MISS_FACE, MISS_VOXEL, NO_RAY, RAY_DTYPE, Camera, CastParams, VrtError,
+                   check, lib, ptr)
+
+__all__ = ["World", "Camera", "look_at", "synth_terrain", "synth_mix", "random_rays", "SectorData", "VrtError",
+           "RAY_DTYPE", "HIT_DTYPE", "EDIT_DTYPE", "MISS_VOXEL", "MISS_FACE", "NO_RAY", "unpack_voxel", "sector_index",
+           "lib"]
+
+
+def sector_index(x: int, y: int, z: int) -> int:
+    """WorldSectorIndexer packing (VoxelMap.h:100)."""
+    return lib().vrt_sector_index(x, y, z)
+
+
+def unpack_voxel(v: np.ndarray) -> np.ndarray:
+    """Packed x | y<<11 | z<<21 hit voxels -> (n, 3) int array (misses give 2047/1023/2047)."""
+    v = np.asarray(v, dtype=np.uint32)
+    return np.stack([v & 0x7FF, (v >> 11) & 0x3FF, v >> 21], axis=-1).astype(np.int64)
+
+
+def look_at(pos, target, vfov_deg: float, width: int, height: int) -> Camera:
+    cam = Camera()
+    p = (C.c_double * 3)(*map(float, pos))
+    t = (C.c_double * 3)(*map(float, target))
+    check(lib().vrt_camera_look_at(p, t, float(vfov_deg), int(width), int(height), C.byref(cam)))
+    return cam
+
+
+class SectorData:
+    """A sector stream in host memory: records (sector_idx, alloc_mask) + packed bricks."""
+
+    def __init__(self, sectors, sector_idx, alloc_mask, bricks, owner=None):
+        self.sectors = tuple(int(s) for s in sectors)
+        self.sector_idx = np.ascontiguousarray(sector_idx, dtype=np.int32)
+        self.alloc_mask = np.ascontiguousarray(alloc_mask, dtype=np.uint64)
+        self.bricks = np.ascontiguousarray(bricks, dtype=np.uint8).reshape(-1, 512)
+        self._owner = owner
+
+    @property
+    def n_bricks(self) -> int:
+        return self.bricks.shape[0]
+
+    @classmethod
+    def _from_native(cls, sp) -> "SectorData":
+        s = sp.contents
+        n, nb = s.n_sectors, s.n_bricks
+        idx = np.ctypeslib.as_array(s.sector_idx, shape=(max(n, 1),))[:n].copy()
+        mask = np.ctypeslib.as_array(s.alloc_mask, shape=(max(n, 1),))[:n].copy()
+        bricks = np.ctypeslib.as_array(s.bricks, shape=(max(nb, 1) * 512,))[: nb * 512].copy()
+        sectors = (s.sectors_x, s.sectors_y, s.sectors_z)
+        lib().vrt_sector_stream_free(sp)
+        return cls(sectors, idx, mask, bricks)
+
+    def dense(self) -> np.ndarray:
+        """Dense (Y, Z, X) voxel volume (tests and small worlds only)."""
+        sx, sy, sz = self.sectors
+        vol = np.zeros((sy * 32, sz * 32, sx * 32), np.uint8)
+        k = 0
+        for idx, m in zip(self.sector_idx.tolist(), self.alloc_mask.tolist()):
+            x, z, y = idx & 4095, (idx >> 12) & 4095, (idx >> 24) & 255
+            for b in range(64):
+                if (m >> b) & 1:
+                    bx, bz, by = b & 3, (b >> 2) & 3, b >> 4
+                    brick = self.bricks[k].reshape(8, 8, 8)  # (y, z, x)
+                    y0, z0, x0 = y * 32 + by * 8, z * 32 + bz * 8, x * 32 + bx * 8
+                    vol[y0:y0 + 8, z0:z0 + 8, x0:x0 + 8] = brick
+                    k += 1
+        return vol
+
+
+def synth_terrain(size, base, amplitude, seed, scale=128.0, octaves=4, cave_octaves=0, cave_scale=64.0,
+                  cave_threshold=0.35, cave_seed=0, threads=0) -> SectorData:
+    d = _terrain_desc(size, base, amplitude, seed, scale, octaves, cave_octaves, cave_scale, cave_threshold, cave_seed)
+    out = C.POINTER(capi.SectorStream)()
+    check(lib().vrt_synth_terrain_world(C.byref(d), int(threads), C.byref(out)))
+    return SectorData._from_native(out)
+
+
+def terrain_height(x, z, size, base, amplitude, seed, scale=128.0, octaves=4) -> float:
+    d = _terrain_desc(size, base, amplitude, seed, scale, octaves, 0, 64.0, 0.35, 0)
+    return lib().vrt_synth_terrain_height(C.byref(d), float(x), float(z))
+
+
+def _terrain_desc(size, base, amplitude, seed, scale, octaves, cave_octaves, cave_scale, cave_threshold, cave_seed):
+    d = capi.SynthTerrain()
+    d.size[:] = [int(v) for v in size]
+    d.base, d.amplitude, d.scale = float(base), float(amplitude), float(scale)
+    d.octaves, d.seed = int(octaves), int(seed)
+    d.cave_octaves, d.cave_scale, d.cave_threshold, d.cave_seed = (int(cave_octaves), float(cave_scale),
+                                                                    float(cave_threshold), int(cave_seed))
+    return d
+
+
+def synth_mix(edge: int, seed: int, threads: int = 0) -> SectorData:
+    out = C.POINTER(capi.SectorStream)()
+    check(lib().vrt_synth_mix_world(int(edge), int(seed), int(threads), C.byref(out)))
+    return SectorData._from_native(out)
+
+
+def random_rays(size, seed: int, n: int, first: int = 0, threads: int = 0) -> np.ndarray:
+    rays = np.zeros(n, RAY_DTYPE)
+    s = (C.c_uint32 * 3)(*[int(v) for v in size])
+    check(lib().vrt_synth_random_rays(s, int(seed), int(first), int(n), int(threads), rays.ctypes.data))
+    return rays
+
+
+def _stream_ptr(stream) -> int | None:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream  # torch.cuda.Stream
+
+
+class World:
+    """A device-resident brickmap (vrt_world)."""
+
+    def __init__(self, sectors, brick_capacity: int = 0, device: int = 0, flags: int = 0):
+        d = capi.WorldDesc(int(sectors[0]), int(sectors[1]), int(sectors[2]), int(brick_capacity), int(device),
+                           int(flags))
+        h = C.c_void_p()
+        check(lib().vrt_world_create(C.byref(d), C.byref(h)))
+        self._h = h
+        self.sectors = tuple(int(s) for s in sectors)
+        self.size = tuple(32 * s for s in self.sectors)
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def close(self) -> None:
+        if self._h:
+            lib().vrt_world_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def stats(self) -> dict:
+        s = capi.WorldStats()
+        check(lib().vrt_world_get_stats(self._h, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
+    def sync_sectors(self, sector_idx, alloc_mask, bricks=None, dirty_mask=None, stream=None) -> None:
+        sector_idx = np.ascontiguousarray(sector_idx, dtype=np.int32)
+        alloc_mask = np.ascontiguousarray(alloc_mask, dtype=np.uint64)
+        dirty = None if dirty_mask is None else np.ascontiguousarray(dirty_mask, dtype=np.uint64)
+        b = None if bricks is None else np.ascontiguousarray(bricks, dtype=np.uint8)
+        check(lib().vrt_world_sync_sectors(self._h, len(sector_idx), ptr(sector_idx), ptr(alloc_mask), ptr(dirty),
+                                           ptr(b), _stream_ptr(stream)))
+
+    def upload(self, data: SectorData, stream=None) -> None:
+        self.sync_sectors(data.sector_idx, data.alloc_mask, data.bricks, None, stream)
+
+    def read_sector(self, sector_idx: int):
+        mask = C.c_uint64()
+        check(lib().vrt_world_read_sector(self._h, int(sector_idx), C.byref(mask), None, 0, None))
+        n = bin(mask.value).count("1")
+        bricks = np.zeros((n, 512), np.uint8)
+        check(lib().vrt_world_read_sector(self._h, int(sector_idx), C.byref(mask), ptr(bricks), bricks.nbytes, None))
+        return mask.value, bricks
+
+    def cast(self, rays: np.ndarray, world_origin=(0, 0, 0), max_iters: int = 0, stream=None) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
+        hits = np.zeros(len(rays), HIT_DTYPE)
+        p = CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), 0)
+        check(lib().vrt_cast(self._h, ptr(rays), len(rays), C.byref(p), ptr(hits), _stream_ptr(stream)))
+        return hits
+
+    def cast_device(self, rays, n: int, hits, world_origin=(0, 0, 0), max_iters: int = 0, stream=None) -> None:
+        p = CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), 0)
+        check(lib().vrt_cast_device(self._h, ptr(rays), int(n), C.byref(p), ptr(hits), _stream_ptr(stream)))
+
+    def render_view(self, cam: Camera, max_iters: int = 0, stream=None) -> np.ndarray:
+        hits = np.zeros(cam.width * cam.height, HIT_DTYPE)
+        check(lib().vrt_render_view(self._h, C.byref(cam), int(max_iters), ptr(hits), _stream_ptr(stream)))
+        return hits
+
+    def render_view_device(self, cam: Camera, hits, max_iters: int = 0, stream=None) -> None:
+        check(lib().vrt_render_view_device(self._h, C.byref(cam), int(max_iters), ptr(hits), _stream_ptr(stream)))

@@ -1,0 +1,158 @@
+"""ctypes binding of libvrt.so (include/vrt.h, include/vrt_synth.h).
+
+Only plumbing: every operation runs in the native library.  Importing this module
+fails loudly when the library has not been built - there is no Python fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+_LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libvrt.so"
+
+VRT_OK = 0
+VRT_ERR_INVALID_ARG = 1
+VRT_ERR_OUT_OF_MEMORY = 2
+VRT_ERR_QUEUE_TIMEOUT = 3
+VRT_ERR_DEVICE = 4
+VRT_ERR_NO_DEVICE = 5
+VRT_ERR_SLOTS_EXHAUSTED = 6
+VRT_ERR_NOT_FOUND = 7
+VRT_ERR_IO = 8
+VRT_ERR_FORMAT = 9
+
+MISS_VOXEL = 0xFFFFFFFF
+MISS_FACE = 0xFF
+NO_RAY = 0xFFFFFFFF
+DEFAULT_MAX_ITERS = 128
+EDIT_FILL = 0
+EDIT_REPLACE = 1
+
+
+class Ray(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("dir", C.c_float * 3), ("tag", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class Hit(C.Structure):
+    _fields_ = [("voxel", C.c_uint32), ("face", C.c_uint8), ("material", C.c_uint8), ("steps", C.c_uint16),
+                ("t", C.c_float), ("tag", C.c_uint32)]
+
+
+class CastParams(C.Structure):
+    _fields_ = [("world_origin", C.c_int32 * 3), ("max_iters", C.c_uint32), ("flags", C.c_uint32)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("world_origin", C.c_int32 * 3), ("origin", C.c_float * 3), ("d0", C.c_float * 3),
+                ("du", C.c_float * 3), ("dv", C.c_float * 3), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class Edit(C.Structure):
+    _fields_ = [("center", C.c_int32 * 3), ("radius", C.c_uint32), ("material", C.c_uint8), ("mode", C.c_uint8),
+                ("reserved", C.c_uint16)]
+
+
+class WorldDesc(C.Structure):
+    _fields_ = [("sectors_x", C.c_uint32), ("sectors_y", C.c_uint32), ("sectors_z", C.c_uint32),
+                ("brick_capacity", C.c_uint32), ("device", C.c_int32), ("flags", C.c_uint32)]
+
+
+class WorldStats(C.Structure):
+    _fields_ = [("sectors_x", C.c_uint32), ("sectors_y", C.c_uint32), ("sectors_z", C.c_uint32),
+                ("allocated_bricks", C.c_uint32), ("brick_capacity", C.c_uint32), ("free_ranges", C.c_uint32),
+                ("device_bytes", C.c_uint64)]
+
+
+class SectorStream(C.Structure):
+    _fields_ = [("sectors_x", C.c_uint32), ("sectors_y", C.c_uint32), ("sectors_z", C.c_uint32),
+                ("n_sectors", C.c_uint32), ("n_bricks", C.c_uint64), ("sector_idx", C.POINTER(C.c_int32)),
+                ("alloc_mask", C.POINTER(C.c_uint64)), ("bricks", C.POINTER(C.c_uint8))]
+
+
+class SynthTerrain(C.Structure):
+    _fields_ = [("size", C.c_uint32 * 3), ("base", C.c_double), ("amplitude", C.c_double), ("scale", C.c_double),
+                ("octaves", C.c_uint32), ("seed", C.c_uint64), ("cave_octaves", C.c_uint32),
+                ("cave_scale", C.c_double), ("cave_threshold", C.c_double), ("cave_seed", C.c_uint64)]
+
+
+RAY_DTYPE = np.dtype([("origin", "<f4", 3), ("dir", "<f4", 3), ("tag", "<u4"), ("reserved", "<u4")])
+HIT_DTYPE = np.dtype([("voxel", "<u4"), ("face", "u1"), ("material", "u1"), ("steps", "<u2"), ("t", "<f4"),
+                      ("tag", "<u4")])
+EDIT_DTYPE = np.dtype([("center", "<i4", 3), ("radius", "<u4"), ("material", "u1"), ("mode", "u1"),
+                       ("reserved", "<u2")])
+assert RAY_DTYPE.itemsize == C.sizeof(Ray) == 32
+assert HIT_DTYPE.itemsize == C.sizeof(Hit) == 16
+assert EDIT_DTYPE.itemsize == C.sizeof(Edit) == 20
+
+_vp = C.c_void_p
+_st = C.c_int
+_u32 = C.c_uint32
+_i32 = C.c_int32
+_u64 = C.c_uint64
+
+# name -> (restype, argtypes); every symbol declared in include/*.h
+PROTOTYPES = {
+    "vrt_last_error": (C.c_char_p, []),
+    "vrt_abi_version": (_u32, []),
+    "vrt_sector_index": (_i32, [_i32, _i32, _i32]),
+    "vrt_world_create": (_st, [C.POINTER(WorldDesc), C.POINTER(_vp)]),
+    "vrt_world_destroy": (_st, [_vp]),
+    "vrt_world_get_stats": (_st, [_vp, C.POINTER(WorldStats)]),
+    "vrt_world_sync_sectors": (_st, [_vp, _u32, _vp, _vp, _vp, _vp, _vp]),
+    "vrt_world_read_sector": (_st, [_vp, _i32, C.POINTER(_u64), _vp, C.c_size_t, _vp]),
+    "vrt_cast": (_st, [_vp, _vp, _u32, C.POINTER(CastParams), _vp, _vp]),
+    "vrt_cast_device": (_st, [_vp, _vp, _u32, C.POINTER(CastParams), _vp, _vp]),
+    "vrt_render_view": (_st, [_vp, C.POINTER(Camera), _u32, _vp, _vp]),
+    "vrt_render_view_device": (_st, [_vp, C.POINTER(Camera), _u32, _vp, _vp]),
+    "vrt_camera_look_at": (_st, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_double, _u32, _u32,
+                                 C.POINTER(Camera)]),
+    "vrt_synth_terrain_world": (_st, [C.POINTER(SynthTerrain), C.c_int, C.POINTER(C.POINTER(SectorStream))]),
+    "vrt_synth_terrain_height": (C.c_double, [C.POINTER(SynthTerrain), C.c_double, C.c_double]),
+    "vrt_synth_mix_world": (_st, [_u32, _u64, C.c_int, C.POINTER(C.POINTER(SectorStream))]),
+    "vrt_sector_stream_free": (None, [C.POINTER(SectorStream)]),
+    "vrt_synth_random_rays": (_st, [C.POINTER(_u32), _u64, _u64, _u64, C.c_int, _vp]),
+}
+
+
+class VrtError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"vrt status {status}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libvrt.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not _LIB_PATH.exists():
+            raise ImportError(f"{_LIB_PATH} is missing: run `python -m voxelrt_gb300.build` first")
+        L = C.CDLL(str(_LIB_PATH))
+        for name, (res, args) in PROTOTYPES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != VRT_OK:
+        raise VrtError(status, lib().vrt_last_error().decode(errors="replace"))
+
+
+def ptr(a) -> int | None:
+    """Address of a numpy array, a torch tensor, or None."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    if isinstance(a, int):
+        return a
+    raise TypeError(type(a))

@@ -1,0 +1,192 @@
+// trace.cu - per-view and explicit-ray traversal kernels and their C ABI.
+//
+// vrt_render_view* is the one-launch-per-view path of GpuRenderer::RenderFrame
+// (src/VoxelRT/GpuRenderer.cpp:239-273): 8x8 thread blocks over the image, one
+// primary ray per pixel (Shaders/VoxelRender.comp:27-30), writing a headless hit
+// buffer instead of the G-buffer.  vrt_cast* traverses caller-supplied rays.
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "trace_core.cuh"
+#include "world.h"
+
+namespace vrt {
+namespace {
+
+uint32_t eff_iters(uint32_t max_iters) {
+    if (max_iters == 0) return VRT_DEFAULT_MAX_ITERS;
+    return max_iters > 65535u ? 65535u : max_iters;
+}
+
+__global__ void __launch_bounds__(64) render_view_kernel(DevWorld w, vrt_camera cam, uint32_t max_iters,
+                                                        uint4* __restrict__ out) {
+    const uint32_t px = blockIdx.x * 8 + threadIdx.x;
+    const uint32_t py = blockIdx.y * 8 + threadIdx.y;
+    if (px >= cam.width || py >= cam.height) return;
+    float dx, dy, dz;
+    camera_ray(cam, px, py, dx, dy, dz);
+    TraceResult r;
+    TraceCounters cnt;
+    trace_ray<false>(w, cam.origin[0], cam.origin[1], cam.origin[2], dx, dy, dz, cam.world_origin[0],
+                     cam.world_origin[1], cam.world_origin[2], max_iters, r, cnt);
+    const uint32_t pix = py * cam.width + px;
+    out[pix] = pack_hit(r, dx, dy, dz, pix);
+}
+
+__global__ void __launch_bounds__(256) cast_kernel(DevWorld w, const float4* __restrict__ rays, uint32_t n,
+                                                  int32_t wox, int32_t woy, int32_t woz, uint32_t max_iters,
+                                                  uint4* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 a = rays[2 * (size_t)i], b = rays[2 * (size_t)i + 1];
+    TraceResult r;
+    TraceCounters cnt;
+    trace_ray<false>(w, a.x, a.y, a.z, a.w, b.x, b.y, wox, woy, woz, max_iters, r, cnt);
+    out[i] = pack_hit(r, a.w, b.x, b.y, __float_as_uint(b.z));
+}
+
+vrt_status check_camera(const vrt_camera* cam) {
+    if (!cam || cam->width == 0 || cam->height == 0 || cam->width > 16384 || cam->height > 16384) {
+        set_error("camera must be 1..16384 pixels on each side");
+        return VRT_ERR_INVALID_ARG;
+    }
+    return VRT_OK;
+}
+
+vrt_status launch_render(vrt_world* w, const vrt_camera* cam, uint32_t max_iters, vrt_hit* hits,
+                         cudaStream_t stream) {
+    dim3 block(8, 8);
+    dim3 grid((cam->width + 7) / 8, (cam->height + 7) / 8);
+    render_view_kernel<<<grid, block, 0, stream>>>(w->dev(), *cam, eff_iters(max_iters),
+                                                   reinterpret_cast<uint4*>(hits));
+    VRT_CUDA(cudaGetLastError());
+    return VRT_OK;
+}
+
+vrt_status launch_cast(vrt_world* w, const vrt_ray* rays, uint32_t n, const vrt_cast_params* p, vrt_hit* hits,
+                       cudaStream_t stream) {
+    if (n == 0) return VRT_OK;
+    cast_kernel<<<(n + 255) / 256, 256, 0, stream>>>(w->dev(), reinterpret_cast<const float4*>(rays), n,
+                                                     p->world_origin[0], p->world_origin[1], p->world_origin[2],
+                                                     eff_iters(p->max_iters), reinterpret_cast<uint4*>(hits));
+    VRT_CUDA(cudaGetLastError());
+    return VRT_OK;
+}
+
+vrt_status check_params(const vrt_cast_params* p) {
+    if (!p || p->flags != 0) {
+        set_error("cast params missing or flags not 0");
+        return VRT_ERR_INVALID_ARG;
+    }
+    return VRT_OK;
+}
+
+}  // namespace
+}  // namespace vrt
+
+using namespace vrt;
+
+extern "C" {
+
+vrt_status vrt_cast_device(vrt_world* w, const vrt_ray* rays, uint32_t n, const vrt_cast_params* params,
+                           vrt_hit* hits, void* stream) {
+    vrt_status st = world_enter(w);
+    if (st != VRT_OK || (st = check_params(params)) != VRT_OK) return st;
+    if (n && (!rays || !hits)) {
+        set_error("null ray or hit buffer");
+        return VRT_ERR_INVALID_ARG;
+    }
+    return launch_cast(w, rays, n, params, hits, (cudaStream_t)stream);
+}
+
+vrt_status vrt_cast(vrt_world* w, const vrt_ray* rays, uint32_t n, const vrt_cast_params* params, vrt_hit* hits,
+                    void* stream_) {
+    vrt_status st = world_enter(w);
+    if (st != VRT_OK || (st = check_params(params)) != VRT_OK) return st;
+    if (n == 0) return VRT_OK;
+    if (!rays || !hits) {
+        set_error("null ray or hit buffer");
+        return VRT_ERR_INVALID_ARG;
+    }
+    std::lock_guard<std::mutex> lock(w->mu);
+    cudaStream_t stream = (cudaStream_t)stream_;
+    const size_t rb = (size_t)n * sizeof(vrt_ray), hb = (size_t)n * sizeof(vrt_hit);
+    VRT_CUDA(w->d_io.reserve(rb + hb));
+    vrt_ray* d_rays = (vrt_ray*)w->d_io.ptr;
+    vrt_hit* d_hits = (vrt_hit*)((uint8_t*)w->d_io.ptr + rb);
+    VRT_CUDA(cudaMemcpyAsync(d_rays, rays, rb, cudaMemcpyHostToDevice, stream));
+    if ((st = launch_cast(w, d_rays, n, params, d_hits, stream)) != VRT_OK) return st;
+    VRT_CUDA(cudaMemcpyAsync(hits, d_hits, hb, cudaMemcpyDeviceToHost, stream));
+    VRT_CUDA(cudaStreamSynchronize(stream));
+    return VRT_OK;
+}
+
+vrt_status vrt_render_view_device(vrt_world* w, const vrt_camera* cam, uint32_t max_iters, vrt_hit* hits,
+                                  void* stream) {
+    vrt_status st = world_enter(w);
+    if (st != VRT_OK || (st = check_camera(cam)) != VRT_OK) return st;
+    if (!hits) {
+        set_error("null hit buffer");
+        return VRT_ERR_INVALID_ARG;
+    }
+    return launch_render(w, cam, max_iters, hits, (cudaStream_t)stream);
+}
+
+vrt_status vrt_render_view(vrt_world* w, const vrt_camera* cam, uint32_t max_iters, vrt_hit* hits, void* stream_) {
+    vrt_status st = world_enter(w);
+    if (st != VRT_OK || (st = check_camera(cam)) != VRT_OK) return st;
+    if (!hits) {
+        set_error("null hit buffer");
+        return VRT_ERR_INVALID_ARG;
+    }
+    std::lock_guard<std::mutex> lock(w->mu);
+    cudaStream_t stream = (cudaStream_t)stream_;
+    const size_t hb = (size_t)cam->width * cam->height * sizeof(vrt_hit);
+    VRT_CUDA(w->d_io.reserve(hb));
+    if ((st = launch_render(w, cam, max_iters, (vrt_hit*)w->d_io.ptr, stream)) != VRT_OK) return st;
+    VRT_CUDA(cudaMemcpyAsync(hits, w->d_io.ptr, hb, cudaMemcpyDeviceToHost, stream));
+    VRT_CUDA(cudaStreamSynchronize(stream));
+    return VRT_OK;
+}
+
+vrt_status vrt_camera_look_at(const double pos[3], const double target[3], double vfov_deg, uint32_t width,
+                              uint32_t height, vrt_camera* out) {
+    if (!pos || !target || !out || width == 0 || height == 0 || !(vfov_deg > 0.0 && vfov_deg < 180.0)) {
+        set_error("bad camera arguments");
+        return VRT_ERR_INVALID_ARG;
+    }
+    double f[3] = {target[0] - pos[0], target[1] - pos[1], target[2] - pos[2]};
+    double fl = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+    if (!(fl > 0.0)) {
+        set_error("camera target equals position");
+        return VRT_ERR_INVALID_ARG;
+    }
+    for (double& c : f) c /= fl;
+    // right = forward x worldUp (y up); fall back to z when looking straight up/down
+    double up[3] = {0.0, 1.0, 0.0};
+    if (std::fabs(f[1]) > 0.999999) {
+        up[1] = 0.0;
+        up[2] = 1.0;
+    }
+    double r[3] = {f[1] * up[2] - f[2] * up[1], f[2] * up[0] - f[0] * up[2], f[0] * up[1] - f[1] * up[0]};
+    double rl = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    for (double& c : r) c /= rl;
+    double u[3] = {r[1] * f[2] - r[2] * f[1], r[2] * f[0] - r[0] * f[2], r[0] * f[1] - r[1] * f[0]};
+    const double th = std::tan(vfov_deg * 0.5 * 3.14159265358979323846 / 180.0);
+    const double aspect = (double)width / (double)height;
+    for (int c = 0; c < 3; c++) {
+        const double fp = std::floor(pos[c]);
+        out->world_origin[c] = (int32_t)fp;
+        out->origin[c] = (float)(pos[c] - fp);
+        out->d0[c] = (float)(f[c] - r[c] * th * aspect + u[c] * th);
+        out->du[c] = (float)(r[c] * (2.0 * th * aspect / width));
+        out->dv[c] = (float)(-u[c] * (2.0 * th / height));
+    }
+    out->width = width;
+    out->height = height;
+    return VRT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,416 @@
+// world.cu - device-resident brickmap storage: create/destroy, dirty-brick sync,
+// brick-slot repacking and occupancy re-derivation.
+//
+// Replaces GpuVoxelStorage (src/VoxelRT/GpuRenderer.cpp:17-167) and the
+// UpdateOccupancy dispatch (GpuRenderer.cpp:163-166, Shaders/UpdateOccupancy.comp).
+// Unlike the reference, bricks that keep their content but change slot are moved
+// on the device instead of being re-uploaded from the host
+// (BrickSlotAllocator.cpp:84-87 marks the whole sector dirty).
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <unordered_set>
+#include <vector>
+
+#include "world.h"
+
+namespace vrt {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+const char* last_error_cstr() { return g_last_error.c_str(); }
+
+vrt_status cuda_fail(cudaError_t e, const char* what) {
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    if (e == cudaErrorMemoryAllocation) return VRT_ERR_OUT_OF_MEMORY;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return VRT_ERR_NO_DEVICE;
+    return VRT_ERR_DEVICE;
+}
+
+vrt_status world_enter(vrt_world* world) {
+    if (!world) {
+        set_error("null world");
+        return VRT_ERR_INVALID_ARG;
+    }
+    VRT_CUDA(cudaSetDevice(world->device));
+    return VRT_OK;
+}
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Brick operations, one warp per brick.
+
+enum : uint32_t { kOpMove = 0u, kOpUpload = 1u, kOpZero = 2u };
+
+struct BrickOp {
+    uint32_t dst;  // 0-based destination slot
+    uint32_t src;  // kind << 30 | index (scratch brick or staged brick)
+};
+
+constexpr int kOpsWarps = 8;
+
+// Occupancy of one 512-byte brick held by a warp in shared memory: round r tests,
+// in lane l, voxel (4cx + (l&3), 4cy + 2h + (l>>4), 4cz + ((l>>2)&3)) of cell
+// c = r>>1 (cx = c&1, cz = (c>>1)&1, cy = c>>2), half h = r&1, so the ballot is
+// bits 32h..32h+31 of cell c's mask (bit vx + vz*4 + vy*16, CpuRenderer.cpp:78).
+// Lane c < 8 returns cell c's 64-bit mask.
+__device__ __forceinline__ uint64_t warp_cell_mask(const uint8_t* sb, uint32_t lane) {
+    uint64_t mine = 0;
+#pragma unroll
+    for (uint32_t r = 0; r < 16; r++) {
+        const uint32_t c = r >> 1, h = r & 1;
+        const uint32_t x = (c & 1) * 4 + (lane & 3);
+        const uint32_t z = ((c >> 1) & 1) * 4 + ((lane >> 2) & 3);
+        const uint32_t y = (c >> 2) * 4 + 2 * h + (lane >> 4);
+        const uint32_t bits = __ballot_sync(0xffffffffu, sb[x | z << 3 | y << 6] != 0);
+        if (lane == c) mine |= (uint64_t)bits << (32 * h);
+    }
+    return mine;
+}
+
+__global__ void gather_bricks_kernel(const uint32_t* __restrict__ src_slots, uint32_t n,
+                                     const uint8_t* __restrict__ payload, const uint64_t* __restrict__ occ,
+                                     uint8_t* __restrict__ scratch_payload, uint64_t* __restrict__ scratch_occ) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t k = warp; k < n; k += nwarps) {
+        const size_t s = src_slots[k];
+        const uint4 v = reinterpret_cast<const uint4*>(payload + s * 512)[lane];
+        reinterpret_cast<uint4*>(scratch_payload + (size_t)k * 512)[lane] = v;
+        if (lane < 8) scratch_occ[(size_t)k * 8 + lane] = occ[s * 8 + lane];
+    }
+}
+
+__global__ void __launch_bounds__(kOpsWarps * 32)
+    brick_ops_kernel(const BrickOp* __restrict__ ops, uint32_t n, const uint8_t* __restrict__ stage,
+                     const uint8_t* __restrict__ scratch_payload, const uint64_t* __restrict__ scratch_occ,
+                     uint8_t* __restrict__ payload, uint64_t* __restrict__ occ) {
+    __shared__ __align__(16) uint8_t sbrick[kOpsWarps][512];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t wib = threadIdx.x >> 5;
+    const uint32_t warp = blockIdx.x * kOpsWarps + wib;
+    const uint32_t nwarps = gridDim.x * kOpsWarps;
+    for (uint32_t k = warp; k < n; k += nwarps) {
+        const BrickOp op = ops[k];
+        const uint32_t kind = op.src >> 30, si = op.src & 0x3fffffffu;
+        const size_t d = op.dst;
+        if (kind == kOpMove) {
+            const uint4 v = reinterpret_cast<const uint4*>(scratch_payload + (size_t)si * 512)[lane];
+            reinterpret_cast<uint4*>(payload + d * 512)[lane] = v;
+            if (lane < 8) occ[d * 8 + lane] = scratch_occ[(size_t)si * 8 + lane];
+        } else if (kind == kOpZero) {
+            reinterpret_cast<uint4*>(payload + d * 512)[lane] = make_uint4(0, 0, 0, 0);
+            if (lane < 8) occ[d * 8 + lane] = 0;
+        } else {
+            const uint4 v = reinterpret_cast<const uint4*>(stage + (size_t)si * 512)[lane];
+            reinterpret_cast<uint4*>(payload + d * 512)[lane] = v;
+            reinterpret_cast<uint4*>(sbrick[wib])[lane] = v;
+            __syncwarp();
+            const uint64_t m = warp_cell_mask(sbrick[wib], lane);
+            if (lane < 8) occ[d * 8 + lane] = m;
+            __syncwarp();
+        }
+    }
+}
+
+uint32_t ops_grid(uint32_t n) {
+    uint32_t blocks = (n + kOpsWarps - 1) / kOpsWarps;
+    return std::max(1u, std::min(blocks, 152u * 16u));
+}
+
+// ---------------------------------------------------------------------------
+
+// Grow the brick pools to at least min_capacity slots (at least doubling);
+// slots keep their content, so planned moves stay valid.
+vrt_status grow_pool(vrt_world* w, uint32_t min_capacity, cudaStream_t stream) {
+    uint64_t want = std::max<uint64_t>({(uint64_t)w->capacity * 2, (uint64_t)min_capacity, 1024});
+    want = std::min<uint64_t>(want, 0x3fffffffull);
+    if (want <= w->capacity) {
+        set_error("brick pool cannot grow further");
+        return VRT_ERR_SLOTS_EXHAUSTED;
+    }
+    uint32_t cap = (uint32_t)want;
+    uint64_t* occ = nullptr;
+    uint8_t* payload = nullptr;
+    cudaError_t e = cudaMalloc(&occ, (size_t)cap * 64);
+    if (e == cudaSuccess) e = cudaMalloc(&payload, (size_t)cap * 512);
+    if (e != cudaSuccess) {
+        if (occ) cudaFree(occ);
+        cudaGetLastError();
+        return cuda_fail(e, "grow brick pool");
+    }
+    if (w->capacity) {
+        VRT_CUDA(cudaMemcpyAsync(occ, w->d_occ, (size_t)w->capacity * 64, cudaMemcpyDeviceToDevice, stream));
+        VRT_CUDA(cudaMemcpyAsync(payload, w->d_payload, (size_t)w->capacity * 512, cudaMemcpyDeviceToDevice, stream));
+        VRT_CUDA(cudaStreamSynchronize(stream));
+    }
+    if (w->d_occ) cudaFree(w->d_occ);
+    if (w->d_payload) cudaFree(w->d_payload);
+    w->d_occ = occ;
+    w->d_payload = payload;
+    w->capacity = cap;
+    w->arena.grow(cap);
+    return VRT_OK;
+}
+
+// One self-consistent batch of sector updates: plan, then move, upload, zero.
+struct SyncBatch {
+    std::vector<uint32_t> gathers;   // old slots copied to scratch first
+    std::vector<BrickOp> ops;
+    const uint8_t* src = nullptr;    // first input brick of the batch
+    uint64_t n_stage = 0;            // bricks staged from the input
+    std::vector<uint32_t> touched;   // sector linear indices
+};
+
+vrt_status plan_sector(vrt_world* w, SyncBatch& b, uint32_t s, uint64_t am, uint64_t dm, uint64_t stage_first,
+                       cudaStream_t stream) {
+    SectorSlots& cur = w->slots[s];
+    const SectorSlots old = cur;
+    sector_free(w->arena, cur, old.mask & ~am);
+    while (!sector_alloc(w->arena, cur, am)) {
+        vrt_status st = grow_pool(w, w->capacity + 64, stream);
+        if (st != VRT_OK) return st;
+    }
+    uint64_t rank_in = 0;
+    for (uint64_t r = cur.mask; r; r &= r - 1) {
+        const uint32_t brick = (uint32_t)__builtin_ctzll(r);
+        const uint32_t dst = cur.slot_of(brick) - 1;
+        const uint64_t bit = 1ull << brick;
+        if (dm & bit) {
+            rank_in = (uint64_t)__builtin_popcountll(dm & (bit - 1));
+            b.ops.push_back({dst, kOpUpload << 30 | (uint32_t)(stage_first + rank_in)});
+        } else if (old.mask & bit) {
+            const uint32_t src = old.slot_of(brick) - 1;
+            if (src != dst) {
+                b.ops.push_back({dst, kOpMove << 30 | (uint32_t)b.gathers.size()});
+                b.gathers.push_back(src);
+            }
+        } else {
+            b.ops.push_back({dst, kOpZero << 30});
+        }
+    }
+    SectorRec& rec = w->h_table[s];
+    rec.mask_lo = (uint32_t)cur.mask;
+    rec.mask_hi = (uint32_t)(cur.mask >> 32);
+    rec.base = cur.base ? cur.base - 1 : 0;
+    rec.flags = 0;
+    b.touched.push_back(s);
+    return VRT_OK;
+}
+
+vrt_status run_batch(vrt_world* w, SyncBatch& b, cudaStream_t stream) {
+    if (b.ops.empty() && b.touched.empty()) return VRT_OK;
+    const size_t stage_bytes = (size_t)b.n_stage * 512;
+    if (stage_bytes) {
+        VRT_CUDA(w->d_stage.reserve(stage_bytes));
+        VRT_CUDA(cudaMemcpyAsync(w->d_stage.ptr, b.src, stage_bytes, cudaMemcpyHostToDevice, stream));
+    }
+    const size_t gbytes = b.gathers.size() * sizeof(uint32_t);
+    const size_t obytes = b.ops.size() * sizeof(BrickOp);
+    const size_t ooff = (gbytes + 15) & ~size_t(15);
+    if (gbytes + obytes) {
+        VRT_CUDA(w->d_ops.reserve(ooff + obytes));
+        if (gbytes) VRT_CUDA(cudaMemcpyAsync(w->d_ops.ptr, b.gathers.data(), gbytes, cudaMemcpyHostToDevice, stream));
+        if (obytes)
+            VRT_CUDA(cudaMemcpyAsync((uint8_t*)w->d_ops.ptr + ooff, b.ops.data(), obytes, cudaMemcpyHostToDevice, stream));
+    }
+    const size_t ng = b.gathers.size();
+    if (ng) {
+        VRT_CUDA(w->d_scratch.reserve(ng * 576));
+        uint8_t* sp = (uint8_t*)w->d_scratch.ptr;
+        uint64_t* so = (uint64_t*)(sp + ng * 512);
+        gather_bricks_kernel<<<ops_grid((uint32_t)ng), kOpsWarps * 32, 0, stream>>>(
+            (const uint32_t*)w->d_ops.ptr, (uint32_t)ng, w->d_payload, w->d_occ, sp, so);
+        VRT_CUDA(cudaGetLastError());
+    }
+    if (!b.ops.empty()) {
+        uint8_t* sp = (uint8_t*)w->d_scratch.ptr;
+        uint64_t* so = sp ? (uint64_t*)(sp + ng * 512) : nullptr;
+        brick_ops_kernel<<<ops_grid((uint32_t)b.ops.size()), kOpsWarps * 32, 0, stream>>>(
+            (const BrickOp*)((uint8_t*)w->d_ops.ptr + ooff), (uint32_t)b.ops.size(), (const uint8_t*)w->d_stage.ptr,
+            sp, so, w->d_payload, w->d_occ);
+        VRT_CUDA(cudaGetLastError());
+    }
+    // sector headers: copy the span of touched records
+    if (!b.touched.empty()) {
+        auto mm = std::minmax_element(b.touched.begin(), b.touched.end());
+        const uint32_t lo = *mm.first, hi = *mm.second + 1;
+        VRT_CUDA(cudaMemcpyAsync(w->d_sectors + lo, w->h_table.data() + lo, (size_t)(hi - lo) * sizeof(SectorRec),
+                                 cudaMemcpyHostToDevice, stream));
+    }
+    VRT_CUDA(cudaStreamSynchronize(stream));
+    b = SyncBatch();
+    return VRT_OK;
+}
+
+}  // namespace
+
+}  // namespace vrt
+
+using namespace vrt;
+
+extern "C" {
+
+const char* vrt_last_error(void) { return vrt::last_error_cstr(); }
+
+uint32_t vrt_abi_version(void) { return VRT_ABI_VERSION; }
+
+int32_t vrt_sector_index(int32_t sx, int32_t sy, int32_t sz) { return sector_index_pack(sx, sy, sz); }
+
+vrt_status vrt_world_create(const vrt_world_desc* desc, vrt_world** out) {
+    if (!desc || !out) {
+        set_error("null argument");
+        return VRT_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    if (desc->sectors_x == 0 || desc->sectors_y == 0 || desc->sectors_z == 0 ||
+        desc->sectors_x * 32 > VRT_MAX_WORLD_X || desc->sectors_y * 32 > VRT_MAX_WORLD_Y ||
+        desc->sectors_z * 32 > VRT_MAX_WORLD_Z) {
+        set_error("world extent must be 1..64 x 1..32 x 1..64 sectors");
+        return VRT_ERR_INVALID_ARG;
+    }
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        set_error("no CUDA device");
+        return VRT_ERR_NO_DEVICE;
+    }
+    if (desc->device < 0 || desc->device >= ndev) {
+        set_error("device ordinal out of range");
+        return VRT_ERR_INVALID_ARG;
+    }
+    vrt_world* w = new vrt_world;
+    w->device = desc->device;
+    w->sx = desc->sectors_x;
+    w->sy = desc->sectors_y;
+    w->sz = desc->sectors_z;
+    w->flags = desc->flags;
+    w->slots.assign(w->num_sectors(), SectorSlots{});
+    w->h_table.assign(w->num_sectors(), SectorRec{0, 0, 0, 0});
+    w->arena.reset(0);
+    vrt_status st = world_enter(w);
+    if (st == VRT_OK) {
+        e = cudaMalloc(&w->d_sectors, (size_t)w->num_sectors() * sizeof(SectorRec));
+        if (e == cudaSuccess) e = cudaMemset(w->d_sectors, 0, (size_t)w->num_sectors() * sizeof(SectorRec));
+        if (e != cudaSuccess) st = cuda_fail(e, "allocate sector table");
+    }
+    if (st == VRT_OK) st = grow_pool(w, desc->brick_capacity ? desc->brick_capacity : 4096, 0);
+    if (st != VRT_OK) {
+        vrt_world_destroy(w);
+        return st;
+    }
+    *out = w;
+    return VRT_OK;
+}
+
+vrt_status vrt_world_destroy(vrt_world* w) {
+    if (!w) return VRT_OK;
+    cudaSetDevice(w->device);
+    cudaDeviceSynchronize();
+    if (w->d_sectors) cudaFree(w->d_sectors);
+    if (w->d_occ) cudaFree(w->d_occ);
+    if (w->d_payload) cudaFree(w->d_payload);
+    w->d_stage.release();
+    w->d_ops.release();
+    w->d_scratch.release();
+    w->d_io.release();
+    delete w;
+    return VRT_OK;
+}
+
+vrt_status vrt_world_get_stats(const vrt_world* w, vrt_world_stats* out) {
+    if (!w || !out) {
+        set_error("null argument");
+        return VRT_ERR_INVALID_ARG;
+    }
+    out->sectors_x = w->sx;
+    out->sectors_y = w->sy;
+    out->sectors_z = w->sz;
+    out->allocated_bricks = w->arena.allocated();
+    out->brick_capacity = w->capacity;
+    out->free_ranges = (uint32_t)w->arena.num_ranges();
+    out->device_bytes = (uint64_t)w->num_sectors() * sizeof(SectorRec) + (uint64_t)w->capacity * 576 +
+                        w->d_stage.bytes + w->d_ops.bytes + w->d_scratch.bytes + w->d_io.bytes;
+    return VRT_OK;
+}
+
+vrt_status vrt_world_sync_sectors(vrt_world* w, uint32_t n, const int32_t* sector_idx, const uint64_t* alloc_mask,
+                                  const uint64_t* dirty_mask, const uint8_t* bricks, void* stream_) {
+    vrt_status st = world_enter(w);
+    if (st != VRT_OK) return st;
+    if (n && (!sector_idx || !alloc_mask)) {
+        set_error("null sector arrays");
+        return VRT_ERR_INVALID_ARG;
+    }
+    std::lock_guard<std::mutex> lock(w->mu);
+    cudaStream_t stream = (cudaStream_t)stream_;
+    const uint64_t kBatchBricks = 1ull << 19;  // 256 MiB of staged bricks per batch
+    SyncBatch batch;
+    std::unordered_set<uint32_t> seen;
+    uint64_t in_brick = 0;  // index of the next brick in the input stream
+    for (uint32_t i = 0; i < n; i++) {
+        const uint64_t am = alloc_mask[i];
+        const uint64_t dm = dirty_mask ? (dirty_mask[i] & am) : am;
+        const uint64_t cnt = (uint64_t)__builtin_popcountll(dm);
+        if (cnt && !bricks) {
+            set_error("null brick data");
+            return VRT_ERR_INVALID_ARG;
+        }
+        int32_t x, y, z;
+        sector_index_unpack(sector_idx[i], x, y, z);
+        if (w->sector_in(x, y, z)) {
+            const uint32_t s = w->lin(x, y, z);
+            if (seen.count(s) || batch.n_stage + cnt > kBatchBricks) {
+                if ((st = run_batch(w, batch, stream)) != VRT_OK) return st;
+                seen.clear();
+            }
+            if (batch.ops.empty() && batch.touched.empty()) {
+                batch.src = bricks ? bricks + in_brick * 512 : nullptr;
+                batch.n_stage = 0;
+            }
+            // stage index relative to the batch's first input brick
+            const uint64_t first = (bricks ? (in_brick - (uint64_t)(batch.src - bricks) / 512) : 0);
+            if ((st = plan_sector(w, batch, s, am, dm, first, stream)) != VRT_OK) return st;
+            batch.n_stage = first + cnt;
+            seen.insert(s);
+        }
+        in_brick += cnt;
+    }
+    return run_batch(w, batch, stream);
+}
+
+vrt_status vrt_world_read_sector(vrt_world* w, int32_t sector_idx, uint64_t* alloc_mask, uint8_t* bricks,
+                                 size_t bricks_capacity, void* stream_) {
+    vrt_status st = world_enter(w);
+    if (st != VRT_OK) return st;
+    int32_t x, y, z;
+    sector_index_unpack(sector_idx, x, y, z);
+    if (!w->sector_in(x, y, z)) {
+        set_error("sector outside the world");
+        return VRT_ERR_INVALID_ARG;
+    }
+    std::lock_guard<std::mutex> lock(w->mu);
+    const SectorSlots& s = w->slots[w->lin(x, y, z)];
+    if (alloc_mask) *alloc_mask = s.mask;
+    const size_t need = (size_t)__builtin_popcountll(s.mask) * 512;
+    if (!bricks || need == 0) return VRT_OK;
+    if (bricks_capacity < need) {
+        set_error("brick buffer too small");
+        return VRT_ERR_INVALID_ARG;
+    }
+    cudaStream_t stream = (cudaStream_t)stream_;
+    VRT_CUDA(cudaMemcpyAsync(bricks, w->d_payload + (size_t)(s.base - 1) * 512, need, cudaMemcpyDeviceToHost, stream));
+    VRT_CUDA(cudaStreamSynchronize(stream));
+    return VRT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,98 @@
+// world.h - host-side state of one device-resident world (vrt_world).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "freelist.h"
+#include "vrt_internal.h"
+
+namespace vrt {
+
+// thread-local error message behind vrt_last_error()
+void set_error(const std::string& msg);
+const char* last_error_cstr();
+vrt_status cuda_fail(cudaError_t e, const char* what);
+
+#define VRT_CUDA(call)                                             \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return ::vrt::cuda_fail(e_, #call); \
+    } while (0)
+
+// Grow-only device buffer.
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t reserve(size_t n) {
+        if (n <= bytes) return cudaSuccess;
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e != cudaSuccess) return e;
+        if (ptr) cudaFree(ptr);
+        ptr = p;
+        bytes = n;
+        return cudaSuccess;
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+};
+
+}  // namespace vrt
+
+struct vrt_world {
+    int device = 0;
+    uint32_t sx = 0, sy = 0, sz = 0;
+    uint32_t flags = 0;
+    std::mutex mu;
+
+    // host mirror of the allocation state (BrickSlotAllocator, GpuRenderer.cpp:23)
+    std::vector<vrt::SectorSlots> slots;
+    vrt::FreeList arena;
+
+    // device storage
+    vrt::SectorRec* d_sectors = nullptr;
+    uint64_t* d_occ = nullptr;
+    uint8_t* d_payload = nullptr;
+    uint32_t capacity = 0;  // brick slots in the device pools
+
+    // scratch reused across sync/edit calls
+    vrt::DevBuf d_stage;    // uploaded brick bytes
+    vrt::DevBuf d_ops;      // brick operation lists
+    vrt::DevBuf d_scratch;  // bricks in flight during a repack
+    vrt::DevBuf d_io;       // ray/hit staging for host-buffer calls
+    std::vector<vrt::SectorRec> h_table;  // host copy of the sector table
+
+    uint32_t num_sectors() const { return sx * sy * sz; }
+    uint32_t lin(int32_t x, int32_t y, int32_t z) const {
+        return (uint32_t)x + (uint32_t)z * sx + (uint32_t)y * sx * sz;
+    }
+    bool sector_in(int32_t x, int32_t y, int32_t z) const {
+        return (uint32_t)x < sx && (uint32_t)y < sy && (uint32_t)z < sz;
+    }
+    vrt::DevWorld dev() const {
+        vrt::DevWorld w;
+        w.sectors = d_sectors;
+        w.occ = d_occ;
+        w.payload = d_payload;
+        w.sx = sx;
+        w.sz = sz;
+        w.sxz = sx * sz;
+        w.size_x = sx * 32;
+        w.size_y = sy * 32;
+        w.size_z = sz * 32;
+        return w;
+    }
+};
+
+namespace vrt {
+// Make `world` current on the calling thread.
+vrt_status world_enter(vrt_world* world);
+}  // namespace vrt
