@@ -70,25 +70,24 @@ def test_single_voxel_axis_rays(gpu):
     origins, dirs = [], []
     for axis in range(3):
         for s in (-1.0, 1.0):
-            d = [0.0, 0.0, 0.0]
-            d[axis] = s
             p = [37.5, 21.5, 45.5]
             p[axis] -= s * 20.0
-            origins.append(p)
-            dirs.append(d)
-            # -0.0 components and grazing offsets
-            d2 = [(-0.0 if c == 0.0 else c) for c in d]
-            origins.append(p)
-            dirs.append(d2)
+            for eps in (0.0, -0.0, 1e-3, -1e-3):
+                d = [eps, eps, eps]
+                d[axis] = s
+                origins.append(p)
+                dirs.append(d)
             p3 = list(p)
             p3[(axis + 1) % 3] = float(int(p3[(axis + 1) % 3]))  # exactly on a voxel boundary
+            d = [1e-3, 1e-3, 1e-3]
+            d[axis] = s
             origins.append(p3)
             dirs.append(d)
     rays = make_rays(origins, dirs)
     got, want = w.cast(rays), o.cast(rays)
     assert_hits_equal(got, want)
     hit = want["voxel"] != v.MISS_VOXEL
-    assert hit.sum() >= 6
+    assert hit.sum() >= 12
     assert (v.unpack_voxel(want["voxel"][hit]) == [37, 21, 45]).all()
     assert (want["material"][hit] == 7).all()
 
