@@ -1,0 +1,388 @@
+#!/usr/bin/env python3
+"""Benchmark of the brickmap traversal path (one JSON line on stdout).
+
+Default workload: the uneven batch - 128 seeded worlds (edge 64..512 voxels) with
+1-16 views each at 64^2..1280x720, every view's primary rays in ONE persistent
+launch fed by the device tile queue and replayed from a CUDA graph.  The same line
+reports the plain one-launch-per-view kernel on the same views (the comparison the
+metric names), the end-to-end host-buffer call, the HBM roofline of the persistent
+kernel and the CPU oracle timed on a bounded sample.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload uneven_batch|large_world|incoherent|single_view]
+
+Multi-GPU (torchrun, one rank per GPU): every rank traverses its own batch of the
+same shape (weak scaling, no collective on the data path); the time is the max
+over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Grays/s batched vs per-view launch (bit-exact hits); p50/p99 request latency"
+HIT_BYTES = 16
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="uneven_batch",
+                    choices=["uneven_batch", "large_world", "incoherent", "single_view"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="bounded CPU-oracle sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-per-view", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        pg = dist
+    return ws, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x: float) -> float:
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def build_workload(name: str, rank: int):
+    from voxelrt_gb300 import workloads as W
+    if name == "uneven_batch":
+        return W.uneven_batch(seed=2 + 1000 * rank)
+    if name == "large_world":
+        return W.large_world()
+    if name == "incoherent":
+        return W.incoherent()
+    return W.single_view()
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.2)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peak_hbm():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def traffic_from_profile(workload: str):
+    """DRAM bytes per launch of the persistent kernel from a committed ncu summary."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    try:
+        return json.loads(p.read_text()).get(workload)
+    except Exception:
+        return None
+
+
+def cpu_oracle_sample(wl, seconds: float, threads: int = 0):
+    """Time the CPU oracle on whole views of the workload until `seconds` of work."""
+    from oracle.oracle import OracleWorld
+    order = np.argsort([vw.cam.width * vw.cam.height for vw in wl.views], kind="stable")
+    cache = {}
+    rays, elapsed, nviews = 0, 0.0, 0
+    for i in order:
+        vw = wl.views[int(i)]
+        if vw.world not in cache:
+            cache.clear()
+            o = OracleWorld(wl.worlds[vw.world].sectors)
+            o.upload(wl.worlds[vw.world])
+            cache[vw.world] = o
+        o = cache[vw.world]
+        t0 = time.perf_counter()
+        if vw.flags & 1:
+            o.render_view_shadow(vw.cam, np.array(vw.sun_dir[:], np.float32), vw.max_iters, threads)
+        elif vw.n_bounces:
+            o.render_view_bounces(vw.cam, vw.n_bounces, vw.max_iters, threads)
+        else:
+            o.render_view(vw.cam, vw.max_iters, threads)
+        elapsed += time.perf_counter() - t0
+        rays += o.last_stats["rays"]
+        nviews += 1
+        if elapsed >= seconds:
+            break
+    return rays, elapsed, nviews
+
+
+def run_reference(args):
+    """Reference arm: the CPU restatement of the reference traversal on all host cores."""
+    ws, rank, _, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0, None
+    if rank != 0:
+        return
+    from voxelrt_gb300 import build
+    build.build_all()
+    wl = build_workload(args.workload, 0)
+    cores = os.cpu_count() or 1
+    per_step = max(2.0, min(20.0, args.cpu_seconds))
+    for _ in range(args.warmup):
+        cpu_oracle_sample(wl, 0.5)
+    tot_rays, tot_t = 0, 0.0
+    nv = 0
+    for _ in range(args.steps):
+        r, t, nv = cpu_oracle_sample(wl, per_step)
+        tot_rays += r
+        tot_t += t
+    value = tot_rays / tot_t / 1e9
+    sample = (f"{nv} smallest views of the {wl.name} workload per step ({tot_rays // max(args.steps, 1)} rays), "
+              f"scalar C++ restatement of CpuRenderer.cpp RayCast, all {cores} host threads")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Grays/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / max(args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": wl.name, "description": wl.description},
+        "cpu_baseline": {"value": value, "unit": "Grays/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "Grays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    import voxelrt_gb300 as v
+    from voxelrt_gb300 import autotune
+
+    ws, rank, local, pg = dist_setup(args)
+    torch.cuda.set_device(local)
+    dev = local
+    wl = build_workload(args.workload, rank)
+    worlds = []
+    for d in wl.worlds:
+        w = v.World(d.sectors, brick_capacity=d.n_bricks + 64, device=dev)
+        w.upload(d)
+        worlds.append(w)
+    cfg, cfg_src = autotune.lookup(wl.name)
+    batch = v.Batch(worlds, wl.views, cfg)
+    n_rec = batch.total_records
+    stream = torch.cuda.Stream()
+    hits = torch.empty(n_rec * HIT_BYTES, dtype=torch.uint8, device=f"cuda:{dev}")
+
+    # parity sample: a few views of the batch vs the CPU oracle (bit-exact integer fields)
+    parity = None
+    if rank == 0:
+        parity = parity_sample(wl, batch, hits, stream)
+
+    # counting launch (untimed): algorithmic bytes of one launch
+    meas = batch.measure(hits, stream)
+    rays_per_step = meas["rays_cast"]
+    alg_bytes = 8 * meas["step_calls"] + 12 * meas["occ_fetches"] + 1 * meas["hits"] + HIT_BYTES * n_rec
+
+    with torch.cuda.stream(stream):
+        for _ in range(max(3, args.warmup)):
+            batch.launch(hits, stream, graph=True)
+    stream.synchronize()
+    barrier(pg)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        torch.cuda.synchronize()
+        barrier(pg)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            batch.launch(hits, stream, graph=True)
+        ev1.record(stream)
+        ev1.synchronize()
+        torch.cuda.synchronize()
+    barrier(pg)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    ms = max_over_ranks(pg, ms)
+    value = rays_per_step * ws / (ms * 1e-3) / 1e9
+
+    # per-view baseline: one plain launch per view, same views and records
+    per_view = None
+    if not args.no_per_view:
+        with torch.cuda.stream(stream):
+            for _ in range(2):
+                batch.launch_per_view(hits, stream)
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        k = max(1, min(args.steps, 5))
+        e0.record(stream)
+        for _ in range(k):
+            batch.launch_per_view(hits, stream)
+        e1.record(stream)
+        e1.synchronize()
+        pms = max_over_ranks(pg, e0.elapsed_time(e1) / k)
+        per_view = {"value": rays_per_step * ws / (pms * 1e-3) / 1e9, "unit": "Grays/s", "ms_per_step": pms,
+                    "launches_per_step": len(wl.views), "steps": k,
+                    "kernel": "view_path_kernel, 8x8 blocks, thread per pixel"}
+
+    # end to end through the host-buffer API: new cameras in (H2D), all records out (D2H, pinned)
+    host = torch.empty(n_rec * HIT_BYTES, dtype=torch.uint8, pin_memory=True)
+    host_np = host.numpy()
+    cams = [vw.cam for vw in wl.views]
+    batch.update_cameras(cams, stream)
+    batch.run(host_np, stream)
+    ke = max(1, min(args.steps, 5))
+    barrier(pg)
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        batch.update_cameras(cams, stream)
+        batch.run(host_np, stream)
+    e2e_s = max_over_ranks(pg, (time.perf_counter() - t0) / ke)
+    e2e = {"value": rays_per_step * ws / e2e_s / 1e9, "unit": "Grays/s", "ms_per_step": e2e_s * 1e3,
+           "h2d_bytes_per_step": 120 * len(wl.views), "d2h_bytes_per_step": n_rec * HIT_BYTES,
+           "api": "vrt_batch_update_cameras + vrt_batch_run (pinned host records)"}
+
+    peak, peak_src = peak_hbm()
+    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic_from_profile(wl.name), "peak_source": peak_src,
+                "algorithmic_bytes_per_launch": alg_bytes,
+                "bytes_formula": "8*step_calls + 12*occ_fetches + 1*hits + 16*records"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        r, t, nv = cpu_oracle_sample(wl, args.cpu_seconds)
+        cpu = {"value": r / t / 1e9, "unit": "Grays/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{nv} smallest views of the workload, {r} rays, CPU oracle (scalar restatement of "
+                         f"CpuRenderer.cpp RayCast) on all host threads"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Grays/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": wl.name, "description": wl.description, "worlds": len(wl.worlds),
+                       "views": len(wl.views), "rays_per_step": rays_per_step, "records_per_step": n_rec,
+                       "world_bytes": int(sum(d.n_bricks for d in wl.worlds) * 576),
+                       "l2": "inputs larger than L2 (brick pools of all worlds)",
+                       "batch_config": autotune.describe(cfg), "batch_config_source": cfg_src,
+                       "launch": "persistent kernel + queue reset, CUDA graph replay"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
+            "clocks": clk.summary(), "per_view": per_view,
+            "batched_over_per_view": (value / per_view["value"]) if per_view else None,
+            "parity_sample": parity,
+            "traversal": {"step_calls": meas["step_calls"], "occ_fetches": meas["occ_fetches"],
+                          "hits": meas["hits"], "mean_steps_per_ray": meas["step_calls"] / max(rays_per_step, 1)},
+        }
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+def parity_sample(wl, batch, hits, stream, max_views=3):
+    """Compare a few views of one batch launch with the CPU oracle."""
+    import voxelrt_gb300 as v
+    from oracle.oracle import OracleWorld
+    batch.launch(hits, stream)
+    stream.synchronize()
+    order = np.argsort([vw.cam.width * vw.cam.height for vw in wl.views], kind="stable")[:max_views]
+    rays, ok = 0, True
+    for i in order.tolist():
+        vw = wl.views[i]
+        o = OracleWorld(wl.worlds[vw.world].sectors)
+        o.upload(wl.worlds[vw.world])
+        if vw.flags & 1:
+            want = np.stack(o.render_view_shadow(vw.cam, np.array(vw.sun_dir[:], np.float32), vw.max_iters))
+        elif vw.n_bounces:
+            want = o.render_view_bounces(vw.cam, vw.n_bounces, vw.max_iters)
+        else:
+            want = o.render_view(vw.cam, vw.max_iters)[None]
+        a, b = int(batch.offsets[i]), int(batch.offsets[i + 1])
+        got = hits[a * HIT_BYTES:b * HIT_BYTES].cpu().numpy().view(v.HIT_DTYPE).reshape(want.shape)
+        for f in ("voxel", "face", "material", "steps", "tag"):
+            ok &= bool(np.array_equal(got[f], want[f]))
+        fin = np.isfinite(want["t"])
+        ok &= bool(np.array_equal(np.isfinite(got["t"]), fin))
+        ok &= bool(np.allclose(got["t"][fin], want["t"][fin], rtol=1e-6, atol=0))
+        rays += want.size
+        o.close()
+    return {"views": len(order), "records": rays, "bit_exact": ok}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -206,6 +206,79 @@ vrt_status vrt_render_view_device(vrt_world* world, const vrt_camera* cam, uint3
 vrt_status vrt_camera_look_at(const double pos[3], const double target[3], double vfov_deg,
                               uint32_t width, uint32_t height, vrt_camera* out);
 
+/* ---- views: primary rays plus secondary rays per pixel ---- */
+/* A view is one RenderFrame of the reference's renderers: a primary ray per pixel
+ * (VoxelRender.comp:27-30, CpuRenderer.cpp:326-333), then optionally
+ *   - one shadow ray from hitPos + normal*0.01 toward sun_dir for every hit
+ *     (VoxelRender.comp:51-61, origin offset as CpuRenderer.cpp:389), or
+ *   - up to n_bounces diffuse bounces (CpuRenderer.cpp:342-393): origin
+ *     hitPos + normal*0.01, direction normalize(normal + s), s uniform on the unit
+ *     sphere by rejection from [-1,1]^3 with PCG32(initstate = pixel ^ bounce,
+ *     initseq = 0x9E3779B97F4A7C15); a path ends at its first miss.
+ * Records are laid out per view as [primary w*h][shadow w*h] or
+ * [primary w*h][bounce 1 w*h]...[bounce n w*h]; rays never cast (shadow of a miss,
+ * bounces after a miss) get a miss record with steps 0 and tag VRT_NO_RAY. */
+typedef struct vrt_view {
+    vrt_camera cam;
+    uint32_t world;     /* index into the batch's world list */
+    uint32_t max_iters; /* 0 = VRT_DEFAULT_MAX_ITERS */
+    uint32_t n_bounces; /* 0..15, exclusive with VRT_VIEW_SHADOW */
+    uint32_t flags;     /* VRT_VIEW_SHADOW */
+    float sun_dir[3];
+} vrt_view;
+
+#define VRT_VIEW_SHADOW 1u
+#define VRT_MAX_BOUNCES 15u
+
+/* One view with its secondary rays, one plain launch (thread per pixel, no
+ * compaction).  `world` in the view is ignored.  Host / device record buffers
+ * of vrt_view_records(view) entries. */
+uint64_t vrt_view_records(const vrt_view* view);
+vrt_status vrt_render_path(vrt_world* world, const vrt_view* view, vrt_hit* hits, void* stream);
+vrt_status vrt_render_path_device(vrt_world* world, const vrt_view* view, vrt_hit* hits, void* stream);
+
+/* ---- batched persistent traversal over many worlds and views ---- */
+typedef struct vrt_batch_config {
+    uint32_t tile_w, tile_h;   /* ray tile: 8x8, 16x4 or 32x1 (0,0 = 8x8) */
+    uint32_t morton;           /* 1: Z-order inside 8x8 tiles */
+    uint32_t warps_per_block;  /* 1..16 (0 = 4) */
+    uint32_t blocks_per_sm;    /* 0 = as many as fit */
+    uint32_t refill_threshold; /* refill idle lanes when fewer lanes are active (1..32, 0 = 16) */
+    uint32_t chunk_tiles;      /* tiles taken from the device queue per atomic (0 = 2) */
+    uint32_t inner_iters;      /* DDA iterations between refill checks (0 = 4) */
+} vrt_batch_config;
+
+typedef struct vrt_batch_stats {
+    uint64_t rays_cast;   /* primary + secondary rays traversed by the last launch */
+    uint64_t step_calls;  /* GetStepPos calls (vrt_batch_measure only) */
+    uint64_t occ_fetches; /* calls that fetched a voxel-cell mask (vrt_batch_measure only) */
+    uint64_t hits;        /* rays that hit (vrt_batch_measure only) */
+} vrt_batch_stats;
+
+typedef struct vrt_batch vrt_batch;
+
+/* Worlds must outlive the batch; they may be re-synced between launches. */
+vrt_status vrt_batch_create(vrt_world* const* worlds, uint32_t n_worlds, const vrt_view* views, uint32_t n_views,
+                            const vrt_batch_config* cfg, vrt_batch** out);
+vrt_status vrt_batch_destroy(vrt_batch* batch);
+/* offsets[v] = first record of view v; offsets[n_views] = total records. */
+vrt_status vrt_batch_output_layout(const vrt_batch* batch, uint64_t* offsets);
+/* Persistent kernel over the device tile queue (queue reset included). */
+vrt_status vrt_batch_launch(vrt_batch* batch, vrt_hit* hits_device, void* stream);
+/* Same launch captured once into a CUDA graph and replayed. */
+vrt_status vrt_batch_launch_graph(vrt_batch* batch, vrt_hit* hits_device, void* stream);
+/* Baseline: one plain vrt_render_path launch per view. */
+vrt_status vrt_batch_launch_per_view(vrt_batch* batch, vrt_hit* hits_device, void* stream);
+/* New cameras for every view (same resolutions), copied to the device. */
+vrt_status vrt_batch_update_cameras(vrt_batch* batch, const vrt_camera* cams, void* stream);
+/* Host-buffer form: graph launch into a batch-owned device buffer, then the records
+ * are copied to hits_host (pinned memory makes the copy asynchronous-fast). */
+vrt_status vrt_batch_run(vrt_batch* batch, vrt_hit* hits_host, void* stream);
+/* Counters of the last launch (synchronises the stream of that launch). */
+vrt_status vrt_batch_get_stats(vrt_batch* batch, vrt_batch_stats* out);
+/* One launch of the counting variant: fills step_calls/occ_fetches/hits. */
+vrt_status vrt_batch_measure(vrt_batch* batch, vrt_hit* hits_device, void* stream, vrt_batch_stats* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,154 @@
+"""Paths (shadow rays, diffuse bounces) and the batched persistent kernel vs the oracle.
+
+Every record of every view is compared bit-exactly (t within 1e-6 relative) with
+the CPU oracle, for the plain per-view launch, the persistent launch under each
+tile shape / refill setting, and the CUDA-graph replay.
+"""
+import numpy as np
+import pytest
+
+import voxelrt_gb300 as v
+from oracle.oracle import OracleWorld
+from tests.helpers import assert_hits_equal, both_worlds, cfg0_camera, cfg0_world
+
+pytestmark = pytest.mark.gpu
+
+SUN = np.array([0.3, 0.8, 0.5]) / np.linalg.norm([0.3, 0.8, 0.5])
+
+
+def torch_or_skip():
+    return pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def cfg0(gpu):
+    data = cfg0_world()
+    w, o = both_worlds(data)
+    yield data, w, o
+    w.close()
+
+
+def test_shadow_path_matches_oracle(cfg0):
+    _, w, o = cfg0
+    cam = cfg0_camera(320, 180)
+    view = v.make_view(cam, shadow_dir=SUN.astype(np.float32))
+    got = v.render_path(w, view)
+    prim, shad = o.render_view_shadow(cam, SUN.astype(np.float32))
+    assert_hits_equal(got[0], prim)
+    assert_hits_equal(got[1], shad)
+    assert (shad["tag"] != v.NO_RAY).sum() == (prim["voxel"] != v.MISS_VOXEL).sum()
+
+
+@pytest.mark.parametrize("n_bounces", [1, 4])
+def test_bounce_path_matches_oracle(cfg0, n_bounces):
+    _, w, o = cfg0
+    cam = cfg0_camera(200, 120)
+    view = v.make_view(cam, n_bounces=n_bounces)
+    got = v.render_path(w, view)
+    want = o.render_view_bounces(cam, n_bounces)
+    for k in range(n_bounces + 1):
+        assert_hits_equal(got[k], want[k])
+    assert (want[n_bounces]["tag"] != v.NO_RAY).any()
+
+
+def mix_batch_setup(n_worlds=5, seed=0):
+    rng = np.random.default_rng(seed)
+    datas, worlds, oracles, views = [], [], [], []
+    for i in range(n_worlds):
+        edge = int(rng.choice([64, 96, 128]))
+        d = v.synth_mix(edge, seed=100 + i)
+        datas.append(d)
+        w, o = both_worlds(d)
+        worlds.append(w)
+        oracles.append(o)
+        for _ in range(int(rng.integers(1, 4))):
+            res = [(64, 64), (70, 37), (96, 54), (33, 65)][int(rng.integers(0, 4))]
+            pos = rng.uniform(0, edge, 3)
+            tgt = rng.uniform(0, edge, 3)
+            cam = v.look_at(pos, tgt, float(rng.uniform(50, 90)), *res)
+            kind = int(rng.integers(0, 3))
+            if kind == 0:
+                views.append(v.make_view(cam, world=i))
+            elif kind == 1:
+                views.append(v.make_view(cam, world=i, shadow_dir=SUN))
+            else:
+                views.append(v.make_view(cam, world=i, n_bounces=2, max_iters=64))
+    return worlds, oracles, views
+
+
+def oracle_view(o: OracleWorld, view) -> np.ndarray:
+    if view.flags & v.VIEW_SHADOW:
+        p, s = o.render_view_shadow(view.cam, np.array(view.sun_dir[:], np.float32), view.max_iters)
+        return np.stack([p, s])
+    if view.n_bounces:
+        return o.render_view_bounces(view.cam, view.n_bounces, view.max_iters)
+    return o.render_view(view.cam, view.max_iters)[None]
+
+
+@pytest.fixture(scope="module")
+def mix(gpu):
+    worlds, oracles, views = mix_batch_setup()
+    want = [oracle_view(oracles[vw.world], vw) for vw in views]
+    yield worlds, views, want
+    for w in worlds:
+        w.close()
+
+
+CONFIGS = [
+    dict(),
+    dict(tile_w=8, tile_h=8, morton=1, refill_threshold=32, inner_iters=1),
+    dict(tile_w=16, tile_h=4, refill_threshold=1, inner_iters=8, chunk_tiles=1),
+    dict(tile_w=32, tile_h=1, warps_per_block=8, refill_threshold=24, chunk_tiles=5, blocks_per_sm=1),
+]
+
+
+@pytest.mark.parametrize("cfg", CONFIGS)
+def test_batch_matches_oracle(mix, cfg):
+    worlds, views, want = mix
+    bc = v.BatchConfig(**{k: cfg.get(k, 0) for k in ("tile_w", "tile_h", "morton", "warps_per_block",
+                                                       "blocks_per_sm", "refill_threshold", "chunk_tiles",
+                                                       "inner_iters")})
+    b = v.Batch(worlds, views, bc)
+    hits = b.run()
+    for i in range(len(views)):
+        got = b.view_hits(hits, i)
+        assert got.shape == want[i].shape
+        for k in range(got.shape[0]):
+            assert_hits_equal(got[k], want[i][k])
+    cast = sum(int((w["tag"] != v.NO_RAY).sum()) for w in want)
+    assert b.stats()["rays_cast"] == cast
+    b.close()
+
+
+def test_batch_launch_modes_agree(mix):
+    torch = torch_or_skip()
+    worlds, views, want = mix
+    b = v.Batch(worlds, views)
+    n = b.total_records
+    outs = []
+    for mode in ("launch", "graph", "graph", "per_view"):
+        t = torch.zeros(n * 16, dtype=torch.uint8, device="cuda")
+        if mode == "per_view":
+            b.launch_per_view(t)
+        else:
+            b.launch(t, graph=(mode == "graph"))
+        torch.cuda.synchronize()
+        outs.append(t.cpu().numpy().view(v.HIT_DTYPE))
+    for o in outs[1:]:
+        assert np.array_equal(o.view(np.uint8), outs[0].view(np.uint8))
+    st = b.measure(torch.zeros(n * 16, dtype=torch.uint8, device="cuda"))
+    assert st["rays_cast"] == b.stats()["rays_cast"]
+    assert st["step_calls"] > 0 and st["hits"] <= st["rays_cast"]
+    b.close()
+
+
+def test_batch_rejects_bad_input(mix):
+    worlds, views, _ = mix
+    bad = v.make_view(cfg0_camera(8, 8), world=len(worlds))
+    with pytest.raises(v.VrtError):
+        v.Batch(worlds, [bad])
+    with pytest.raises(v.VrtError):
+        v.Batch(worlds, views, v.BatchConfig(tile_w=4, tile_h=4))
+    both = v.make_view(cfg0_camera(8, 8), n_bounces=1, shadow_dir=SUN)
+    with pytest.raises(v.VrtError):
+        v.Batch(worlds, [both])

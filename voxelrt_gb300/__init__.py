@@ -17,10 +17,10 @@ import ctypes as C
 import numpy as np
 
 from . import capi
-from .capi import (EDIT_DTYPE, HIT_DTYPE, MISS_FACE, MISS_VOXEL, NO_RAY, RAY_DTYPE, Camera, CastParams, VrtError,
-                   check, lib, ptr)
+from .capi import (EDIT_DTYPE, HIT_DTYPE, MISS_FACE, MISS_VOXEL, NO_RAY, RAY_DTYPE, VIEW_SHADOW, BatchConfig, Camera,
+                   CastParams, View, VrtError, check, lib, ptr)
 
-__all__ = ["World", "Camera", "look_at", "synth_terrain", "synth_mix", "random_rays", "SectorData", "VrtError",
+__all__ = ["World", "Camera", "View", "make_view", "Batch", "BatchConfig", "VIEW_SHADOW", "look_at", "synth_terrain", "synth_mix", "random_rays", "SectorData", "VrtError",
            "RAY_DTYPE", "HIT_DTYPE", "EDIT_DTYPE", "MISS_VOXEL", "MISS_FACE", "NO_RAY", "unpack_voxel", "sector_index",
            "lib"]
 
@@ -205,3 +205,90 @@ class World:
 
     def render_view_device(self, cam: Camera, hits, max_iters: int = 0, stream=None) -> None:
         check(lib().vrt_render_view_device(self._h, C.byref(cam), int(max_iters), ptr(hits), _stream_ptr(stream)))
+
+
+def make_view(cam: Camera, world: int = 0, max_iters: int = 0, n_bounces: int = 0, shadow_dir=None) -> View:
+    """A view: primary rays plus shadow rays toward shadow_dir, or n_bounces diffuse bounces."""
+    vw = View()
+    vw.cam = cam
+    vw.world = int(world)
+    vw.max_iters = int(max_iters)
+    vw.n_bounces = int(n_bounces)
+    vw.flags = VIEW_SHADOW if shadow_dir is not None else 0
+    if shadow_dir is not None:
+        vw.sun_dir[:] = [float(c) for c in shadow_dir]
+    return vw
+
+
+def view_records(view: View) -> int:
+    return lib().vrt_view_records(C.byref(view))
+
+
+def render_path(world: "World", view: View, stream=None) -> np.ndarray:
+    """One view with its secondary rays, one plain launch; (kinds, h*w) records."""
+    n = view_records(view)
+    hits = np.zeros(n, HIT_DTYPE)
+    check(lib().vrt_render_path(world.handle, C.byref(view), ptr(hits), _stream_ptr(stream)))
+    return hits.reshape(-1, view.cam.width * view.cam.height)
+
+
+class Batch:
+    """Many views over many worlds behind one persistent launch (vrt_batch)."""
+
+    def __init__(self, worlds, views, config: BatchConfig | None = None):
+        self.worlds = list(worlds)
+        self.views = list(views)
+        wh = (C.c_void_p * len(self.worlds))(*[w.handle.value for w in self.worlds])
+        va = (View * len(self.views))(*self.views)
+        h = C.c_void_p()
+        check(lib().vrt_batch_create(wh, len(self.worlds), va, len(self.views),
+                                     C.byref(config) if config is not None else None, C.byref(h)))
+        self._h = h
+        offs = (C.c_uint64 * (len(self.views) + 1))()
+        check(lib().vrt_batch_output_layout(h, offs))
+        self.offsets = np.array(offs[:], np.uint64)
+        self.total_records = int(self.offsets[-1])
+
+    def close(self):
+        if self._h:
+            lib().vrt_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def launch(self, hits_device, stream=None, graph: bool = False) -> None:
+        fn = lib().vrt_batch_launch_graph if graph else lib().vrt_batch_launch
+        check(fn(self._h, ptr(hits_device), _stream_ptr(stream)))
+
+    def launch_per_view(self, hits_device, stream=None) -> None:
+        check(lib().vrt_batch_launch_per_view(self._h, ptr(hits_device), _stream_ptr(stream)))
+
+    def run(self, hits_host=None, stream=None) -> np.ndarray:
+        """Launch and copy all records to host memory (hits_host: numpy array or pinned tensor)."""
+        if hits_host is None:
+            hits_host = np.zeros(self.total_records, HIT_DTYPE)
+        check(lib().vrt_batch_run(self._h, ptr(hits_host), _stream_ptr(stream)))
+        return hits_host
+
+    def update_cameras(self, cams, stream=None) -> None:
+        arr = (Camera * len(cams))(*cams)
+        check(lib().vrt_batch_update_cameras(self._h, arr, _stream_ptr(stream)))
+
+    def stats(self) -> dict:
+        s = capi.BatchStats()
+        check(lib().vrt_batch_get_stats(self._h, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
+    def measure(self, hits_device, stream=None) -> dict:
+        s = capi.BatchStats()
+        check(lib().vrt_batch_measure(self._h, ptr(hits_device), _stream_ptr(stream), C.byref(s)))
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
+    def view_hits(self, hits: np.ndarray, v: int) -> np.ndarray:
+        a, b = int(self.offsets[v]), int(self.offsets[v + 1])
+        cam = self.views[v].cam
+        return hits[a:b].reshape(-1, cam.width * cam.height)

@@ -54,6 +54,25 @@ class Edit(C.Structure):
                 ("reserved", C.c_uint16)]
 
 
+class View(C.Structure):
+    _fields_ = [("cam", Camera), ("world", C.c_uint32), ("max_iters", C.c_uint32), ("n_bounces", C.c_uint32),
+                ("flags", C.c_uint32), ("sun_dir", C.c_float * 3)]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [("tile_w", C.c_uint32), ("tile_h", C.c_uint32), ("morton", C.c_uint32),
+                ("warps_per_block", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("refill_threshold", C.c_uint32),
+                ("chunk_tiles", C.c_uint32), ("inner_iters", C.c_uint32)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("rays_cast", C.c_uint64), ("step_calls", C.c_uint64), ("occ_fetches", C.c_uint64),
+                ("hits", C.c_uint64)]
+
+
+VIEW_SHADOW = 1
+
+
 class WorldDesc(C.Structure):
     _fields_ = [("sectors_x", C.c_uint32), ("sectors_y", C.c_uint32), ("sectors_z", C.c_uint32),
                 ("brick_capacity", C.c_uint32), ("device", C.c_int32), ("flags", C.c_uint32)]
@@ -108,6 +127,19 @@ PROTOTYPES = {
     "vrt_render_view_device": (_st, [_vp, C.POINTER(Camera), _u32, _vp, _vp]),
     "vrt_camera_look_at": (_st, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_double, _u32, _u32,
                                  C.POINTER(Camera)]),
+    "vrt_view_records": (_u64, [C.POINTER(View)]),
+    "vrt_render_path": (_st, [_vp, C.POINTER(View), _vp, _vp]),
+    "vrt_render_path_device": (_st, [_vp, C.POINTER(View), _vp, _vp]),
+    "vrt_batch_create": (_st, [C.POINTER(_vp), _u32, C.POINTER(View), _u32, C.POINTER(BatchConfig), C.POINTER(_vp)]),
+    "vrt_batch_destroy": (_st, [_vp]),
+    "vrt_batch_output_layout": (_st, [_vp, C.POINTER(_u64)]),
+    "vrt_batch_launch": (_st, [_vp, _vp, _vp]),
+    "vrt_batch_launch_graph": (_st, [_vp, _vp, _vp]),
+    "vrt_batch_launch_per_view": (_st, [_vp, _vp, _vp]),
+    "vrt_batch_run": (_st, [_vp, _vp, _vp]),
+    "vrt_batch_update_cameras": (_st, [_vp, C.POINTER(Camera), _vp]),
+    "vrt_batch_get_stats": (_st, [_vp, C.POINTER(BatchStats)]),
+    "vrt_batch_measure": (_st, [_vp, _vp, _vp, C.POINTER(BatchStats)]),
     "vrt_synth_terrain_world": (_st, [C.POINTER(SynthTerrain), C.c_int, C.POINTER(C.POINTER(SectorStream))]),
     "vrt_synth_terrain_height": (C.c_double, [C.POINTER(SynthTerrain), C.c_double, C.c_double]),
     "vrt_synth_mix_world": (_st, [_u32, _u64, C.c_int, C.POINTER(C.POINTER(SectorStream))]),

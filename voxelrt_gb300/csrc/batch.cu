@@ -1,0 +1,635 @@
+// batch.cu - view paths (primary + shadow / diffuse bounces) and the batched
+// persistent traversal over many worlds and views.
+//
+// The reference dispatches one VoxelRender.comp per frame (GpuRenderer.cpp:267-268)
+// with one invocation per pixel tracing its whole path (VoxelRender.comp:27-93).
+// vrt_render_path keeps that structure (the per-view baseline).  vrt_batch_* puts
+// the views of many worlds behind one device queue of ray tiles: persistent warps
+// take chunks of tiles with one atomic, hand rays to idle lanes (regeneration),
+// refill when fewer than `refill_threshold` lanes are still tracing (compaction),
+// and a lane that finishes a ray continues its pixel's path in place.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "trace_core.cuh"
+#include "world.h"
+
+namespace vrt {
+namespace {
+
+struct ViewDev {
+    vrt_camera cam;
+    uint32_t world;
+    uint32_t max_iters;
+    uint32_t n_bounces;
+    uint32_t shadow;
+    float sun[3];
+    uint32_t tiles_x;
+    uint32_t n_rays;      // tile-padded ray space of the view
+    uint32_t chunk_base;  // first queue chunk of the view
+    uint64_t out_base;    // first record of the view
+};
+
+static_assert(sizeof(ViewDev) == 120, "view table entry is 120 bytes (copied per camera update)");
+
+struct BatchParams {
+    const DevWorld* worlds;
+    const ViewDev* views;
+    const uint32_t* chunk_base;  // n_views + 1 entries
+    uint32_t n_views;
+    uint32_t total_chunks;
+    uint32_t* queue;
+    unsigned long long* counters;  // rays, step calls, occ fetches, hits
+    uint4* out;
+    uint32_t tile_w_log2, tile_size_log2, morton;
+    uint32_t chunk_rays;
+    uint32_t refill;
+    uint32_t inner;
+};
+
+uint32_t eff_iters(uint32_t m) { return m == 0 ? VRT_DEFAULT_MAX_ITERS : (m > 65535u ? 65535u : m); }
+
+__device__ __forceinline__ uint32_t compact_even_bits(uint32_t k) {
+    k &= 0x55u;
+    k = (k | (k >> 1)) & 0x33u;
+    k = (k | (k >> 2)) & 0x0Fu;
+    return k;
+}
+
+template <bool kCount>
+__device__ __forceinline__ bool run_ray(RayState& s, const DevWorld& w, int32_t wox, int32_t woy, int32_t woz,
+                                        uint32_t max_iters, uint32_t& steps, TraceCounters& cnt) {
+    uint32_t st = kStepOut, i = 0;
+    for (; i < max_iters; i++) {
+        st = ray_step<kCount>(s, w, wox, woy, woz, cnt);
+        if (st != kStepContinue) break;
+    }
+    steps = i;
+    return st == kStepHit && i < max_iters;
+}
+
+// One thread per pixel, whole path (VoxelRender.comp:27-93 structure).
+__global__ void __launch_bounds__(64) view_path_kernel(DevWorld w, ViewDev v, uint4* __restrict__ out) {
+    const uint32_t px = blockIdx.x * 8 + threadIdx.x;
+    const uint32_t py = blockIdx.y * 8 + threadIdx.y;
+    if (px >= v.cam.width || py >= v.cam.height) return;
+    const uint32_t pixel = py * v.cam.width + px;
+    const uint64_t plane = (uint64_t)v.cam.width * v.cam.height;
+    const int32_t wox = v.cam.world_origin[0], woy = v.cam.world_origin[1], woz = v.cam.world_origin[2];
+    TraceCounters cnt{0, 0};
+    float ox = v.cam.origin[0], oy = v.cam.origin[1], oz = v.cam.origin[2], dx, dy, dz;
+    camera_ray(v.cam, px, py, dx, dy, dz);
+    RayState s;
+    ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
+    uint32_t steps;
+    bool hit = run_ray<false>(s, w, wox, woy, woz, v.max_iters, steps, cnt);
+    uint4* o = out + v.out_base + pixel;
+    o[0] = pack_state(s, hit, steps, pixel);
+    const uint32_t last = v.shadow ? 1u : v.n_bounces;
+    for (uint32_t k = 1; k <= last; k++) {
+        if (!hit) {
+            o[k * plane] = no_ray_hit();
+            continue;
+        }
+        next_path_ray(s, v.shadow != 0, v.sun, pixel, k, ox, oy, oz, dx, dy, dz);
+        ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
+        hit = run_ray<false>(s, w, wox, woy, woz, v.max_iters, steps, cnt);
+        o[k * plane] = pack_state(s, hit, steps, pixel);
+    }
+}
+
+template <bool kCount>
+__global__ void persistent_kernel(BatchParams p) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lt = (1u << lane) - 1u;
+    // warp-uniform queue state: rays [q_next, q_end) of view q_view
+    uint32_t q_view = 0, q_next = 0, q_end = 0;
+    bool q_empty = false;
+    // lane state
+    bool active = false;
+    uint32_t pixel = 0, kind = 0, iter = 0, max_iters = 0, last_kind = 0, plane = 0, shadow = 0;
+    uint4* rec = nullptr;
+    DevWorld w{};
+    int32_t wox = 0, woy = 0, woz = 0;
+    const ViewDev* V = nullptr;
+    RayState s;
+    uint32_t rays = 0, hits = 0;
+    TraceCounters cnt{0, 0};
+
+    for (;;) {
+        const uint32_t act = __ballot_sync(0xffffffffu, active);
+        if ((uint32_t)__popc(act) < p.refill && !q_empty) {
+            uint32_t idle = ~act;
+            while (idle) {
+                if (q_next >= q_end) {
+                    uint32_t c = 0;
+                    if (lane == 0) c = atomicAdd(p.queue, 1u);
+                    c = __shfl_sync(0xffffffffu, c, 0);
+                    if (c >= p.total_chunks) {
+                        q_empty = true;
+                        break;
+                    }
+                    uint32_t lo = 0, hi = p.n_views;
+                    while (hi - lo > 1) {
+                        const uint32_t mid = (lo + hi) >> 1;
+                        if (__ldg(p.chunk_base + mid) <= c)
+                            lo = mid;
+                        else
+                            hi = mid;
+                    }
+                    q_view = lo;
+                    q_next = (c - __ldg(p.chunk_base + lo)) * p.chunk_rays;
+                    q_end = min(q_next + p.chunk_rays, __ldg(&p.views[lo].n_rays));
+                    continue;
+                }
+                const uint32_t take = min(q_end - q_next, (uint32_t)__popc(idle));
+                const uint32_t rank = __popc(idle & lt);
+                const bool mine = ((idle >> lane) & 1u) && rank < take;
+                const uint32_t assigned = __ballot_sync(0xffffffffu, mine);
+                if (mine) {
+                    const ViewDev* v = p.views + q_view;
+                    const uint32_t r = q_next + rank;
+                    const uint32_t t = r >> p.tile_size_log2, k = r & ((1u << p.tile_size_log2) - 1u);
+                    const uint32_t tiles_x = __ldg(&v->tiles_x);
+                    uint32_t kx, ky;
+                    if (p.morton) {
+                        kx = compact_even_bits(k);
+                        ky = compact_even_bits(k >> 1);
+                    } else {
+                        kx = k & ((1u << p.tile_w_log2) - 1u);
+                        ky = k >> p.tile_w_log2;
+                    }
+                    const uint32_t tw = 1u << p.tile_w_log2, th = 1u << (p.tile_size_log2 - p.tile_w_log2);
+                    const uint32_t px = (t % tiles_x) * tw + kx, py = (t / tiles_x) * th + ky;
+                    const uint32_t width = __ldg(&v->cam.width), height = __ldg(&v->cam.height);
+                    if (px < width && py < height) {
+                        V = v;
+                        pixel = py * width + px;
+                        plane = width * height;
+                        kind = 0;
+                        iter = 0;
+                        max_iters = __ldg(&v->max_iters);
+                        shadow = __ldg(&v->shadow);
+                        last_kind = shadow ? 1u : __ldg(&v->n_bounces);
+                        rec = p.out + __ldg(&v->out_base) + pixel;
+                        w = p.worlds[__ldg(&v->world)];
+                        wox = __ldg(&v->cam.world_origin[0]);
+                        woy = __ldg(&v->cam.world_origin[1]);
+                        woz = __ldg(&v->cam.world_origin[2]);
+                        float dx, dy, dz;
+                        camera_ray(v->cam, px, py, dx, dy, dz);
+                        ray_init(s, w, __ldg(&v->cam.origin[0]), __ldg(&v->cam.origin[1]), __ldg(&v->cam.origin[2]),
+                                 dx, dy, dz, wox, woy, woz);
+                        active = true;
+                    }
+                }
+                idle &= ~assigned;
+                q_next += take;
+            }
+        }
+        if (__ballot_sync(0xffffffffu, active) == 0 && q_empty) break;
+        if (active) {
+            for (uint32_t k = 0; k < p.inner; k++) {
+                const uint32_t st = ray_step<kCount>(s, w, wox, woy, woz, cnt);
+                if (st == kStepContinue && ++iter < max_iters) continue;
+                const bool hit = st == kStepHit;
+                rec[(size_t)kind * plane] = pack_state(s, hit, iter, pixel);
+                rays++;
+                if (kCount && hit) hits++;
+                if (hit && kind < last_kind) {
+                    kind++;
+                    float ox, oy, oz, dx, dy, dz;
+                    next_path_ray(s, shadow != 0, V->sun, pixel, kind, ox, oy, oz, dx, dy, dz);
+                    ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
+                    iter = 0;
+                    continue;
+                }
+                for (uint32_t kk = kind + 1; kk <= last_kind; kk++) rec[(size_t)kk * plane] = no_ray_hit();
+                active = false;
+                break;
+            }
+        }
+    }
+    // warp totals, one atomic per warp
+    for (int off = 16; off > 0; off >>= 1) {
+        rays += __shfl_xor_sync(0xffffffffu, rays, off);
+        if (kCount) {
+            hits += __shfl_xor_sync(0xffffffffu, hits, off);
+            cnt.step_calls += __shfl_xor_sync(0xffffffffu, cnt.step_calls, off);
+            cnt.occ_fetches += __shfl_xor_sync(0xffffffffu, cnt.occ_fetches, off);
+        }
+    }
+    if (lane == 0) {
+        atomicAdd(p.counters + 0, (unsigned long long)rays);
+        if (kCount) {
+            atomicAdd(p.counters + 1, (unsigned long long)cnt.step_calls);
+            atomicAdd(p.counters + 2, (unsigned long long)cnt.occ_fetches);
+            atomicAdd(p.counters + 3, (unsigned long long)hits);
+        }
+    }
+}
+
+uint32_t log2u(uint32_t v) {
+    uint32_t r = 0;
+    while ((1u << r) < v) r++;
+    return r;
+}
+
+vrt_status check_view(const vrt_view* v) {
+    if (!v || v->cam.width == 0 || v->cam.height == 0 || v->cam.width > 16384 || v->cam.height > 16384 ||
+        v->n_bounces > VRT_MAX_BOUNCES || (v->flags & ~VRT_VIEW_SHADOW) ||
+        ((v->flags & VRT_VIEW_SHADOW) && v->n_bounces)) {
+        set_error("bad view: camera 1..16384 px, n_bounces <= 15, shadow and bounces exclusive");
+        return VRT_ERR_INVALID_ARG;
+    }
+    return VRT_OK;
+}
+
+uint64_t view_records(const vrt_view& v) {
+    const uint64_t kinds = 1 + ((v.flags & VRT_VIEW_SHADOW) ? 1 : v.n_bounces);
+    return kinds * v.cam.width * v.cam.height;
+}
+
+ViewDev make_view_dev(const vrt_view& v) {
+    ViewDev d{};
+    d.cam = v.cam;
+    d.world = v.world;
+    d.max_iters = eff_iters(v.max_iters);
+    d.n_bounces = (v.flags & VRT_VIEW_SHADOW) ? 0 : v.n_bounces;
+    d.shadow = (v.flags & VRT_VIEW_SHADOW) ? 1 : 0;
+    for (int c = 0; c < 3; c++) d.sun[c] = v.sun_dir[c];
+    return d;
+}
+
+vrt_status launch_view_path(vrt_world* w, const ViewDev& v, vrt_hit* hits, cudaStream_t stream) {
+    dim3 block(8, 8), grid((v.cam.width + 7) / 8, (v.cam.height + 7) / 8);
+    view_path_kernel<<<grid, block, 0, stream>>>(w->dev(), v, reinterpret_cast<uint4*>(hits));
+    VRT_CUDA(cudaGetLastError());
+    return VRT_OK;
+}
+
+}  // namespace
+}  // namespace vrt
+
+using namespace vrt;
+
+struct vrt_batch {
+    int device = 0;
+    std::vector<vrt_world*> worlds;
+    std::vector<vrt_view> views;
+    std::vector<ViewDev> vdev;
+    std::vector<uint32_t> chunk_base;
+    std::vector<DevWorld> wtab;  // last uploaded world table
+    uint64_t total_records = 0;
+    uint32_t total_chunks = 0;
+    vrt_batch_config cfg{};
+    uint32_t tile_w_log2 = 3, tile_size_log2 = 6;
+    int blocks = 0, threads = 0, blocks_count = 0;
+    // device
+    DevWorld* d_worlds = nullptr;
+    ViewDev* d_views = nullptr;
+    uint32_t* d_chunk_base = nullptr;
+    uint32_t* d_queue = nullptr;  // queue counter followed by 4 u64 counters (16-byte aligned)
+    unsigned long long* d_counters = nullptr;
+    cudaStream_t last_stream = nullptr;
+    DevBuf d_out;  // record buffer of vrt_batch_run
+    // graph
+    cudaGraphExec_t graph_exec = nullptr;
+    vrt_hit* graph_hits = nullptr;
+};
+
+namespace {
+
+vrt_status refresh_worlds(vrt_batch* b, cudaStream_t stream) {
+    std::vector<DevWorld> t(b->worlds.size());
+    for (size_t i = 0; i < t.size(); i++) t[i] = b->worlds[i]->dev();
+    if (t.size() == b->wtab.size() && std::memcmp(t.data(), b->wtab.data(), t.size() * sizeof(DevWorld)) == 0)
+        return VRT_OK;
+    VRT_CUDA(cudaMemcpyAsync(b->d_worlds, t.data(), t.size() * sizeof(DevWorld), cudaMemcpyHostToDevice, stream));
+    VRT_CUDA(cudaStreamSynchronize(stream));
+    b->wtab = t;
+    return VRT_OK;
+}
+
+BatchParams batch_params(vrt_batch* b, vrt_hit* hits) {
+    BatchParams p{};
+    p.worlds = b->d_worlds;
+    p.views = b->d_views;
+    p.chunk_base = b->d_chunk_base;
+    p.n_views = (uint32_t)b->views.size();
+    p.total_chunks = b->total_chunks;
+    p.queue = b->d_queue;
+    p.counters = b->d_counters;
+    p.out = reinterpret_cast<uint4*>(hits);
+    p.tile_w_log2 = b->tile_w_log2;
+    p.tile_size_log2 = b->tile_size_log2;
+    p.morton = b->cfg.morton;
+    p.chunk_rays = b->cfg.chunk_tiles << b->tile_size_log2;
+    p.refill = b->cfg.refill_threshold;
+    p.inner = b->cfg.inner_iters;
+    return p;
+}
+
+vrt_status enqueue_batch(vrt_batch* b, vrt_hit* hits, cudaStream_t stream, bool count) {
+    VRT_CUDA(cudaMemsetAsync(b->d_queue, 0, 64, stream));
+    BatchParams p = batch_params(b, hits);
+    if (count)
+        persistent_kernel<true><<<b->blocks_count, b->threads, 0, stream>>>(p);
+    else
+        persistent_kernel<false><<<b->blocks, b->threads, 0, stream>>>(p);
+    VRT_CUDA(cudaGetLastError());
+    return VRT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint64_t vrt_view_records(const vrt_view* v) { return check_view(v) == VRT_OK ? view_records(*v) : 0; }
+
+vrt_status vrt_render_path_device(vrt_world* w, const vrt_view* view, vrt_hit* hits, void* stream) {
+    vrt_status st = world_enter(w);
+    if (st != VRT_OK || (st = check_view(view)) != VRT_OK) return st;
+    if (!hits) {
+        set_error("null hit buffer");
+        return VRT_ERR_INVALID_ARG;
+    }
+    ViewDev d = make_view_dev(*view);
+    d.out_base = 0;
+    return launch_view_path(w, d, hits, (cudaStream_t)stream);
+}
+
+vrt_status vrt_render_path(vrt_world* w, const vrt_view* view, vrt_hit* hits, void* stream_) {
+    vrt_status st = world_enter(w);
+    if (st != VRT_OK || (st = check_view(view)) != VRT_OK) return st;
+    if (!hits) {
+        set_error("null hit buffer");
+        return VRT_ERR_INVALID_ARG;
+    }
+    std::lock_guard<std::mutex> lock(w->mu);
+    cudaStream_t stream = (cudaStream_t)stream_;
+    const size_t hb = view_records(*view) * sizeof(vrt_hit);
+    VRT_CUDA(w->d_io.reserve(hb));
+    ViewDev d = make_view_dev(*view);
+    if ((st = launch_view_path(w, d, (vrt_hit*)w->d_io.ptr, stream)) != VRT_OK) return st;
+    VRT_CUDA(cudaMemcpyAsync(hits, w->d_io.ptr, hb, cudaMemcpyDeviceToHost, stream));
+    VRT_CUDA(cudaStreamSynchronize(stream));
+    return VRT_OK;
+}
+
+vrt_status vrt_batch_create(vrt_world* const* worlds, uint32_t n_worlds, const vrt_view* views, uint32_t n_views,
+                            const vrt_batch_config* cfg_in, vrt_batch** out) {
+    if (!out || !worlds || n_worlds == 0 || !views || n_views == 0) {
+        set_error("batch needs worlds and views");
+        return VRT_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    vrt_batch_config cfg = cfg_in ? *cfg_in : vrt_batch_config{};
+    if (cfg.tile_w == 0 && cfg.tile_h == 0) cfg.tile_w = 8, cfg.tile_h = 8;
+    const bool shape_ok = (cfg.tile_w == 8 && cfg.tile_h == 8) || (cfg.tile_w == 16 && cfg.tile_h == 4) ||
+                          (cfg.tile_w == 32 && cfg.tile_h == 1);
+    if (!shape_ok || (cfg.morton && cfg.tile_w != 8)) {
+        set_error("tile must be 8x8 (optionally Morton), 16x4 or 32x1");
+        return VRT_ERR_INVALID_ARG;
+    }
+    if (cfg.warps_per_block == 0) cfg.warps_per_block = 4;
+    if (cfg.refill_threshold == 0) cfg.refill_threshold = 16;
+    if (cfg.chunk_tiles == 0) cfg.chunk_tiles = 2;
+    if (cfg.inner_iters == 0) cfg.inner_iters = 4;
+    if (cfg.warps_per_block > 16 || cfg.refill_threshold > 32 || cfg.chunk_tiles > 64 || cfg.inner_iters > 1024) {
+        set_error("batch config out of range");
+        return VRT_ERR_INVALID_ARG;
+    }
+    for (uint32_t i = 0; i < n_worlds; i++)
+        if (!worlds[i] || worlds[i]->device != worlds[0]->device) {
+            set_error("worlds must be non-null and on one device");
+            return VRT_ERR_INVALID_ARG;
+        }
+    vrt_status st;
+    for (uint32_t i = 0; i < n_views; i++) {
+        if ((st = check_view(&views[i])) != VRT_OK) return st;
+        if (views[i].world >= n_worlds) {
+            set_error("view references a world outside the list");
+            return VRT_ERR_INVALID_ARG;
+        }
+    }
+    auto* b = new vrt_batch;
+    b->device = worlds[0]->device;
+    b->worlds.assign(worlds, worlds + n_worlds);
+    b->views.assign(views, views + n_views);
+    b->cfg = cfg;
+    b->tile_w_log2 = log2u(cfg.tile_w);
+    b->tile_size_log2 = log2u(cfg.tile_w * cfg.tile_h);
+    const uint32_t th = cfg.tile_h;
+    uint64_t chunks = 0, records = 0;
+    b->vdev.resize(n_views);
+    b->chunk_base.resize(n_views + 1);
+    for (uint32_t i = 0; i < n_views; i++) {
+        ViewDev d = make_view_dev(views[i]);
+        const uint32_t tx = (d.cam.width + cfg.tile_w - 1) / cfg.tile_w, ty = (d.cam.height + th - 1) / th;
+        const uint64_t tiles = (uint64_t)tx * ty;
+        d.tiles_x = tx;
+        d.n_rays = (uint32_t)(tiles << b->tile_size_log2);
+        d.chunk_base = (uint32_t)chunks;
+        d.out_base = records;
+        b->chunk_base[i] = (uint32_t)chunks;
+        chunks += (tiles + cfg.chunk_tiles - 1) / cfg.chunk_tiles;
+        records += view_records(views[i]);
+        b->vdev[i] = d;
+    }
+    if (chunks >= 0xffffffffull) {
+        delete b;
+        set_error("batch too large");
+        return VRT_ERR_INVALID_ARG;
+    }
+    b->chunk_base[n_views] = (uint32_t)chunks;
+    b->total_chunks = (uint32_t)chunks;
+    b->total_records = records;
+    auto fail = [&](vrt_status s) {
+        vrt_batch_destroy(b);
+        return s;
+    };
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_worlds, sizeof(DevWorld) * n_worlds);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_views, sizeof(ViewDev) * n_views);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_chunk_base, sizeof(uint32_t) * (n_views + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_queue, 64);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_views, b->vdev.data(), sizeof(ViewDev) * n_views, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_chunk_base, b->chunk_base.data(), sizeof(uint32_t) * (n_views + 1), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(cuda_fail(e, "batch allocation"));
+    b->d_counters = reinterpret_cast<unsigned long long*>(reinterpret_cast<uint8_t*>(b->d_queue) + 16);
+    if ((st = refresh_worlds(b, 0)) != VRT_OK) return fail(st);
+    // grid: every SM, as many blocks as fit (or as configured)
+    int dev_sms = 0, occ = 0, occ_c = 0;
+    b->threads = (int)cfg.warps_per_block * 32;
+    e = cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, b->device);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<false>, b->threads, 0);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, persistent_kernel<true>, b->threads, 0);
+    if (e != cudaSuccess) return fail(cuda_fail(e, "occupancy query"));
+    const int per_sm = cfg.blocks_per_sm ? std::min<int>((int)cfg.blocks_per_sm, std::max(occ, 1)) : std::max(occ, 1);
+    b->blocks = dev_sms * per_sm;
+    b->blocks_count = dev_sms * std::max(occ_c, 1);
+    *out = b;
+    return VRT_OK;
+}
+
+vrt_status vrt_batch_destroy(vrt_batch* b) {
+    if (!b) return VRT_OK;
+    cudaSetDevice(b->device);
+    cudaDeviceSynchronize();
+    if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
+    if (b->d_worlds) cudaFree(b->d_worlds);
+    if (b->d_views) cudaFree(b->d_views);
+    if (b->d_chunk_base) cudaFree(b->d_chunk_base);
+    if (b->d_queue) cudaFree(b->d_queue);
+    b->d_out.release();
+    delete b;
+    return VRT_OK;
+}
+
+vrt_status vrt_batch_output_layout(const vrt_batch* b, uint64_t* offsets) {
+    if (!b || !offsets) {
+        set_error("null argument");
+        return VRT_ERR_INVALID_ARG;
+    }
+    for (size_t i = 0; i < b->vdev.size(); i++) offsets[i] = b->vdev[i].out_base;
+    offsets[b->vdev.size()] = b->total_records;
+    return VRT_OK;
+}
+
+vrt_status vrt_batch_update_cameras(vrt_batch* b, const vrt_camera* cams, void* stream_) {
+    if (!b || !cams) {
+        set_error("null argument");
+        return VRT_ERR_INVALID_ARG;
+    }
+    for (size_t i = 0; i < b->vdev.size(); i++)
+        if (cams[i].width != b->vdev[i].cam.width || cams[i].height != b->vdev[i].cam.height) {
+            set_error("camera resolution differs from the batch's view");
+            return VRT_ERR_INVALID_ARG;
+        }
+    VRT_CUDA(cudaSetDevice(b->device));
+    for (size_t i = 0; i < b->vdev.size(); i++) {
+        b->vdev[i].cam = cams[i];
+        b->views[i].cam = cams[i];
+    }
+    cudaStream_t stream = (cudaStream_t)stream_;
+    VRT_CUDA(cudaMemcpyAsync(b->d_views, b->vdev.data(), sizeof(ViewDev) * b->vdev.size(), cudaMemcpyHostToDevice,
+                             stream));
+    VRT_CUDA(cudaStreamSynchronize(stream));
+    return VRT_OK;
+}
+
+vrt_status vrt_batch_launch(vrt_batch* b, vrt_hit* hits, void* stream_) {
+    if (!b || !hits) {
+        set_error("null argument");
+        return VRT_ERR_INVALID_ARG;
+    }
+    VRT_CUDA(cudaSetDevice(b->device));
+    cudaStream_t stream = (cudaStream_t)stream_;
+    vrt_status st = refresh_worlds(b, stream);
+    if (st != VRT_OK) return st;
+    b->last_stream = stream;
+    return enqueue_batch(b, hits, stream, false);
+}
+
+vrt_status vrt_batch_launch_graph(vrt_batch* b, vrt_hit* hits, void* stream_) {
+    if (!b || !hits) {
+        set_error("null argument");
+        return VRT_ERR_INVALID_ARG;
+    }
+    VRT_CUDA(cudaSetDevice(b->device));
+    cudaStream_t stream = (cudaStream_t)stream_;
+    vrt_status st = refresh_worlds(b, stream);
+    if (st != VRT_OK) return st;
+    if (!b->graph_exec || b->graph_hits != hits) {
+        if (b->graph_exec) {
+            cudaGraphExecDestroy(b->graph_exec);
+            b->graph_exec = nullptr;
+        }
+        cudaStream_t cap;
+        VRT_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            st = enqueue_batch(b, hits, cap, false);
+            e = cudaStreamEndCapture(cap, &g);
+        }
+        if (e == cudaSuccess && st == VRT_OK) e = cudaGraphInstantiate(&b->graph_exec, g, 0);
+        if (g) cudaGraphDestroy(g);
+        cudaStreamDestroy(cap);
+        if (st != VRT_OK) return st;
+        if (e != cudaSuccess) return cuda_fail(e, "capture batch graph");
+        b->graph_hits = hits;
+    }
+    b->last_stream = stream;
+    VRT_CUDA(cudaGraphLaunch(b->graph_exec, stream));
+    return VRT_OK;
+}
+
+vrt_status vrt_batch_launch_per_view(vrt_batch* b, vrt_hit* hits, void* stream_) {
+    if (!b || !hits) {
+        set_error("null argument");
+        return VRT_ERR_INVALID_ARG;
+    }
+    VRT_CUDA(cudaSetDevice(b->device));
+    cudaStream_t stream = (cudaStream_t)stream_;
+    for (size_t i = 0; i < b->vdev.size(); i++) {
+        vrt_status st = launch_view_path(b->worlds[b->vdev[i].world], b->vdev[i], hits, stream);
+        if (st != VRT_OK) return st;
+    }
+    b->last_stream = stream;
+    return VRT_OK;
+}
+
+vrt_status vrt_batch_run(vrt_batch* b, vrt_hit* hits_host, void* stream_) {
+    if (!b || !hits_host) {
+        set_error("null argument");
+        return VRT_ERR_INVALID_ARG;
+    }
+    VRT_CUDA(cudaSetDevice(b->device));
+    cudaStream_t stream = (cudaStream_t)stream_;
+    VRT_CUDA(b->d_out.reserve(b->total_records * sizeof(vrt_hit)));
+    vrt_status st = vrt_batch_launch_graph(b, (vrt_hit*)b->d_out.ptr, stream);
+    if (st != VRT_OK) return st;
+    VRT_CUDA(cudaMemcpyAsync(hits_host, b->d_out.ptr, b->total_records * sizeof(vrt_hit), cudaMemcpyDeviceToHost,
+                             stream));
+    VRT_CUDA(cudaStreamSynchronize(stream));
+    return VRT_OK;
+}
+
+vrt_status vrt_batch_get_stats(vrt_batch* b, vrt_batch_stats* out) {
+    if (!b || !out) {
+        set_error("null argument");
+        return VRT_ERR_INVALID_ARG;
+    }
+    VRT_CUDA(cudaSetDevice(b->device));
+    VRT_CUDA(cudaStreamSynchronize(b->last_stream));
+    unsigned long long c[4];
+    VRT_CUDA(cudaMemcpy(c, b->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
+    out->rays_cast = c[0];
+    out->step_calls = c[1];
+    out->occ_fetches = c[2];
+    out->hits = c[3];
+    return VRT_OK;
+}
+
+vrt_status vrt_batch_measure(vrt_batch* b, vrt_hit* hits, void* stream_, vrt_batch_stats* out) {
+    if (!b || !hits || !out) {
+        set_error("null argument");
+        return VRT_ERR_INVALID_ARG;
+    }
+    VRT_CUDA(cudaSetDevice(b->device));
+    cudaStream_t stream = (cudaStream_t)stream_;
+    vrt_status st = refresh_worlds(b, stream);
+    if (st != VRT_OK || (st = enqueue_batch(b, hits, stream, true)) != VRT_OK) return st;
+    b->last_stream = stream;
+    return vrt_batch_get_stats(b, out);
+}
+
+}  // extern "C"

@@ -53,97 +53,137 @@ __device__ __forceinline__ void camera_ray(const vrt_camera& cam, uint32_t px, u
     dz = __fdiv_rn(z, len);
 }
 
+// Per-ray traversal state: RayCast's loop-carried values (CpuRenderer.cpp:173-184).
+struct RayState {
+    float ox, oy, oz, dx, dy, dz;
+    float ix, iy, iz;     // invDir
+    float tsx, tsy, tsz;  // tStart
+    float cx, cy, cz;     // currPos
+    float sx, sy, sz;     // sideDist
+    int32_t vx, vy, vz;   // voxel of the last step (hit voxel on a hit)
+    uint32_t i;           // iteration
+    uint32_t material;
+};
+
+// invDir, tStart and the clipped start position (VoxelTraversal.glsl:133-145,163-167).
+__device__ __forceinline__ void ray_init(RayState& s, const DevWorld& w, float ox, float oy, float oz, float dx,
+                                         float dy, float dz, int32_t wox, int32_t woy, int32_t woz) {
+    s.ox = ox;
+    s.oy = oy;
+    s.oz = oz;
+    s.dx = dx;
+    s.dy = dy;
+    s.dz = dz;
+    s.ix = __fdiv_rn(1.0f, dx);
+    s.iy = __fdiv_rn(1.0f, dy);
+    s.iz = __fdiv_rn(1.0f, dz);
+    s.tsx = __fmul_rn(__fsub_rn(dx < 0.0f ? 0.0f : 1.0f, ox), s.ix);
+    s.tsy = __fmul_rn(__fsub_rn(dy < 0.0f ? 0.0f : 1.0f, oy), s.iy);
+    s.tsz = __fmul_rn(__fsub_rn(dz < 0.0f ? 0.0f : 1.0f, oz), s.iz);
+    const float t1x = __fmul_rn(__fsub_rn(__int2float_rn(1 - wox), ox), s.ix);
+    const float t1y = __fmul_rn(__fsub_rn(__int2float_rn(1 - woy), oy), s.iy);
+    const float t1z = __fmul_rn(__fsub_rn(__int2float_rn(1 - woz), oz), s.iz);
+    const float t2x = __fmul_rn(__fsub_rn(__fsub_rn(__fsub_rn(__uint2float_rn(w.size_x), __int2float_rn(wox)), 1.0f), ox), s.ix);
+    const float t2y = __fmul_rn(__fsub_rn(__fsub_rn(__fsub_rn(__uint2float_rn(w.size_y), __int2float_rn(woy)), 1.0f), oy), s.iy);
+    const float t2z = __fmul_rn(__fsub_rn(__fsub_rn(__fsub_rn(__uint2float_rn(w.size_z), __int2float_rn(woz)), 1.0f), oz), s.iz);
+    const float tmin = max_x86(min_x86(t1x, t2x), max_x86(min_x86(t1y, t2y), min_x86(t1z, t2z)));
+    const float tmax = min_x86(max_x86(t1x, t2x), min_x86(max_x86(t1y, t2y), max_x86(t1z, t2z)));
+    const bool clip = tmin > 0.0f && tmin < tmax;
+    s.cx = clip ? __fadd_rn(ox, __fmul_rn(dx, tmin)) : ox;
+    s.cy = clip ? __fadd_rn(oy, __fmul_rn(dy, tmin)) : oy;
+    s.cz = clip ? __fadd_rn(oz, __fmul_rn(dz, tmin)) : oz;
+    s.sx = s.sy = s.sz = 0.0f;
+    s.vx = s.vy = s.vz = 0;
+    s.i = 0;
+    s.material = 0;
+}
+
+enum : uint32_t { kStepContinue = 0, kStepHit = 1, kStepOut = 2 };
+
+// One iteration of RayCast (CpuRenderer.cpp:186-201) with GetStepPos (:135-171).
 template <bool kCount>
-__device__ __forceinline__ void trace_ray(const DevWorld& w, float ox, float oy, float oz, float dx,
-                                          float dy, float dz, int32_t wox, int32_t woy, int32_t woz,
-                                          uint32_t max_iters, TraceResult& r, TraceCounters& cnt) {
-    const float ix = __fdiv_rn(1.0f, dx), iy = __fdiv_rn(1.0f, dy), iz = __fdiv_rn(1.0f, dz);
-    const float tsx = __fmul_rn(__fsub_rn(dx < 0.0f ? 0.0f : 1.0f, ox), ix);
-    const float tsy = __fmul_rn(__fsub_rn(dy < 0.0f ? 0.0f : 1.0f, oy), iy);
-    const float tsz = __fmul_rn(__fsub_rn(dz < 0.0f ? 0.0f : 1.0f, oz), iz);
-
-    // clipRayToAABB(origin, dir, 1 - wo, size - wo - 1)
-    float cx, cy, cz;
-    {
-        float t1x = __fmul_rn(__fsub_rn(__int2float_rn(1 - wox), ox), ix);
-        float t1y = __fmul_rn(__fsub_rn(__int2float_rn(1 - woy), oy), iy);
-        float t1z = __fmul_rn(__fsub_rn(__int2float_rn(1 - woz), oz), iz);
-        float t2x = __fmul_rn(__fsub_rn(__fsub_rn(__fsub_rn(__uint2float_rn(w.size_x), __int2float_rn(wox)), 1.0f), ox), ix);
-        float t2y = __fmul_rn(__fsub_rn(__fsub_rn(__fsub_rn(__uint2float_rn(w.size_y), __int2float_rn(woy)), 1.0f), oy), iy);
-        float t2z = __fmul_rn(__fsub_rn(__fsub_rn(__fsub_rn(__uint2float_rn(w.size_z), __int2float_rn(woz)), 1.0f), oz), iz);
-        float tmin = max_x86(min_x86(t1x, t2x), max_x86(min_x86(t1y, t2y), min_x86(t1z, t2z)));
-        float tmax = min_x86(max_x86(t1x, t2x), min_x86(max_x86(t1y, t2y), max_x86(t1z, t2z)));
-        bool clip = tmin > 0.0f && tmin < tmax;
-        cx = clip ? __fadd_rn(ox, __fmul_rn(dx, tmin)) : ox;
-        cy = clip ? __fadd_rn(oy, __fmul_rn(dy, tmin)) : oy;
-        cz = clip ? __fadd_rn(oz, __fmul_rn(dz, tmin)) : oz;
+__device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int32_t wox, int32_t woy, int32_t woz,
+                                             TraceCounters& cnt) {
+    int32_t vx = wadd(wox, floor2i(s.cx));
+    int32_t vy = wadd(woy, floor2i(s.cy));
+    int32_t vz = wadd(woz, floor2i(s.cz));
+    if (!((uint32_t)vx < w.size_x && (uint32_t)vy < w.size_y && (uint32_t)vz < w.size_z)) {
+        s.vx = vx;
+        s.vy = vy;
+        s.vz = vz;
+        return kStepOut;
     }
-    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-    int32_t vx = 0, vy = 0, vz = 0;
-    uint32_t steps = max_iters, material = 0;
-    bool hit = false;
-
-    for (uint32_t i = 0; i < max_iters; i++) {
-        vx = wadd(wox, floor2i(cx));
-        vy = wadd(woy, floor2i(cy));
-        vz = wadd(woz, floor2i(cz));
-        if (!((uint32_t)vx < w.size_x && (uint32_t)vy < w.size_y && (uint32_t)vz < w.size_z)) {
-            steps = i;
-            break;
-        }
-        // GetStepPos: sector allocation mask at lod 3
-        const uint32_t sidx = (uint32_t)(vx >> 5) + (uint32_t)(vz >> 5) * w.sx + (uint32_t)(vy >> 5) * w.sxz;
-        const uint4 rec = __ldg(reinterpret_cast<const uint4*>(w.sectors) + sidx);
-        uint32_t lo = rec.x, hi = rec.y;
-        uint32_t idx = ((vx >> 3) & 3) | ((vz >> 3) & 3) << 2 | ((vy >> 3) & 3) << 4;
-        int32_t lod = 3;
-        if (kCount) cnt.step_calls++;
+    // sector allocation mask at lod 3
+    const uint32_t sidx = (uint32_t)(vx >> 5) + (uint32_t)(vz >> 5) * w.sx + (uint32_t)(vy >> 5) * w.sxz;
+    const uint4 rec = __ldg(reinterpret_cast<const uint4*>(w.sectors) + sidx);
+    uint32_t lo = rec.x, hi = rec.y;
+    uint32_t idx = ((vx >> 3) & 3) | ((vz >> 3) & 3) << 2 | ((vy >> 3) & 3) << 4;
+    int32_t lod = 3;
+    if (kCount) cnt.step_calls++;
+    if ((((idx < 32 ? lo : hi) >> (idx & 31)) & 1u) != 0) {
+        // brick allocated: slot = base + popcount of the mask below the brick bit
+        const uint32_t below = (1u << (idx & 31)) - 1u;
+        const uint32_t slot = rec.z + (idx < 32 ? __popc(lo & below) : __popc(lo) + __popc(hi & below));
+        const uint32_t cell = ((vx >> 2) & 1) | ((vz >> 2) & 1) << 1 | ((vy >> 2) & 1) << 2;
+        const uint2 cm = __ldg(reinterpret_cast<const uint2*>(w.occ) + (size_t)slot * 8 + cell);
+        lo = cm.x;
+        hi = cm.y;
+        idx = (vx & 3) | (vz & 3) << 2 | (vy & 3) << 4;
+        lod = 0;
+        if (kCount) cnt.occ_fetches++;
         if ((((idx < 32 ? lo : hi) >> (idx & 31)) & 1u) != 0) {
-            // brick allocated: slot = base + popcount of the mask below the brick bit
-            const uint32_t below = (1u << (idx & 31)) - 1u;
-            const uint32_t slot = rec.z + (idx < 32 ? __popc(lo & below) : __popc(lo) + __popc(hi & below));
-            const uint32_t cell = ((vx >> 2) & 1) | ((vz >> 2) & 1) << 1 | ((vy >> 2) & 1) << 2;
-            const uint2 cm = __ldg(reinterpret_cast<const uint2*>(w.occ) + (size_t)slot * 8 + cell);
-            lo = cm.x;
-            hi = cm.y;
-            idx = (vx & 3) | (vz & 3) << 2 | (vy & 3) << 4;
-            lod = 0;
-            if (kCount) cnt.occ_fetches++;
-            if ((((idx < 32 ? lo : hi) >> (idx & 31)) & 1u) != 0) {
-                const uint32_t vi = (vx & 7) | (vz & 7) << 3 | (vy & 7) << 6;
-                material = __ldg(w.payload + (size_t)slot * 512 + vi);
-                hit = true;
-                steps = i;
-                break;
-            }
+            const uint32_t vi = (vx & 7) | (vz & 7) << 3 | (vy & 7) << 6;
+            s.material = __ldg(w.payload + (size_t)slot * 512 + vi);
+            s.vx = vx;
+            s.vy = vy;
+            s.vz = vz;
+            return kStepHit;
         }
-        const uint32_t half = idx < 32 ? lo : hi;
-        lod += (lo | hi) == 0 ? 2 : (((half >> (idx & 0xA)) & 0x00330033u) == 0 ? 1 : 0);
-        const int32_t m = (1 << lod) - 1;
-        vx = dx < 0.0f ? (vx & ~m) : (vx | m);
-        vy = dy < 0.0f ? (vy & ~m) : (vy | m);
-        vz = dz < 0.0f ? (vz & ~m) : (vz | m);
-
-        sx = __fadd_rn(tsx, __fmul_rn(__int2float_rn(wsub(vx, wox)), ix));
-        sy = __fadd_rn(tsy, __fmul_rn(__int2float_rn(wsub(vy, woy)), iy));
-        sz = __fadd_rn(tsz, __fmul_rn(__int2float_rn(wsub(vz, woz)), iz));
-        const float t = __fadd_rn(min_x86(min_x86(sx, sy), sz), 0.001f);
-        cx = __fadd_rn(ox, __fmul_rn(t, dx));
-        cy = __fadd_rn(oy, __fmul_rn(t, dy));
-        cz = __fadd_rn(oz, __fmul_rn(t, dz));
     }
-    r.cx = cx;
-    r.cy = cy;
-    r.cz = cz;
-    r.sx = sx;
-    r.sy = sy;
-    r.sz = sz;
-    r.vx = vx;
-    r.vy = vy;
-    r.vz = vz;
-    r.steps = steps;
-    r.material = material;
-    r.hit = hit;
+    // level4 (+2) / level2 (+1) from the same mask, then align to the cell boundary
+    const uint32_t half = idx < 32 ? lo : hi;
+    lod += (lo | hi) == 0 ? 2 : (((half >> (idx & 0xA)) & 0x00330033u) == 0 ? 1 : 0);
+    const int32_t m = (1 << lod) - 1;
+    vx = s.dx < 0.0f ? (vx & ~m) : (vx | m);
+    vy = s.dy < 0.0f ? (vy & ~m) : (vy | m);
+    vz = s.dz < 0.0f ? (vz & ~m) : (vz | m);
+    s.vx = vx;
+    s.vy = vy;
+    s.vz = vz;
+    s.sx = __fadd_rn(s.tsx, __fmul_rn(__int2float_rn(wsub(vx, wox)), s.ix));
+    s.sy = __fadd_rn(s.tsy, __fmul_rn(__int2float_rn(wsub(vy, woy)), s.iy));
+    s.sz = __fadd_rn(s.tsz, __fmul_rn(__int2float_rn(wsub(vz, woz)), s.iz));
+    const float t = __fadd_rn(min_x86(min_x86(s.sx, s.sy), s.sz), 0.001f);
+    s.cx = __fadd_rn(s.ox, __fmul_rn(t, s.dx));
+    s.cy = __fadd_rn(s.oy, __fmul_rn(t, s.dy));
+    s.cz = __fadd_rn(s.oz, __fmul_rn(t, s.dz));
+    return kStepContinue;
+}
+
+// Whole RayCast for one ray.
+template <bool kCount>
+__device__ __forceinline__ void trace_ray(const DevWorld& w, float ox, float oy, float oz, float dx, float dy,
+                                          float dz, int32_t wox, int32_t woy, int32_t woz, uint32_t max_iters,
+                                          TraceResult& r, TraceCounters& cnt) {
+    RayState s;
+    ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
+    uint32_t st = kStepOut, i = 0;
+    for (; i < max_iters; i++) {
+        st = ray_step<kCount>(s, w, wox, woy, woz, cnt);
+        if (st != kStepContinue) break;
+    }
+    r.cx = s.cx;
+    r.cy = s.cy;
+    r.cz = s.cz;
+    r.sx = s.sx;
+    r.sy = s.sy;
+    r.sz = s.sz;
+    r.vx = s.vx;
+    r.vy = s.vy;
+    r.vz = s.vz;
+    r.steps = i;  // == max_iters when the cap ran out
+    r.material = s.material;
+    r.hit = st == kStepHit && i < max_iters;
 }
 
 // The 16-byte vrt_hit record as one vector store.
@@ -176,6 +216,99 @@ __device__ __forceinline__ void secondary_origin(const TraceResult& r, float dx,
     ox = __fadd_rn(r.cx, __fmul_rn(nx, 0.01f));
     oy = __fadd_rn(r.cy, __fmul_rn(ny, 0.01f));
     oz = __fadd_rn(r.cz, __fmul_rn(nz, 0.01f));
+}
+
+}  // namespace vrt
+
+namespace vrt {
+
+// PCG32 (O'Neill, pcg-random.org: 64-bit LCG state, XSH-RR output).
+struct DevPcg32 {
+    uint64_t state, inc;
+    __device__ __forceinline__ DevPcg32(uint64_t initstate, uint64_t initseq) {
+        state = 0;
+        inc = (initseq << 1) | 1u;
+        next();
+        state += initstate;
+        next();
+    }
+    __device__ __forceinline__ uint32_t next() {
+        const uint64_t old = state;
+        state = old * 6364136223846793005ULL + inc;
+        const uint32_t xs = (uint32_t)(((old >> 18) ^ old) >> 27);
+        const uint32_t rot = (uint32_t)(old >> 59);
+        return (xs >> rot) | (xs << ((32 - rot) & 31));
+    }
+    // uniform in [-1, 1) with 2^-23 spacing; every op exact
+    __device__ __forceinline__ float next_signed() {
+        return __fsub_rn(__fmul_rn(__uint2float_rn(next() >> 8), 0x1p-23f), 1.0f);
+    }
+};
+
+constexpr uint64_t kBounceStream = 0x9E3779B97F4A7C15ULL;
+
+// Lambertian bounce normalize(n + s), s uniform on the sphere by rejection from the
+// cube (the structure of CpuRenderer.cpp:392 with IEEE-exact sampling).
+__device__ __forceinline__ void bounce_dir(uint32_t pixel, uint32_t bounce, float nx, float ny, float nz, float& dx,
+                                           float& dy, float& dz) {
+    DevPcg32 rng(pixel ^ bounce, kBounceStream);
+    for (int attempt = 0; attempt < 64; attempt++) {
+        const float x = rng.next_signed(), y = rng.next_signed(), z = rng.next_signed();
+        const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z));
+        if (!(r2 > 1e-6f && r2 <= 1.0f)) continue;
+        const float r = __fsqrt_rn(r2);
+        const float ax = __fadd_rn(nx, __fdiv_rn(x, r)), ay = __fadd_rn(ny, __fdiv_rn(y, r)),
+                    az = __fadd_rn(nz, __fdiv_rn(z, r));
+        const float l2 = __fadd_rn(__fadd_rn(__fmul_rn(ax, ax), __fmul_rn(ay, ay)), __fmul_rn(az, az));
+        if (!(l2 > 1e-12f)) continue;
+        const float l = __fsqrt_rn(l2);
+        dx = __fdiv_rn(ax, l);
+        dy = __fdiv_rn(ay, l);
+        dz = __fdiv_rn(az, l);
+        return;
+    }
+    const float l = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)), __fmul_rn(nz, nz)));
+    dx = __fdiv_rn(nx, l);
+    dy = __fdiv_rn(ny, l);
+    dz = __fdiv_rn(nz, l);
+}
+
+// Hit record from a finished RayState (steps = iteration index at exit).
+__device__ __forceinline__ uint4 pack_state(const RayState& s, bool hit, uint32_t steps, uint32_t tag) {
+    TraceResult r;
+    r.sx = s.sx;
+    r.sy = s.sy;
+    r.sz = s.sz;
+    r.vx = s.vx;
+    r.vy = s.vy;
+    r.vz = s.vz;
+    r.steps = steps;
+    r.material = s.material;
+    r.hit = hit;
+    return pack_hit(r, s.dx, s.dy, s.dz, tag);
+}
+
+// Origin and direction of the next ray of a path after a hit: the shadow ray
+// (kind 1 with shadows) or bounce `bounce` (1-based).
+__device__ __forceinline__ void next_path_ray(const RayState& s, bool shadow, const float* sun, uint32_t pixel,
+                                              uint32_t bounce, float& ox, float& oy, float& oz, float& dx, float& dy,
+                                              float& dz) {
+    TraceResult r;
+    r.cx = s.cx;
+    r.cy = s.cy;
+    r.cz = s.cz;
+    r.sx = s.sx;
+    r.sy = s.sy;
+    r.sz = s.sz;
+    float nx, ny, nz;
+    secondary_origin(r, s.dx, s.dy, s.dz, ox, oy, oz, nx, ny, nz);
+    if (shadow) {
+        dx = sun[0];
+        dy = sun[1];
+        dz = sun[2];
+    } else {
+        bounce_dir(pixel, bounce, nx, ny, nz, dx, dy, dz);
+    }
 }
 
 }  // namespace vrt
