@@ -1,0 +1,17 @@
+#!/bin/sh
+# Builds oracle/_ref/libvrt_ref.so from the reference's own sources, in place, with
+# the shim headers of oracle/ref_pin/shim.  x86-64 with AVX-512 only (the reference's
+# SIMD layer supports nothing else); run where the reference checkout exists.
+# Float semantics: no -ffast-math and no FMA contraction (the reading the oracle pins).
+set -e
+REF=${1:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT="$HERE/../_ref"
+mkdir -p "$OUT"
+g++ -std=gnu++20 -O2 -ffp-contract=off -fno-fast-math -fPIC -shared -w \
+    -mavx512f -mavx512cd -mavx512bw -mavx512dq -mavx512vl -mavx512vbmi -mavx512vpopcntdq -mavx512bitalg \
+    -mgfni -mfma -mbmi -mbmi2 -mlzcnt -mpopcnt -mf16c \
+    -I "$HERE/shim" -I "$REF/src/LibGlimpsw" -iquote "$REF/src/VoxelRT" \
+    "$HERE/ref_driver.cpp" -o "$OUT/libvrt_ref.so.tmp"
+mv "$OUT/libvrt_ref.so.tmp" "$OUT/libvrt_ref.so"
+echo "$OUT/libvrt_ref.so"

@@ -1,0 +1,105 @@
+// ref_driver.cpp - TEST INFRASTRUCTURE.  Compiles the reference's own CPU traversal
+// (src/VoxelRT/CpuRenderer.cpp) and host world model (src/VoxelRT/VoxelMap.cpp) in
+// place from the reference checkout, with the shim headers of oracle/ref_pin/shim/
+// standing in for GLM, ImGui and the OpenGL wrapper, and exposes a C entry point
+// that runs the reference's static RayCast (CpuRenderer.cpp:172-224) over
+// FlatVoxelStorage (CpuRenderer.cpp:20-84) filled through VoxelMap and SyncBuffers.
+// The AVX-512 code only runs on x86-64; its outputs are committed as golden
+// vectors (tests/golden/) that pin the portable oracle.
+#include "CpuRenderer.cpp"
+#include "VoxelMap.cpp"
+
+#include <stdexcept>
+
+namespace glim::io {
+void WriteCompressed(std::ostream&, const void*, size_t) { throw std::runtime_error("zstd is not available"); }
+void ReadCompressed(std::istream&, void*, size_t) { throw std::runtime_error("zstd is not available"); }
+}  // namespace glim::io
+
+namespace {
+struct RefWorld {
+    std::shared_ptr<VoxelMap> map = std::make_shared<VoxelMap>();
+    std::unique_ptr<FlatVoxelStorage> storage = std::make_unique<FlatVoxelStorage>();
+};
+}  // namespace
+
+extern "C" {
+
+uint32_t ref_lanes(void) { return simd::VectorWidth; }
+
+// View extent of FlatVoxelStorage in sectors (x, y, z): CpuRenderer.cpp:14-16.
+void ref_view_sectors(uint32_t out[3]) {
+    out[0] = ViewSectorIndexer::SizeXZ;
+    out[1] = ViewSectorIndexer::SizeY;
+    out[2] = ViewSectorIndexer::SizeXZ;
+}
+
+void* ref_world_create(void) {
+    auto* w = new RefWorld;
+    // palette entry i encodes i in its RGB565 bits, so MaterialData & 0xFFFF is the voxel id
+    for (uint32_t i = 0; i < 256; i++) {
+        Material& m = w->map->Palette[i];
+        m.Color[0] = 0;
+        m.Color[1] = (uint8_t)((i >> 5) << 2);
+        m.Color[2] = (uint8_t)((i & 31) << 3);
+        m.Emission = 0.0f;
+    }
+    return w;
+}
+
+void ref_world_destroy(void* p) { delete static_cast<RefWorld*>(p); }
+
+// Sector records (WorldSectorIndexer index, allocation mask, bricks in bit order)
+// go into VoxelMap::Sectors and DirtyLocs; SyncBuffers then builds the flat layout.
+int ref_world_load(void* p, uint32_t n, const int32_t* sector_idx, const uint64_t* masks, const uint8_t* bricks) {
+    auto* w = static_cast<RefWorld*>(p);
+    for (uint32_t i = 0; i < n; i++) {
+        Sector& s = w->map->Sectors[(uint32_t)sector_idx[i]];
+        for (uint64_t m = masks[i]; m; m &= m - 1) {
+            uint32_t b = (uint32_t)std::countr_zero(m);
+            std::memcpy(s.GetBrick(b, true)->Data, bricks, 512);
+            bricks += 512;
+        }
+        w->map->DirtyLocs[(uint32_t)sector_idx[i]] |= masks[i];
+    }
+    w->storage->SyncBuffers(*w->map);
+    return 0;
+}
+
+// RayCast over n rays in SIMD groups; per ray: hit flag, Pos (3), Normal (3),
+// Distance, MaterialData.
+int ref_raycast(void* p, uint64_t n, const float* origins, const float* dirs, const int32_t wo[3], uint8_t* hit,
+                float* pos, float* normal, float* dist, int32_t* material) {
+    auto* w = static_cast<RefWorld*>(p);
+    const uint32_t L = simd::VectorWidth;
+    for (uint64_t base = 0; base < n; base += L) {
+        VFloat3 o, d;
+        VMask mask = 0;
+        for (uint32_t l = 0; l < L; l++) {
+            uint64_t i = base + l < n ? base + l : n - 1;
+            o.x[l] = origins[i * 3 + 0];
+            o.y[l] = origins[i * 3 + 1];
+            o.z[l] = origins[i * 3 + 2];
+            d.x[l] = dirs[i * 3 + 0];
+            d.y[l] = dirs[i * 3 + 1];
+            d.z[l] = dirs[i * 3 + 2];
+            if (base + l < n) mask |= (VMask)(1u << l);
+        }
+        VHitResult r = RayCast(*w->storage, o, d, mask, glm::ivec3(wo[0], wo[1], wo[2]));
+        for (uint32_t l = 0; l < L && base + l < n; l++) {
+            uint64_t i = base + l;
+            hit[i] = (r.Mask >> l) & 1;
+            pos[i * 3 + 0] = r.Pos.x[l];
+            pos[i * 3 + 1] = r.Pos.y[l];
+            pos[i * 3 + 2] = r.Pos.z[l];
+            normal[i * 3 + 0] = r.Normal.x[l];
+            normal[i * 3 + 1] = r.Normal.y[l];
+            normal[i * 3 + 2] = r.Normal.z[l];
+            dist[i] = r.Distance[l];
+            material[i] = r.MaterialData[l];
+        }
+    }
+    return 0;
+}
+
+}  // extern "C"
