@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="bounded CPU-oracle sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-per-view", action="store_true")
+    ap.add_argument("--worlds", type=int, default=128, help="uneven_batch: number of worlds")
+    ap.add_argument("--max-views", type=int, default=16, help="uneven_batch: views per world, at most")
     return ap.parse_args()
 
 
@@ -76,10 +78,12 @@ def max_over_ranks(pg, x: float) -> float:
     return float(t.item())
 
 
-def build_workload(name: str, rank: int):
+def build_workload(name: str, rank: int, args=None):
     from voxelrt_gb300 import workloads as W
     if name == "uneven_batch":
-        return W.uneven_batch(seed=2 + 1000 * rank)
+        nw = args.worlds if args is not None else 128
+        mv = args.max_views if args is not None else 16
+        return W.uneven_batch(n_worlds=nw, max_views=mv, seed=2 + 1000 * rank)
     if name == "large_world":
         return W.large_world()
     if name == "incoherent":
@@ -197,7 +201,7 @@ def run_reference(args):
         return
     from voxelrt_gb300 import build
     build.build_all()
-    wl = build_workload(args.workload, 0)
+    wl = build_workload(args.workload, 0, args)
     cores = os.cpu_count() or 1
     per_step = max(2.0, min(20.0, args.cpu_seconds))
     for _ in range(args.warmup):
@@ -231,7 +235,7 @@ def run_ours(args):
     ws, rank, local, pg = dist_setup(args)
     torch.cuda.set_device(local)
     dev = local
-    wl = build_workload(args.workload, rank)
+    wl = build_workload(args.workload, rank, args)
     worlds = []
     for d in wl.worlds:
         w = v.World(d.sectors, brick_capacity=d.n_bricks + 64, device=dev)

@@ -182,6 +182,13 @@ vrt_status vrt_world_sync_sectors(vrt_world* world, uint32_t n, const int32_t* s
                                   const uint64_t* alloc_mask, const uint64_t* dirty_mask,
                                   const uint8_t* bricks, void* stream);
 
+/* Apply sphere edits in order (VoxelMap::RegionDispatchSIMD + brick GC,
+ * VoxelMap.h:222-263): bricks are allocated for fills, voxels written on the device,
+ * cell masks re-derived, and bricks that became empty are freed, so the allocation
+ * mask stays the set of non-empty bricks.  Ordered on `stream` after earlier work
+ * (edits land between frames); returns when done. */
+vrt_status vrt_world_edit(vrt_world* world, const vrt_edit* edits, uint32_t n, void* stream);
+
 /* Read one sector back: its allocation mask and popcount(mask) x 512 bytes. */
 vrt_status vrt_world_read_sector(vrt_world* world, int32_t sector_idx, uint64_t* alloc_mask,
                                  uint8_t* bricks, size_t bricks_capacity, void* stream);

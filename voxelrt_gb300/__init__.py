@@ -179,6 +179,11 @@ class World:
     def upload(self, data: SectorData, stream=None) -> None:
         self.sync_sectors(data.sector_idx, data.alloc_mask, data.bricks, None, stream)
 
+    def edit(self, edits, stream=None) -> None:
+        """Apply vrt_edit records (EDIT_DTYPE array) in order."""
+        e = np.ascontiguousarray(edits, dtype=EDIT_DTYPE)
+        check(lib().vrt_world_edit(self._h, ptr(e), len(e), _stream_ptr(stream)))
+
     def read_sector(self, sector_idx: int):
         mask = C.c_uint64()
         check(lib().vrt_world_read_sector(self._h, int(sector_idx), C.byref(mask), None, 0, None))

@@ -120,6 +120,7 @@ PROTOTYPES = {
     "vrt_world_destroy": (_st, [_vp]),
     "vrt_world_get_stats": (_st, [_vp, C.POINTER(WorldStats)]),
     "vrt_world_sync_sectors": (_st, [_vp, _u32, _vp, _vp, _vp, _vp, _vp]),
+    "vrt_world_edit": (_st, [_vp, _vp, _u32, _vp]),
     "vrt_world_read_sector": (_st, [_vp, _i32, C.POINTER(_u64), _vp, C.c_size_t, _vp]),
     "vrt_cast": (_st, [_vp, _vp, _u32, C.POINTER(CastParams), _vp, _vp]),
     "vrt_cast_device": (_st, [_vp, _vp, _u32, C.POINTER(CastParams), _vp, _vp]),

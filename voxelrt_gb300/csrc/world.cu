@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <map>
 #include <string>
 #include <unordered_set>
 #include <vector>
@@ -252,6 +253,17 @@ vrt_status run_batch(vrt_world* w, SyncBatch& b, cudaStream_t stream) {
 }
 
 }  // namespace
+
+// Re-lay out sectors to new allocation masks, keeping the content of bricks that
+// stay and zero-filling bricks that appear (used by the edit path).
+vrt_status world_repack(vrt_world* w, const std::map<uint32_t, uint64_t>& new_masks, cudaStream_t stream) {
+    SyncBatch batch;
+    for (const auto& kv : new_masks) {
+        vrt_status st = plan_sector(w, batch, kv.first, kv.second, 0, 0, stream);
+        if (st != VRT_OK) return st;
+    }
+    return run_batch(w, batch, stream);
+}
 
 }  // namespace vrt
 
