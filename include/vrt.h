@@ -286,6 +286,65 @@ vrt_status vrt_batch_get_stats(vrt_batch* batch, vrt_batch_stats* out);
 /* One launch of the counting variant: fills step_calls/occ_fetches/hits. */
 vrt_status vrt_batch_measure(vrt_batch* batch, vrt_hit* hits_device, void* stream, vrt_batch_stats* out);
 
+/* ---- pinned host memory (asynchronous copies for host-buffer calls) ---- */
+vrt_status vrt_host_alloc(size_t bytes, void** out);
+vrt_status vrt_host_free(void* ptr);
+
+/* ---- request server: continuous batching over resident worlds ---- */
+/* Render and edit requests are queued as they arrive.  A scheduler thread packs
+ * the render requests at the head of the queue into one persistent launch per
+ * in-flight slot (up to max_inflight launches overlap on the device, each on its
+ * own stream), admitting a request only while the output records of admitted
+ * requests fit the HBM budget; records are copied to the caller's host buffer
+ * (pinned memory: see vrt_host_alloc).  An edit waits until the launches in flight
+ * have finished and is applied before any later request starts, so every request
+ * sees the world as of its place in the submission order (edits between frames,
+ * as the reference applies them, Main.cpp:229-256). */
+typedef struct vrt_server vrt_server;
+
+typedef struct vrt_server_config {
+    uint32_t max_inflight;          /* concurrent launches (0 = 2) */
+    uint32_t max_batch_requests;    /* requests per launch at most (0 = 256) */
+    uint64_t hbm_budget_bytes;      /* output records in flight (0 = 1/4 of free HBM at creation) */
+    vrt_batch_config batch;         /* persistent launch configuration */
+} vrt_server_config;
+
+#define VRT_REQ_QUEUED 0u
+#define VRT_REQ_RUNNING 1u
+#define VRT_REQ_DONE 2u
+#define VRT_REQ_FAILED 3u
+
+typedef struct vrt_request_info {
+    uint32_t state;      /* VRT_REQ_* */
+    uint32_t kind;       /* 0 render, 1 edit */
+    vrt_status status;   /* result of a finished request */
+    uint32_t batch_size; /* requests in the launch that carried it */
+    uint64_t rays;       /* records written (renders) */
+    double submit_us, start_us, done_us; /* server clock, microseconds */
+} vrt_request_info;
+
+typedef struct vrt_server_stats {
+    uint64_t renders_done, edits_done, rejected, launches;
+    uint64_t records;
+    double p50_us, p99_us, p999_us, max_us; /* render latency, submit -> records in host memory */
+    double busy_seconds;                    /* wall time with at least one launch in flight */
+} vrt_server_stats;
+
+vrt_status vrt_server_create(vrt_world* const* worlds, uint32_t n_worlds, const vrt_server_config* cfg,
+                             vrt_server** out);
+/* Waits (bounded by timeout_ms) for queued work, then stops the scheduler. */
+vrt_status vrt_server_destroy(vrt_server* server, uint32_t timeout_ms);
+/* hits_host: vrt_view_records(view) records, owned by the caller until the request is done. */
+vrt_status vrt_server_submit_render(vrt_server* server, const vrt_view* view, vrt_hit* hits_host, uint64_t* ticket);
+vrt_status vrt_server_submit_edit(vrt_server* server, uint32_t world, const vrt_edit* edits, uint32_t n,
+                                  uint64_t* ticket);
+/* Bounded wait for one request: VRT_ERR_QUEUE_TIMEOUT when it is not done in time. */
+vrt_status vrt_server_wait(vrt_server* server, uint64_t ticket, uint32_t timeout_ms, vrt_request_info* info);
+/* Bounded wait until every submitted request is done. */
+vrt_status vrt_server_drain(vrt_server* server, uint32_t timeout_ms);
+/* Latency percentiles over renders finished since the last reset. */
+vrt_status vrt_server_get_stats(vrt_server* server, int reset, vrt_server_stats* out);
+
 #ifdef __cplusplus
 }
 #endif

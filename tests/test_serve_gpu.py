@@ -1,0 +1,160 @@
+"""Request server: continuous batching, edits between frames, HBM admission.
+
+The key property: a request's records are the same whether it runs alone or inside
+a mix of concurrent requests (bit-exact, t within 1e-6 relative), and they equal
+the oracle replaying the same request log.
+"""
+import threading
+
+import numpy as np
+import pytest
+
+import voxelrt_gb300 as v
+from oracle.oracle import OracleWorld
+from tests.helpers import assert_hits_equal
+
+pytestmark = pytest.mark.gpu
+
+
+def make_worlds(n=4, seed=0):
+    rng = np.random.default_rng(seed)
+    datas = [v.synth_mix(int(rng.choice([64, 96, 128])), seed=500 + i) for i in range(n)]
+    worlds = []
+    for d in datas:
+        w = v.World(d.sectors)
+        w.upload(d)
+        worlds.append(w)
+    return datas, worlds
+
+
+def random_view(rng, world, edge, res=None):
+    w, h = res or [(64, 64), (96, 54), (160, 90), (33, 17)][int(rng.integers(0, 4))]
+    cam = v.look_at(rng.uniform(0, edge, 3), rng.uniform(0, edge, 3) + 0.5, float(rng.uniform(50, 90)), w, h)
+    kind = int(rng.integers(0, 3))
+    if kind == 1:
+        return v.make_view(cam, world=world, shadow_dir=(0.3, 0.8, 0.5))
+    if kind == 2:
+        return v.make_view(cam, world=world, n_bounces=2)
+    return v.make_view(cam, world=world)
+
+
+def oracle_records(o: OracleWorld, view) -> np.ndarray:
+    if view.flags & v.VIEW_SHADOW:
+        return np.concatenate(o.render_view_shadow(view.cam, np.array(view.sun_dir[:], np.float32)))
+    if view.n_bounces:
+        return o.render_view_bounces(view.cam, view.n_bounces).reshape(-1)
+    return o.render_view(view.cam)
+
+
+@pytest.fixture(scope="module")
+def setup(gpu):
+    datas, worlds = make_worlds()
+    oracles = []
+    for d in datas:
+        o = OracleWorld(d.sectors)
+        o.upload(d)
+        oracles.append(o)
+    yield datas, worlds, oracles
+    for w in worlds:
+        w.close()
+
+
+def test_alone_equals_mix_equals_oracle(setup):
+    datas, worlds, oracles = setup
+    rng = np.random.default_rng(1)
+    srv = v.Server(worlds, max_inflight=3)
+    views = [random_view(rng, i % 4, datas[i % 4].sectors[0] * 32) for i in range(40)]
+    probe = views[7]
+    # alone
+    alone = v.PinnedHits(v.view_records(probe))
+    srv.wait(srv.submit_render(probe, alone.array))
+    # in a mix submitted from several threads at once
+    outs = [v.PinnedHits(v.view_records(vw)) for vw in views]
+    tickets = [None] * len(views)
+
+    def submit(idx):
+        for i in idx:
+            tickets[i] = srv.submit_render(views[i], outs[i].array)
+
+    ths = [threading.Thread(target=submit, args=(list(range(k, len(views), 4)),)) for k in range(4)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    infos = [srv.wait(t) for t in tickets]
+    assert max(i["batch_size"] for i in infos) > 1  # requests were batched together
+    assert np.array_equal(outs[7].array.view(np.uint8), alone.array.view(np.uint8))
+    for i, vw in enumerate(views):
+        assert_hits_equal(outs[i].array, oracle_records(oracles[vw.world], vw))
+    st = srv.stats()
+    assert st["renders_done"] == len(views) + 1 and st["p99_us"] >= st["p50_us"] > 0
+    srv.close()
+
+
+def test_edits_apply_between_frames_in_order(gpu):
+    datas, worlds = make_worlds(2, seed=3)
+    oracles = []
+    for d in datas:
+        o = OracleWorld(d.sectors)
+        o.upload(d)
+        oracles.append(o)
+    rng = np.random.default_rng(2)
+    srv = v.Server(worlds, max_inflight=2)
+    log = []  # replayed on the oracle in submission order
+    outs = []
+    for step in range(30):
+        if step % 5 == 4:
+            e = np.zeros(2, v.EDIT_DTYPE)
+            edge = datas[0].sectors[0] * 32
+            e["center"] = rng.integers(0, edge, (2, 3))
+            e["radius"] = rng.integers(4, 20, 2)
+            e["material"] = [0, int(rng.integers(1, 256))]
+            srv.submit_edit(0, e)
+            log.append(("edit", 0, e))
+        else:
+            vw = random_view(rng, int(rng.integers(0, 2)), datas[0].sectors[0] * 32)
+            out = v.PinnedHits(v.view_records(vw))
+            t = srv.submit_render(vw, out.array)
+            outs.append((t, out))
+            log.append(("render", vw, out))
+    srv.drain()
+    for entry in log:
+        if entry[0] == "edit":
+            oracles[entry[1]].edit(entry[2])
+        else:
+            vw, out = entry[1], entry[2]
+            assert_hits_equal(out.array, oracle_records(oracles[vw.world], vw))
+    assert srv.stats()["edits_done"] == 6
+    srv.close()
+    for w in worlds:
+        w.close()
+
+
+def test_admission_by_budget(setup):
+    datas, worlds, oracles = setup
+    rng = np.random.default_rng(4)
+    # budget of 4 pages (256 KiB): one 160x90 request needs 225 KiB
+    srv = v.Server(worlds, max_inflight=2, hbm_budget_bytes=4 * 65536)
+    views = [random_view(rng, 0, 64, res=(160, 90)) for _ in range(6)]
+    views = [v.make_view(vw.cam, world=0) for vw in views]
+    outs = [v.PinnedHits(v.view_records(vw)) for vw in views]
+    ts = [srv.submit_render(vw, o.array) for vw, o in zip(views, outs)]
+    infos = [srv.wait(t) for t in ts]
+    assert all(i["batch_size"] == 1 for i in infos)  # one fits at a time
+    for vw, o in zip(views, outs):
+        assert_hits_equal(o.array, oracle_records(oracles[0], vw))
+    big = v.make_view(v.look_at((1, 1, 1), (9, 9, 9), 60.0, 512, 512), world=0)
+    with pytest.raises(v.VrtError) as ei:
+        srv.submit_render(big, np.zeros(512 * 512, v.HIT_DTYPE))
+    assert ei.value.status == v.capi.VRT_ERR_OUT_OF_MEMORY
+    assert srv.stats()["rejected"] == 1
+    srv.close()
+
+
+def test_wait_timeout_and_unknown_ticket(setup):
+    _, worlds, _ = setup
+    srv = v.Server(worlds)
+    with pytest.raises(v.VrtError) as ei:
+        srv.wait(12345, timeout_ms=1)
+    assert ei.value.status == v.capi.VRT_ERR_NOT_FOUND
+    srv.close()

@@ -297,3 +297,83 @@ class Batch:
         a, b = int(self.offsets[v]), int(self.offsets[v + 1])
         cam = self.views[v].cam
         return hits[a:b].reshape(-1, cam.width * cam.height)
+
+
+class PinnedHits:
+    """Pinned host buffer of hit records (vrt_host_alloc), viewed as a numpy array."""
+
+    def __init__(self, n: int):
+        p = C.c_void_p()
+        check(lib().vrt_host_alloc(max(1, n) * HIT_DTYPE.itemsize, C.byref(p)))
+        self._p = p
+        buf = (C.c_uint8 * (max(1, n) * HIT_DTYPE.itemsize)).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=HIT_DTYPE)[:n]
+
+    def close(self):
+        if self._p:
+            self.array = None
+            lib().vrt_host_free(self._p)
+            self._p = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Request server with continuous batching over resident worlds (vrt_server)."""
+
+    def __init__(self, worlds, max_inflight: int = 2, max_batch_requests: int = 0, hbm_budget_bytes: int = 0,
+                 batch: BatchConfig | None = None):
+        self.worlds = list(worlds)
+        cfg = capi.ServerConfig(int(max_inflight), int(max_batch_requests), int(hbm_budget_bytes),
+                                batch if batch is not None else BatchConfig())
+        wh = (C.c_void_p * len(self.worlds))(*[w.handle.value for w in self.worlds])
+        h = C.c_void_p()
+        check(lib().vrt_server_create(wh, len(self.worlds), C.byref(cfg), C.byref(h)))
+        self._h = h
+        self._keep = {}
+
+    def close(self, timeout_ms: int = 60000):
+        if self._h:
+            st = lib().vrt_server_destroy(self._h, int(timeout_ms))
+            self._h = C.c_void_p()
+            self._keep.clear()
+            check(st)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit_render(self, view: View, out: np.ndarray) -> int:
+        """out: HIT_DTYPE array of view_records(view) entries (pinned for asynchronous copies)."""
+        assert out.dtype == HIT_DTYPE and out.size >= view_records(view) and out.flags.c_contiguous
+        t = C.c_uint64()
+        check(lib().vrt_server_submit_render(self._h, C.byref(view), ptr(out), C.byref(t)))
+        self._keep[t.value] = out
+        return t.value
+
+    def submit_edit(self, world: int, edits) -> int:
+        e = np.ascontiguousarray(edits, dtype=EDIT_DTYPE)
+        t = C.c_uint64()
+        check(lib().vrt_server_submit_edit(self._h, int(world), ptr(e), len(e), C.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = 60000) -> dict:
+        info = capi.RequestInfo()
+        st = lib().vrt_server_wait(self._h, int(ticket), int(timeout_ms), C.byref(info))
+        self._keep.pop(ticket, None)
+        check(st)
+        return {f: getattr(info, f) for f, _ in info._fields_}
+
+    def drain(self, timeout_ms: int = 60000) -> None:
+        check(lib().vrt_server_drain(self._h, int(timeout_ms)))
+
+    def stats(self, reset: bool = False) -> dict:
+        s = capi.ServerStats()
+        check(lib().vrt_server_get_stats(self._h, int(reset), C.byref(s)))
+        return {f: getattr(s, f) for f, _ in s._fields_}

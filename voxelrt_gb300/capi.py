@@ -73,6 +73,25 @@ class BatchStats(C.Structure):
 VIEW_SHADOW = 1
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("max_inflight", C.c_uint32), ("max_batch_requests", C.c_uint32), ("hbm_budget_bytes", C.c_uint64),
+                ("batch", BatchConfig)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("state", C.c_uint32), ("kind", C.c_uint32), ("status", C.c_int), ("batch_size", C.c_uint32),
+                ("rays", C.c_uint64), ("submit_us", C.c_double), ("start_us", C.c_double), ("done_us", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("renders_done", C.c_uint64), ("edits_done", C.c_uint64), ("rejected", C.c_uint64),
+                ("launches", C.c_uint64), ("records", C.c_uint64), ("p50_us", C.c_double), ("p99_us", C.c_double),
+                ("p999_us", C.c_double), ("max_us", C.c_double), ("busy_seconds", C.c_double)]
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+
+
 class WorldDesc(C.Structure):
     _fields_ = [("sectors_x", C.c_uint32), ("sectors_y", C.c_uint32), ("sectors_z", C.c_uint32),
                 ("brick_capacity", C.c_uint32), ("device", C.c_int32), ("flags", C.c_uint32)]
@@ -141,6 +160,15 @@ PROTOTYPES = {
     "vrt_batch_update_cameras": (_st, [_vp, C.POINTER(Camera), _vp]),
     "vrt_batch_get_stats": (_st, [_vp, C.POINTER(BatchStats)]),
     "vrt_batch_measure": (_st, [_vp, _vp, _vp, C.POINTER(BatchStats)]),
+    "vrt_host_alloc": (_st, [C.c_size_t, C.POINTER(_vp)]),
+    "vrt_host_free": (_st, [_vp]),
+    "vrt_server_create": (_st, [C.POINTER(_vp), _u32, C.POINTER(ServerConfig), C.POINTER(_vp)]),
+    "vrt_server_destroy": (_st, [_vp, _u32]),
+    "vrt_server_submit_render": (_st, [_vp, C.POINTER(View), _vp, C.POINTER(_u64)]),
+    "vrt_server_submit_edit": (_st, [_vp, _u32, _vp, _u32, C.POINTER(_u64)]),
+    "vrt_server_wait": (_st, [_vp, _u64, _u32, C.POINTER(RequestInfo)]),
+    "vrt_server_drain": (_st, [_vp, _u32]),
+    "vrt_server_get_stats": (_st, [_vp, C.c_int, C.POINTER(ServerStats)]),
     "vrt_synth_terrain_world": (_st, [C.POINTER(SynthTerrain), C.c_int, C.POINTER(C.POINTER(SectorStream))]),
     "vrt_synth_terrain_height": (C.c_double, [C.POINTER(SynthTerrain), C.c_double, C.c_double]),
     "vrt_synth_mix_world": (_st, [_u32, _u64, C.c_int, C.POINTER(C.POINTER(SectorStream))]),

@@ -15,43 +15,12 @@
 #include <cstring>
 #include <vector>
 
+#include "batch_internal.h"
 #include "trace_core.cuh"
 #include "world.h"
 
 namespace vrt {
 namespace {
-
-struct ViewDev {
-    vrt_camera cam;
-    uint32_t world;
-    uint32_t max_iters;
-    uint32_t n_bounces;
-    uint32_t shadow;
-    float sun[3];
-    uint32_t tiles_x;
-    uint32_t n_rays;      // tile-padded ray space of the view
-    uint32_t chunk_base;  // first queue chunk of the view
-    uint64_t out_base;    // first record of the view
-};
-
-static_assert(sizeof(ViewDev) == 120, "view table entry is 120 bytes (copied per camera update)");
-
-struct BatchParams {
-    const DevWorld* worlds;
-    const ViewDev* views;
-    const uint32_t* chunk_base;  // n_views + 1 entries
-    uint32_t n_views;
-    uint32_t total_chunks;
-    uint32_t* queue;
-    unsigned long long* counters;  // rays, step calls, occ fetches, hits
-    uint4* out;
-    uint32_t tile_w_log2, tile_size_log2, morton;
-    uint32_t chunk_rays;
-    uint32_t refill;
-    uint32_t inner;
-};
-
-uint32_t eff_iters(uint32_t m) { return m == 0 ? VRT_DEFAULT_MAX_ITERS : (m > 65535u ? 65535u : m); }
 
 __device__ __forceinline__ uint32_t compact_even_bits(uint32_t k) {
     k &= 0x55u;
@@ -239,21 +208,6 @@ uint32_t log2u(uint32_t v) {
     return r;
 }
 
-vrt_status check_view(const vrt_view* v) {
-    if (!v || v->cam.width == 0 || v->cam.height == 0 || v->cam.width > 16384 || v->cam.height > 16384 ||
-        v->n_bounces > VRT_MAX_BOUNCES || (v->flags & ~VRT_VIEW_SHADOW) ||
-        ((v->flags & VRT_VIEW_SHADOW) && v->n_bounces)) {
-        set_error("bad view: camera 1..16384 px, n_bounces <= 15, shadow and bounces exclusive");
-        return VRT_ERR_INVALID_ARG;
-    }
-    return VRT_OK;
-}
-
-uint64_t view_records(const vrt_view& v) {
-    const uint64_t kinds = 1 + ((v.flags & VRT_VIEW_SHADOW) ? 1 : v.n_bounces);
-    return kinds * v.cam.width * v.cam.height;
-}
-
 ViewDev make_view_dev(const vrt_view& v) {
     ViewDev d{};
     d.cam = v.cam;
@@ -273,6 +227,128 @@ vrt_status launch_view_path(vrt_world* w, const ViewDev& v, vrt_hit* hits, cudaS
 }
 
 }  // namespace
+
+uint32_t eff_iters(uint32_t m) { return m == 0 ? VRT_DEFAULT_MAX_ITERS : (m > 65535u ? 65535u : m); }
+
+vrt_status check_view(const vrt_view* v) {
+    if (!v || v->cam.width == 0 || v->cam.height == 0 || v->cam.width > 16384 || v->cam.height > 16384 ||
+        v->n_bounces > VRT_MAX_BOUNCES || (v->flags & ~VRT_VIEW_SHADOW) ||
+        ((v->flags & VRT_VIEW_SHADOW) && v->n_bounces)) {
+        set_error("bad view: camera 1..16384 px, n_bounces <= 15, shadow and bounces exclusive");
+        return VRT_ERR_INVALID_ARG;
+    }
+    return VRT_OK;
+}
+
+uint64_t view_record_count(const vrt_view& v) {
+    const uint64_t kinds = 1 + ((v.flags & VRT_VIEW_SHADOW) ? 1 : v.n_bounces);
+    return kinds * v.cam.width * v.cam.height;
+}
+
+vrt_status normalize_batch_config(const vrt_batch_config* in, vrt_batch_config& cfg) {
+    cfg = in ? *in : vrt_batch_config{};
+    if (cfg.tile_w == 0 && cfg.tile_h == 0) cfg.tile_w = 8, cfg.tile_h = 8;
+    const bool shape_ok = (cfg.tile_w == 8 && cfg.tile_h == 8) || (cfg.tile_w == 16 && cfg.tile_h == 4) ||
+                          (cfg.tile_w == 32 && cfg.tile_h == 1);
+    if (!shape_ok || (cfg.morton && cfg.tile_w != 8)) {
+        set_error("tile must be 8x8 (optionally Morton), 16x4 or 32x1");
+        return VRT_ERR_INVALID_ARG;
+    }
+    if (cfg.warps_per_block == 0) cfg.warps_per_block = 4;
+    if (cfg.refill_threshold == 0) cfg.refill_threshold = 16;
+    if (cfg.chunk_tiles == 0) cfg.chunk_tiles = 2;
+    if (cfg.inner_iters == 0) cfg.inner_iters = 4;
+    if (cfg.warps_per_block > 16 || cfg.refill_threshold > 32 || cfg.chunk_tiles > 64 || cfg.inner_iters > 1024) {
+        set_error("batch config out of range");
+        return VRT_ERR_INVALID_ARG;
+    }
+    return VRT_OK;
+}
+
+vrt_status plan_views(const vrt_view* views, uint32_t n, uint32_t n_worlds, const vrt_batch_config& cfg,
+                      LaunchPlan& plan) {
+    vrt_status st;
+    for (uint32_t i = 0; i < n; i++) {
+        if ((st = check_view(&views[i])) != VRT_OK) return st;
+        if (views[i].world >= n_worlds) {
+            set_error("view references a world outside the list");
+            return VRT_ERR_INVALID_ARG;
+        }
+    }
+    plan.cfg = cfg;
+    plan.tile_w_log2 = log2u(cfg.tile_w);
+    plan.tile_size_log2 = log2u(cfg.tile_w * cfg.tile_h);
+    plan.views.resize(n);
+    plan.chunk_base.resize(n + 1);
+    uint64_t chunks = 0, records = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        ViewDev d = make_view_dev(views[i]);
+        const uint32_t tx = (d.cam.width + cfg.tile_w - 1) / cfg.tile_w;
+        const uint32_t ty = (d.cam.height + cfg.tile_h - 1) / cfg.tile_h;
+        const uint64_t tiles = (uint64_t)tx * ty;
+        d.tiles_x = tx;
+        d.n_rays = (uint32_t)(tiles << plan.tile_size_log2);
+        d.chunk_base = (uint32_t)chunks;
+        d.out_base = records;
+        plan.chunk_base[i] = (uint32_t)chunks;
+        chunks += (tiles + cfg.chunk_tiles - 1) / cfg.chunk_tiles;
+        records += view_record_count(views[i]);
+        plan.views[i] = d;
+        if (chunks >= 0xffffffffull) {
+            set_error("batch too large");
+            return VRT_ERR_INVALID_ARG;
+        }
+    }
+    plan.chunk_base[n] = (uint32_t)chunks;
+    plan.chunks = (uint32_t)chunks;
+    plan.records = records;
+    return VRT_OK;
+}
+
+vrt_status persistent_grid(int device, const vrt_batch_config& cfg, bool count, int& blocks, int& threads) {
+    int sms = 0, occ = 0;
+    threads = (int)cfg.warps_per_block * 32;
+    VRT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    if (count)
+        VRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<true>, threads, 0));
+    else
+        VRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<false>, threads, 0));
+    occ = std::max(occ, 1);
+    const int per_sm = (!count && cfg.blocks_per_sm) ? std::min<int>((int)cfg.blocks_per_sm, occ) : occ;
+    blocks = sms * per_sm;
+    return VRT_OK;
+}
+
+BatchParams make_params(const LaunchPlan& plan, const DevWorld* worlds, const ViewDev* views,
+                        const uint32_t* chunk_base, uint32_t* queue, vrt_hit* out) {
+    BatchParams p{};
+    p.worlds = worlds;
+    p.views = views;
+    p.chunk_base = chunk_base;
+    p.n_views = (uint32_t)plan.views.size();
+    p.total_chunks = plan.chunks;
+    p.queue = queue;
+    p.counters = reinterpret_cast<unsigned long long*>(reinterpret_cast<uint8_t*>(queue) + 16);
+    p.out = reinterpret_cast<uint4*>(out);
+    p.tile_w_log2 = plan.tile_w_log2;
+    p.tile_size_log2 = plan.tile_size_log2;
+    p.morton = plan.cfg.morton;
+    p.chunk_rays = plan.cfg.chunk_tiles << plan.tile_size_log2;
+    p.refill = plan.cfg.refill_threshold;
+    p.inner = plan.cfg.inner_iters;
+    return p;
+}
+
+vrt_status launch_persistent(const BatchParams& p, int blocks, int threads, bool count, cudaStream_t stream) {
+    VRT_CUDA(cudaMemsetAsync(p.queue, 0, 64, stream));
+    if (count)
+        persistent_kernel<true><<<blocks, threads, 0, stream>>>(p);
+    else
+        persistent_kernel<false><<<blocks, threads, 0, stream>>>(p);
+    VRT_CUDA(cudaGetLastError());
+    return VRT_OK;
+}
+
 }  // namespace vrt
 
 using namespace vrt;
@@ -281,14 +357,9 @@ struct vrt_batch {
     int device = 0;
     std::vector<vrt_world*> worlds;
     std::vector<vrt_view> views;
-    std::vector<ViewDev> vdev;
-    std::vector<uint32_t> chunk_base;
+    LaunchPlan plan;
     std::vector<DevWorld> wtab;  // last uploaded world table
-    uint64_t total_records = 0;
-    uint32_t total_chunks = 0;
-    vrt_batch_config cfg{};
-    uint32_t tile_w_log2 = 3, tile_size_log2 = 6;
-    int blocks = 0, threads = 0, blocks_count = 0;
+    int blocks = 0, threads = 0, blocks_count = 0, threads_count = 0;
     // device
     DevWorld* d_worlds = nullptr;
     ViewDev* d_views = nullptr;
@@ -315,41 +386,17 @@ vrt_status refresh_worlds(vrt_batch* b, cudaStream_t stream) {
     return VRT_OK;
 }
 
-BatchParams batch_params(vrt_batch* b, vrt_hit* hits) {
-    BatchParams p{};
-    p.worlds = b->d_worlds;
-    p.views = b->d_views;
-    p.chunk_base = b->d_chunk_base;
-    p.n_views = (uint32_t)b->views.size();
-    p.total_chunks = b->total_chunks;
-    p.queue = b->d_queue;
-    p.counters = b->d_counters;
-    p.out = reinterpret_cast<uint4*>(hits);
-    p.tile_w_log2 = b->tile_w_log2;
-    p.tile_size_log2 = b->tile_size_log2;
-    p.morton = b->cfg.morton;
-    p.chunk_rays = b->cfg.chunk_tiles << b->tile_size_log2;
-    p.refill = b->cfg.refill_threshold;
-    p.inner = b->cfg.inner_iters;
-    return p;
-}
-
 vrt_status enqueue_batch(vrt_batch* b, vrt_hit* hits, cudaStream_t stream, bool count) {
-    VRT_CUDA(cudaMemsetAsync(b->d_queue, 0, 64, stream));
-    BatchParams p = batch_params(b, hits);
-    if (count)
-        persistent_kernel<true><<<b->blocks_count, b->threads, 0, stream>>>(p);
-    else
-        persistent_kernel<false><<<b->blocks, b->threads, 0, stream>>>(p);
-    VRT_CUDA(cudaGetLastError());
-    return VRT_OK;
+    BatchParams p = make_params(b->plan, b->d_worlds, b->d_views, b->d_chunk_base, b->d_queue, hits);
+    return count ? launch_persistent(p, b->blocks_count, b->threads_count, true, stream)
+                 : launch_persistent(p, b->blocks, b->threads, false, stream);
 }
 
 }  // namespace
 
 extern "C" {
 
-uint64_t vrt_view_records(const vrt_view* v) { return check_view(v) == VRT_OK ? view_records(*v) : 0; }
+uint64_t vrt_view_records(const vrt_view* v) { return check_view(v) == VRT_OK ? view_record_count(*v) : 0; }
 
 vrt_status vrt_render_path_device(vrt_world* w, const vrt_view* view, vrt_hit* hits, void* stream) {
     vrt_status st = world_enter(w);
@@ -372,7 +419,7 @@ vrt_status vrt_render_path(vrt_world* w, const vrt_view* view, vrt_hit* hits, vo
     }
     std::lock_guard<std::mutex> lock(w->mu);
     cudaStream_t stream = (cudaStream_t)stream_;
-    const size_t hb = view_records(*view) * sizeof(vrt_hit);
+    const size_t hb = view_record_count(*view) * sizeof(vrt_hit);
     VRT_CUDA(w->d_io.reserve(hb));
     ViewDev d = make_view_dev(*view);
     if ((st = launch_view_path(w, d, (vrt_hit*)w->d_io.ptr, stream)) != VRT_OK) return st;
@@ -388,67 +435,22 @@ vrt_status vrt_batch_create(vrt_world* const* worlds, uint32_t n_worlds, const v
         return VRT_ERR_INVALID_ARG;
     }
     *out = nullptr;
-    vrt_batch_config cfg = cfg_in ? *cfg_in : vrt_batch_config{};
-    if (cfg.tile_w == 0 && cfg.tile_h == 0) cfg.tile_w = 8, cfg.tile_h = 8;
-    const bool shape_ok = (cfg.tile_w == 8 && cfg.tile_h == 8) || (cfg.tile_w == 16 && cfg.tile_h == 4) ||
-                          (cfg.tile_w == 32 && cfg.tile_h == 1);
-    if (!shape_ok || (cfg.morton && cfg.tile_w != 8)) {
-        set_error("tile must be 8x8 (optionally Morton), 16x4 or 32x1");
-        return VRT_ERR_INVALID_ARG;
-    }
-    if (cfg.warps_per_block == 0) cfg.warps_per_block = 4;
-    if (cfg.refill_threshold == 0) cfg.refill_threshold = 16;
-    if (cfg.chunk_tiles == 0) cfg.chunk_tiles = 2;
-    if (cfg.inner_iters == 0) cfg.inner_iters = 4;
-    if (cfg.warps_per_block > 16 || cfg.refill_threshold > 32 || cfg.chunk_tiles > 64 || cfg.inner_iters > 1024) {
-        set_error("batch config out of range");
-        return VRT_ERR_INVALID_ARG;
-    }
+    vrt_batch_config cfg;
+    vrt_status st = normalize_batch_config(cfg_in, cfg);
+    if (st != VRT_OK) return st;
     for (uint32_t i = 0; i < n_worlds; i++)
         if (!worlds[i] || worlds[i]->device != worlds[0]->device) {
             set_error("worlds must be non-null and on one device");
             return VRT_ERR_INVALID_ARG;
         }
-    vrt_status st;
-    for (uint32_t i = 0; i < n_views; i++) {
-        if ((st = check_view(&views[i])) != VRT_OK) return st;
-        if (views[i].world >= n_worlds) {
-            set_error("view references a world outside the list");
-            return VRT_ERR_INVALID_ARG;
-        }
-    }
     auto* b = new vrt_batch;
+    if ((st = plan_views(views, n_views, n_worlds, cfg, b->plan)) != VRT_OK) {
+        delete b;
+        return st;
+    }
     b->device = worlds[0]->device;
     b->worlds.assign(worlds, worlds + n_worlds);
     b->views.assign(views, views + n_views);
-    b->cfg = cfg;
-    b->tile_w_log2 = log2u(cfg.tile_w);
-    b->tile_size_log2 = log2u(cfg.tile_w * cfg.tile_h);
-    const uint32_t th = cfg.tile_h;
-    uint64_t chunks = 0, records = 0;
-    b->vdev.resize(n_views);
-    b->chunk_base.resize(n_views + 1);
-    for (uint32_t i = 0; i < n_views; i++) {
-        ViewDev d = make_view_dev(views[i]);
-        const uint32_t tx = (d.cam.width + cfg.tile_w - 1) / cfg.tile_w, ty = (d.cam.height + th - 1) / th;
-        const uint64_t tiles = (uint64_t)tx * ty;
-        d.tiles_x = tx;
-        d.n_rays = (uint32_t)(tiles << b->tile_size_log2);
-        d.chunk_base = (uint32_t)chunks;
-        d.out_base = records;
-        b->chunk_base[i] = (uint32_t)chunks;
-        chunks += (tiles + cfg.chunk_tiles - 1) / cfg.chunk_tiles;
-        records += view_records(views[i]);
-        b->vdev[i] = d;
-    }
-    if (chunks >= 0xffffffffull) {
-        delete b;
-        set_error("batch too large");
-        return VRT_ERR_INVALID_ARG;
-    }
-    b->chunk_base[n_views] = (uint32_t)chunks;
-    b->total_chunks = (uint32_t)chunks;
-    b->total_records = records;
     auto fail = [&](vrt_status s) {
         vrt_batch_destroy(b);
         return s;
@@ -458,23 +460,16 @@ vrt_status vrt_batch_create(vrt_world* const* worlds, uint32_t n_worlds, const v
     if (e == cudaSuccess) e = cudaMalloc(&b->d_views, sizeof(ViewDev) * n_views);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_chunk_base, sizeof(uint32_t) * (n_views + 1));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_queue, 64);
-    if (e == cudaSuccess) e = cudaMemcpy(b->d_views, b->vdev.data(), sizeof(ViewDev) * n_views, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
-        e = cudaMemcpy(b->d_chunk_base, b->chunk_base.data(), sizeof(uint32_t) * (n_views + 1), cudaMemcpyHostToDevice);
+        e = cudaMemcpy(b->d_views, b->plan.views.data(), sizeof(ViewDev) * n_views, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_chunk_base, b->plan.chunk_base.data(), sizeof(uint32_t) * (n_views + 1),
+                       cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return fail(cuda_fail(e, "batch allocation"));
     b->d_counters = reinterpret_cast<unsigned long long*>(reinterpret_cast<uint8_t*>(b->d_queue) + 16);
     if ((st = refresh_worlds(b, 0)) != VRT_OK) return fail(st);
-    // grid: every SM, as many blocks as fit (or as configured)
-    int dev_sms = 0, occ = 0, occ_c = 0;
-    b->threads = (int)cfg.warps_per_block * 32;
-    e = cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, b->device);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<false>, b->threads, 0);
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, persistent_kernel<true>, b->threads, 0);
-    if (e != cudaSuccess) return fail(cuda_fail(e, "occupancy query"));
-    const int per_sm = cfg.blocks_per_sm ? std::min<int>((int)cfg.blocks_per_sm, std::max(occ, 1)) : std::max(occ, 1);
-    b->blocks = dev_sms * per_sm;
-    b->blocks_count = dev_sms * std::max(occ_c, 1);
+    if ((st = persistent_grid(b->device, cfg, false, b->blocks, b->threads)) != VRT_OK) return fail(st);
+    if ((st = persistent_grid(b->device, cfg, true, b->blocks_count, b->threads_count)) != VRT_OK) return fail(st);
     *out = b;
     return VRT_OK;
 }
@@ -498,8 +493,8 @@ vrt_status vrt_batch_output_layout(const vrt_batch* b, uint64_t* offsets) {
         set_error("null argument");
         return VRT_ERR_INVALID_ARG;
     }
-    for (size_t i = 0; i < b->vdev.size(); i++) offsets[i] = b->vdev[i].out_base;
-    offsets[b->vdev.size()] = b->total_records;
+    for (size_t i = 0; i < b->plan.views.size(); i++) offsets[i] = b->plan.views[i].out_base;
+    offsets[b->plan.views.size()] = b->plan.records;
     return VRT_OK;
 }
 
@@ -508,18 +503,18 @@ vrt_status vrt_batch_update_cameras(vrt_batch* b, const vrt_camera* cams, void* 
         set_error("null argument");
         return VRT_ERR_INVALID_ARG;
     }
-    for (size_t i = 0; i < b->vdev.size(); i++)
-        if (cams[i].width != b->vdev[i].cam.width || cams[i].height != b->vdev[i].cam.height) {
+    for (size_t i = 0; i < b->plan.views.size(); i++)
+        if (cams[i].width != b->plan.views[i].cam.width || cams[i].height != b->plan.views[i].cam.height) {
             set_error("camera resolution differs from the batch's view");
             return VRT_ERR_INVALID_ARG;
         }
     VRT_CUDA(cudaSetDevice(b->device));
-    for (size_t i = 0; i < b->vdev.size(); i++) {
-        b->vdev[i].cam = cams[i];
+    for (size_t i = 0; i < b->plan.views.size(); i++) {
+        b->plan.views[i].cam = cams[i];
         b->views[i].cam = cams[i];
     }
     cudaStream_t stream = (cudaStream_t)stream_;
-    VRT_CUDA(cudaMemcpyAsync(b->d_views, b->vdev.data(), sizeof(ViewDev) * b->vdev.size(), cudaMemcpyHostToDevice,
+    VRT_CUDA(cudaMemcpyAsync(b->d_views, b->plan.views.data(), sizeof(ViewDev) * b->plan.views.size(), cudaMemcpyHostToDevice,
                              stream));
     VRT_CUDA(cudaStreamSynchronize(stream));
     return VRT_OK;
@@ -579,8 +574,8 @@ vrt_status vrt_batch_launch_per_view(vrt_batch* b, vrt_hit* hits, void* stream_)
     }
     VRT_CUDA(cudaSetDevice(b->device));
     cudaStream_t stream = (cudaStream_t)stream_;
-    for (size_t i = 0; i < b->vdev.size(); i++) {
-        vrt_status st = launch_view_path(b->worlds[b->vdev[i].world], b->vdev[i], hits, stream);
+    for (size_t i = 0; i < b->plan.views.size(); i++) {
+        vrt_status st = launch_view_path(b->worlds[b->plan.views[i].world], b->plan.views[i], hits, stream);
         if (st != VRT_OK) return st;
     }
     b->last_stream = stream;
@@ -594,10 +589,10 @@ vrt_status vrt_batch_run(vrt_batch* b, vrt_hit* hits_host, void* stream_) {
     }
     VRT_CUDA(cudaSetDevice(b->device));
     cudaStream_t stream = (cudaStream_t)stream_;
-    VRT_CUDA(b->d_out.reserve(b->total_records * sizeof(vrt_hit)));
+    VRT_CUDA(b->d_out.reserve(b->plan.records * sizeof(vrt_hit)));
     vrt_status st = vrt_batch_launch_graph(b, (vrt_hit*)b->d_out.ptr, stream);
     if (st != VRT_OK) return st;
-    VRT_CUDA(cudaMemcpyAsync(hits_host, b->d_out.ptr, b->total_records * sizeof(vrt_hit), cudaMemcpyDeviceToHost,
+    VRT_CUDA(cudaMemcpyAsync(hits_host, b->d_out.ptr, b->plan.records * sizeof(vrt_hit), cudaMemcpyDeviceToHost,
                              stream));
     VRT_CUDA(cudaStreamSynchronize(stream));
     return VRT_OK;

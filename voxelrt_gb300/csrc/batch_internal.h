@@ -1,0 +1,68 @@
+// batch_internal.h - launch planning shared by vrt_batch and the request server.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "vrt_internal.h"
+
+namespace vrt {
+
+// Device view-table entry of the persistent kernel.
+struct ViewDev {
+    vrt_camera cam;
+    uint32_t world;
+    uint32_t max_iters;
+    uint32_t n_bounces;
+    uint32_t shadow;
+    float sun[3];
+    uint32_t tiles_x;
+    uint32_t n_rays;      // tile-padded ray space of the view
+    uint32_t chunk_base;  // first queue chunk of the view
+    uint64_t out_base;    // first record of the view
+};
+static_assert(sizeof(ViewDev) == 120, "view table entry is 120 bytes (copied per camera update)");
+
+struct BatchParams {
+    const DevWorld* worlds;
+    const ViewDev* views;
+    const uint32_t* chunk_base;  // n_views + 1 entries
+    uint32_t n_views;
+    uint32_t total_chunks;
+    uint32_t* queue;
+    unsigned long long* counters;  // rays, step calls, occ fetches, hits
+    uint4* out;
+    uint32_t tile_w_log2, tile_size_log2, morton;
+    uint32_t chunk_rays;
+    uint32_t refill;
+    uint32_t inner;
+};
+
+// Views laid out behind one tile queue.
+struct LaunchPlan {
+    vrt_batch_config cfg{};
+    uint32_t tile_w_log2 = 3, tile_size_log2 = 6;
+    std::vector<ViewDev> views;
+    std::vector<uint32_t> chunk_base;  // n_views + 1
+    uint64_t records = 0;
+    uint32_t chunks = 0;
+};
+
+uint32_t eff_iters(uint32_t max_iters);
+uint64_t view_record_count(const vrt_view& v);
+vrt_status check_view(const vrt_view* v);
+// Fill defaults and validate a batch config.
+vrt_status normalize_batch_config(const vrt_batch_config* in, vrt_batch_config& out);
+// Validate views against n_worlds and lay them out (tiles, queue chunks, record offsets).
+vrt_status plan_views(const vrt_view* views, uint32_t n, uint32_t n_worlds, const vrt_batch_config& cfg,
+                      LaunchPlan& plan);
+// Grid of the persistent kernel: every SM, as many blocks as fit (or cfg.blocks_per_sm).
+vrt_status persistent_grid(int device, const vrt_batch_config& cfg, bool count, int& blocks, int& threads);
+BatchParams make_params(const LaunchPlan& plan, const DevWorld* worlds, const ViewDev* views,
+                        const uint32_t* chunk_base, uint32_t* queue, vrt_hit* out);
+// Queue reset (64 bytes at params.queue) + persistent kernel launch.
+vrt_status launch_persistent(const BatchParams& p, int blocks, int threads, bool count, cudaStream_t stream);
+
+}  // namespace vrt

@@ -1,0 +1,545 @@
+// serve.cu - request server: continuous batching of render requests over
+// resident worlds, edits between frames, admission by an HBM budget, latency stats.
+//
+// The reference renders one view per frame on the main thread and applies brush
+// edits between frames (Main.cpp:83-130, 229-256).  Here many clients submit
+// requests concurrently; a scheduler thread packs queued renders into persistent
+// launches (vrt_batch's kernel) on up to max_inflight streams, so requests that
+// arrive while others run start as soon as a slot and budget free up and their
+// work overlaps on the device.  Completion is signalled by a host callback queued
+// after each launch's copies, so no thread polls the device.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "batch_internal.h"
+#include "freelist.h"
+#include "world.h"
+
+namespace vrt {
+namespace {
+
+constexpr uint64_t kPageBytes = 64 * 1024;  // output-arena allocation unit
+constexpr uint64_t kPageRecords = kPageBytes / sizeof(vrt_hit);
+
+struct Request {
+    uint64_t id = 0;
+    uint32_t kind = 0;  // 0 render, 1 edit
+    uint32_t state = VRT_REQ_QUEUED;
+    vrt_status status = VRT_OK;
+    vrt_view view{};
+    vrt_hit* host_out = nullptr;
+    uint64_t records = 0;
+    uint32_t pages = 0, page_base = 0;  // output arena allocation (1-based, 0 = none)
+    uint32_t world = 0;
+    std::vector<vrt_edit> edits;
+    uint32_t batch_size = 0;
+    double submit_us = 0, start_us = 0, done_us = 0;
+};
+
+struct Slot {
+    cudaStream_t stream = nullptr;
+    DevBuf views, chunk_base, queue;
+    ViewDev* h_views = nullptr;  // pinned staging
+    uint32_t* h_cb = nullptr;
+    size_t staged_cap = 0;
+    std::vector<Request*> reqs;
+    bool busy = false;
+    std::atomic<bool> complete{false};
+    struct vrt_server* server = nullptr;
+};
+
+double now_us(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace
+}  // namespace vrt
+
+using namespace vrt;
+
+struct vrt_server {
+    int device = 0;
+    std::vector<vrt_world*> worlds;
+    vrt_server_config cfg{};
+    vrt_batch_config bcfg{};
+    int blocks = 0, threads = 0;
+    DevWorld* d_worlds = nullptr;
+    uint8_t* arena = nullptr;  // output records of admitted requests
+    FreeList pages;
+    cudaStream_t edit_stream = nullptr;
+    std::vector<std::unique_ptr<Slot>> slots;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+
+    std::mutex mu;  // queue, requests, stats
+    std::condition_variable done_cv;
+    std::deque<Request*> queue;
+    std::unordered_map<uint64_t, std::unique_ptr<Request>> reqs;
+    uint64_t next_id = 1;
+    uint64_t outstanding = 0;
+    bool stop = false;
+    std::thread worker;
+
+    std::mutex sig_mu;  // worker wake-ups (submissions, completions)
+    std::condition_variable sig_cv;
+    uint64_t signals = 0;
+
+    // stats
+    std::vector<double> lat;
+    uint64_t renders_done = 0, edits_done = 0, rejected = 0, launches = 0, records_done = 0;
+    double busy_since = -1, busy_total = 0;
+    int busy_slots = 0;
+
+    void signal() {
+        {
+            std::lock_guard<std::mutex> g(sig_mu);
+            signals++;
+        }
+        sig_cv.notify_one();
+    }
+};
+
+namespace {
+
+void CUDART_CB slot_done_cb(void* p) {
+    auto* s = static_cast<Slot*>(p);
+    s->complete.store(true);
+    s->server->signal();
+}
+
+vrt_status refresh_world_table(vrt_server* sv) {
+    std::vector<DevWorld> t(sv->worlds.size());
+    for (size_t i = 0; i < t.size(); i++) t[i] = sv->worlds[i]->dev();
+    VRT_CUDA(cudaMemcpy(sv->d_worlds, t.data(), t.size() * sizeof(DevWorld), cudaMemcpyHostToDevice));
+    return VRT_OK;
+}
+
+void finish(vrt_server* sv, Request* r, vrt_status st, double t) {
+    r->status = st;
+    r->state = st == VRT_OK ? VRT_REQ_DONE : VRT_REQ_FAILED;
+    r->done_us = t;
+    if (r->pages) {
+        sv->pages.free(r->page_base, r->pages);
+        r->pages = 0;
+    }
+    if (r->kind == 0) {
+        if (st == VRT_OK) {
+            sv->lat.push_back(r->done_us - r->submit_us);
+            sv->renders_done++;
+            sv->records_done += r->records;
+        }
+    } else {
+        sv->edits_done++;
+    }
+    sv->outstanding--;
+}
+
+// Launch the render requests `rs` on slot `s` (called with sv->mu held).
+vrt_status launch_slot(vrt_server* sv, Slot& s, std::vector<Request*>& rs) {
+    std::vector<vrt_view> views(rs.size());
+    for (size_t i = 0; i < rs.size(); i++) views[i] = rs[i]->view;
+    LaunchPlan plan;
+    vrt_status st = plan_views(views.data(), (uint32_t)views.size(), (uint32_t)sv->worlds.size(), sv->bcfg, plan);
+    if (st != VRT_OK) return st;
+    // each request writes into its own arena pages
+    for (size_t i = 0; i < rs.size(); i++) plan.views[i].out_base = (uint64_t)(rs[i]->page_base - 1) * kPageRecords;
+    const size_t nv = plan.views.size();
+    if (s.staged_cap < nv) {
+        if (s.h_views) cudaFreeHost(s.h_views);
+        if (s.h_cb) cudaFreeHost(s.h_cb);
+        s.h_views = nullptr;
+        s.h_cb = nullptr;
+        const size_t cap = std::max<size_t>(nv, 64);
+        VRT_CUDA(cudaHostAlloc(&s.h_views, cap * sizeof(ViewDev), cudaHostAllocDefault));
+        VRT_CUDA(cudaHostAlloc(&s.h_cb, (cap + 1) * sizeof(uint32_t), cudaHostAllocDefault));
+        s.staged_cap = cap;
+    }
+    std::memcpy(s.h_views, plan.views.data(), nv * sizeof(ViewDev));
+    std::memcpy(s.h_cb, plan.chunk_base.data(), (nv + 1) * sizeof(uint32_t));
+    VRT_CUDA(s.views.reserve(nv * sizeof(ViewDev)));
+    VRT_CUDA(s.chunk_base.reserve((nv + 1) * sizeof(uint32_t)));
+    VRT_CUDA(cudaMemcpyAsync(s.views.ptr, s.h_views, nv * sizeof(ViewDev), cudaMemcpyHostToDevice, s.stream));
+    VRT_CUDA(cudaMemcpyAsync(s.chunk_base.ptr, s.h_cb, (nv + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                             s.stream));
+    BatchParams p = make_params(plan, sv->d_worlds, (const ViewDev*)s.views.ptr, (const uint32_t*)s.chunk_base.ptr,
+                                (uint32_t*)s.queue.ptr, (vrt_hit*)sv->arena);
+    if ((st = launch_persistent(p, sv->blocks, sv->threads, false, s.stream)) != VRT_OK) return st;
+    for (size_t i = 0; i < rs.size(); i++) {
+        const Request* r = rs[i];
+        VRT_CUDA(cudaMemcpyAsync(r->host_out, sv->arena + plan.views[i].out_base * sizeof(vrt_hit),
+                                 r->records * sizeof(vrt_hit), cudaMemcpyDeviceToHost, s.stream));
+    }
+    s.complete.store(false);
+    VRT_CUDA(cudaLaunchHostFunc(s.stream, slot_done_cb, &s));
+    return VRT_OK;
+}
+
+void worker_main(vrt_server* sv) {
+    cudaSetDevice(sv->device);
+    uint64_t seen = 0;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    for (;;) {
+        bool progressed = false;
+        const double t = now_us(sv->t0);
+        // retire finished launches
+        for (auto& sp : sv->slots) {
+            Slot& s = *sp;
+            if (!s.busy || !s.complete.load()) continue;
+            cudaError_t e = cudaStreamQuery(s.stream);
+            const vrt_status st = e == cudaSuccess ? VRT_OK : cuda_fail(e, "server launch");
+            for (Request* r : s.reqs) finish(sv, r, st, t);
+            s.reqs.clear();
+            s.busy = false;
+            if (--sv->busy_slots == 0 && sv->busy_since >= 0) {
+                sv->busy_total += t - sv->busy_since;
+                sv->busy_since = -1;
+            }
+            progressed = true;
+        }
+        if (progressed) sv->done_cv.notify_all();
+        if (sv->stop && sv->queue.empty() && sv->busy_slots == 0) break;
+        // an edit runs once nothing is in flight (between frames)
+        if (!sv->queue.empty() && sv->queue.front()->kind == 1) {
+            if (sv->busy_slots == 0) {
+                Request* r = sv->queue.front();
+                sv->queue.pop_front();
+                r->state = VRT_REQ_RUNNING;
+                r->start_us = now_us(sv->t0);
+                lk.unlock();
+                vrt_status st = vrt_world_edit(sv->worlds[r->world], r->edits.data(), (uint32_t)r->edits.size(),
+                                               sv->edit_stream);
+                if (st == VRT_OK) st = refresh_world_table(sv);
+                lk.lock();
+                finish(sv, r, st, now_us(sv->t0));
+                sv->done_cv.notify_all();
+                continue;
+            }
+        } else if (!sv->queue.empty()) {
+            Slot* free_slot = nullptr;
+            for (auto& sp : sv->slots)
+                if (!sp->busy) {
+                    free_slot = sp.get();
+                    break;
+                }
+            if (free_slot) {
+                std::vector<Request*> rs;
+                while (!sv->queue.empty() && sv->queue.front()->kind == 0 && rs.size() < sv->cfg.max_batch_requests) {
+                    Request* r = sv->queue.front();
+                    const uint32_t base = sv->pages.realloc(0, 0, r->pages);
+                    if (base == 0) break;  // budget full: wait for launches to retire
+                    r->page_base = base;
+                    sv->queue.pop_front();
+                    rs.push_back(r);
+                }
+                if (!rs.empty()) {
+                    const double ts = now_us(sv->t0);
+                    for (Request* r : rs) {
+                        r->state = VRT_REQ_RUNNING;
+                        r->start_us = ts;
+                        r->batch_size = (uint32_t)rs.size();
+                    }
+                    free_slot->reqs = rs;
+                    free_slot->busy = true;
+                    if (sv->busy_slots++ == 0) sv->busy_since = ts;
+                    sv->launches++;
+                    vrt_status st = launch_slot(sv, *free_slot, rs);
+                    if (st != VRT_OK) {
+                        cudaStreamSynchronize(free_slot->stream);
+                        for (Request* r : rs) finish(sv, r, st, now_us(sv->t0));
+                        free_slot->reqs.clear();
+                        free_slot->busy = false;
+                        sv->busy_slots--;
+                        sv->done_cv.notify_all();
+                    }
+                    continue;
+                }
+            }
+        }
+        // sleep until a submission or a completion (1 ms safety net)
+        lk.unlock();
+        {
+            std::unique_lock<std::mutex> g(sv->sig_mu);
+            sv->sig_cv.wait_for(g, std::chrono::milliseconds(1), [&] { return sv->signals != seen; });
+            seen = sv->signals;
+        }
+        lk.lock();
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+vrt_status vrt_host_alloc(size_t bytes, void** out) {
+    if (!out) {
+        set_error("null argument");
+        return VRT_ERR_INVALID_ARG;
+    }
+    VRT_CUDA(cudaHostAlloc(out, bytes ? bytes : 1, cudaHostAllocDefault));
+    return VRT_OK;
+}
+
+vrt_status vrt_host_free(void* p) {
+    if (p) VRT_CUDA(cudaFreeHost(p));
+    return VRT_OK;
+}
+
+vrt_status vrt_server_create(vrt_world* const* worlds, uint32_t n_worlds, const vrt_server_config* cfg_in,
+                             vrt_server** out) {
+    if (!out || !worlds || n_worlds == 0) {
+        set_error("server needs worlds");
+        return VRT_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    for (uint32_t i = 0; i < n_worlds; i++)
+        if (!worlds[i] || worlds[i]->device != worlds[0]->device) {
+            set_error("worlds must be non-null and on one device");
+            return VRT_ERR_INVALID_ARG;
+        }
+    auto* sv = new vrt_server;
+    sv->device = worlds[0]->device;
+    sv->worlds.assign(worlds, worlds + n_worlds);
+    sv->cfg = cfg_in ? *cfg_in : vrt_server_config{};
+    if (sv->cfg.max_inflight == 0) sv->cfg.max_inflight = 2;
+    if (sv->cfg.max_batch_requests == 0) sv->cfg.max_batch_requests = 256;
+    auto fail = [&](vrt_status st) {
+        vrt_server_destroy(sv, 0);
+        return st;
+    };
+    vrt_status st = normalize_batch_config(&sv->cfg.batch, sv->bcfg);
+    if (st != VRT_OK || sv->cfg.max_inflight > 16) {
+        delete sv;
+        if (st == VRT_OK) set_error("max_inflight must be <= 16");
+        return st == VRT_OK ? VRT_ERR_INVALID_ARG : st;
+    }
+    cudaError_t e = cudaSetDevice(sv->device);
+    if (e != cudaSuccess) return fail(cuda_fail(e, "set device"));
+    if (sv->cfg.hbm_budget_bytes == 0) {
+        size_t fr = 0, tot = 0;
+        if ((e = cudaMemGetInfo(&fr, &tot)) != cudaSuccess) return fail(cuda_fail(e, "query free HBM"));
+        sv->cfg.hbm_budget_bytes = fr / 4;
+    }
+    const uint64_t npages = std::max<uint64_t>(1, sv->cfg.hbm_budget_bytes / kPageBytes);
+    if (npages > 0x3fffffffull) return fail((set_error("budget too large"), VRT_ERR_INVALID_ARG));
+    if ((e = cudaMalloc(&sv->arena, npages * kPageBytes)) != cudaSuccess) return fail(cuda_fail(e, "output arena"));
+    sv->pages.reset((uint32_t)npages);
+    if ((e = cudaMalloc(&sv->d_worlds, sizeof(DevWorld) * n_worlds)) != cudaSuccess)
+        return fail(cuda_fail(e, "world table"));
+    if ((st = refresh_world_table(sv)) != VRT_OK) return fail(st);
+    if ((e = cudaStreamCreateWithFlags(&sv->edit_stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return fail(cuda_fail(e, "edit stream"));
+    if ((st = persistent_grid(sv->device, sv->bcfg, false, sv->blocks, sv->threads)) != VRT_OK) return fail(st);
+    for (uint32_t i = 0; i < sv->cfg.max_inflight; i++) {
+        auto s = std::make_unique<Slot>();
+        s->server = sv;
+        if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess)
+            return fail(cuda_fail(e, "slot stream"));
+        if ((e = s->queue.reserve(64)) != cudaSuccess) return fail(cuda_fail(e, "slot queue"));
+        sv->slots.push_back(std::move(s));
+    }
+    sv->worker = std::thread(worker_main, sv);
+    *out = sv;
+    return VRT_OK;
+}
+
+vrt_status vrt_server_destroy(vrt_server* sv, uint32_t timeout_ms) {
+    if (!sv) return VRT_OK;
+    vrt_status st = VRT_OK;
+    if (sv->worker.joinable()) {
+        st = vrt_server_drain(sv, timeout_ms);
+        {
+            std::lock_guard<std::mutex> lk(sv->mu);
+            sv->stop = true;
+            // requests still queued after the wait are failed; launches in flight finish
+            const double t = now_us(sv->t0);
+            while (!sv->queue.empty()) {
+                finish(sv, sv->queue.front(), VRT_ERR_QUEUE_TIMEOUT, t);
+                sv->queue.pop_front();
+            }
+        }
+        sv->signal();
+        sv->worker.join();
+    }
+    cudaSetDevice(sv->device);
+    for (auto& s : sv->slots) {
+        if (s->stream) {
+            cudaStreamSynchronize(s->stream);
+            cudaStreamDestroy(s->stream);
+        }
+        s->views.release();
+        s->chunk_base.release();
+        s->queue.release();
+        if (s->h_views) cudaFreeHost(s->h_views);
+        if (s->h_cb) cudaFreeHost(s->h_cb);
+    }
+    if (sv->edit_stream) cudaStreamDestroy(sv->edit_stream);
+    if (sv->arena) cudaFree(sv->arena);
+    if (sv->d_worlds) cudaFree(sv->d_worlds);
+    delete sv;
+    return st;
+}
+
+vrt_status vrt_server_submit_render(vrt_server* sv, const vrt_view* view, vrt_hit* hits_host, uint64_t* ticket) {
+    if (!sv || !view || !hits_host) {
+        set_error("null argument");
+        return VRT_ERR_INVALID_ARG;
+    }
+    vrt_status st = check_view(view);
+    if (st != VRT_OK) return st;
+    if (view->world >= sv->worlds.size()) {
+        set_error("view references a world the server does not hold");
+        return VRT_ERR_INVALID_ARG;
+    }
+    auto r = std::make_unique<Request>();
+    r->kind = 0;
+    r->view = *view;
+    r->host_out = hits_host;
+    r->records = view_record_count(*view);
+    r->pages = (uint32_t)((r->records + kPageRecords - 1) / kPageRecords);
+    r->submit_us = now_us(sv->t0);
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        if (sv->stop) {
+            set_error("server is stopping");
+            return VRT_ERR_INVALID_ARG;
+        }
+        if (r->pages > sv->pages.capacity()) {
+            sv->rejected++;
+            set_error("request output exceeds the server's HBM budget");
+            return VRT_ERR_OUT_OF_MEMORY;
+        }
+        r->id = sv->next_id++;
+        if (ticket) *ticket = r->id;
+        sv->queue.push_back(r.get());
+        sv->reqs[r->id] = std::move(r);
+        sv->outstanding++;
+    }
+    sv->signal();
+    return VRT_OK;
+}
+
+vrt_status vrt_server_submit_edit(vrt_server* sv, uint32_t world, const vrt_edit* edits, uint32_t n,
+                                  uint64_t* ticket) {
+    if (!sv || (n && !edits) || world >= (sv ? sv->worlds.size() : 0)) {
+        set_error("bad edit request");
+        return VRT_ERR_INVALID_ARG;
+    }
+    auto r = std::make_unique<Request>();
+    r->kind = 1;
+    r->world = world;
+    r->edits.assign(edits, edits + n);
+    r->submit_us = now_us(sv->t0);
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        if (sv->stop) {
+            set_error("server is stopping");
+            return VRT_ERR_INVALID_ARG;
+        }
+        r->id = sv->next_id++;
+        if (ticket) *ticket = r->id;
+        sv->queue.push_back(r.get());
+        sv->reqs[r->id] = std::move(r);
+        sv->outstanding++;
+    }
+    sv->signal();
+    return VRT_OK;
+}
+
+vrt_status vrt_server_wait(vrt_server* sv, uint64_t ticket, uint32_t timeout_ms, vrt_request_info* info) {
+    if (!sv) {
+        set_error("null server");
+        return VRT_ERR_INVALID_ARG;
+    }
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto it = sv->reqs.find(ticket);
+    if (it == sv->reqs.end()) {
+        set_error("unknown ticket");
+        return VRT_ERR_NOT_FOUND;
+    }
+    Request* r = it->second.get();
+    const bool ok = sv->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] {
+        return r->state == VRT_REQ_DONE || r->state == VRT_REQ_FAILED;
+    });
+    if (info) {
+        info->state = r->state;
+        info->kind = r->kind;
+        info->status = r->status;
+        info->batch_size = r->batch_size;
+        info->rays = r->records;
+        info->submit_us = r->submit_us;
+        info->start_us = r->start_us;
+        info->done_us = r->done_us;
+    }
+    if (!ok) {
+        set_error("request not finished within the timeout");
+        return VRT_ERR_QUEUE_TIMEOUT;
+    }
+    if (r->state == VRT_REQ_FAILED) {
+        set_error("request failed");
+        return r->status;
+    }
+    return VRT_OK;
+}
+
+vrt_status vrt_server_drain(vrt_server* sv, uint32_t timeout_ms) {
+    if (!sv) {
+        set_error("null server");
+        return VRT_ERR_INVALID_ARG;
+    }
+    std::unique_lock<std::mutex> lk(sv->mu);
+    if (!sv->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return sv->outstanding == 0; })) {
+        set_error("requests still outstanding after the timeout");
+        return VRT_ERR_QUEUE_TIMEOUT;
+    }
+    return VRT_OK;
+}
+
+vrt_status vrt_server_get_stats(vrt_server* sv, int reset, vrt_server_stats* out) {
+    if (!sv || !out) {
+        set_error("null argument");
+        return VRT_ERR_INVALID_ARG;
+    }
+    std::lock_guard<std::mutex> lk(sv->mu);
+    std::memset(out, 0, sizeof(*out));
+    out->renders_done = sv->renders_done;
+    out->edits_done = sv->edits_done;
+    out->rejected = sv->rejected;
+    out->launches = sv->launches;
+    out->records = sv->records_done;
+    double busy = sv->busy_total;
+    if (sv->busy_since >= 0) busy += now_us(sv->t0) - sv->busy_since;
+    out->busy_seconds = busy * 1e-6;
+    if (!sv->lat.empty()) {
+        std::vector<double> v = sv->lat;
+        auto pct = [&](double q) {
+            size_t k = (size_t)std::min<double>((double)v.size() - 1, std::floor(q * (double)(v.size() - 1) + 0.5));
+            std::nth_element(v.begin(), v.begin() + (long)k, v.end());
+            return v[k];
+        };
+        out->p50_us = pct(0.50);
+        out->p99_us = pct(0.99);
+        out->p999_us = pct(0.999);
+        out->max_us = *std::max_element(v.begin(), v.end());
+    }
+    if (reset) {
+        sv->lat.clear();
+        sv->renders_done = sv->edits_done = sv->rejected = sv->launches = sv->records_done = 0;
+        sv->busy_total = 0;
+        if (sv->busy_since >= 0) sv->busy_since = now_us(sv->t0);
+    }
+    return VRT_OK;
+}
+
+}  // extern "C"
