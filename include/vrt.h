@@ -286,6 +286,20 @@ vrt_status vrt_batch_get_stats(vrt_batch* batch, vrt_batch_stats* out);
 /* One launch of the counting variant: fills step_calls/occ_fetches/hits. */
 vrt_status vrt_batch_measure(vrt_batch* batch, vrt_hit* hits_device, void* stream, vrt_batch_stats* out);
 
+/* Same traversal as vrt_batch_create + vrt_batch_launch, in one call that allocates
+ * no memory: no counterpart in the reference.  For callers that cannot call
+ * cudaMalloc once their frame loop runs (it may synchronise the device) or whose
+ * host application owns all device memory.  The launch scratch (world table, view
+ * table, tile-queue counter) lives in one fixed 136.5 KiB device array that every GPU
+ * loading the library holds until the process exits, so a call takes at most 256
+ * worlds and 1024 views (VRT_ERR_INVALID_ARG beyond).  The first call on a device
+ * looks up that array's address; make it before any stream capture.  All calls
+ * share the array: calls whose launches overlap on the GPU race, so order them on
+ * one stream.  Records are laid out as for vrt_batch (views back to back). */
+vrt_status vrt_render_views_static(vrt_world* const* worlds, uint32_t n_worlds, const vrt_view* views,
+                                   uint32_t n_views, const vrt_batch_config* cfg, vrt_hit* hits_device,
+                                   void* stream);
+
 /* ---- pinned host memory (asynchronous copies for host-buffer calls) ---- */
 vrt_status vrt_host_alloc(size_t bytes, void** out);
 vrt_status vrt_host_free(void* ptr);

@@ -160,6 +160,8 @@ PROTOTYPES = {
     "vrt_batch_update_cameras": (_st, [_vp, C.POINTER(Camera), _vp]),
     "vrt_batch_get_stats": (_st, [_vp, C.POINTER(BatchStats)]),
     "vrt_batch_measure": (_st, [_vp, _vp, _vp, C.POINTER(BatchStats)]),
+    "vrt_render_views_static": (_st, [C.POINTER(_vp), _u32, C.POINTER(View), _u32, C.POINTER(BatchConfig), _vp,
+                                       _vp]),
     "vrt_host_alloc": (_st, [C.c_size_t, C.POINTER(_vp)]),
     "vrt_host_free": (_st, [_vp]),
     "vrt_server_create": (_st, [C.POINTER(_vp), _u32, C.POINTER(ServerConfig), C.POINTER(_vp)]),
