@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(64) view_path_kernel(DevWorld w, ViewDev v, ui
 }
 
 template <bool kCount>
-__global__ void persistent_kernel(BatchParams p) {
+__global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt = (1u << lane) - 1u;
     // warp-uniform queue state: rays [q_next, q_end) of view q_view
@@ -80,11 +80,11 @@ __global__ void persistent_kernel(BatchParams p) {
     bool q_empty = false;
     // lane state
     bool active = false;
-    uint32_t pixel = 0, kind = 0, iter = 0, max_iters = 0, last_kind = 0, plane = 0, shadow = 0;
-    uint4* rec = nullptr;
+    // path: kind of the current ray (0 primary, then shadow or bounce number) in bits
+    // 0-7, last kind of the pixel's path in bits 8-15, shadow flag in bit 16
+    uint32_t pixel = 0, path = 0, iter = 0, max_iters = 0, plane = 0, vidx = 0;
     DevWorld w{};
     int32_t wox = 0, woy = 0, woz = 0;
-    const ViewDev* V = nullptr;
     RayState s;
     uint32_t rays = 0, hits = 0;
     TraceCounters cnt{0, 0};
@@ -133,18 +133,20 @@ __global__ void persistent_kernel(BatchParams p) {
                         ky = k >> p.tile_w_log2;
                     }
                     const uint32_t tw = 1u << p.tile_w_log2, th = 1u << (p.tile_size_log2 - p.tile_w_log2);
-                    const uint32_t px = (t % tiles_x) * tw + kx, py = (t / tiles_x) * th + ky;
+                    // t / tiles_x by multiply-high: the estimate is the quotient or one more
+                    const uint32_t magic = __ldg(&v->tiles_x_magic);
+                    uint32_t trow = magic ? __umulhi(t, magic) : t;
+                    if (trow * tiles_x > t) trow--;
+                    const uint32_t px = (t - trow * tiles_x) * tw + kx, py = trow * th + ky;
                     const uint32_t width = __ldg(&v->cam.width), height = __ldg(&v->cam.height);
                     if (px < width && py < height) {
-                        V = v;
+                        vidx = q_view;
                         pixel = py * width + px;
                         plane = width * height;
-                        kind = 0;
                         iter = 0;
                         max_iters = __ldg(&v->max_iters);
-                        shadow = __ldg(&v->shadow);
-                        last_kind = shadow ? 1u : __ldg(&v->n_bounces);
-                        rec = p.out + __ldg(&v->out_base) + pixel;
+                        const uint32_t shadow = __ldg(&v->shadow);
+                        path = (shadow ? 1u : __ldg(&v->n_bounces)) << 8 | shadow << 16;
                         w = p.worlds[__ldg(&v->world)];
                         wox = __ldg(&v->cam.world_origin[0]);
                         woy = __ldg(&v->cam.world_origin[1]);
@@ -166,13 +168,18 @@ __global__ void persistent_kernel(BatchParams p) {
                 const uint32_t st = ray_step<kCount>(s, w, wox, woy, woz, cnt);
                 if (st == kStepContinue && ++iter < max_iters) continue;
                 const bool hit = st == kStepHit;
+                const ViewDev* v = p.views + vidx;
+                uint4* rec = p.out + __ldg(&v->out_base) + pixel;
+                uint32_t kind = path & 0xFF;
+                const uint32_t last_kind = (path >> 8) & 0xFF;
                 rec[(size_t)kind * plane] = pack_state(s, hit, iter, pixel);
                 rays++;
                 if (kCount && hit) hits++;
                 if (hit && kind < last_kind) {
+                    path++;
                     kind++;
                     float ox, oy, oz, dx, dy, dz;
-                    next_path_ray(s, shadow != 0, V->sun, pixel, kind, ox, oy, oz, dx, dy, dz);
+                    next_path_ray(s, (path >> 16) != 0, v->sun, pixel, kind, ox, oy, oz, dx, dy, dz);
                     ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
                     iter = 0;
                     continue;
@@ -233,8 +240,9 @@ uint32_t eff_iters(uint32_t m) { return m == 0 ? VRT_DEFAULT_MAX_ITERS : (m > 65
 vrt_status check_view(const vrt_view* v) {
     if (!v || v->cam.width == 0 || v->cam.height == 0 || v->cam.width > 16384 || v->cam.height > 16384 ||
         v->n_bounces > VRT_MAX_BOUNCES || (v->flags & ~VRT_VIEW_SHADOW) ||
-        ((v->flags & VRT_VIEW_SHADOW) && v->n_bounces)) {
-        set_error("bad view: camera 1..16384 px, n_bounces <= 15, shadow and bounces exclusive");
+        ((v->flags & VRT_VIEW_SHADOW) && v->n_bounces) || !world_origin_ok(v->cam.world_origin)) {
+        set_error("bad view: camera 1..16384 px, |world origin| <= 2^30, n_bounces <= 15, shadow and bounces "
+                  "exclusive");
         return VRT_ERR_INVALID_ARG;
     }
     return VRT_OK;
@@ -287,6 +295,7 @@ vrt_status plan_views(const vrt_view* views, uint32_t n, uint32_t n_worlds, cons
         const uint32_t ty = (d.cam.height + cfg.tile_h - 1) / cfg.tile_h;
         const uint64_t tiles = (uint64_t)tx * ty;
         d.tiles_x = tx;
+        d.tiles_x_magic = div_magic(tx);
         d.n_rays = (uint32_t)(tiles << plan.tile_size_log2);
         d.chunk_base = (uint32_t)chunks;
         d.out_base = records;

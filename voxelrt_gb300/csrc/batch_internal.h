@@ -19,11 +19,17 @@ struct ViewDev {
     uint32_t shadow;
     float sun[3];
     uint32_t tiles_x;
-    uint32_t n_rays;      // tile-padded ray space of the view
-    uint32_t chunk_base;  // first queue chunk of the view
-    uint64_t out_base;    // first record of the view
+    uint32_t tiles_x_magic;  // ceil(2^32 / tiles_x): tile row by a multiply-high
+    uint32_t n_rays;         // tile-padded ray space of the view
+    uint32_t chunk_base;     // first queue chunk of the view
+    uint64_t out_base;       // first record of the view
 };
 static_assert(sizeof(ViewDev) == 120, "view table entry is 120 bytes (copied per camera update)");
+
+// ceil(2^32 / d) for 2 <= d < 2^32; 0 marks d == 1 (the quotient is the numerator).
+inline uint32_t div_magic(uint32_t d) {
+    return d <= 1 ? 0u : (uint32_t)((0x100000000ull + d - 1) / d);
+}
 
 struct BatchParams {
     const DevWorld* worlds;

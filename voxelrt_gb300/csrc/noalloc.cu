@@ -115,6 +115,7 @@ extern "C" vrt_status vrt_render_views_static(vrt_world* const* worlds, uint32_t
         const uint32_t ty = (v.cam.height + cfg.tile_h - 1) / cfg.tile_h;
         const uint64_t tiles = (uint64_t)tx * ty;
         d.tiles_x = tx;
+        d.tiles_x_magic = div_magic(tx);
         d.n_rays = (uint32_t)(tiles << ts_log2);
         d.chunk_base = (uint32_t)chunks;
         d.out_base = records;

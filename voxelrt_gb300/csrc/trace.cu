@@ -48,8 +48,9 @@ __global__ void __launch_bounds__(256) cast_kernel(DevWorld w, const float4* __r
 }
 
 vrt_status check_camera(const vrt_camera* cam) {
-    if (!cam || cam->width == 0 || cam->height == 0 || cam->width > 16384 || cam->height > 16384) {
-        set_error("camera must be 1..16384 pixels on each side");
+    if (!cam || cam->width == 0 || cam->height == 0 || cam->width > 16384 || cam->height > 16384 ||
+        !world_origin_ok(cam->world_origin)) {
+        set_error("camera must be 1..16384 pixels on each side with |world origin| <= 2^30");
         return VRT_ERR_INVALID_ARG;
     }
     return VRT_OK;
@@ -76,8 +77,8 @@ vrt_status launch_cast(vrt_world* w, const vrt_ray* rays, uint32_t n, const vrt_
 }
 
 vrt_status check_params(const vrt_cast_params* p) {
-    if (!p || p->flags != 0) {
-        set_error("cast params missing or flags not 0");
+    if (!p || p->flags != 0 || !world_origin_ok(p->world_origin)) {
+        set_error("cast params missing, flags not 0 or |world origin| > 2^30");
         return VRT_ERR_INVALID_ARG;
     }
     return VRT_OK;

@@ -61,7 +61,9 @@ struct RayState {
     float cx, cy, cz;     // currPos
     float sx, sy, sz;     // sideDist
     int32_t vx, vy, vz;   // voxel of the last step (hit voxel on a hit)
-    uint32_t i;           // iteration
+    int32_t gx, gy, gz;   // -1 where dir < 0, else 0 (cell alignment side)
+    uint32_t slot;        // 1 + brick slot of the last step when its brick is allocated, else 0
+    uint32_t clo, chi;    // voxel-cell mask of the last step (valid while slot != 0)
     uint32_t material;
 };
 
@@ -94,7 +96,11 @@ __device__ __forceinline__ void ray_init(RayState& s, const DevWorld& w, float o
     s.cz = clip ? __fadd_rn(oz, __fmul_rn(dz, tmin)) : oz;
     s.sx = s.sy = s.sz = 0.0f;
     s.vx = s.vy = s.vz = 0;
-    s.i = 0;
+    s.gx = dx < 0.0f ? -1 : 0;
+    s.gy = dy < 0.0f ? -1 : 0;
+    s.gz = dz < 0.0f ? -1 : 0;
+    s.slot = 0;
+    s.clo = s.chi = 0;
     s.material = 0;
 }
 
@@ -104,36 +110,62 @@ enum : uint32_t { kStepContinue = 0, kStepHit = 1, kStepOut = 2 };
 template <bool kCount>
 __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int32_t wox, int32_t woy, int32_t woz,
                                              TraceCounters& cnt) {
-    int32_t vx = wadd(wox, floor2i(s.cx));
-    int32_t vy = wadd(woy, floor2i(s.cy));
-    int32_t vz = wadd(woz, floor2i(s.cz));
+    // floor2i: a NaN coordinate converts to INT32_MIN on x86 and leaves the grid;
+    // cvt.rmi saturates infinities and out-of-range values, which leave the grid
+    // too (|world origin| <= 2^30 is enforced at the API), so only NaN needs a test
+    // and one NaN among the three shows in their sum.
+    const float nan_probe = __fadd_rn(__fadd_rn(s.cx, s.cy), s.cz);
+    if (nan_probe != nan_probe) {
+        s.vx = s.vy = s.vz = INT32_MIN;
+        return kStepOut;
+    }
+    int32_t vx = wadd(wox, __float2int_rd(s.cx));
+    int32_t vy = wadd(woy, __float2int_rd(s.cy));
+    int32_t vz = wadd(woz, __float2int_rd(s.cz));
     if (!((uint32_t)vx < w.size_x && (uint32_t)vy < w.size_y && (uint32_t)vz < w.size_z)) {
         s.vx = vx;
         s.vy = vy;
         s.vz = vz;
         return kStepOut;
     }
-    // sector allocation mask at lod 3
-    const uint32_t sidx = (uint32_t)(vx >> 5) + (uint32_t)(vz >> 5) * w.sx + (uint32_t)(vy >> 5) * w.sxz;
-    const uint4 rec = __ldg(reinterpret_cast<const uint4*>(w.sectors) + sidx);
-    uint32_t lo = rec.x, hi = rec.y;
-    uint32_t idx = ((vx >> 3) & 3) | ((vz >> 3) & 3) << 2 | ((vy >> 3) & 3) << 4;
-    int32_t lod = 3;
+    // Consecutive steps mostly stay in one brick, often in one 4^3 cell: the last
+    // step's aligned position is in the same brick (lod <= 3) and, inside an
+    // allocated brick, in the same cell (lod <= 2), so its slot and cell mask are
+    // reused instead of re-reading the sector record and the cell mask.
+    const uint32_t moved = (uint32_t)((vx ^ s.vx) | (vy ^ s.vy) | (vz ^ s.vz));
+    uint32_t lo, hi, idx;
+    int32_t lod;
     if (kCount) cnt.step_calls++;
-    if ((((idx < 32 ? lo : hi) >> (idx & 31)) & 1u) != 0) {
-        // brick allocated: slot = base + popcount of the mask below the brick bit
-        const uint32_t below = (1u << (idx & 31)) - 1u;
-        const uint32_t slot = rec.z + (idx < 32 ? __popc(lo & below) : __popc(lo) + __popc(hi & below));
-        const uint32_t cell = ((vx >> 2) & 1) | ((vz >> 2) & 1) << 1 | ((vy >> 2) & 1) << 2;
-        const uint2 cm = __ldg(reinterpret_cast<const uint2*>(w.occ) + (size_t)slot * 8 + cell);
-        lo = cm.x;
-        hi = cm.y;
+    if (moved >= 8 || s.slot == 0) {
+        // sector allocation mask at lod 3
+        const uint32_t sidx = (uint32_t)(vx >> 5) + (uint32_t)(vz >> 5) * w.sx + (uint32_t)(vy >> 5) * w.sxz;
+        const uint4 rec = __ldg(reinterpret_cast<const uint4*>(w.sectors) + sidx);
+        lo = rec.x;
+        hi = rec.y;
+        idx = ((vx >> 3) & 3) | ((vz >> 3) & 3) << 2 | ((vy >> 3) & 3) << 4;
+        lod = 3;
+        s.slot = 0;
+        if ((((idx < 32 ? lo : hi) >> (idx & 31)) & 1u) != 0) {
+            // brick allocated: slot = base + popcount of the mask below the brick bit
+            const uint32_t below = (1u << (idx & 31)) - 1u;
+            s.slot = 1 + rec.z + (idx < 32 ? __popc(lo & below) : __popc(lo) + __popc(hi & below));
+        }
+    }
+    if (s.slot != 0) {
+        if (moved >= 4) {
+            const uint32_t cell = ((vx >> 2) & 1) | ((vz >> 2) & 1) << 1 | ((vy >> 2) & 1) << 2;
+            const uint2 cm = __ldg(reinterpret_cast<const uint2*>(w.occ) + (size_t)(s.slot - 1) * 8 + cell);
+            s.clo = cm.x;
+            s.chi = cm.y;
+        }
+        lo = s.clo;
+        hi = s.chi;
         idx = (vx & 3) | (vz & 3) << 2 | (vy & 3) << 4;
         lod = 0;
         if (kCount) cnt.occ_fetches++;
         if ((((idx < 32 ? lo : hi) >> (idx & 31)) & 1u) != 0) {
             const uint32_t vi = (vx & 7) | (vz & 7) << 3 | (vy & 7) << 6;
-            s.material = __ldg(w.payload + (size_t)slot * 512 + vi);
+            s.material = __ldg(w.payload + (size_t)(s.slot - 1) * 512 + vi);
             s.vx = vx;
             s.vy = vy;
             s.vz = vz;
@@ -143,10 +175,11 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
     // level4 (+2) / level2 (+1) from the same mask, then align to the cell boundary
     const uint32_t half = idx < 32 ? lo : hi;
     lod += (lo | hi) == 0 ? 2 : (((half >> (idx & 0xA)) & 0x00330033u) == 0 ? 1 : 0);
+    // dir < 0 ? pos & ~m : pos | m, as (pos | m) ^ (g & m) with g = -1 for dir < 0
     const int32_t m = (1 << lod) - 1;
-    vx = s.dx < 0.0f ? (vx & ~m) : (vx | m);
-    vy = s.dy < 0.0f ? (vy & ~m) : (vy | m);
-    vz = s.dz < 0.0f ? (vz & ~m) : (vz | m);
+    vx = (vx | m) ^ (s.gx & m);
+    vy = (vy | m) ^ (s.gy & m);
+    vz = (vz | m) ^ (s.gz & m);
     s.vx = vx;
     s.vy = vy;
     s.vz = vz;

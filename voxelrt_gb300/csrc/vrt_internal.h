@@ -35,6 +35,15 @@ struct DevWorld {
     uint32_t size_x, size_y, size_z;  // voxels
 };
 
+// World origins stay within +-2^30 so that saturated float->int conversions of
+// far-away positions always land outside the grid (the traversal relies on it).
+constexpr int32_t kMaxWorldOrigin = 1 << 30;
+inline bool world_origin_ok(const int32_t wo[3]) {
+    for (int c = 0; c < 3; c++)
+        if (wo[c] > kMaxWorldOrigin || wo[c] < -kMaxWorldOrigin) return false;
+    return true;
+}
+
 inline int32_t sector_index_pack(int32_t x, int32_t y, int32_t z) {
     return (int32_t)(((uint32_t)x & 4095u) | ((uint32_t)z & 4095u) << 12 | ((uint32_t)y & 255u) << 24);
 }
