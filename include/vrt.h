@@ -213,6 +213,28 @@ vrt_status vrt_render_view_device(vrt_world* world, const vrt_camera* cam, uint3
 vrt_status vrt_camera_look_at(const double pos[3], const double target[3], double vfov_deg,
                               uint32_t width, uint32_t height, vrt_camera* out);
 
+/* ---- picking (VoxelMap::RayCast, VoxelMap.cpp:125-170) ---- */
+/* The reference's scalar double-precision ray cast used for mouse picking and brush
+ * placement: steps of 32/8/1 voxels from the sector map, brick presence and voxel
+ * emptiness, a +1e-4 bias, no bounds test (sectors outside the world are empty). */
+typedef struct vrt_pick_ray {
+    double origin[3]; /* world voxel coordinates */
+    double dir[3];
+} vrt_pick_ray;
+
+typedef struct vrt_pick_hit {
+    double distance;  /* HitResult::Distance: biased tmin of the hit, -1 on a miss */
+    int32_t voxel[3]; /* HitResult::VoxelPos */
+    float normal[3];  /* HitResult::Normal: -sign(dir) on axes with tmin >= sideDist */
+    float uv[2];      /* HitResult::UV */
+    uint32_t iters;   /* iteration of the hit, max_iters on a miss */
+    uint32_t reserved;
+} vrt_pick_hit;
+
+/* max_iters 0 = 1024 (VoxelMap.h:214).  Host buffers. */
+vrt_status vrt_pick(vrt_world* world, const vrt_pick_ray* rays, uint32_t n, uint32_t max_iters, vrt_pick_hit* hits,
+                    void* stream);
+
 /* ---- views: primary rays plus secondary rays per pixel ---- */
 /* A view is one RenderFrame of the reference's renderers: a primary ray per pixel
  * (VoxelRender.comp:27-30, CpuRenderer.cpp:326-333), then optionally

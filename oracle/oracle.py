@@ -17,6 +17,8 @@ LIB_PATH = _HERE / "_build" / "libvrt_oracle.so"
 RAY_DTYPE = np.dtype([("origin", "<f4", 3), ("dir", "<f4", 3), ("tag", "<u4"), ("reserved", "<u4")])
 HIT_DTYPE = np.dtype([("voxel", "<u4"), ("face", "u1"), ("material", "u1"), ("steps", "<u2"), ("t", "<f4"),
                       ("tag", "<u4")])
+PICK_DTYPE = np.dtype([("distance", "<f8"), ("voxel", "<i4", 3), ("normal", "<f4", 3), ("uv", "<f4", 2),
+                       ("iters", "<u4"), ("reserved", "<u4")])
 EDIT_DTYPE = np.dtype([("center", "<i4", 3), ("radius", "<u4"), ("material", "u1"), ("mode", "u1"),
                        ("reserved", "<u2")])
 
@@ -58,6 +60,7 @@ def lib() -> C.CDLL:
         L.ora_render_view_shadow.argtypes = [_vp, _vp, _vp, C.c_uint32, _vp, _vp, C.c_int, C.POINTER(Stats)]
         L.ora_render_view_bounces.argtypes = [_vp, _vp, C.c_uint32, C.c_uint32, _vp, C.c_int, C.POINTER(Stats)]
         L.ora_world_edit.argtypes = [_vp, _vp, C.c_uint32]
+        L.ora_pick.argtypes = [_vp, _vp, C.c_uint64, C.c_uint32, _vp]
         _lib = L
     return _lib
 
@@ -159,6 +162,13 @@ class OracleWorld:
                                            hits.ctypes.data, int(threads), C.byref(s)))
         self.last_stats = _stats(s)
         return hits.reshape(n_bounces + 1, n)
+
+    def pick(self, rays: np.ndarray, max_iters: int = 0) -> np.ndarray:
+        """rays: (n, 6) float64 (origin, dir) -> PICK_DTYPE records."""
+        r = np.ascontiguousarray(rays, dtype=np.float64).reshape(-1, 6)
+        out = np.zeros(len(r), PICK_DTYPE)
+        _chk(lib().ora_pick(self._h, r.ctypes.data, len(r), int(max_iters), out.ctypes.data))
+        return out
 
     def edit(self, edits) -> None:
         e = np.ascontiguousarray(edits, dtype=EDIT_DTYPE)

@@ -102,4 +102,22 @@ int ref_raycast(void* p, uint64_t n, const float* origins, const float* dirs, co
     return 0;
 }
 
+// VoxelMap::RayCast (VoxelMap.cpp:140-170) on the loaded map; rays: 6 doubles each.
+int ref_pick(void* p, uint64_t n, const double* rays, uint32_t max_iters, double* dist, float* normal, float* uv,
+             int32_t* voxel) {
+    auto* w = static_cast<RefWorld*>(p);
+    for (uint64_t i = 0; i < n; i++) {
+        const double* r = rays + i * 6;
+        HitResult h = w->map->RayCast(glm::dvec3(r[0], r[1], r[2]), glm::dvec3(r[3], r[4], r[5]), max_iters);
+        dist[i] = h.Distance;
+        for (int c = 0; c < 3; c++) {
+            normal[i * 3 + c] = h.Normal[c];
+            voxel[i * 3 + c] = h.VoxelPos[c];
+        }
+        uv[i * 2 + 0] = h.UV.x;
+        uv[i * 2 + 1] = h.UV.y;
+    }
+    return 0;
+}
+
 }  // extern "C"

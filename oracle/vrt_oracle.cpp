@@ -578,6 +578,78 @@ int ora_render_view_bounces(const ora_world* w, const vrt_camera* cam, uint32_t 
     return 0;
 }
 
+// VoxelMap::RayCast (VoxelMap.cpp:140-170) with GetStepLevel (:125-139) over the
+// oracle's sectors; glm::min(x, y) = y < x ? y : x, glm::step(0, d) = d < 0 ? 0 : 1,
+// double -> int as x86 cvttsd2si (INT32_MIN out of range).
+int ora_pick(const ora_world* w, const double* rays, uint64_t n, uint32_t max_iters, vrt_pick_hit* hits) {
+    if (!w || (n && (!rays || !hits))) return -1;
+    if (max_iters == 0) max_iters = 1024;
+    auto gmin = [](double x, double y) { return y < x ? y : x; };
+    auto d2i = [](double f) { return (f >= -2147483648.0 && f < 2147483648.0) ? (int32_t)f : INT32_MIN; };
+    for (uint64_t r = 0; r < n; r++) {
+        const double* ray = rays + r * 6;
+        double o[3], d[3], inv[3], ts[3];
+        int32_t pos[3];
+        for (int c = 0; c < 3; c++) {
+            o[c] = ray[c];
+            d[c] = ray[3 + c];
+            inv[c] = 1.0 / d[c];
+            ts[c] = ((d[c] < 0.0 ? 0.0 : 1.0) - o[c]) * inv[c];
+            pos[c] = d2i(std::floor(o[c]));
+        }
+        vrt_pick_hit h{};
+        h.distance = -1.0;
+        h.iters = max_iters;
+        for (uint32_t i = 0; i < max_iters; i++) {
+            double side[3], hp[3];
+            for (int c = 0; c < 3; c++) side[c] = ts[c] + (double)pos[c] * inv[c];
+            const double tmin = gmin(gmin(side[0], side[1]), side[2]) + 0.0001;
+            for (int c = 0; c < 3; c++) {
+                hp[c] = o[c] + tmin * d[c];
+                pos[c] = d2i(std::floor(hp[c]));
+            }
+            // sector key wraps like WorldSectorIndexer (12/8/12 signed bits)
+            const int32_t sx = (int32_t)((uint32_t)(pos[0] >> 5) << 20) >> 20;
+            const int32_t sy = (int32_t)((uint32_t)(pos[1] >> 5) << 24) >> 24;
+            const int32_t sz = (int32_t)((uint32_t)(pos[2] >> 5) << 20) >> 20;
+            int32_t k = 5;
+            if (w->sector_in(sx, sy, sz)) {
+                const uint32_t s = w->lin(sx, sy, sz);
+                const uint64_t mask = w->masks[s];
+                if (mask) {
+                    const uint32_t b = ((pos[0] >> 3) & 3) | ((pos[2] >> 3) & 3) << 2 | ((pos[1] >> 3) & 3) << 4;
+                    k = 3;
+                    if ((mask >> b) & 1) {
+                        const uint32_t vi = (pos[0] & 7) | (pos[2] & 7) << 3 | (pos[1] & 7) << 6;
+                        k = w->data[s]->vox[b * 512 + vi] == 0 ? 0 : -1;
+                    }
+                }
+            }
+            if (k < 0) {
+                bool m[3];
+                for (int c = 0; c < 3; c++) m[c] = tmin >= side[c];
+                h.distance = tmin;
+                for (int c = 0; c < 3; c++) {
+                    const double sg = (double)((0.0 < d[c]) - (d[c] < 0.0));
+                    h.normal[c] = m[c] ? (float)(-sg) : 0.0f;
+                    h.voxel[c] = pos[c];
+                }
+                const float ax = (float)hp[0], az = (float)hp[2], b = (float)hp[1];
+                const float tx = m[0] ? 1.0f : 0.0f, tz = m[2] ? 1.0f : 0.0f;
+                const float ux = ax * (1.0f - tx) + b * tx, uz = az * (1.0f - tz) + b * tz;
+                h.uv[0] = ux - std::floor(ux);
+                h.uv[1] = uz - std::floor(uz);
+                h.iters = i;
+                break;
+            }
+            const int32_t msk = (1 << k) - 1;
+            for (int c = 0; c < 3; c++) pos[c] = d[c] < 0.0 ? (pos[c] & ~msk) : (pos[c] | msk);
+        }
+        hits[r] = h;
+    }
+    return 0;
+}
+
 // VoxelMap::RegionDispatchSIMD + GC (VoxelMap.h:222-263) driving the sphere brush
 // (Brush.cpp:10-31) with an exact integer sphere test.
 int ora_world_edit(ora_world* w, const vrt_edit* edits, uint32_t n) {

@@ -68,6 +68,10 @@ int ora_render_view_shadow(const ora_world* w, const vrt_camera* cam, const floa
 int ora_render_view_bounces(const ora_world* w, const vrt_camera* cam, uint32_t n_bounces,
                             uint32_t max_iters, vrt_hit* hits, int threads, ora_stats* stats);
 
+/* Picking ray cast (VoxelMap::RayCast, VoxelMap.cpp:125-170), double precision.
+ * rays: 6 doubles each (origin, dir).  max_iters 0 = 1024. */
+int ora_pick(const ora_world* w, const double* rays, uint64_t n, uint32_t max_iters, vrt_pick_hit* hits);
+
 /* Apply sphere edits in order with the reference's region dispatch + empty-brick GC. */
 int ora_world_edit(ora_world* w, const vrt_edit* edits, uint32_t n);
 

@@ -30,6 +30,7 @@ sys.path.insert(0, str(ROOT))
 import voxelrt_gb300 as v  # noqa: E402
 
 OUT = Path(__file__).resolve().parent / "refcast.npz"
+OUT_PICK = Path(__file__).resolve().parent / "refpick.npz"
 
 # world recipes: (name, kind, params)
 WORLDS = {
@@ -113,11 +114,40 @@ def main(ref: str) -> None:
         arrays[f"{case}/dist"] = dist
         arrays[f"{case}/material"] = (mat & 0xFFFF).astype(np.uint16)
         print(f"{case}: {n} rays, {int(hit.sum())} hits")
-    for h in worlds.values():
-        L.ref_world_destroy(h)
     arrays["cases"] = np.array(names)
     np.savez_compressed(OUT, **arrays)
     print(OUT, OUT.stat().st_size, "bytes")
+
+    # picking: VoxelMap::RayCast (VoxelMap.cpp:140-170) over the same maps, double precision
+    L.ref_pick.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint32] + [C.c_void_p] * 4
+    pick = {}
+    rng = np.random.default_rng(77)
+    for world, edge in (("terrain256", 256), ("mix128", 128), ("mix64", 64)):
+        n = 1500
+        o = rng.uniform(-0.25 * edge, 1.25 * edge, (n, 3))
+        tgt = rng.uniform(0, edge, (n, 3))
+        d = tgt - o
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        d[: n // 10, rng.integers(0, 3)] = 0.0  # some zero components
+        rays = np.ascontiguousarray(np.concatenate([o, d], 1), np.float64)
+        dist = np.zeros(n, np.float64)
+        nrm = np.zeros((n, 3), np.float32)
+        uv = np.zeros((n, 2), np.float32)
+        vox = np.zeros((n, 3), np.int32)
+        L.ref_pick(worlds[world], n, rays.ctypes.data, 1024, dist.ctypes.data, nrm.ctypes.data, uv.ctypes.data,
+                   vox.ctypes.data)
+        pick[f"{world}/rays"] = rays
+        pick[f"{world}/distance"] = dist
+        pick[f"{world}/normal"] = nrm
+        pick[f"{world}/uv"] = uv
+        pick[f"{world}/voxel"] = vox
+        print(f"pick {world}: {n} rays, {int((dist > 0).sum())} hits")
+    pick["worlds"] = np.array(["terrain256", "mix128", "mix64"])
+    pick["view_sectors"] = arrays["view_sectors"]
+    np.savez_compressed(OUT_PICK, **pick)
+    print(OUT_PICK, OUT_PICK.stat().st_size, "bytes")
+    for h in worlds.values():
+        L.ref_world_destroy(h)
 
 
 if __name__ == "__main__":

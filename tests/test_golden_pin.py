@@ -106,3 +106,34 @@ def test_device_matches_reference(gpu, case):
         rays = make_rays(z[f"{case}/origin"], z[f"{case}/dir"])
         hits = w.cast(rays, world_origin=tuple(int(c) for c in z[f"{case}/world_origin"]), max_iters=128)
     check_against_reference(z, case, hits)
+
+
+PICK_FIXTURE = Path(__file__).resolve().parent / "golden" / "refpick.npz"
+_P = np.load(PICK_FIXTURE, allow_pickle=False)
+_PICK_WORLDS = [str(w) for w in _P["worlds"]]
+
+
+def check_pick(z, world, got):
+    """VoxelMap::RayCast outputs: Distance, VoxelPos, Normal, UV, bit-exact."""
+    dist = z[f"{world}/distance"]
+    assert np.array_equal(got["distance"].view(np.uint64), dist.view(np.uint64)), f"{world}: distance"
+    hit = dist > 0
+    assert np.array_equal(got["voxel"][hit], z[f"{world}/voxel"][hit]), f"{world}: voxel"
+    assert np.array_equal(got["normal"][hit].view(np.uint32), z[f"{world}/normal"][hit].view(np.uint32))
+    assert np.array_equal(got["uv"][hit].view(np.uint32), z[f"{world}/uv"][hit].view(np.uint32))
+    assert hit.mean() > 0.5
+
+
+@pytest.mark.parametrize("world", _PICK_WORLDS)
+def test_oracle_pick_matches_reference(world):
+    o = OracleWorld(tuple(int(c) for c in _P["view_sectors"]))
+    o.upload(build_world(world))
+    check_pick(_P, world, o.pick(_P[f"{world}/rays"], 1024))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("world", _PICK_WORLDS)
+def test_device_pick_matches_reference(gpu, world):
+    with v.World(tuple(int(c) for c in _P["view_sectors"])) as w:
+        w.upload(build_world(world))
+        check_pick(_P, world, w.pick(_P[f"{world}/rays"], 1024))

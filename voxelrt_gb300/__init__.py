@@ -179,6 +179,13 @@ class World:
     def upload(self, data: SectorData, stream=None) -> None:
         self.sync_sectors(data.sector_idx, data.alloc_mask, data.bricks, None, stream)
 
+    def pick(self, rays, max_iters: int = 0, stream=None) -> np.ndarray:
+        """Picking ray cast (VoxelMap::RayCast): rays (n, 6) float64 origin+dir -> PICK_DTYPE records."""
+        r = np.ascontiguousarray(rays, dtype=np.float64).reshape(-1, 6)
+        out = np.zeros(len(r), capi.PICK_DTYPE)
+        check(lib().vrt_pick(self._h, ptr(r), len(r), int(max_iters), ptr(out), _stream_ptr(stream)))
+        return out
+
     def edit(self, edits, stream=None) -> None:
         """Apply vrt_edit records (EDIT_DTYPE array) in order."""
         e = np.ascontiguousarray(edits, dtype=EDIT_DTYPE)

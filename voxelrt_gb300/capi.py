@@ -118,11 +118,14 @@ class SynthTerrain(C.Structure):
 RAY_DTYPE = np.dtype([("origin", "<f4", 3), ("dir", "<f4", 3), ("tag", "<u4"), ("reserved", "<u4")])
 HIT_DTYPE = np.dtype([("voxel", "<u4"), ("face", "u1"), ("material", "u1"), ("steps", "<u2"), ("t", "<f4"),
                       ("tag", "<u4")])
+PICK_DTYPE = np.dtype([("distance", "<f8"), ("voxel", "<i4", 3), ("normal", "<f4", 3), ("uv", "<f4", 2),
+                       ("iters", "<u4"), ("reserved", "<u4")])
 EDIT_DTYPE = np.dtype([("center", "<i4", 3), ("radius", "<u4"), ("material", "u1"), ("mode", "u1"),
                        ("reserved", "<u2")])
 assert RAY_DTYPE.itemsize == C.sizeof(Ray) == 32
 assert HIT_DTYPE.itemsize == C.sizeof(Hit) == 16
 assert EDIT_DTYPE.itemsize == C.sizeof(Edit) == 20
+assert PICK_DTYPE.itemsize == 48
 
 _vp = C.c_void_p
 _st = C.c_int
@@ -145,6 +148,7 @@ PROTOTYPES = {
     "vrt_cast_device": (_st, [_vp, _vp, _u32, C.POINTER(CastParams), _vp, _vp]),
     "vrt_render_view": (_st, [_vp, C.POINTER(Camera), _u32, _vp, _vp]),
     "vrt_render_view_device": (_st, [_vp, C.POINTER(Camera), _u32, _vp, _vp]),
+    "vrt_pick": (_st, [_vp, _vp, _u32, _u32, _vp, _vp]),
     "vrt_camera_look_at": (_st, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_double, _u32, _u32,
                                  C.POINTER(Camera)]),
     "vrt_view_records": (_u64, [C.POINTER(View)]),
