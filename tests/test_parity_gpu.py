@@ -136,3 +136,25 @@ def test_degenerate_directions(cfg0):
     orig[: n // 4] = np.floor(orig[: n // 4])  # origins on voxel corners
     rays = make_rays(orig, d)
     assert_hits_equal(w.cast(rays), o.cast(rays))
+
+
+def test_rays_near_the_grid_corner_and_brick_edges(gpu):
+    # dense random voxels; origins in the first cells of the grid and on brick edges,
+    # where state carried from one step to the next must not leak between rays
+    rng = np.random.default_rng(12)
+    vol = ((rng.random((64, 64, 64)) < 0.08) * rng.integers(1, 256, (64, 64, 64))).astype(np.uint8)
+    data = dense_to_stream(vol)
+    w, o = both_worlds(data)
+    n = 40_000
+    orig = rng.uniform(0, 6, (n, 3)).astype(np.float32)
+    orig[n // 2:] = (rng.integers(0, 8, (n - n // 2, 3)) * 8 + rng.choice([0.0, 0.25, 7.75], (n - n // 2, 3))).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    rays = make_rays(orig, d)
+    assert_hits_equal(w.cast(rays), o.cast(rays))
+    cam = v.look_at((0.5, 0.5, 0.5), (40, 30, 50), 80.0, 64, 48)
+    assert_hits_equal(w.render_view(cam), o.render_view(cam))
+    view = v.make_view(cam, n_bounces=3)
+    got = v.render_path(w, view)
+    want = o.render_view_bounces(cam, 3)
+    for k in range(4):
+        assert_hits_equal(got[k], want[k])

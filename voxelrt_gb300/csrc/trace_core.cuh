@@ -95,7 +95,8 @@ __device__ __forceinline__ void ray_init(RayState& s, const DevWorld& w, float o
     s.cy = clip ? __fadd_rn(oy, __fmul_rn(dy, tmin)) : oy;
     s.cz = clip ? __fadd_rn(oz, __fmul_rn(dz, tmin)) : oz;
     s.sx = s.sy = s.sz = 0.0f;
-    s.vx = s.vy = s.vz = 0;
+    // far from every grid voxel, so the first step never reuses a brick or cell
+    s.vx = s.vy = s.vz = INT32_MIN;
     s.gx = dx < 0.0f ? -1 : 0;
     s.gy = dy < 0.0f ? -1 : 0;
     s.gz = dz < 0.0f ? -1 : 0;
