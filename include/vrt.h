@@ -193,6 +193,30 @@ vrt_status vrt_world_edit(vrt_world* world, const vrt_edit* edits, uint32_t n, v
 vrt_status vrt_world_read_sector(vrt_world* world, int32_t sector_idx, uint64_t* alloc_mask,
                                  uint8_t* bricks, size_t bricks_capacity, void* stream);
 
+/* ---- world files (cvox v4: VoxelMap::Serialize/Deserialize, VoxelMap.cpp:205-273) ---- */
+/* A sector stream in host memory (records as vrt_world_sync_sectors takes them). */
+typedef struct vrt_sector_stream {
+    uint32_t sectors_x, sectors_y, sectors_z;
+    uint32_t n_sectors;   /* records */
+    uint64_t n_bricks;    /* bricks in `bricks` */
+    int32_t* sector_idx;  /* WorldSectorIndexer packing, ascending linear order */
+    uint64_t* alloc_mask;
+    uint8_t* bricks;      /* n_bricks x 512 */
+} vrt_sector_stream;
+void vrt_sector_stream_free(vrt_sector_stream* s);
+
+/* Write / read a cvox v4 file from / into a sector stream.  Blobs are zstd frames:
+ * written with stored blocks (any zstd decoder, the reference's included, reads
+ * them); read natively when stored or RLE, through the system libzstd.so.1 when
+ * compressed (VRT_ERR_FORMAT when that library is absent).  The palette is
+ * written as default materials and ignored on reading (voxels are raw ids). */
+vrt_status vrt_cvox_write(const char* path, uint32_t n, const int32_t* sector_idx, const uint64_t* alloc_mask,
+                          const uint8_t* bricks);
+vrt_status vrt_cvox_read(const char* path, vrt_sector_stream** out);
+/* Device worlds to / from files (every allocated sector in ascending index order). */
+vrt_status vrt_world_save_cvox(vrt_world* world, const char* path);
+vrt_status vrt_world_load_cvox(vrt_world* world, const char* path, void* stream);
+
 /* ---- traversal ---- */
 /* Cast n explicit rays (host buffers): copies in, traverses, copies out. */
 vrt_status vrt_cast(vrt_world* world, const vrt_ray* rays, uint32_t n, const vrt_cast_params* params,

@@ -19,15 +19,6 @@
 extern "C" {
 #endif
 
-typedef struct vrt_sector_stream {
-    uint32_t sectors_x, sectors_y, sectors_z;
-    uint32_t n_sectors;   /* records */
-    uint64_t n_bricks;    /* bricks in `bricks` */
-    int32_t* sector_idx;  /* WorldSectorIndexer packing, ascending linear order */
-    uint64_t* alloc_mask;
-    uint8_t* bricks;      /* n_bricks x 512 */
-} vrt_sector_stream;
-
 /* Heightfield terrain, optionally minus caves:
  *   solid(x,y,z) = y < base + amplitude * fbm2(x/scale, z/scale)   (octaves, lacunarity 2, gain 0.5)
  *                  and not (caves && fbm3(x/cave_scale, y/cave_scale, z/cave_scale) > cave_threshold)
@@ -53,8 +44,6 @@ double vrt_synth_terrain_height(const vrt_synth_terrain* desc, double x, double 
  * spheres of radius 2..40 filling 0..20% of the volume, and uniform random voxels
  * at density 1..30%.  Spheres win over terrain, terrain over random voxels. */
 vrt_status vrt_synth_mix_world(uint32_t edge, uint64_t seed, int threads, vrt_sector_stream** out);
-
-void vrt_sector_stream_free(vrt_sector_stream* s);
 
 /* n rays with origins uniform in [0,size) (world frame, world origin 0) and
  * directions uniform on the unit sphere (rejection from the cube, IEEE ops only),

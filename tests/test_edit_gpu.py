@@ -138,3 +138,21 @@ def test_invalid_arguments(gpu):
     with pytest.raises(v.VrtError):
         w.sync_sectors([0], [1], None)  # brick data missing
     w.close()
+
+
+def test_world_cvox_save_load(gpu, tmp_path):
+    data = v.synth_mix(96, seed=21)
+    w, o = both_worlds(data)
+    e = np.zeros(2, v.EDIT_DTYPE)
+    e["center"] = [(40, 40, 40), (10, 80, 10)]
+    e["radius"] = [15, 9]
+    e["material"] = [0, 99]
+    w.edit(e)
+    o.edit(e)
+    p = tmp_path / "world.cvox"
+    w.save_cvox(p)
+    w2 = v.World(data.sectors)
+    w2.load_cvox(p)
+    assert_worlds_equal(w2, o)
+    w.close()
+    w2.close()

@@ -109,6 +109,19 @@ def _terrain_desc(size, base, amplitude, seed, scale, octaves, cave_octaves, cav
     return d
 
 
+def cvox_write(path, data: SectorData) -> None:
+    """Write a cvox v4 world file (VoxelMap::Serialize format)."""
+    check(lib().vrt_cvox_write(str(path).encode(), len(data.sector_idx), ptr(data.sector_idx), ptr(data.alloc_mask),
+                               ptr(data.bricks)))
+
+
+def cvox_read(path) -> SectorData:
+    """Read a cvox v4 world file (VoxelMap::Deserialize format)."""
+    out = C.POINTER(capi.SectorStream)()
+    check(lib().vrt_cvox_read(str(path).encode(), C.byref(out)))
+    return SectorData._from_native(out)
+
+
 def synth_mix(edge: int, seed: int, threads: int = 0) -> SectorData:
     out = C.POINTER(capi.SectorStream)()
     check(lib().vrt_synth_mix_world(int(edge), int(seed), int(threads), C.byref(out)))
@@ -190,6 +203,12 @@ class World:
         """Apply vrt_edit records (EDIT_DTYPE array) in order."""
         e = np.ascontiguousarray(edits, dtype=EDIT_DTYPE)
         check(lib().vrt_world_edit(self._h, ptr(e), len(e), _stream_ptr(stream)))
+
+    def save_cvox(self, path) -> None:
+        check(lib().vrt_world_save_cvox(self._h, str(path).encode()))
+
+    def load_cvox(self, path, stream=None) -> None:
+        check(lib().vrt_world_load_cvox(self._h, str(path).encode(), _stream_ptr(stream)))
 
     def read_sector(self, sector_idx: int):
         mask = C.c_uint64()

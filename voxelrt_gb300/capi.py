@@ -144,6 +144,10 @@ PROTOTYPES = {
     "vrt_world_sync_sectors": (_st, [_vp, _u32, _vp, _vp, _vp, _vp, _vp]),
     "vrt_world_edit": (_st, [_vp, _vp, _u32, _vp]),
     "vrt_world_read_sector": (_st, [_vp, _i32, C.POINTER(_u64), _vp, C.c_size_t, _vp]),
+    "vrt_cvox_write": (_st, [C.c_char_p, _u32, _vp, _vp, _vp]),
+    "vrt_cvox_read": (_st, [C.c_char_p, C.POINTER(C.POINTER(SectorStream))]),
+    "vrt_world_save_cvox": (_st, [_vp, C.c_char_p]),
+    "vrt_world_load_cvox": (_st, [_vp, C.c_char_p, _vp]),
     "vrt_cast": (_st, [_vp, _vp, _u32, C.POINTER(CastParams), _vp, _vp]),
     "vrt_cast_device": (_st, [_vp, _vp, _u32, C.POINTER(CastParams), _vp, _vp]),
     "vrt_render_view": (_st, [_vp, C.POINTER(Camera), _u32, _vp, _vp]),

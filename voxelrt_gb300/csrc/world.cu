@@ -400,6 +400,40 @@ vrt_status vrt_world_sync_sectors(vrt_world* w, uint32_t n, const int32_t* secto
     return run_batch(w, batch, stream);
 }
 
+vrt_status vrt_world_save_cvox(vrt_world* w, const char* path) {
+    vrt_status st = world_enter(w);
+    if (st != VRT_OK) return st;
+    std::vector<int32_t> idx;
+    std::vector<uint64_t> masks;
+    std::vector<uint8_t> bricks;
+    {
+        std::lock_guard<std::mutex> lock(w->mu);
+        for (uint32_t y = 0; y < w->sy; y++)
+            for (uint32_t z = 0; z < w->sz; z++)
+                for (uint32_t x = 0; x < w->sx; x++) {
+                    const SectorSlots& s = w->slots[w->lin((int32_t)x, (int32_t)y, (int32_t)z)];
+                    if (!s.mask) continue;
+                    idx.push_back(sector_index_pack((int32_t)x, (int32_t)y, (int32_t)z));
+                    masks.push_back(s.mask);
+                    const size_t nb = (size_t)__builtin_popcountll(s.mask);
+                    const size_t off = bricks.size();
+                    bricks.resize(off + nb * 512);
+                    VRT_CUDA(cudaMemcpy(bricks.data() + off, w->d_payload + (size_t)(s.base - 1) * 512, nb * 512,
+                                        cudaMemcpyDeviceToHost));
+                }
+    }
+    return vrt_cvox_write(path, (uint32_t)idx.size(), idx.data(), masks.data(), bricks.data());
+}
+
+vrt_status vrt_world_load_cvox(vrt_world* w, const char* path, void* stream) {
+    vrt_sector_stream* s = nullptr;
+    vrt_status st = vrt_cvox_read(path, &s);
+    if (st != VRT_OK) return st;
+    st = vrt_world_sync_sectors(w, s->n_sectors, s->sector_idx, s->alloc_mask, nullptr, s->bricks, stream);
+    vrt_sector_stream_free(s);
+    return st;
+}
+
 vrt_status vrt_world_read_sector(vrt_world* w, int32_t sector_idx, uint64_t* alloc_mask, uint8_t* bricks,
                                  size_t bricks_capacity, void* stream_) {
     vrt_status st = world_enter(w);
