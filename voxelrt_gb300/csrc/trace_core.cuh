@@ -62,8 +62,6 @@ struct RayState {
     float sx, sy, sz;     // sideDist
     int32_t vx, vy, vz;   // voxel of the last step (hit voxel on a hit)
     int32_t gx, gy, gz;   // -1 where dir < 0, else 0 (cell alignment side)
-    uint32_t slot;        // 1 + brick slot of the last step when its brick is allocated, else 0
-    uint32_t clo, chi;    // voxel-cell mask of the last step (valid while slot != 0)
     uint32_t material;
 };
 
@@ -95,13 +93,10 @@ __device__ __forceinline__ void ray_init(RayState& s, const DevWorld& w, float o
     s.cy = clip ? __fadd_rn(oy, __fmul_rn(dy, tmin)) : oy;
     s.cz = clip ? __fadd_rn(oz, __fmul_rn(dz, tmin)) : oz;
     s.sx = s.sy = s.sz = 0.0f;
-    // far from every grid voxel, so the first step never reuses a brick or cell
     s.vx = s.vy = s.vz = INT32_MIN;
     s.gx = dx < 0.0f ? -1 : 0;
     s.gy = dy < 0.0f ? -1 : 0;
     s.gz = dz < 0.0f ? -1 : 0;
-    s.slot = 0;
-    s.clo = s.chi = 0;
     s.material = 0;
 }
 
@@ -129,44 +124,27 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
         s.vz = vz;
         return kStepOut;
     }
-    // Consecutive steps mostly stay in one brick, often in one 4^3 cell: the last
-    // step's aligned position is in the same brick (lod <= 3) and, inside an
-    // allocated brick, in the same cell (lod <= 2), so its slot and cell mask are
-    // reused instead of re-reading the sector record and the cell mask.
-    const uint32_t moved = (uint32_t)((vx ^ s.vx) | (vy ^ s.vy) | (vz ^ s.vz));
-    uint32_t lo, hi, idx;
-    int32_t lod;
+    // sector allocation mask at lod 3
     if (kCount) cnt.step_calls++;
-    if (moved >= 8 || s.slot == 0) {
-        // sector allocation mask at lod 3
-        const uint32_t sidx = (uint32_t)(vx >> 5) + (uint32_t)(vz >> 5) * w.sx + (uint32_t)(vy >> 5) * w.sxz;
-        const uint4 rec = __ldg(reinterpret_cast<const uint4*>(w.sectors) + sidx);
-        lo = rec.x;
-        hi = rec.y;
-        idx = ((vx >> 3) & 3) | ((vz >> 3) & 3) << 2 | ((vy >> 3) & 3) << 4;
-        lod = 3;
-        s.slot = 0;
-        if ((((idx < 32 ? lo : hi) >> (idx & 31)) & 1u) != 0) {
-            // brick allocated: slot = base + popcount of the mask below the brick bit
-            const uint32_t below = (1u << (idx & 31)) - 1u;
-            s.slot = 1 + rec.z + (idx < 32 ? __popc(lo & below) : __popc(lo) + __popc(hi & below));
-        }
-    }
-    if (s.slot != 0) {
-        if (moved >= 4) {
-            const uint32_t cell = ((vx >> 2) & 1) | ((vz >> 2) & 1) << 1 | ((vy >> 2) & 1) << 2;
-            const uint2 cm = __ldg(reinterpret_cast<const uint2*>(w.occ) + (size_t)(s.slot - 1) * 8 + cell);
-            s.clo = cm.x;
-            s.chi = cm.y;
-        }
-        lo = s.clo;
-        hi = s.chi;
+    const uint32_t sidx = (uint32_t)(vx >> 5) + (uint32_t)(vz >> 5) * w.sx + (uint32_t)(vy >> 5) * w.sxz;
+    const uint4 rec = __ldg(reinterpret_cast<const uint4*>(w.sectors) + sidx);
+    uint32_t lo = rec.x, hi = rec.y;
+    uint32_t idx = ((vx >> 3) & 3) | ((vz >> 3) & 3) << 2 | ((vy >> 3) & 3) << 4;
+    int32_t lod = 3;
+    if ((((idx < 32 ? lo : hi) >> (idx & 31)) & 1u) != 0) {
+        // brick allocated: slot = base + popcount of the mask below the brick bit
+        const uint32_t below = (1u << (idx & 31)) - 1u;
+        const uint32_t slot = rec.z + (idx < 32 ? __popc(lo & below) : __popc(lo) + __popc(hi & below));
+        const uint32_t cell = ((vx >> 2) & 1) | ((vz >> 2) & 1) << 1 | ((vy >> 2) & 1) << 2;
+        const uint2 cm = __ldg(reinterpret_cast<const uint2*>(w.occ) + (size_t)slot * 8 + cell);
+        lo = cm.x;
+        hi = cm.y;
         idx = (vx & 3) | (vz & 3) << 2 | (vy & 3) << 4;
         lod = 0;
         if (kCount) cnt.occ_fetches++;
         if ((((idx < 32 ? lo : hi) >> (idx & 31)) & 1u) != 0) {
             const uint32_t vi = (vx & 7) | (vz & 7) << 3 | (vy & 7) << 6;
-            s.material = __ldg(w.payload + (size_t)(s.slot - 1) * 512 + vi);
+            s.material = __ldg(w.payload + (size_t)slot * 512 + vi);
             s.vx = vx;
             s.vy = vy;
             s.vz = vz;
