@@ -45,6 +45,11 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="bounded CPU-oracle sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-per-view", action="store_true")
+    ap.add_argument("--no-serving", action="store_true", help="skip the request-server run")
+    ap.add_argument("--serve-rates", default="50,200,1000,2000", help="render requests per second to sweep")
+    ap.add_argument("--serve-seconds", type=float, default=2.0, help="duration of each arrival-rate run")
+    ap.add_argument("--serve-worlds", type=int, default=32)
+    ap.add_argument("--serve-max-edge", type=int, default=1024)
     ap.add_argument("--worlds", type=int, default=128, help="uneven_batch: number of worlds")
     ap.add_argument("--max-views", type=int, default=16, help="uneven_batch: views per world, at most")
     return ap.parse_args()
@@ -327,6 +332,15 @@ def run_ours(args):
                "sample": f"{nv} smallest views of the workload, {r} rays, CPU oracle (scalar restatement of "
                          f"CpuRenderer.cpp RayCast) on all host threads"}
 
+    serving = None
+    if rank == 0 and not args.no_serving and args.workload == "uneven_batch":
+        del hits, host, batch
+        for w in worlds:
+            w.close()
+        worlds = []
+        torch.cuda.empty_cache()
+        serving = run_serving(args, dev)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "Grays/s", "n_gpus": ws, "steps": args.steps,
@@ -342,12 +356,134 @@ def run_ours(args):
             "clocks": clk.summary(), "per_view": per_view,
             "batched_over_per_view": (value / per_view["value"]) if per_view else None,
             "parity_sample": parity,
+            "serving": serving,
             "traversal": {"step_calls": meas["step_calls"], "occ_fetches": meas["occ_fetches"],
                           "hits": meas["hits"], "mean_steps_per_ray": meas["step_calls"] / max(rays_per_step, 1)},
         }
         print(json.dumps(line), flush=True)
     if pg is not None:
         pg.destroy_process_group()
+
+
+def surface_points(w, edge, n, seed):
+    """Random surface voxels: rays cast straight down from the top of random columns."""
+    import voxelrt_gb300 as v
+    rng = np.random.default_rng(seed)
+    org = np.stack([rng.uniform(0, edge, n), np.full(n, edge - 0.5), rng.uniform(0, edge, n)], 1)
+    d = np.tile(np.array([[1e-4, -1.0, 1e-4]], np.float32), (n, 1))
+    rays = np.zeros(n, v.RAY_DTYPE)
+    rays["origin"], rays["dir"] = org.astype(np.float32), d
+    h = w.cast(rays, max_iters=1000)
+    vox = v.unpack_voxel(h["voxel"][h["voxel"] != v.MISS_VOXEL])
+    return vox if len(vox) else np.array([[edge // 2, edge // 2, edge // 2]])
+
+
+def run_serving(args, dev):
+    """Poisson render arrivals (+100 edits/s) against the request server, per arrival rate."""
+    import collections
+
+    import voxelrt_gb300 as v
+    from oracle.oracle import OracleWorld
+    from voxelrt_gb300 import workloads as W
+    datas = W.serving_worlds(n_worlds=args.serve_worlds, max_edge=args.serve_max_edge)
+    worlds, edges, surf = [], [], []
+    for i, d in enumerate(datas):
+        w = v.World(d.sectors, brick_capacity=d.n_bricks + 4096, device=dev)
+        w.upload(d)
+        worlds.append(w)
+        edges.append(d.sectors[0] * 32)
+        surf.append(surface_points(w, edges[-1], 256, seed=i))
+    srv = v.Server(worlds, max_inflight=3)
+    max_rec = 1920 * 1080
+    bufs = [v.PinnedHits(max_rec) for _ in range(24)]
+    out = []
+    check_world = int(np.argmin(edges))
+    replay = {"renders": 0, "bit_exact": True}
+    for ri, lam in enumerate(float(x) for x in args.serve_rates.split(",")):
+        sched = W.serving_schedule(lam, args.serve_seconds, len(worlds), edges, seed=100 + ri)
+        srv.stats(reset=True)
+        free = list(range(len(bufs)))
+        inflight = collections.deque()
+        infos, log, samples = [], [], []
+        rng = np.random.default_rng(ri)
+
+        def retire():
+            t, b, res, sample = inflight.popleft()
+            info = srv.wait(t, timeout_ms=60000)
+            info["res"] = res
+            infos.append(info)
+            if sample is not None:
+                sample["got"] = bufs[b].array[:sample["n"]].copy()
+            free.append(b)
+
+        t0 = time.perf_counter()
+        for (t, kind, wi, payload) in sched:
+            while True:
+                now = time.perf_counter() - t0
+                if now >= t:
+                    break
+                time.sleep(min(t - now, 2e-4))
+            if kind == "render":
+                while not free:
+                    retire()
+                b = free.pop()
+                n = v.view_records(payload)
+                sample = None
+                if ri == 0 and wi == check_world and len(samples) < 6:
+                    sample = {"view": payload, "n": n, "order": len(log)}
+                    samples.append(sample)
+                tk = srv.submit_render(payload, bufs[b].array[:n])
+                inflight.append((tk, b, (payload.cam.width, payload.cam.height), sample))
+                log.append(("render", wi, None))
+            else:
+                radius, material, pick = payload
+                c = surf[wi][pick % len(surf[wi])]
+                e = np.zeros(1, v.EDIT_DTYPE)
+                e["center"], e["radius"], e["material"] = c, radius, material
+                srv.submit_edit(wi, e)
+                log.append(("edit", wi, e))
+        while inflight:
+            retire()
+        srv.drain()
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        lat = np.array([i["done_us"] - i["submit_us"] for i in infos]) / 1e3
+        hd = np.array([i["done_us"] - i["submit_us"] for i in infos if i["res"] == (1920, 1080)]) / 1e3
+        rays = sum(i["rays"] for i in infos)
+        out.append({"rate_req_s": lam, "renders": len(infos), "edits": st["edits_done"], "launches": st["launches"],
+                    "grays_s": rays / wall / 1e9, "p50_ms": float(np.percentile(lat, 50)),
+                    "p99_ms": float(np.percentile(lat, 99)), "p999_ms": float(np.percentile(lat, 99.9)),
+                    "p99_1080p_ms": float(np.percentile(hd, 99)) if len(hd) else None,
+                    "mean_batch": float(np.mean([i["batch_size"] for i in infos])), "busy_s": st["busy_seconds"],
+                    "wall_s": wall})
+        if ri == 0 and samples:
+            # replay the log of the checked world on the oracle: edits in submission order
+            o = OracleWorld(datas[check_world].sectors)
+            o.upload(datas[check_world])
+            si = 0
+            for k, (kind, wi, e) in enumerate(log):
+                while si < len(samples) and samples[si]["order"] == k:
+                    vw = samples[si]["view"]
+                    want = o.render_view(vw.cam, vw.max_iters)
+                    got = samples[si]["got"]
+                    ok = all(np.array_equal(got[f], want[f]) for f in ("voxel", "face", "material", "steps", "tag"))
+                    fin = np.isfinite(want["t"])
+                    ok &= bool(np.allclose(got["t"][fin], want["t"][fin], rtol=1e-6, atol=0))
+                    replay["bit_exact"] &= ok
+                    replay["renders"] += 1
+                    si += 1
+                if kind == "edit" and wi == check_world:
+                    o.edit(e)
+            o.close()
+    srv.close()
+    for b in bufs:
+        b.close()
+    for w in worlds:
+        w.close()
+    return {"worlds": len(datas), "max_edge": max(edges), "world_bytes": int(sum(d.n_bricks for d in datas) * 576),
+            "resolutions": "256^2 / 1280x720 / 1920x1080 at p 0.5 / 0.3 / 0.2", "edits_per_s": 100,
+            "seconds_per_rate": args.serve_seconds, "rates": out, "oracle_replay": replay,
+            "latency": "submit to records in pinned host memory, server clock"}
 
 
 def parity_sample(wl, batch, hits, stream, max_views=3):

@@ -20,7 +20,8 @@ from . import capi
 from .capi import (EDIT_DTYPE, HIT_DTYPE, MISS_FACE, MISS_VOXEL, NO_RAY, RAY_DTYPE, VIEW_SHADOW, BatchConfig, Camera,
                    CastParams, View, VrtError, check, lib, ptr)
 
-__all__ = ["World", "Camera", "View", "make_view", "Batch", "BatchConfig", "VIEW_SHADOW", "look_at", "synth_terrain", "synth_mix", "random_rays", "SectorData", "VrtError",
+__all__ = ["Server", "PinnedHits", "view_records", "render_path", "cvox_read", "cvox_write", "World", "Camera", "View",
+           "make_view", "Batch", "BatchConfig", "VIEW_SHADOW", "look_at", "synth_terrain", "synth_mix", "random_rays", "SectorData", "VrtError",
            "RAY_DTYPE", "HIT_DTYPE", "EDIT_DTYPE", "MISS_VOXEL", "MISS_FACE", "NO_RAY", "unpack_voxel", "sector_index",
            "lib"]
 

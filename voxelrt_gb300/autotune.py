@@ -117,3 +117,47 @@ def tune(worlds, views, hits, stream, log=print) -> tuple[dict, float, list]:
             if ms < best_ms:
                 best, best_ms = d, ms
     return best, best_ms, trials
+
+
+def main(argv=None) -> None:
+    """python -m voxelrt_gb300.autotune [--workload uneven_batch] [--out PATH]
+
+    Tunes the batched launch on a workload of voxelrt_gb300.workloads and stores the
+    winner under this GPU's name (default: the user cache)."""
+    import argparse
+    import json as _json
+
+    import torch
+
+    from . import World
+    from . import workloads as W
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="uneven_batch", choices=["uneven_batch", "large_world", "incoherent"])
+    ap.add_argument("--out", default=None)
+    ap.add_argument("--worlds", type=int, default=128)
+    a = ap.parse_args(argv)
+    if a.workload == "uneven_batch":
+        wl = W.uneven_batch(n_worlds=a.worlds)
+    elif a.workload == "large_world":
+        wl = W.large_world()
+    else:
+        wl = W.incoherent()
+    worlds = []
+    for d in wl.worlds:
+        w = World(d.sectors, brick_capacity=d.n_bricks + 64)
+        w.upload(d)
+        worlds.append(w)
+    from . import Batch
+    records = Batch(worlds, wl.views).total_records
+    hits = torch.empty(records * 16, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+    best, ms, trials = tune(worlds, wl.views, hits, stream)
+    rays = wl.primary_rays
+    path = store(wl.name, best, {"ms": ms, "primary_rays": rays, "trials": len(trials)},
+                 path=Path(a.out) if a.out else None)
+    print(_json.dumps({"workload": wl.name, "best": best, "ms": ms, "gpu": gpu_name(), "stored": str(path)}))
+
+
+if __name__ == "__main__":
+    main()

@@ -20,6 +20,7 @@
 #include <deque>
 #include <memory>
 #include <mutex>
+#include <string>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -47,6 +48,7 @@ struct Request {
     std::vector<vrt_edit> edits;
     uint32_t batch_size = 0;
     double submit_us = 0, start_us = 0, done_us = 0;
+    std::string error;  // why the request failed (the scheduler thread's error text)
 };
 
 struct Slot {
@@ -55,6 +57,9 @@ struct Slot {
     ViewDev* h_views = nullptr;  // pinned staging
     uint32_t* h_cb = nullptr;
     size_t staged_cap = 0;
+    // recorded after a launch's copies; its status, not the stream's, says whether the
+    // launch succeeded (the stream is still busy with the completion callback itself)
+    cudaEvent_t done = nullptr;
     std::vector<Request*> reqs;
     bool busy = false;
     std::atomic<bool> complete{false};
@@ -128,6 +133,7 @@ vrt_status refresh_world_table(vrt_server* sv) {
 
 void finish(vrt_server* sv, Request* r, vrt_status st, double t) {
     r->status = st;
+    if (st != VRT_OK) r->error = last_error_cstr();
     r->state = st == VRT_OK ? VRT_REQ_DONE : VRT_REQ_FAILED;
     r->done_us = t;
     if (r->pages) {
@@ -182,6 +188,7 @@ vrt_status launch_slot(vrt_server* sv, Slot& s, std::vector<Request*>& rs) {
                                  r->records * sizeof(vrt_hit), cudaMemcpyDeviceToHost, s.stream));
     }
     s.complete.store(false);
+    VRT_CUDA(cudaEventRecord(s.done, s.stream));
     VRT_CUDA(cudaLaunchHostFunc(s.stream, slot_done_cb, &s));
     return VRT_OK;
 }
@@ -197,7 +204,10 @@ void worker_main(vrt_server* sv) {
         for (auto& sp : sv->slots) {
             Slot& s = *sp;
             if (!s.busy || !s.complete.load()) continue;
-            cudaError_t e = cudaStreamQuery(s.stream);
+            // the event completed before the callback ran, so it reports the launch's
+            // own status (or a sticky error), never "not ready"
+            cudaError_t e = cudaEventQuery(s.done);
+            if (e == cudaErrorNotReady) continue;
             const vrt_status st = e == cudaSuccess ? VRT_OK : cuda_fail(e, "server launch");
             for (Request* r : s.reqs) finish(sv, r, st, t);
             s.reqs.clear();
@@ -346,7 +356,15 @@ vrt_status vrt_server_create(vrt_world* const* worlds, uint32_t n_worlds, const 
         s->server = sv;
         if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess)
             return fail(cuda_fail(e, "slot stream"));
-        if ((e = s->queue.reserve(64)) != cudaSuccess) return fail(cuda_fail(e, "slot queue"));
+        if ((e = cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming)) != cudaSuccess) {
+            cudaStreamDestroy(s->stream);
+            return fail(cuda_fail(e, "slot event"));
+        }
+        if ((e = s->queue.reserve(64)) != cudaSuccess) {
+            cudaEventDestroy(s->done);
+            cudaStreamDestroy(s->stream);
+            return fail(cuda_fail(e, "slot queue"));
+        }
         sv->slots.push_back(std::move(s));
     }
     sv->worker = std::thread(worker_main, sv);
@@ -378,6 +396,7 @@ vrt_status vrt_server_destroy(vrt_server* sv, uint32_t timeout_ms) {
             cudaStreamSynchronize(s->stream);
             cudaStreamDestroy(s->stream);
         }
+        if (s->done) cudaEventDestroy(s->done);
         s->views.release();
         s->chunk_base.release();
         s->queue.release();
@@ -487,7 +506,7 @@ vrt_status vrt_server_wait(vrt_server* sv, uint64_t ticket, uint32_t timeout_ms,
         return VRT_ERR_QUEUE_TIMEOUT;
     }
     if (r->state == VRT_REQ_FAILED) {
-        set_error("request failed");
+        set_error("request failed: " + r->error);
         return r->status;
     }
     return VRT_OK;

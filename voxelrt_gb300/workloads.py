@@ -98,3 +98,49 @@ def incoherent(n_bounces=4, threads=0) -> Workload:
     cam = look_at((512, 300, 0), (512, 100, 512), 90.0, 1280, 720)
     return Workload("incoherent", [d], [make_view(cam, world=0, n_bounces=n_bounces)],
                     f"1024^3 terrain+caves seed 4, 1280x720 primary + {n_bounces} diffuse bounces")
+
+
+SERVING_RESOLUTIONS = [(256, 256), (1280, 720), (1920, 1080)]
+SERVING_RES_P = [0.5, 0.3, 0.2]
+
+
+def serving_worlds(n_worlds=32, max_edge=1024, seed=4, threads=0) -> list:
+    """Resident worlds of the serving workload: mixed worlds, edge log-uniform in [64, max_edge]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_worlds):
+        edge = int(round(math.exp(rng.uniform(math.log(64), math.log(max_edge))) / 32.0)) * 32
+        out.append(synth_mix(min(max_edge, max(64, edge)), seed=seed * 100019 + i, threads=threads))
+    return out
+
+
+def serving_schedule(rate: float, seconds: float, n_worlds: int, edges, seed: int = 0, edit_rate: float = 100.0):
+    """Poisson arrivals of render requests (rate per second) and sphere edits (edit_rate per
+    second): list of (time, kind, world, payload) sorted by time.  Render payload is a
+    vrt_view; edit payload is (radius, material) for a surface point chosen at run time."""
+    rng = np.random.default_rng(seed)
+    events = []
+    t = 0.0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= seconds:
+            break
+        wi = int(rng.integers(0, n_worlds))
+        edge = edges[wi]
+        w, h = SERVING_RESOLUTIONS[int(rng.choice(3, p=SERVING_RES_P))]
+        pos = rng.uniform(0, edge, 3)
+        tgt = rng.uniform(0, edge, 3)
+        if np.linalg.norm(tgt - pos) < 1.0:
+            tgt = pos + np.array([1.0, 0.0, 0.0])
+        cam = look_at(pos, tgt, float(rng.uniform(60, 90)), w, h)
+        events.append((t, "render", wi, make_view(cam, world=wi)))
+    t = 0.0
+    while edit_rate > 0:
+        t += rng.exponential(1.0 / edit_rate)
+        if t >= seconds:
+            break
+        wi = int(rng.integers(0, n_worlds))
+        events.append((t, "edit", wi, (int(rng.integers(4, 33)), 0 if rng.random() < 0.5 else int(rng.integers(1, 256)),
+                                       int(rng.integers(0, 1 << 30)))))
+    events.sort(key=lambda e: e[0])
+    return events
