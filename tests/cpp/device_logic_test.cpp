@@ -1,8 +1,9 @@
 // device_logic_test.cpp - compiles the device traversal step (trace_core.cuh) for the
 // host, with the CUDA rounding intrinsics mapped to their IEEE host equivalents, and
 // runs it over a world and ray batch dumped by the Python test; the records go back
-// to be compared with the oracle.  This checks the kernel's control logic (brick and
-// cell reuse, alignment, NaN handling) on every CPU test run, without a GPU.
+// to be compared with the oracle.  This checks the kernel's control logic (brick
+// table and voxel codes, alignment, clipping, NaN handling) on every CPU test run,
+// without a GPU.
 //
 //   device_logic_test <world.bin> <rays.bin> <out.bin> <max_iters> <wox> <woy> <woz>
 #include <cmath>
@@ -26,6 +27,7 @@ inline float __fadd_rn(float a, float b) { return a + b; }
 inline float __fsub_rn(float a, float b) { return a - b; }
 inline float __fmul_rn(float a, float b) { return a * b; }
 inline float __fdiv_rn(float a, float b) { return a / b; }
+inline float __frcp_rn(float a) { return 1.0f / a; }
 inline float __fsqrt_rn(float a) { return std::sqrt(a); }
 inline float __int2float_rn(int a) { return (float)a; }
 inline float __uint2float_rn(unsigned a) { return (float)a; }
@@ -57,22 +59,22 @@ int main(int argc, char** argv) {
     if (argc < 8) return 2;
     FILE* f = std::fopen(argv[1], "rb");
     if (!f) return 3;
-    uint32_t dims[3], nsec, nslots;
-    if (std::fread(dims, 4, 3, f) != 3 || std::fread(&nsec, 4, 1, f) != 1 || std::fread(&nslots, 4, 1, f) != 1) return 4;
-    std::vector<SectorRec> sectors(nsec);
-    std::vector<uint64_t> occ((size_t)nslots * 8);
+    uint32_t dims[3], nslots;
+    if (std::fread(dims, 4, 3, f) != 3 || std::fread(&nslots, 4, 1, f) != 1) return 4;
+    const size_t npos = (size_t)dims[0] * dims[1] * dims[2] * 64;
+    std::vector<uint32_t> bricks(npos);
+    std::vector<uint32_t> codes((size_t)nslots * 32);
     std::vector<uint8_t> payload((size_t)nslots * 512);
-    if (std::fread(sectors.data(), sizeof(SectorRec), nsec, f) != nsec) return 5;
-    if (std::fread(occ.data(), 8, occ.size(), f) != occ.size()) return 6;
+    if (std::fread(bricks.data(), 4, npos, f) != npos) return 5;
+    if (std::fread(codes.data(), 4, codes.size(), f) != codes.size()) return 6;
     if (std::fread(payload.data(), 1, payload.size(), f) != payload.size()) return 7;
     std::fclose(f);
-    DevWorld w;
-    w.sectors = sectors.data();
-    w.occ = occ.data();
+    DevWorld w{};
+    w.bricks = bricks.data();
+    w.codes = codes.data();
     w.payload = payload.data();
-    w.sx = dims[0];
-    w.sz = dims[2];
-    w.sxz = dims[0] * dims[2];
+    w.bsx = dims[0] * 4;
+    w.bsxz = dims[0] * 4 * dims[2] * 4;
     w.size_x = dims[0] * 32;
     w.size_y = dims[1] * 32;
     w.size_z = dims[2] * 32;

@@ -2,7 +2,7 @@
 
 tests/cpp/device_logic_test.cpp includes voxelrt_gb300/csrc/trace_core.cuh with the
 CUDA rounding intrinsics mapped to IEEE host operations; the worlds are laid out
-exactly as the device stores them (sector records, brick-slot pools).  Every record
+exactly as the device stores them (brick table, voxel codes, brick-slot pools).  Every record
 must match the oracle, which checks the kernel's control flow on each CPU run.
 """
 import subprocess
@@ -29,26 +29,41 @@ def exe():
 
 
 def device_layout(data: v.SectorData) -> bytes:
-    """Sector table + slot pools as the device holds them (sectors in stream order)."""
+    """Brick table + slot pools as the device holds them (slots in stream order).
+
+    Derived here from the geometric definitions, independently of the device's bit
+    tricks: an empty brick position skips to level 5 when its sector holds no brick,
+    to 4 when the aligned 2x2x2 group of bricks around it is empty, else 3; an empty
+    voxel of an allocated brick codes 3 when its aligned 4^3 cell is empty, 2 when its
+    aligned 2^3 block is, else 1; a solid voxel codes 0."""
     sx, sy, sz = data.sectors
-    table = np.zeros((sx * sy * sz, 4), np.uint32)
-    nb = data.n_bricks
-    occ = np.zeros((nb, 8), np.uint64)
+    alloc = np.zeros((sy * 4, sz * 4, sx * 4), bool)          # (by, bz, bx)
+    slot_of = np.zeros((sy * 4, sz * 4, sx * 4), np.uint32)
     slot = 0
     for idx, m in zip(data.sector_idx.tolist(), data.alloc_mask.tolist()):
         x, z, y = idx & 4095, (idx >> 12) & 4095, (idx >> 24) & 255
-        s = x + z * sx + y * sx * sz
-        table[s] = [m & 0xFFFFFFFF, m >> 32, slot, 0]
-        slot += bin(m).count("1")
-    # cell masks: bit vx + vz*4 + vy*16 of cell cx | cz<<1 | cy<<2
-    b = data.bricks.reshape(nb, 8, 8, 8) != 0  # (y, z, x)
-    for c in range(8):
-        cx, cz, cy = c & 1, (c >> 1) & 1, c >> 2
-        cell = b[:, cy * 4:cy * 4 + 4, cz * 4:cz * 4 + 4, cx * 4:cx * 4 + 4]  # (n, vy, vz, vx)
-        bits = cell.reshape(nb, 64).astype(np.uint64)
-        occ[:, c] = (bits << np.arange(64, dtype=np.uint64)).sum(axis=1, dtype=np.uint64)
-    head = np.array([sx, sy, sz, len(table), nb], np.uint32).tobytes()
-    return head + table.tobytes() + occ.tobytes() + data.bricks.tobytes()
+        for b in range(64):
+            if m >> b & 1:
+                bx, bz, by = x * 4 + (b & 3), z * 4 + ((b >> 2) & 3), y * 4 + (b >> 4)
+                alloc[by, bz, bx] = True
+                slot_of[by, bz, bx] = slot
+                slot += 1
+    sector_any = alloc.reshape(sy, 4, sz, 4, sx, 4).any(axis=(1, 3, 5))
+    group_any = alloc.reshape(sy * 2, 2, sz * 2, 2, sx * 2, 2).any(axis=(1, 3, 5))
+    up4 = lambda a: a.repeat(4, 0).repeat(4, 1).repeat(4, 2)
+    up2 = lambda a: a.repeat(2, 0).repeat(2, 1).repeat(2, 2)
+    level = np.where(~up4(sector_any), 5, np.where(~up2(group_any), 4, 3)).astype(np.uint32)
+    table = np.where(alloc, slot_of, np.uint32(0x80000000) | level).astype(np.uint32)
+    nb = data.n_bricks
+    solid = data.bricks.reshape(nb, 8, 8, 8) != 0             # (n, y, z, x)
+    cell_any = solid.reshape(nb, 2, 4, 2, 4, 2, 4).any(axis=(2, 4, 6))
+    block_any = solid.reshape(nb, 4, 2, 4, 2, 4, 2).any(axis=(2, 4, 6))
+    up = lambda a, k: a.repeat(k, 1).repeat(k, 2).repeat(k, 3)
+    code = np.where(solid, 0, np.where(~up(cell_any, 4), 3, np.where(~up(block_any, 2), 2, 1))).astype(np.uint32)
+    code = code.reshape(nb, 32, 16)                          # voxel x | z<<3 | y<<6 -> word, position
+    words = (code << (2 * np.arange(16, dtype=np.uint32))).sum(axis=2, dtype=np.uint64).astype(np.uint32)
+    head = np.array([sx, sy, sz, nb], np.uint32).tobytes()
+    return head + table.tobytes() + words.tobytes() + data.bricks.tobytes()
 
 
 def run(exe, tmp_path, data, rays, max_iters=128, wo=(0, 0, 0)):

@@ -105,8 +105,8 @@ def tune(worlds, views, hits, stream, log=print) -> tuple[dict, float, list]:
     stages = [
         [dict(tile_w=tw, tile_h=th, morton=m, warps_per_block=wp)
          for (tw, th, m), wp in itertools.product([(8, 8, 0), (8, 8, 1), (16, 4, 0), (32, 1, 0)], [2, 4, 8])],
-        [dict(refill_threshold=r, inner_iters=i) for r, i in itertools.product([4, 12, 20, 28, 32], [1, 2, 4, 8])],
-        [dict(chunk_tiles=c) for c in (1, 2, 4, 8)],
+        [dict(refill_threshold=r, inner_iters=i) for r, i in itertools.product([4, 8, 12, 16, 20, 24, 28], [2, 4, 8, 16])],
+        [dict(chunk_tiles=c) for c in (1, 2, 4, 8, 16, 32, 64)],
     ]
     for stage in stages:
         for delta in stage:

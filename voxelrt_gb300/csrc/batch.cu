@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(64) view_path_kernel(DevWorld w, ViewDev v, ui
 }
 
 template <bool kCount>
-__global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
+__global__ void __maxnreg__(64) persistent_kernel(BatchParams p) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt = (1u << lane) - 1u;
     // warp-uniform queue state: rays [q_next, q_end) of view q_view

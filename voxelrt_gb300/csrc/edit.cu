@@ -8,7 +8,8 @@
 // Because voxels are independent, the batch is applied as
 //   1. host: bricks a fill reaches that are not allocated get slots (sector repack);
 //   2. device: one warp per touched brick applies every edit of the batch in order,
-//      derives the 8 cell masks by ballot and flags empty bricks;
+//      derives the 8 cell masks by ballot, stores the voxel codes and flags empty
+//      bricks;
 //   3. host: empty bricks are freed (sector repack).
 // The final state equals applying the edits one by one.
 
@@ -18,6 +19,7 @@
 #include <map>
 #include <vector>
 
+#include "brick_codes.cuh"
 #include "world.h"
 
 namespace vrt {
@@ -44,7 +46,7 @@ constexpr int kEditWarps = 8;
 
 __global__ void __launch_bounds__(kEditWarps * 32)
     edit_bricks_kernel(const TouchedBrick* __restrict__ bricks, uint32_t n, const EditDev* __restrict__ edits,
-                       uint32_t n_edits, uint8_t* __restrict__ payload, uint64_t* __restrict__ occ,
+                       uint32_t n_edits, uint8_t* __restrict__ payload, uint32_t* __restrict__ codes,
                        uint8_t* __restrict__ empty) {
     __shared__ __align__(16) uint8_t sb[kEditWarps][512];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -73,20 +75,9 @@ __global__ void __launch_bounds__(kEditWarps * 32)
         reinterpret_cast<uint4*>(payload + (size_t)tb.slot * 512)[lane] = v;
         reinterpret_cast<uint4*>(sb[wib])[lane] = v;
         __syncwarp();
-        // cell masks: round r = cell c (r>>1), half h (r&1); lane l tests voxel
-        // (4cx + (l&3), 4cy + 2h + (l>>4), 4cz + ((l>>2)&3)) -> bit l of half h
-        uint64_t mine = 0;
-        bool any = false;
-#pragma unroll
-        for (uint32_t r = 0; r < 16; r++) {
-            const uint32_t c = r >> 1, h = r & 1;
-            const uint32_t x = (c & 1) * 4 + (lane & 3), zz = ((c >> 1) & 1) * 4 + ((lane >> 2) & 3);
-            const uint32_t yy = (c >> 2) * 4 + 2 * h + (lane >> 4);
-            const uint32_t bits = __ballot_sync(0xffffffffu, sb[wib][x | zz << 3 | yy << 6] != 0);
-            any |= bits != 0;
-            if (lane == c) mine |= (uint64_t)bits << (32 * h);
-        }
-        if (lane < 8) occ[(size_t)tb.slot * 8 + lane] = mine;
+        const uint64_t cells = warp_cell_mask(sb[wib], lane);
+        codes[(size_t)tb.slot * 32 + lane] = warp_voxel_codes(sb[wib], cells, lane);
+        const bool any = __any_sync(0xffffffffu, cells != 0);
         if (lane == 0) empty[k] = any ? 0 : 1;
         __syncwarp();
     }
@@ -187,7 +178,7 @@ extern "C" vrt_status vrt_world_edit(vrt_world* w, const vrt_edit* edits, uint32
     VRT_CUDA(cudaMemcpyAsync(base + boff, tb.data(), bb, cudaMemcpyHostToDevice, stream));
     const uint32_t blocks = std::max(1u, std::min<uint32_t>(((uint32_t)tb.size() + kEditWarps - 1) / kEditWarps, 152u * 16u));
     edit_bricks_kernel<<<blocks, kEditWarps * 32, 0, stream>>>((const TouchedBrick*)(base + boff), (uint32_t)tb.size(),
-                                                               (const EditDev*)base, n, w->d_payload, w->d_occ,
+                                                               (const EditDev*)base, n, w->d_payload, w->d_codes,
                                                                base + foff);
     VRT_CUDA(cudaGetLastError());
     std::vector<uint8_t> empty(tb.size());

@@ -1,10 +1,10 @@
 // trace_core.cuh - per-ray brickmap traversal on the device.
 //
-// One thread walks one ray through sector mask -> brick cell mask -> voxel, the
+// One thread walks one ray through brick table -> voxel code -> voxel, the
 // loop of RayCast/GetStepPos (src/VoxelRT/CpuRenderer.cpp:135-224) with the entry
 // clip of clipRayToAABB (src/VoxelRT/Shaders/VoxelTraversal.glsl:133-145).
 // Every float op is an explicitly rounded intrinsic (__fadd_rn, __fmul_rn,
-// __fdiv_rn, __fsqrt_rn) in the reference's source order, so results do not
+// __fdiv_rn, __frcp_rn, __fsqrt_rn) in the reference's source order, so results do not
 // depend on -fmad; min/max use the x86 minps/maxps NaN rule and floor->int uses
 // the x86 out-of-range value INT32_MIN (SIMD_AVX512.h:109,123).
 #pragma once
@@ -74,21 +74,35 @@ __device__ __forceinline__ void ray_init(RayState& s, const DevWorld& w, float o
     s.dx = dx;
     s.dy = dy;
     s.dz = dz;
-    s.ix = __fdiv_rn(1.0f, dx);
-    s.iy = __fdiv_rn(1.0f, dy);
-    s.iz = __fdiv_rn(1.0f, dz);
+    // correctly rounded 1/dir, the same value as the IEEE division 1.0f / dir
+    s.ix = __frcp_rn(dx);
+    s.iy = __frcp_rn(dy);
+    s.iz = __frcp_rn(dz);
     s.tsx = __fmul_rn(__fsub_rn(dx < 0.0f ? 0.0f : 1.0f, ox), s.ix);
     s.tsy = __fmul_rn(__fsub_rn(dy < 0.0f ? 0.0f : 1.0f, oy), s.iy);
     s.tsz = __fmul_rn(__fsub_rn(dz < 0.0f ? 0.0f : 1.0f, oz), s.iz);
-    const float t1x = __fmul_rn(__fsub_rn(__int2float_rn(1 - wox), ox), s.ix);
-    const float t1y = __fmul_rn(__fsub_rn(__int2float_rn(1 - woy), oy), s.iy);
-    const float t1z = __fmul_rn(__fsub_rn(__int2float_rn(1 - woz), oz), s.iz);
-    const float t2x = __fmul_rn(__fsub_rn(__fsub_rn(__fsub_rn(__uint2float_rn(w.size_x), __int2float_rn(wox)), 1.0f), ox), s.ix);
-    const float t2y = __fmul_rn(__fsub_rn(__fsub_rn(__fsub_rn(__uint2float_rn(w.size_y), __int2float_rn(woy)), 1.0f), oy), s.iy);
-    const float t2z = __fmul_rn(__fsub_rn(__fsub_rn(__fsub_rn(__uint2float_rn(w.size_z), __int2float_rn(woz)), 1.0f), oz), s.iz);
-    const float tmin = max_x86(min_x86(t1x, t2x), max_x86(min_x86(t1y, t2y), min_x86(t1z, t2z)));
-    const float tmax = min_x86(max_x86(t1x, t2x), min_x86(max_x86(t1y, t2y), max_x86(t1z, t2z)));
-    const bool clip = tmin > 0.0f && tmin < tmax;
+    // clip box [1 - worldOrigin, size - 1 - worldOrigin] (VoxelTraversal.glsl:166)
+    const float lx = __int2float_rn(1 - wox), ly = __int2float_rn(1 - woy), lz = __int2float_rn(1 - woz);
+    const float hx = __fsub_rn(__fsub_rn(__uint2float_rn(w.size_x), __int2float_rn(wox)), 1.0f);
+    const float hy = __fsub_rn(__fsub_rn(__uint2float_rn(w.size_y), __int2float_rn(woy)), 1.0f);
+    const float hz = __fsub_rn(__fsub_rn(__uint2float_rn(w.size_z), __int2float_rn(woz)), 1.0f);
+    // An origin strictly inside the box never clips: per axis l - o < 0 < h - o, so
+    // min(t1, t2) is negative (or -inf, or NaN when dir is NaN, which minps/maxps drop)
+    // and tmin <= 0 on every path.  Camera rays of a view share the origin, so the
+    // slab test below runs only for views from outside the world.
+    bool clip = false;
+    float tmin = 0.0f;
+    if (!(lx < ox && ox < hx && ly < oy && oy < hy && lz < oz && oz < hz)) {
+        const float t1x = __fmul_rn(__fsub_rn(lx, ox), s.ix);
+        const float t1y = __fmul_rn(__fsub_rn(ly, oy), s.iy);
+        const float t1z = __fmul_rn(__fsub_rn(lz, oz), s.iz);
+        const float t2x = __fmul_rn(__fsub_rn(hx, ox), s.ix);
+        const float t2y = __fmul_rn(__fsub_rn(hy, oy), s.iy);
+        const float t2z = __fmul_rn(__fsub_rn(hz, oz), s.iz);
+        tmin = max_x86(min_x86(t1x, t2x), max_x86(min_x86(t1y, t2y), min_x86(t1z, t2z)));
+        const float tmax = min_x86(max_x86(t1x, t2x), min_x86(max_x86(t1y, t2y), max_x86(t1z, t2z)));
+        clip = tmin > 0.0f && tmin < tmax;
+    }
     s.cx = clip ? __fadd_rn(ox, __fmul_rn(dx, tmin)) : ox;
     s.cy = clip ? __fadd_rn(oy, __fmul_rn(dy, tmin)) : oy;
     s.cz = clip ? __fadd_rn(oz, __fmul_rn(dz, tmin)) : oz;
@@ -124,36 +138,30 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
         s.vz = vz;
         return kStepOut;
     }
-    // sector allocation mask at lod 3
     if (kCount) cnt.step_calls++;
-    const uint32_t sidx = (uint32_t)(vx >> 5) + (uint32_t)(vz >> 5) * w.sx + (uint32_t)(vy >> 5) * w.sxz;
-    const uint4 rec = __ldg(reinterpret_cast<const uint4*>(w.sectors) + sidx);
-    uint32_t lo = rec.x, hi = rec.y;
-    uint32_t idx = ((vx >> 3) & 3) | ((vz >> 3) & 3) << 2 | ((vy >> 3) & 3) << 4;
-    int32_t lod = 3;
-    if ((((idx < 32 ? lo : hi) >> (idx & 31)) & 1u) != 0) {
-        // brick allocated: slot = base + popcount of the mask below the brick bit
-        const uint32_t below = (1u << (idx & 31)) - 1u;
-        const uint32_t slot = rec.z + (idx < 32 ? __popc(lo & below) : __popc(lo) + __popc(hi & below));
-        const uint32_t cell = ((vx >> 2) & 1) | ((vz >> 2) & 1) << 1 | ((vy >> 2) & 1) << 2;
-        const uint2 cm = __ldg(reinterpret_cast<const uint2*>(w.occ) + (size_t)slot * 8 + cell);
-        lo = cm.x;
-        hi = cm.y;
-        idx = (vx & 3) | (vz & 3) << 2 | (vy & 3) << 4;
-        lod = 0;
+    // The brick table holds the slot of an allocated brick, or for an empty one the
+    // level GetStepPos reaches from the sector mask (3 + skip_levels).  An allocated
+    // brick's voxel code is 0 for a solid voxel (the hit), else 1 + the skip level
+    // of its 4^3 cell mask; both replace the two mask fetches of the reference with
+    // their precomputed outcome.
+    const uint32_t e =
+        __ldg(w.bricks + ((uint32_t)vx >> 3) + ((uint32_t)vz >> 3) * w.bsx + ((uint32_t)vy >> 3) * w.bsxz);
+    int32_t lod;
+    if (e < kBrickEmpty) {
         if (kCount) cnt.occ_fetches++;
-        if ((((idx < 32 ? lo : hi) >> (idx & 31)) & 1u) != 0) {
-            const uint32_t vi = (vx & 7) | (vz & 7) << 3 | (vy & 7) << 6;
-            s.material = __ldg(w.payload + (size_t)slot * 512 + vi);
+        const uint32_t vi = (uint32_t)((vx & 7) | (vz & 7) << 3 | (vy & 7) << 6);
+        const uint32_t code = (__ldg(w.codes + (size_t)e * 32 + (vi >> 4)) >> ((vi & 15) * 2)) & 3u;
+        if (code == 0) {
+            s.material = __ldg(w.payload + (size_t)e * 512 + vi);
             s.vx = vx;
             s.vy = vy;
             s.vz = vz;
             return kStepHit;
         }
+        lod = (int32_t)code - 1;
+    } else {
+        lod = (int32_t)(e & 7u);
     }
-    // level4 (+2) / level2 (+1) from the same mask, then align to the cell boundary
-    const uint32_t half = idx < 32 ? lo : hi;
-    lod += (lo | hi) == 0 ? 2 : (((half >> (idx & 0xA)) & 0x00330033u) == 0 ? 1 : 0);
     // dir < 0 ? pos & ~m : pos | m, as (pos | m) ^ (g & m) with g = -1 for dir < 0
     const int32_t m = (1 << lod) - 1;
     vx = (vx | m) ^ (s.gx & m);

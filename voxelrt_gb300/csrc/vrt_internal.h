@@ -4,12 +4,21 @@
 //   sectors  dense table over the world's sector grid, 16-byte records
 //            {mask lo, mask hi, base slot (0-based), flags}, index
 //            x + z*SX + y*SX*SZ (the order of LinearIndexer3D, VoxelMap.h:95-97);
-//   occ      8 x u64 voxel-cell masks per brick slot (64 B, one line per brick),
-//            cell c = cx | cz<<1 | cy<<2, bit vx + vz*4 + vy*16
-//            (UpdateOccupancy, CpuRenderer.cpp:63-83);
+//            the storage of record: sync, edit, read-back and picking use it;
+//   bricks   the brick table derived from it, one u32 per brick position of the
+//            world, index bx + bz*BX + by*BX*BZ (BX = 4*SX, BZ = 4*SZ): the brick's
+//            slot when its bit is set in the sector mask, else kBrickEmpty | the
+//            skip level GetStepPos takes there (3 + skip_levels of the sector mask,
+//            CpuRenderer.cpp:139-160);
+//   codes    2-bit voxel codes, 32 u32 words (128 B) per brick slot; voxel
+//            v = x | z<<3 | y<<6 sits in word v>>4 at bit 2*(v&15): 0 = solid, else
+//            1 + skip_levels of the 4^3 voxel cell's occupancy mask (cell
+//            cx | cz<<1 | cy<<2, bit vx + vz*4 + vy*16: UpdateOccupancy,
+//            CpuRenderer.cpp:63-83, and GetStepPos :146-160);
 //   payload  512 B of u8 voxel ids per brick slot, voxel x | z<<3 | y<<6.
 // A brick's slot is base + popcount(mask & ((1<<b)-1)) (VoxelMap.glsl:45-64,
-// BrickSlotAllocator.h:37-41).
+// BrickSlotAllocator.h:37-41).  The traversal reads bricks, codes and payload
+// only: one 4-byte load per step, one more on an allocated brick.
 #pragma once
 
 #include <cstdint>
@@ -25,15 +34,35 @@ struct SectorRec {
 };
 static_assert(sizeof(SectorRec) == 16, "sector record is one 16-byte load");
 
+#if defined(__CUDACC__)
+#define VRT_HD __host__ __device__
+#else
+#define VRT_HD
+#endif
+
+// Brick-table entry of an unallocated brick position; the low bits hold the level.
+constexpr uint32_t kBrickEmpty = 0x80000000u;
+
+// Extra levels GetStepPos skips at position idx (0..63) of an empty bit of the
+// 64-bit mask (lo, hi): 2 when the whole mask is 0, 1 when the 2x2x2 block holding
+// idx is empty (bits (idx & 0xA) + {0,1,4,5,16,17,20,21} of the half idx falls
+// in), else 0 (CpuRenderer.cpp:157-159).
+VRT_HD inline uint32_t skip_levels(uint32_t lo, uint32_t hi, uint32_t idx) {
+    const uint32_t half = idx < 32 ? lo : hi;
+    return (lo | hi) == 0 ? 2u : (((half >> (idx & 0xA)) & 0x00330033u) == 0 ? 1u : 0u);
+}
+
 // Kernel-side view of one world (passed by value or stored in a world table).
 struct DevWorld {
-    const SectorRec* sectors;
-    const uint64_t* occ;
+    const uint32_t* bricks;
+    const uint32_t* codes;
     const uint8_t* payload;
-    uint32_t sx, sz;         // sectors along x and z
-    uint32_t sxz;            // sx * sz
+    const SectorRec* sectors;
+    uint32_t bsx, bsxz;               // brick-table strides: 4*SX, 4*SX * 4*SZ
     uint32_t size_x, size_y, size_z;  // voxels
+    uint32_t sx, sz, sxz;             // sector-table strides
 };
+static_assert(sizeof(DevWorld) == 64, "world table entries are 64 bytes");
 
 // World origins stay within +-2^30 so that saturated float->int conversions of
 // far-away positions always land outside the grid (the traversal relies on it).

@@ -1,5 +1,5 @@
 // world.cu - device-resident brickmap storage: create/destroy, dirty-brick sync,
-// brick-slot repacking and occupancy re-derivation.
+// brick-slot repacking, occupancy re-derivation and the brick table.
 //
 // Replaces GpuVoxelStorage (src/VoxelRT/GpuRenderer.cpp:17-167) and the
 // UpdateOccupancy dispatch (GpuRenderer.cpp:163-166, Shaders/UpdateOccupancy.comp).
@@ -16,6 +16,7 @@
 #include <unordered_set>
 #include <vector>
 
+#include "brick_codes.cuh"
 #include "world.h"
 
 namespace vrt {
@@ -57,28 +58,9 @@ struct BrickOp {
 
 constexpr int kOpsWarps = 8;
 
-// Occupancy of one 512-byte brick held by a warp in shared memory: round r tests,
-// in lane l, voxel (4cx + (l&3), 4cy + 2h + (l>>4), 4cz + ((l>>2)&3)) of cell
-// c = r>>1 (cx = c&1, cz = (c>>1)&1, cy = c>>2), half h = r&1, so the ballot is
-// bits 32h..32h+31 of cell c's mask (bit vx + vz*4 + vy*16, CpuRenderer.cpp:78).
-// Lane c < 8 returns cell c's 64-bit mask.
-__device__ __forceinline__ uint64_t warp_cell_mask(const uint8_t* sb, uint32_t lane) {
-    uint64_t mine = 0;
-#pragma unroll
-    for (uint32_t r = 0; r < 16; r++) {
-        const uint32_t c = r >> 1, h = r & 1;
-        const uint32_t x = (c & 1) * 4 + (lane & 3);
-        const uint32_t z = ((c >> 1) & 1) * 4 + ((lane >> 2) & 3);
-        const uint32_t y = (c >> 2) * 4 + 2 * h + (lane >> 4);
-        const uint32_t bits = __ballot_sync(0xffffffffu, sb[x | z << 3 | y << 6] != 0);
-        if (lane == c) mine |= (uint64_t)bits << (32 * h);
-    }
-    return mine;
-}
-
 __global__ void gather_bricks_kernel(const uint32_t* __restrict__ src_slots, uint32_t n,
-                                     const uint8_t* __restrict__ payload, const uint64_t* __restrict__ occ,
-                                     uint8_t* __restrict__ scratch_payload, uint64_t* __restrict__ scratch_occ) {
+                                     const uint8_t* __restrict__ payload, const uint32_t* __restrict__ codes,
+                                     uint8_t* __restrict__ scratch_payload, uint32_t* __restrict__ scratch_codes) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -86,14 +68,14 @@ __global__ void gather_bricks_kernel(const uint32_t* __restrict__ src_slots, uin
         const size_t s = src_slots[k];
         const uint4 v = reinterpret_cast<const uint4*>(payload + s * 512)[lane];
         reinterpret_cast<uint4*>(scratch_payload + (size_t)k * 512)[lane] = v;
-        if (lane < 8) scratch_occ[(size_t)k * 8 + lane] = occ[s * 8 + lane];
+        scratch_codes[(size_t)k * 32 + lane] = codes[s * 32 + lane];
     }
 }
 
 __global__ void __launch_bounds__(kOpsWarps * 32)
     brick_ops_kernel(const BrickOp* __restrict__ ops, uint32_t n, const uint8_t* __restrict__ stage,
-                     const uint8_t* __restrict__ scratch_payload, const uint64_t* __restrict__ scratch_occ,
-                     uint8_t* __restrict__ payload, uint64_t* __restrict__ occ) {
+                     const uint8_t* __restrict__ scratch_payload, const uint32_t* __restrict__ scratch_codes,
+                     uint8_t* __restrict__ payload, uint32_t* __restrict__ codes) {
     __shared__ __align__(16) uint8_t sbrick[kOpsWarps][512];
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t wib = threadIdx.x >> 5;
@@ -106,20 +88,40 @@ __global__ void __launch_bounds__(kOpsWarps * 32)
         if (kind == kOpMove) {
             const uint4 v = reinterpret_cast<const uint4*>(scratch_payload + (size_t)si * 512)[lane];
             reinterpret_cast<uint4*>(payload + d * 512)[lane] = v;
-            if (lane < 8) occ[d * 8 + lane] = scratch_occ[(size_t)si * 8 + lane];
+            codes[d * 32 + lane] = scratch_codes[(size_t)si * 32 + lane];
         } else if (kind == kOpZero) {
             reinterpret_cast<uint4*>(payload + d * 512)[lane] = make_uint4(0, 0, 0, 0);
-            if (lane < 8) occ[d * 8 + lane] = 0;
+            codes[d * 32 + lane] = kEmptyBrickCodes;
         } else {
             const uint4 v = reinterpret_cast<const uint4*>(stage + (size_t)si * 512)[lane];
             reinterpret_cast<uint4*>(payload + d * 512)[lane] = v;
             reinterpret_cast<uint4*>(sbrick[wib])[lane] = v;
             __syncwarp();
             const uint64_t m = warp_cell_mask(sbrick[wib], lane);
-            if (lane < 8) occ[d * 8 + lane] = m;
+            codes[d * 32 + lane] = warp_voxel_codes(sbrick[wib], m, lane);
             __syncwarp();
         }
     }
+}
+
+// Brick-table entries of sectors [s_lo, s_hi), one thread per brick position.
+__global__ void brick_table_kernel(const SectorRec* __restrict__ sectors, uint32_t s_lo, uint32_t s_hi, uint32_t sx,
+                                   uint32_t sz, uint32_t* __restrict__ bricks) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (s_hi - s_lo) * 64u) return;
+    const uint32_t s = s_lo + (i >> 6), b = i & 63;
+    const SectorRec rec = sectors[s];
+    const uint32_t x = s % sx, z = (s / sx) % sz, y = s / (sx * sz);
+    const uint32_t bx = x * 4 + (b & 3), bz = z * 4 + ((b >> 2) & 3), by = y * 4 + (b >> 4);
+    const uint32_t lo = rec.mask_lo, hi = rec.mask_hi;
+    uint32_t e;
+    if ((((b < 32 ? lo : hi) >> (b & 31)) & 1u) != 0) {
+        const uint32_t below = (1u << (b & 31)) - 1u;
+        e = rec.base + (b < 32 ? __popc(lo & below) : __popc(lo) + __popc(hi & below));
+    } else {
+        e = kBrickEmpty | (3u + skip_levels(lo, hi, b));
+    }
+    bricks[bx + bz * (sx * 4) + by * (sx * 4) * (sz * 4)] = e;
 }
 
 uint32_t ops_grid(uint32_t n) {
@@ -139,23 +141,23 @@ vrt_status grow_pool(vrt_world* w, uint32_t min_capacity, cudaStream_t stream) {
         return VRT_ERR_SLOTS_EXHAUSTED;
     }
     uint32_t cap = (uint32_t)want;
-    uint64_t* occ = nullptr;
+    uint32_t* codes = nullptr;
     uint8_t* payload = nullptr;
-    cudaError_t e = cudaMalloc(&occ, (size_t)cap * 64);
+    cudaError_t e = cudaMalloc(&codes, (size_t)cap * 128);
     if (e == cudaSuccess) e = cudaMalloc(&payload, (size_t)cap * 512);
     if (e != cudaSuccess) {
-        if (occ) cudaFree(occ);
+        if (codes) cudaFree(codes);
         cudaGetLastError();
         return cuda_fail(e, "grow brick pool");
     }
     if (w->capacity) {
-        VRT_CUDA(cudaMemcpyAsync(occ, w->d_occ, (size_t)w->capacity * 64, cudaMemcpyDeviceToDevice, stream));
+        VRT_CUDA(cudaMemcpyAsync(codes, w->d_codes, (size_t)w->capacity * 128, cudaMemcpyDeviceToDevice, stream));
         VRT_CUDA(cudaMemcpyAsync(payload, w->d_payload, (size_t)w->capacity * 512, cudaMemcpyDeviceToDevice, stream));
         VRT_CUDA(cudaStreamSynchronize(stream));
     }
-    if (w->d_occ) cudaFree(w->d_occ);
+    if (w->d_codes) cudaFree(w->d_codes);
     if (w->d_payload) cudaFree(w->d_payload);
-    w->d_occ = occ;
+    w->d_codes = codes;
     w->d_payload = payload;
     w->capacity = cap;
     w->arena.grow(cap);
@@ -207,6 +209,13 @@ vrt_status plan_sector(vrt_world* w, SyncBatch& b, uint32_t s, uint64_t am, uint
     return VRT_OK;
 }
 
+// Re-derive the brick-table entries of sectors [lo, hi) from the device sector table.
+cudaError_t rebuild_brick_table(vrt_world* w, uint32_t lo, uint32_t hi, cudaStream_t stream) {
+    const uint32_t n = (hi - lo) * 64;
+    brick_table_kernel<<<(n + 255) / 256, 256, 0, stream>>>(w->d_sectors, lo, hi, w->sx, w->sz, w->d_bricks);
+    return cudaGetLastError();
+}
+
 vrt_status run_batch(vrt_world* w, SyncBatch& b, cudaStream_t stream) {
     if (b.ops.empty() && b.touched.empty()) return VRT_OK;
     const size_t stage_bytes = (size_t)b.n_stage * 512;
@@ -225,19 +234,19 @@ vrt_status run_batch(vrt_world* w, SyncBatch& b, cudaStream_t stream) {
     }
     const size_t ng = b.gathers.size();
     if (ng) {
-        VRT_CUDA(w->d_scratch.reserve(ng * 576));
+        VRT_CUDA(w->d_scratch.reserve(ng * 640));
         uint8_t* sp = (uint8_t*)w->d_scratch.ptr;
-        uint64_t* so = (uint64_t*)(sp + ng * 512);
+        uint32_t* sc = (uint32_t*)(sp + ng * 512);
         gather_bricks_kernel<<<ops_grid((uint32_t)ng), kOpsWarps * 32, 0, stream>>>(
-            (const uint32_t*)w->d_ops.ptr, (uint32_t)ng, w->d_payload, w->d_occ, sp, so);
+            (const uint32_t*)w->d_ops.ptr, (uint32_t)ng, w->d_payload, w->d_codes, sp, sc);
         VRT_CUDA(cudaGetLastError());
     }
     if (!b.ops.empty()) {
         uint8_t* sp = (uint8_t*)w->d_scratch.ptr;
-        uint64_t* so = sp ? (uint64_t*)(sp + ng * 512) : nullptr;
+        uint32_t* sc = sp ? (uint32_t*)(sp + ng * 512) : nullptr;
         brick_ops_kernel<<<ops_grid((uint32_t)b.ops.size()), kOpsWarps * 32, 0, stream>>>(
             (const BrickOp*)((uint8_t*)w->d_ops.ptr + ooff), (uint32_t)b.ops.size(), (const uint8_t*)w->d_stage.ptr,
-            sp, so, w->d_payload, w->d_occ);
+            sp, sc, w->d_payload, w->d_codes);
         VRT_CUDA(cudaGetLastError());
     }
     // sector headers: copy the span of touched records
@@ -246,6 +255,7 @@ vrt_status run_batch(vrt_world* w, SyncBatch& b, cudaStream_t stream) {
         const uint32_t lo = *mm.first, hi = *mm.second + 1;
         VRT_CUDA(cudaMemcpyAsync(w->d_sectors + lo, w->h_table.data() + lo, (size_t)(hi - lo) * sizeof(SectorRec),
                                  cudaMemcpyHostToDevice, stream));
+        VRT_CUDA(rebuild_brick_table(w, lo, hi, stream));
     }
     VRT_CUDA(cudaStreamSynchronize(stream));
     b = SyncBatch();
@@ -313,6 +323,9 @@ vrt_status vrt_world_create(const vrt_world_desc* desc, vrt_world** out) {
     if (st == VRT_OK) {
         e = cudaMalloc(&w->d_sectors, (size_t)w->num_sectors() * sizeof(SectorRec));
         if (e == cudaSuccess) e = cudaMemset(w->d_sectors, 0, (size_t)w->num_sectors() * sizeof(SectorRec));
+        if (e == cudaSuccess) e = cudaMalloc(&w->d_bricks, w->num_brick_positions() * sizeof(uint32_t));
+        if (e == cudaSuccess) e = rebuild_brick_table(w, 0, w->num_sectors(), 0);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(0);
         if (e != cudaSuccess) st = cuda_fail(e, "allocate sector table");
     }
     if (st == VRT_OK) st = grow_pool(w, desc->brick_capacity ? desc->brick_capacity : 4096, 0);
@@ -329,7 +342,8 @@ vrt_status vrt_world_destroy(vrt_world* w) {
     cudaSetDevice(w->device);
     cudaDeviceSynchronize();
     if (w->d_sectors) cudaFree(w->d_sectors);
-    if (w->d_occ) cudaFree(w->d_occ);
+    if (w->d_bricks) cudaFree(w->d_bricks);
+    if (w->d_codes) cudaFree(w->d_codes);
     if (w->d_payload) cudaFree(w->d_payload);
     w->d_stage.release();
     w->d_ops.release();

@@ -59,7 +59,8 @@ struct vrt_world {
 
     // device storage
     vrt::SectorRec* d_sectors = nullptr;
-    uint64_t* d_occ = nullptr;
+    uint32_t* d_bricks = nullptr;  // brick table, derived from the sector table on the device
+    uint32_t* d_codes = nullptr;   // 2-bit voxel codes, 128 B per slot
     uint8_t* d_payload = nullptr;
     uint32_t capacity = 0;  // brick slots in the device pools
 
@@ -71,6 +72,7 @@ struct vrt_world {
     std::vector<vrt::SectorRec> h_table;  // host copy of the sector table
 
     uint32_t num_sectors() const { return sx * sy * sz; }
+    size_t num_brick_positions() const { return (size_t)num_sectors() * 64; }
     uint32_t lin(int32_t x, int32_t y, int32_t z) const {
         return (uint32_t)x + (uint32_t)z * sx + (uint32_t)y * sx * sz;
     }
@@ -79,9 +81,12 @@ struct vrt_world {
     }
     vrt::DevWorld dev() const {
         vrt::DevWorld w;
-        w.sectors = d_sectors;
-        w.occ = d_occ;
+        w.bricks = d_bricks;
+        w.codes = d_codes;
         w.payload = d_payload;
+        w.sectors = d_sectors;
+        w.bsx = sx * 4;
+        w.bsxz = sx * 4 * sz * 4;
         w.sx = sx;
         w.sz = sz;
         w.sxz = sx * sz;
