@@ -30,12 +30,19 @@ __device__ __forceinline__ uint32_t compact_even_bits(uint32_t k) {
 }
 
 template <bool kCount>
-__device__ __forceinline__ bool run_ray(RayState& s, const DevWorld& w, int32_t wox, int32_t woy, int32_t woz,
-                                        uint32_t max_iters, uint32_t& steps, TraceCounters& cnt) {
+__device__ __forceinline__ bool run_ray(RayState& s, bool safe, const DevWorld& w, int32_t wox, int32_t woy,
+                                        int32_t woz, uint32_t max_iters, uint32_t& steps, TraceCounters& cnt) {
     uint32_t st = kStepOut, i = 0;
-    for (; i < max_iters; i++) {
-        st = ray_step<kCount>(s, w, wox, woy, woz, cnt);
-        if (st != kStepContinue) break;
+    if (safe) {
+        for (; i < max_iters; i++) {
+            st = ray_step<kCount, true>(s, w, wox, woy, woz, cnt);
+            if (st != kStepContinue) break;
+        }
+    } else {
+        for (; i < max_iters; i++) {
+            st = ray_step<kCount, false>(s, w, wox, woy, woz, cnt);
+            if (st != kStepContinue) break;
+        }
     }
     steps = i;
     return st == kStepHit && i < max_iters;
@@ -53,9 +60,9 @@ __global__ void __launch_bounds__(64) view_path_kernel(DevWorld w, ViewDev v, ui
     float ox = v.cam.origin[0], oy = v.cam.origin[1], oz = v.cam.origin[2], dx, dy, dz;
     camera_ray(v.cam, px, py, dx, dy, dz);
     RayState s;
-    ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
+    bool safe = ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
     uint32_t steps;
-    bool hit = run_ray<false>(s, w, wox, woy, woz, v.max_iters, steps, cnt);
+    bool hit = run_ray<false>(s, safe, w, wox, woy, woz, v.max_iters, steps, cnt);
     uint4* o = out + v.out_base + pixel;
     o[0] = pack_state(s, hit, steps, pixel);
     const uint32_t last = v.shadow ? 1u : v.n_bounces;
@@ -65,14 +72,14 @@ __global__ void __launch_bounds__(64) view_path_kernel(DevWorld w, ViewDev v, ui
             continue;
         }
         next_path_ray(s, v.shadow != 0, v.sun, pixel, k, ox, oy, oz, dx, dy, dz);
-        ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
-        hit = run_ray<false>(s, w, wox, woy, woz, v.max_iters, steps, cnt);
+        safe = ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
+        hit = run_ray<false>(s, safe, w, wox, woy, woz, v.max_iters, steps, cnt);
         o[k * plane] = pack_state(s, hit, steps, pixel);
     }
 }
 
 template <bool kCount>
-__global__ void __maxnreg__(64) persistent_kernel(BatchParams p) {
+__global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt = (1u << lane) - 1u;
     // warp-uniform queue state: rays [q_next, q_end) of view q_view
@@ -81,7 +88,10 @@ __global__ void __maxnreg__(64) persistent_kernel(BatchParams p) {
     // lane state
     bool active = false;
     // path: kind of the current ray (0 primary, then shadow or bounce number) in bits
-    // 0-7, last kind of the pixel's path in bits 8-15, shadow flag in bit 16
+    // 0-7, last kind of the pixel's path in bits 8-15, shadow flag in bit 16, ray
+    // ended with its record pending in bit 17 (kEnded), that ray hit in bit 18 (kHit),
+    // the ray is safe for ray_step<kCount, true> in bit 19 (kSafe)
+    constexpr uint32_t kEnded = 1u << 17, kHit = 1u << 18, kSafe = 1u << 19;
     uint32_t pixel = 0, path = 0, iter = 0, max_iters = 0, plane = 0, vidx = 0;
     DevWorld w{};
     int32_t wox = 0, woy = 0, woz = 0;
@@ -90,6 +100,32 @@ __global__ void __maxnreg__(64) persistent_kernel(BatchParams p) {
     TraceCounters cnt{0, 0};
 
     for (;;) {
+        // Rays that ended during the last DDA round are retired together here, so the
+        // record store and the next ray of the path run once per round for all of
+        // them instead of once per lane that happens to end on a given step.
+        if (path & kEnded) {
+            const bool hit = (path & kHit) != 0;
+            path &= ~(kEnded | kHit | kSafe);
+            const ViewDev* v = p.views + vidx;
+            uint4* rec = p.out + __ldg(&v->out_base) + pixel;
+            uint32_t kind = path & 0xFF;
+            const uint32_t last_kind = (path >> 8) & 0xFF;
+            rec[(size_t)kind * plane] = pack_state(s, hit, iter, pixel);
+            rays++;
+            if (kCount && hit) hits++;
+            if (hit && kind < last_kind) {
+                path++;
+                kind++;
+                float ox, oy, oz, dx, dy, dz;
+                next_path_ray(s, ((path >> 16) & 1u) != 0, v->sun, pixel, kind, ox, oy, oz, dx, dy, dz);
+                path &= ~kSafe;
+                if (ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz)) path |= kSafe;
+                iter = 0;
+            } else {
+                for (uint32_t kk = kind + 1; kk <= last_kind; kk++) rec[(size_t)kk * plane] = no_ray_hit();
+                active = false;
+            }
+        }
         const uint32_t act = __ballot_sync(0xffffffffu, active);
         if ((uint32_t)__popc(act) < p.refill && !q_empty) {
             uint32_t idle = ~act;
@@ -153,8 +189,9 @@ __global__ void __maxnreg__(64) persistent_kernel(BatchParams p) {
                         woz = __ldg(&v->cam.world_origin[2]);
                         float dx, dy, dz;
                         camera_ray(v->cam, px, py, dx, dy, dz);
-                        ray_init(s, w, __ldg(&v->cam.origin[0]), __ldg(&v->cam.origin[1]), __ldg(&v->cam.origin[2]),
-                                 dx, dy, dz, wox, woy, woz);
+                        if (ray_init(s, w, __ldg(&v->cam.origin[0]), __ldg(&v->cam.origin[1]),
+                                     __ldg(&v->cam.origin[2]), dx, dy, dz, wox, woy, woz))
+                            path |= kSafe;
                         active = true;
                     }
                 }
@@ -163,31 +200,29 @@ __global__ void __maxnreg__(64) persistent_kernel(BatchParams p) {
             }
         }
         if (__ballot_sync(0xffffffffu, active) == 0 && q_empty) break;
+        // one DDA round: up to p.inner steps, fewer when the iteration cap comes first
+        // (an active lane always has iter < max_iters); the fast step when every
+        // tracing lane of the warp is safe
+        const bool all_safe = __all_sync(0xffffffffu, !active || (path & kSafe) != 0);
         if (active) {
-            for (uint32_t k = 0; k < p.inner; k++) {
-                const uint32_t st = ray_step<kCount>(s, w, wox, woy, woz, cnt);
-                if (st == kStepContinue && ++iter < max_iters) continue;
-                const bool hit = st == kStepHit;
-                const ViewDev* v = p.views + vidx;
-                uint4* rec = p.out + __ldg(&v->out_base) + pixel;
-                uint32_t kind = path & 0xFF;
-                const uint32_t last_kind = (path >> 8) & 0xFF;
-                rec[(size_t)kind * plane] = pack_state(s, hit, iter, pixel);
-                rays++;
-                if (kCount && hit) hits++;
-                if (hit && kind < last_kind) {
-                    path++;
-                    kind++;
-                    float ox, oy, oz, dx, dy, dz;
-                    next_path_ray(s, (path >> 16) != 0, v->sun, pixel, kind, ox, oy, oz, dx, dy, dz);
-                    ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
-                    iter = 0;
-                    continue;
+            const uint32_t kmax = min(p.inner, max_iters - iter);
+            uint32_t k = 0, st = kStepContinue;
+            if (all_safe) {
+                for (; k < kmax; k++) {
+                    st = ray_step<kCount, true>(s, w, wox, woy, woz, cnt);
+                    if (st != kStepContinue) break;
                 }
-                for (uint32_t kk = kind + 1; kk <= last_kind; kk++) rec[(size_t)kk * plane] = no_ray_hit();
-                active = false;
-                break;
+            } else {
+                for (; k < kmax; k++) {
+                    st = ray_step<kCount, false>(s, w, wox, woy, woz, cnt);
+                    if (st != kStepContinue) break;
+                }
             }
+            iter += k;  // the iteration a ray left on, or max_iters when the cap ran out
+            if (st != kStepContinue)
+                path |= kEnded | (st == kStepHit ? kHit : 0u);
+            else if (iter >= max_iters)
+                path |= kEnded;
         }
     }
     // warp totals, one atomic per warp

@@ -65,8 +65,15 @@ struct RayState {
     uint32_t material;
 };
 
+// Bounds that keep a ray free of NaN and infinities inside the DDA loop: with
+// |origin| < 2^30 and |1/dir| < 2^95, |tStart| and |(voxel - worldOrigin) * invDir|
+// stay below 2^126 (voxel - worldOrigin < 2^31), so side distances and t are finite,
+// and the position o + t*dir is finite or an infinity (never NaN) that leaves the grid.
+constexpr float kSafeOrigin = 0x1p30f, kSafeInvDir = 0x1p95f;
+
 // invDir, tStart and the clipped start position (VoxelTraversal.glsl:133-145,163-167).
-__device__ __forceinline__ void ray_init(RayState& s, const DevWorld& w, float ox, float oy, float oz, float dx,
+// Returns whether the ray is safe in the sense above (ray_step<kCount, true> applies).
+__device__ __forceinline__ bool ray_init(RayState& s, const DevWorld& w, float ox, float oy, float oz, float dx,
                                          float dy, float dz, int32_t wox, int32_t woy, int32_t woz) {
     s.ox = ox;
     s.oy = oy;
@@ -112,22 +119,29 @@ __device__ __forceinline__ void ray_init(RayState& s, const DevWorld& w, float o
     s.gy = dy < 0.0f ? -1 : 0;
     s.gz = dz < 0.0f ? -1 : 0;
     s.material = 0;
+    return fabsf(ox) < kSafeOrigin && fabsf(oy) < kSafeOrigin && fabsf(oz) < kSafeOrigin &&
+           fabsf(s.ix) < kSafeInvDir && fabsf(s.iy) < kSafeInvDir && fabsf(s.iz) < kSafeInvDir;
 }
 
 enum : uint32_t { kStepContinue = 0, kStepHit = 1, kStepOut = 2 };
 
 // One iteration of RayCast (CpuRenderer.cpp:186-201) with GetStepPos (:135-171).
-template <bool kCount>
+// kSafe: the ray passed the bounds of ray_init, so no NaN can occur; the NaN test
+// is skipped and min uses fminf, which equals the minps rule on non-NaN operands up
+// to the sign of a zero result, which the +0.001 bias removes.
+template <bool kCount, bool kSafe = false>
 __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int32_t wox, int32_t woy, int32_t woz,
                                              TraceCounters& cnt) {
     // floor2i: a NaN coordinate converts to INT32_MIN on x86 and leaves the grid;
     // cvt.rmi saturates infinities and out-of-range values, which leave the grid
     // too (|world origin| <= 2^30 is enforced at the API), so only NaN needs a test
     // and one NaN among the three shows in their sum.
-    const float nan_probe = __fadd_rn(__fadd_rn(s.cx, s.cy), s.cz);
-    if (nan_probe != nan_probe) {
-        s.vx = s.vy = s.vz = INT32_MIN;
-        return kStepOut;
+    if (!kSafe) {
+        const float nan_probe = __fadd_rn(__fadd_rn(s.cx, s.cy), s.cz);
+        if (nan_probe != nan_probe) {
+            s.vx = s.vy = s.vz = INT32_MIN;
+            return kStepOut;
+        }
     }
     int32_t vx = wadd(wox, __float2int_rd(s.cx));
     int32_t vy = wadd(woy, __float2int_rd(s.cy));
@@ -173,7 +187,8 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
     s.sx = __fadd_rn(s.tsx, __fmul_rn(__int2float_rn(wsub(vx, wox)), s.ix));
     s.sy = __fadd_rn(s.tsy, __fmul_rn(__int2float_rn(wsub(vy, woy)), s.iy));
     s.sz = __fadd_rn(s.tsz, __fmul_rn(__int2float_rn(wsub(vz, woz)), s.iz));
-    const float t = __fadd_rn(min_x86(min_x86(s.sx, s.sy), s.sz), 0.001f);
+    const float t = kSafe ? __fadd_rn(fminf(fminf(s.sx, s.sy), s.sz), 0.001f)
+                          : __fadd_rn(min_x86(min_x86(s.sx, s.sy), s.sz), 0.001f);
     s.cx = __fadd_rn(s.ox, __fmul_rn(t, s.dx));
     s.cy = __fadd_rn(s.oy, __fmul_rn(t, s.dy));
     s.cz = __fadd_rn(s.oz, __fmul_rn(t, s.dz));
@@ -186,11 +201,18 @@ __device__ __forceinline__ void trace_ray(const DevWorld& w, float ox, float oy,
                                           float dz, int32_t wox, int32_t woy, int32_t woz, uint32_t max_iters,
                                           TraceResult& r, TraceCounters& cnt) {
     RayState s;
-    ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
+    const bool safe = ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
     uint32_t st = kStepOut, i = 0;
-    for (; i < max_iters; i++) {
-        st = ray_step<kCount>(s, w, wox, woy, woz, cnt);
-        if (st != kStepContinue) break;
+    if (safe) {
+        for (; i < max_iters; i++) {
+            st = ray_step<kCount, true>(s, w, wox, woy, woz, cnt);
+            if (st != kStepContinue) break;
+        }
+    } else {
+        for (; i < max_iters; i++) {
+            st = ray_step<kCount, false>(s, w, wox, woy, woz, cnt);
+            if (st != kStepContinue) break;
+        }
     }
     r.cx = s.cx;
     r.cy = s.cy;
