@@ -170,6 +170,14 @@ def traffic_from_profile(workload: str):
         return None
 
 
+def host_cores() -> int:
+    """CPUs this process may run on (the affinity set), not the machine's count."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
+
+
 def cpu_oracle_sample(wl, seconds: float, threads: int = 0):
     """Time the CPU oracle on whole views of the workload until `seconds` of work."""
     from oracle.oracle import OracleWorld
@@ -207,14 +215,14 @@ def run_reference(args):
     from voxelrt_gb300 import build
     build.build_all()
     wl = build_workload(args.workload, 0, args)
-    cores = os.cpu_count() or 1
+    cores = host_cores()
     per_step = max(2.0, min(20.0, args.cpu_seconds))
     for _ in range(args.warmup):
-        cpu_oracle_sample(wl, 0.5)
+        cpu_oracle_sample(wl, 0.5, cores)
     tot_rays, tot_t = 0, 0.0
     nv = 0
     for _ in range(args.steps):
-        r, t, nv = cpu_oracle_sample(wl, per_step)
+        r, t, nv = cpu_oracle_sample(wl, per_step, cores)
         tot_rays += r
         tot_t += t
     value = tot_rays / tot_t / 1e9
@@ -301,9 +309,10 @@ def run_ours(args):
                     "launches_per_step": len(wl.views), "steps": k,
                     "kernel": "view_path_kernel, 8x8 blocks, thread per pixel"}
 
-    # end to end through the host-buffer API: new cameras in (H2D), all records out (D2H, pinned)
-    host = torch.empty(n_rec * HIT_BYTES, dtype=torch.uint8, pin_memory=True)
-    host_np = host.numpy()
+    # end to end through the host-buffer API: new cameras in (H2D), all records out to
+    # pinned host memory from vrt_host_alloc (the kernel stores them there directly)
+    host = v.PinnedHits(n_rec)
+    host_np = host.array
     cams = [vw.cam for vw in wl.views]
     batch.update_cameras(cams, stream)
     batch.run(host_np, stream)
@@ -327,14 +336,15 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        r, t, nv = cpu_oracle_sample(wl, args.cpu_seconds)
-        cpu = {"value": r / t / 1e9, "unit": "Grays/s", "cores": os.cpu_count(), "kind": "port",
+        cores = host_cores()
+        r, t, nv = cpu_oracle_sample(wl, args.cpu_seconds, cores)
+        cpu = {"value": r / t / 1e9, "unit": "Grays/s", "cores": cores, "kind": "port",
                "sample": f"{nv} smallest views of the workload, {r} rays, CPU oracle (scalar restatement of "
                          f"CpuRenderer.cpp RayCast) on all host threads"}
 
     serving = None
     if rank == 0 and not args.no_serving and args.workload == "uneven_batch":
-        del hits, host, batch
+        del hits, host_np, host, batch
         for w in worlds:
             w.close()
         worlds = []

@@ -324,8 +324,11 @@ vrt_status vrt_batch_launch_graph(vrt_batch* batch, vrt_hit* hits_device, void* 
 vrt_status vrt_batch_launch_per_view(vrt_batch* batch, vrt_hit* hits_device, void* stream);
 /* New cameras for every view (same resolutions), copied to the device. */
 vrt_status vrt_batch_update_cameras(vrt_batch* batch, const vrt_camera* cams, void* stream);
-/* Host-buffer form: graph launch into a batch-owned device buffer, then the records
- * are copied to hits_host (pinned memory makes the copy asynchronous-fast). */
+/* Host-buffer form; returns when the records are in hits_host.  The views are
+ * traced in parts of about equal record count, back to back on `stream`, into a
+ * batch-owned device buffer; each part's records are copied to hits_host as soon as
+ * that part is done, so the host transfer overlaps the tracing of later parts
+ * (pinned memory from vrt_host_alloc keeps the copies asynchronous). */
 vrt_status vrt_batch_run(vrt_batch* batch, vrt_hit* hits_host, void* stream);
 /* Counters of the last launch (synchronises the stream of that launch). */
 vrt_status vrt_batch_get_stats(vrt_batch* batch, vrt_batch_stats* out);

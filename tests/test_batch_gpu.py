@@ -152,3 +152,27 @@ def test_batch_rejects_bad_input(mix):
     both = v.make_view(cfg0_camera(8, 8), n_bounces=1, shadow_dir=SUN)
     with pytest.raises(v.VrtError):
         v.Batch(worlds, [both])
+
+
+def test_run_into_pinned_buffers_matches_pageable(mix):
+    """vrt_batch_run copies the records of each finished part of the batch while later
+    parts trace; into vrt_host_alloc memory (also at an offset inside a larger
+    allocation) or pageable memory, the records are the same."""
+    worlds, views, want = mix
+    b = v.Batch(worlds, views)
+    n = b.total_records
+    pageable = b.run()
+    whole = v.PinnedHits(n)
+    whole.array[:] = np.frombuffer(b"\xab" * (n * 16), v.HIT_DTYPE)
+    got_whole = b.run(whole.array).copy()
+    bigger = v.PinnedHits(n + 100)
+    got_inner = b.run(bigger.array[37:37 + n]).copy()
+    for got in (got_whole, got_inner):
+        assert np.array_equal(got.view(np.uint8), pageable.view(np.uint8))
+    for i in range(len(views)):
+        g = b.view_hits(got_whole, i)
+        for k in range(g.shape[0]):
+            assert_hits_equal(g[k], want[i][k])
+    b.close()
+    whole.close()
+    bigger.close()

@@ -138,6 +138,7 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                         q_empty = true;
                         break;
                     }
+                    c += p.chunk_first;
                     uint32_t lo = 0, hi = p.n_views;
                     while (hi - lo > 1) {
                         const uint32_t mid = (lo + hi) >> 1;
@@ -371,6 +372,7 @@ BatchParams make_params(const LaunchPlan& plan, const DevWorld* worlds, const Vi
     p.chunk_base = chunk_base;
     p.n_views = (uint32_t)plan.views.size();
     p.total_chunks = plan.chunks;
+    p.chunk_first = 0;
     p.queue = queue;
     p.counters = reinterpret_cast<unsigned long long*>(reinterpret_cast<uint8_t*>(queue) + 16);
     p.out = reinterpret_cast<uint4*>(out);
@@ -383,8 +385,9 @@ BatchParams make_params(const LaunchPlan& plan, const DevWorld* worlds, const Vi
     return p;
 }
 
-vrt_status launch_persistent(const BatchParams& p, int blocks, int threads, bool count, cudaStream_t stream) {
-    VRT_CUDA(cudaMemsetAsync(p.queue, 0, 64, stream));
+vrt_status launch_persistent(const BatchParams& p, int blocks, int threads, bool count, cudaStream_t stream,
+                             bool reset_counters) {
+    VRT_CUDA(cudaMemsetAsync(p.queue, 0, reset_counters ? 64 : 4, stream));
     if (count)
         persistent_kernel<true><<<blocks, threads, 0, stream>>>(p);
     else
@@ -412,6 +415,10 @@ struct vrt_batch {
     unsigned long long* d_counters = nullptr;
     cudaStream_t last_stream = nullptr;
     DevBuf d_out;  // record buffer of vrt_batch_run
+    // vrt_batch_run: copies of finished parts overlap the traversal of later parts
+    cudaStream_t copy_stream = nullptr;
+    std::vector<cudaEvent_t> part_done;
+    cudaEvent_t copies_done = nullptr;
     // graph
     cudaGraphExec_t graph_exec = nullptr;
     vrt_hit* graph_hits = nullptr;
@@ -523,6 +530,9 @@ vrt_status vrt_batch_destroy(vrt_batch* b) {
     cudaSetDevice(b->device);
     cudaDeviceSynchronize();
     if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
+    for (cudaEvent_t e : b->part_done) cudaEventDestroy(e);
+    if (b->copies_done) cudaEventDestroy(b->copies_done);
+    if (b->copy_stream) cudaStreamDestroy(b->copy_stream);
     if (b->d_worlds) cudaFree(b->d_worlds);
     if (b->d_views) cudaFree(b->d_views);
     if (b->d_chunk_base) cudaFree(b->d_chunk_base);
@@ -633,11 +643,53 @@ vrt_status vrt_batch_run(vrt_batch* b, vrt_hit* hits_host, void* stream_) {
     }
     VRT_CUDA(cudaSetDevice(b->device));
     cudaStream_t stream = (cudaStream_t)stream_;
-    VRT_CUDA(b->d_out.reserve(b->plan.records * sizeof(vrt_hit)));
-    vrt_status st = vrt_batch_launch_graph(b, (vrt_hit*)b->d_out.ptr, stream);
+    const LaunchPlan& plan = b->plan;
+    const size_t nv = plan.views.size();
+    VRT_CUDA(b->d_out.reserve(plan.records * sizeof(vrt_hit)));
+    vrt_status st = refresh_worlds(b, stream);
     if (st != VRT_OK) return st;
-    VRT_CUDA(cudaMemcpyAsync(hits_host, b->d_out.ptr, b->plan.records * sizeof(vrt_hit), cudaMemcpyDeviceToHost,
-                             stream));
+    // Views are split into parts of about equal record count, at view boundaries.
+    // All parts are launched first, one after another on `stream`; the copy of a
+    // part's records (one contiguous range) waits for that part only, so the host
+    // transfer of finished parts overlaps the traversal of the later ones.
+    constexpr uint64_t kParts = 8;
+    std::vector<size_t> cut{0};
+    for (size_t i = 1; i < nv; i++)
+        if (plan.views[i].out_base * kParts >= plan.records * cut.size()) cut.push_back(i);
+    cut.push_back(nv);
+    const size_t parts = cut.size() - 1;
+    if (!b->copy_stream) {
+        VRT_CUDA(cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking));
+        VRT_CUDA(cudaEventCreateWithFlags(&b->copies_done, cudaEventDisableTiming));
+    }
+    while (b->part_done.size() < parts) {
+        cudaEvent_t e;
+        VRT_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        b->part_done.push_back(e);
+    }
+    auto first_record = [&](size_t v) { return v < nv ? plan.views[v].out_base : plan.records; };
+    for (size_t k = 0; k < parts; k++) {
+        const size_t a = cut[k], e = cut[k + 1];
+        BatchParams p = make_params(plan, b->d_worlds, b->d_views, b->d_chunk_base, b->d_queue,
+                                    (vrt_hit*)b->d_out.ptr);
+        p.views = b->d_views + a;
+        p.chunk_base = b->d_chunk_base + a;
+        p.n_views = (uint32_t)(e - a);
+        p.chunk_first = plan.chunk_base[a];
+        p.total_chunks = plan.chunk_base[e] - plan.chunk_base[a];
+        if ((st = launch_persistent(p, b->blocks, b->threads, false, stream, k == 0)) != VRT_OK) return st;
+        VRT_CUDA(cudaEventRecord(b->part_done[k], stream));
+    }
+    for (size_t k = 0; k < parts; k++) {
+        const uint64_t r0 = first_record(cut[k]), r1 = first_record(cut[k + 1]);
+        VRT_CUDA(cudaStreamWaitEvent(b->copy_stream, b->part_done[k], 0));
+        if (r1 > r0)
+            VRT_CUDA(cudaMemcpyAsync(hits_host + r0, (const vrt_hit*)b->d_out.ptr + r0, (r1 - r0) * sizeof(vrt_hit),
+                                     cudaMemcpyDeviceToHost, b->copy_stream));
+    }
+    VRT_CUDA(cudaEventRecord(b->copies_done, b->copy_stream));
+    VRT_CUDA(cudaStreamWaitEvent(stream, b->copies_done, 0));
+    b->last_stream = stream;
     VRT_CUDA(cudaStreamSynchronize(stream));
     return VRT_OK;
 }

@@ -37,6 +37,7 @@ struct BatchParams {
     const uint32_t* chunk_base;  // n_views + 1 entries
     uint32_t n_views;
     uint32_t total_chunks;
+    uint32_t chunk_first;  // absolute queue chunk of the first view (views may be a sub-range)
     uint32_t* queue;
     unsigned long long* counters;  // rays, step calls, occ fetches, hits
     uint4* out;
@@ -68,7 +69,9 @@ vrt_status plan_views(const vrt_view* views, uint32_t n, uint32_t n_worlds, cons
 vrt_status persistent_grid(int device, const vrt_batch_config& cfg, bool count, int& blocks, int& threads);
 BatchParams make_params(const LaunchPlan& plan, const DevWorld* worlds, const ViewDev* views,
                         const uint32_t* chunk_base, uint32_t* queue, vrt_hit* out);
-// Queue reset (64 bytes at params.queue) + persistent kernel launch.
-vrt_status launch_persistent(const BatchParams& p, int blocks, int threads, bool count, cudaStream_t stream);
+// Queue reset (the tile counter, and with reset_counters the launch counters: 64
+// bytes at params.queue) + persistent kernel launch.
+vrt_status launch_persistent(const BatchParams& p, int blocks, int threads, bool count, cudaStream_t stream,
+                             bool reset_counters = true);
 
 }  // namespace vrt

@@ -30,6 +30,7 @@
 #include "world.h"
 
 namespace vrt {
+
 namespace {
 
 constexpr uint64_t kPageBytes = 64 * 1024;  // output-arena allocation unit
@@ -297,7 +298,7 @@ vrt_status vrt_host_alloc(size_t bytes, void** out) {
         set_error("null argument");
         return VRT_ERR_INVALID_ARG;
     }
-    VRT_CUDA(cudaHostAlloc(out, bytes ? bytes : 1, cudaHostAllocDefault));
+    VRT_CUDA(cudaHostAlloc(out, bytes ? bytes : 1, cudaHostAllocPortable));
     return VRT_OK;
 }
 
