@@ -33,9 +33,10 @@ def device_layout(data: v.SectorData) -> bytes:
 
     Derived here from the geometric definitions, independently of the device's bit
     tricks: an empty brick position skips to level 5 when its sector holds no brick,
-    to 4 when the aligned 2x2x2 group of bricks around it is empty, else 3; an empty
-    voxel of an allocated brick codes 3 when its aligned 4^3 cell is empty, 2 when its
-    aligned 2^3 block is, else 1; a solid voxel codes 0."""
+    to 4 when the aligned 2x2x2 group of bricks around it is empty, else 3, stored as
+    the alignment mask (1 << level) - 1; an empty voxel of an allocated brick skips to
+    level 2 when its aligned 4^3 cell is empty, 1 when its aligned 2^3 block is, else 0,
+    coded as the same mask (3, 1, 0); a solid voxel codes 2."""
     sx, sy, sz = data.sectors
     alloc = np.zeros((sy * 4, sz * 4, sx * 4), bool)          # (by, bz, bx)
     slot_of = np.zeros((sy * 4, sz * 4, sx * 4), np.uint32)
@@ -52,14 +53,14 @@ def device_layout(data: v.SectorData) -> bytes:
     group_any = alloc.reshape(sy * 2, 2, sz * 2, 2, sx * 2, 2).any(axis=(1, 3, 5))
     up4 = lambda a: a.repeat(4, 0).repeat(4, 1).repeat(4, 2)
     up2 = lambda a: a.repeat(2, 0).repeat(2, 1).repeat(2, 2)
-    level = np.where(~up4(sector_any), 5, np.where(~up2(group_any), 4, 3)).astype(np.uint32)
+    level = np.where(~up4(sector_any), 31, np.where(~up2(group_any), 15, 7)).astype(np.uint32)
     table = np.where(alloc, slot_of, np.uint32(0x80000000) | level).astype(np.uint32)
     nb = data.n_bricks
     solid = data.bricks.reshape(nb, 8, 8, 8) != 0             # (n, y, z, x)
     cell_any = solid.reshape(nb, 2, 4, 2, 4, 2, 4).any(axis=(2, 4, 6))
     block_any = solid.reshape(nb, 4, 2, 4, 2, 4, 2).any(axis=(2, 4, 6))
     up = lambda a, k: a.repeat(k, 1).repeat(k, 2).repeat(k, 3)
-    code = np.where(solid, 0, np.where(~up(cell_any, 4), 3, np.where(~up(block_any, 2), 2, 1))).astype(np.uint32)
+    code = np.where(solid, 2, np.where(~up(cell_any, 4), 3, np.where(~up(block_any, 2), 1, 0))).astype(np.uint32)
     code = code.reshape(nb, 32, 16)                          # voxel x | z<<3 | y<<6 -> word, position
     words = (code << (2 * np.arange(16, dtype=np.uint32))).sum(axis=2, dtype=np.uint64).astype(np.uint32)
     head = np.array([sx, sy, sz, nb], np.uint32).tobytes()

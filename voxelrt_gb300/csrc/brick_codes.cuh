@@ -4,8 +4,8 @@
 // 64-bit masks of 4^3-voxel cells per brick; GetStepPos (CpuRenderer.cpp:146-160)
 // then tests the voxel's bit and, when it is clear, derives the skip level from the
 // same mask.  Both are functions of the brick's bytes and the voxel position alone,
-// so the device stores their result per voxel: a 2-bit code, 0 = solid, else
-// 1 + skip level (vrt_internal.h has the word layout).
+// so the device stores their result per voxel: a 2-bit code, kCodeSolid, or the
+// alignment mask (1 << level) - 1 of an empty voxel (vrt_internal.h has the layout).
 #pragma once
 
 #include <cstdint>
@@ -48,14 +48,15 @@ __device__ __forceinline__ uint32_t warp_voxel_codes(const uint8_t* sb, uint64_t
     for (uint32_t j = 0; j < 16; j++) {
         const uint32_t x = j & 7, z = z0 + (j >> 3);
         const uint32_t idx = (x & 3) | (z & 3) << 2 | (y & 3) << 4;  // bit in the cell mask
-        const uint32_t code =
-            sb[x | z << 3 | y << 6] != 0 ? 0u : 1u + (x < 4 ? skip_levels(lo0, hi0, idx) : skip_levels(lo1, hi1, idx));
+        const uint32_t level = x < 4 ? skip_levels(lo0, hi0, idx) : skip_levels(lo1, hi1, idx);
+        const uint32_t code = sb[x | z << 3 | y << 6] != 0 ? kCodeSolid : (1u << level) - 1u;
         word |= code << (2 * j);
     }
     return word;
 }
 
-// Codes of an all-empty brick: every cell mask is 0, so every voxel skips 2 levels.
+// Codes of an all-empty brick: every cell mask is 0, so every voxel skips 2 levels
+// (mask 3 in every 2-bit field).
 constexpr uint32_t kEmptyBrickCodes = 0xFFFFFFFFu;
 
 }  // namespace vrt

@@ -154,30 +154,29 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
     }
     if (kCount) cnt.step_calls++;
     // The brick table holds the slot of an allocated brick, or for an empty one the
-    // level GetStepPos reaches from the sector mask (3 + skip_levels).  An allocated
-    // brick's voxel code is 0 for a solid voxel (the hit), else 1 + the skip level
-    // of its 4^3 cell mask; both replace the two mask fetches of the reference with
-    // their precomputed outcome.
+    // alignment mask of the level GetStepPos reaches from the sector mask
+    // (3 + skip_levels).  An allocated brick's voxel code is kCodeSolid (the hit) or
+    // the alignment mask of the skip level of the voxel's 4^3 cell; both replace the
+    // two mask fetches of the reference with their precomputed outcome.
     const uint32_t e =
         __ldg(w.bricks + ((uint32_t)vx >> 3) + ((uint32_t)vz >> 3) * w.bsx + ((uint32_t)vy >> 3) * w.bsxz);
-    int32_t lod;
+    int32_t m;
     if (e < kBrickEmpty) {
         if (kCount) cnt.occ_fetches++;
         const uint32_t vi = (uint32_t)((vx & 7) | (vz & 7) << 3 | (vy & 7) << 6);
         const uint32_t code = (__ldg(w.codes + (size_t)e * 32 + (vi >> 4)) >> ((vi & 15) * 2)) & 3u;
-        if (code == 0) {
+        if (code == kCodeSolid) {
             s.material = __ldg(w.payload + (size_t)e * 512 + vi);
             s.vx = vx;
             s.vy = vy;
             s.vz = vz;
             return kStepHit;
         }
-        lod = (int32_t)code - 1;
+        m = (int32_t)code;
     } else {
-        lod = (int32_t)(e & 7u);
+        m = (int32_t)(e & 31u);
     }
     // dir < 0 ? pos & ~m : pos | m, as (pos | m) ^ (g & m) with g = -1 for dir < 0
-    const int32_t m = (1 << lod) - 1;
     vx = (vx | m) ^ (s.gx & m);
     vy = (vy | m) ^ (s.gy & m);
     vz = (vz | m) ^ (s.gz & m);

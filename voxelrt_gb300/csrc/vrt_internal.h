@@ -8,13 +8,14 @@
 //   bricks   the brick table derived from it, one u32 per brick position of the
 //            world, index bx + bz*BX + by*BX*BZ (BX = 4*SX, BZ = 4*SZ): the brick's
 //            slot when its bit is set in the sector mask, else kBrickEmpty | the
-//            skip level GetStepPos takes there (3 + skip_levels of the sector mask,
-//            CpuRenderer.cpp:139-160);
+//            alignment mask (1 << level) - 1 of the level GetStepPos reaches there,
+//            level = 3 + skip_levels of the sector mask (CpuRenderer.cpp:139-167);
 //   codes    2-bit voxel codes, 32 u32 words (128 B) per brick slot; voxel
-//            v = x | z<<3 | y<<6 sits in word v>>4 at bit 2*(v&15): 0 = solid, else
-//            1 + skip_levels of the 4^3 voxel cell's occupancy mask (cell
+//            v = x | z<<3 | y<<6 sits in word v>>4 at bit 2*(v&15): kCodeSolid, or
+//            for an empty voxel the alignment mask (1 << level) - 1 (0, 1 or 3) of
+//            level = skip_levels of its 4^3 cell's occupancy mask (cell
 //            cx | cz<<1 | cy<<2, bit vx + vz*4 + vy*16: UpdateOccupancy,
-//            CpuRenderer.cpp:63-83, and GetStepPos :146-160);
+//            CpuRenderer.cpp:63-83, and GetStepPos :146-167);
 //   payload  512 B of u8 voxel ids per brick slot, voxel x | z<<3 | y<<6.
 // A brick's slot is base + popcount(mask & ((1<<b)-1)) (VoxelMap.glsl:45-64,
 // BrickSlotAllocator.h:37-41).  The traversal reads bricks, codes and payload
@@ -40,8 +41,10 @@ static_assert(sizeof(SectorRec) == 16, "sector record is one 16-byte load");
 #define VRT_HD
 #endif
 
-// Brick-table entry of an unallocated brick position; the low bits hold the level.
+// Brick-table entry of an unallocated brick position; the low bits hold the mask.
 constexpr uint32_t kBrickEmpty = 0x80000000u;
+// Voxel code of a solid voxel (the masks of empty voxels are 0, 1 and 3).
+constexpr uint32_t kCodeSolid = 2u;
 
 // Extra levels GetStepPos skips at position idx (0..63) of an empty bit of the
 // 64-bit mask (lo, hi): 2 when the whole mask is 0, 1 when the 2x2x2 block holding

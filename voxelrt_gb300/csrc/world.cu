@@ -119,7 +119,7 @@ __global__ void brick_table_kernel(const SectorRec* __restrict__ sectors, uint32
         const uint32_t below = (1u << (b & 31)) - 1u;
         e = rec.base + (b < 32 ? __popc(lo & below) : __popc(lo) + __popc(hi & below));
     } else {
-        e = kBrickEmpty | (3u + skip_levels(lo, hi, b));
+        e = kBrickEmpty | ((8u << skip_levels(lo, hi, b)) - 1u);
     }
     bricks[bx + bz * (sx * 4) + by * (sx * 4) * (sz * 4)] = e;
 }
