@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--serve-max-edge", type=int, default=1024)
     ap.add_argument("--worlds", type=int, default=128, help="uneven_batch: number of worlds")
     ap.add_argument("--max-views", type=int, default=16, help="uneven_batch: views per world, at most")
+    ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
+                    help="N>1: every rank traces its own batch (weak) or a share, by world, of one batch (strong)")
     return ap.parse_args()
 
 
@@ -70,25 +72,34 @@ def dist_setup(args):
 
 
 def barrier(pg):
-    if pg is not None:
-        pg.barrier()
+    from voxelrt_gb300 import shard
+    shard.barrier(pg)
 
 
 def max_over_ranks(pg, x: float) -> float:
-    if pg is None:
-        return x
-    import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    pg.all_reduce(t, op=pg.ReduceOp.MAX)
-    return float(t.item())
+    from voxelrt_gb300 import shard
+    return shard.max_over_ranks(pg, x, "cuda")
 
 
-def build_workload(name: str, rank: int, args=None):
+def sum_over_ranks(pg, x: float) -> float:
+    from voxelrt_gb300 import shard
+    return shard.sum_over_ranks(pg, x, "cuda")
+
+
+def build_workload(name: str, rank: int, args=None, world_size: int = 1):
+    """The rank's workload: its own seeded batch (weak scaling) or its share, by world, of
+    the one batch (strong scaling, uneven_batch only)."""
+    from voxelrt_gb300 import shard
     from voxelrt_gb300 import workloads as W
     if name == "uneven_batch":
         nw = args.worlds if args is not None else 128
         mv = args.max_views if args is not None else 16
-        return W.uneven_batch(n_worlds=nw, max_views=mv, seed=2 + 1000 * rank)
+        strong = args is not None and getattr(args, "scaling", "weak") == "strong" and world_size > 1
+        wl = W.uneven_batch(n_worlds=nw, max_views=mv, seed=2 if strong else shard.rank_seed(2, rank))
+        if strong:
+            worlds, views, own = shard.shard_batch(wl.worlds, wl.views, rank, world_size)
+            wl = W.Workload(wl.name, worlds, views, f"{wl.description}, worlds {own} of {world_size} ranks")
+        return wl
     if name == "large_world":
         return W.large_world()
     if name == "incoherent":
@@ -248,7 +259,7 @@ def run_ours(args):
     ws, rank, local, pg = dist_setup(args)
     torch.cuda.set_device(local)
     dev = local
-    wl = build_workload(args.workload, rank, args)
+    wl = build_workload(args.workload, rank, args, ws)
     worlds = []
     for d in wl.worlds:
         w = v.World(d.sectors, brick_capacity=d.n_bricks + 64, device=dev)
@@ -288,7 +299,8 @@ def run_ours(args):
     barrier(pg)
     ms = ev0.elapsed_time(ev1) / args.steps
     ms = max_over_ranks(pg, ms)
-    value = rays_per_step * ws / (ms * 1e-3) / 1e9
+    job_rays = sum_over_ranks(pg, rays_per_step)  # all ranks' rays per step
+    value = job_rays / (ms * 1e-3) / 1e9
 
     # per-view baseline: one plain launch per view, same views and records
     per_view = None
@@ -305,7 +317,7 @@ def run_ours(args):
         e1.record(stream)
         e1.synchronize()
         pms = max_over_ranks(pg, e0.elapsed_time(e1) / k)
-        per_view = {"value": rays_per_step * ws / (pms * 1e-3) / 1e9, "unit": "Grays/s", "ms_per_step": pms,
+        per_view = {"value": job_rays / (pms * 1e-3) / 1e9, "unit": "Grays/s", "ms_per_step": pms,
                     "launches_per_step": len(wl.views), "steps": k,
                     "kernel": "view_path_kernel, 8x8 blocks, thread per pixel"}
 
@@ -323,7 +335,7 @@ def run_ours(args):
         batch.update_cameras(cams, stream)
         batch.run(host_np, stream)
     e2e_s = max_over_ranks(pg, (time.perf_counter() - t0) / ke)
-    e2e = {"value": rays_per_step * ws / e2e_s / 1e9, "unit": "Grays/s", "ms_per_step": e2e_s * 1e3,
+    e2e = {"value": job_rays / e2e_s / 1e9, "unit": "Grays/s", "ms_per_step": e2e_s * 1e3,
            "h2d_bytes_per_step": 120 * len(wl.views), "d2h_bytes_per_step": n_rec * HIT_BYTES,
            "api": "vrt_batch_update_cameras + vrt_batch_run (pinned host records)"}
 
@@ -354,11 +366,11 @@ def run_ours(args):
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "Grays/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": args.scaling,
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": wl.name, "description": wl.description, "worlds": len(wl.worlds),
                        "views": len(wl.views), "rays_per_step": rays_per_step, "records_per_step": n_rec,
-                       "world_bytes": int(sum(d.n_bricks for d in wl.worlds) * 576),
+                       "world_bytes": int(sum(d.n_bricks for d in wl.worlds) * 640),
                        "l2": "inputs larger than L2 (brick pools of all worlds)",
                        "batch_config": autotune.describe(cfg), "batch_config_source": cfg_src,
                        "launch": "persistent kernel + queue reset, CUDA graph replay"},
@@ -490,7 +502,7 @@ def run_serving(args, dev):
         b.close()
     for w in worlds:
         w.close()
-    return {"worlds": len(datas), "max_edge": max(edges), "world_bytes": int(sum(d.n_bricks for d in datas) * 576),
+    return {"worlds": len(datas), "max_edge": max(edges), "world_bytes": int(sum(d.n_bricks for d in datas) * 640),
             "resolutions": "256^2 / 1280x720 / 1920x1080 at p 0.5 / 0.3 / 0.2", "edits_per_s": 100,
             "seconds_per_rate": args.serve_seconds, "rates": out, "oracle_replay": replay,
             "latency": "submit to records in pinned host memory, server clock"}
