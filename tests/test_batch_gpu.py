@@ -9,7 +9,7 @@ import pytest
 
 import voxelrt_gb300 as v
 from oracle.oracle import OracleWorld
-from tests.helpers import assert_hits_equal, both_worlds, cfg0_camera, cfg0_world
+from tests.helpers import assert_hits_equal, both_worlds, cfg0_camera, cfg0_world, oracle_view
 
 pytestmark = pytest.mark.gpu
 
@@ -74,15 +74,6 @@ def mix_batch_setup(n_worlds=5, seed=0):
             else:
                 views.append(v.make_view(cam, world=i, n_bounces=2, max_iters=64))
     return worlds, oracles, views
-
-
-def oracle_view(o: OracleWorld, view) -> np.ndarray:
-    if view.flags & v.VIEW_SHADOW:
-        p, s = o.render_view_shadow(view.cam, np.array(view.sun_dir[:], np.float32), view.max_iters)
-        return np.stack([p, s])
-    if view.n_bounces:
-        return o.render_view_bounces(view.cam, view.n_bounces, view.max_iters)
-    return o.render_view(view.cam, view.max_iters)[None]
 
 
 @pytest.fixture(scope="module")
