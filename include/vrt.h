@@ -98,9 +98,29 @@ typedef struct vrt_hit {
 
 typedef struct vrt_cast_params {
     int32_t world_origin[3]; /* FrameConstants::WorldOrigin (CpuRenderer.cpp:447) */
-    uint32_t max_iters;      /* 0 = VRT_DEFAULT_MAX_ITERS; at most 65535 */
-    uint32_t flags;          /* must be 0 */
+    uint32_t max_iters;      /* 0 = VRT_DEFAULT_MAX_ITERS (VRT_GLSL_MAX_ITERS in GLSL mode); at most 65535 */
+    uint32_t flags;          /* 0 or VRT_CAST_GLSL */
 } vrt_cast_params;
+
+/* Traversal modes.  The default is the reference CPU traversal (CpuRenderer.cpp:135-224,
+ * the pinned contract above).  The GLSL mode is the GPU renderer's rayCast
+ * (Shaders/VoxelTraversal.glsl:100-204) with anisotropic LODs off:
+ *   - a 4th level: where a sector holds no brick, the mask of its 4^3 group of sectors
+ *     (bit set per non-empty sector, GpuRenderer.cpp:139-149) gives cells of 32, 64 or
+ *     128 voxels;
+ *   - each iteration first takes the side distances of the current voxel (the start
+ *     voxel on iteration 0, which is therefore never tested), then
+ *     tmin = min(sides) + 5 ulp (integer add on the bits; a NaN tmin stays NaN, as the
+ *     bits of a NaN differ between platforms), pos = origin + tmin*dir,
+ *     voxel = worldOrigin + floor(pos), bounds, getStepPos;
+ *   - a hit reports t = the biased tmin and face = the first axis with tmin >= side;
+ *     secondary rays start at pos + normal*0.01 with normal = -sign(dir) on every such
+ *     axis (sign(0) = 0);
+ *   - the iteration cap defaults to VRT_GLSL_MAX_ITERS.
+ * Entry clip, bounds (per axis, the world's extent) and the x86 min/floor rules are
+ * shared with the default mode. */
+#define VRT_CAST_GLSL 1u
+#define VRT_GLSL_MAX_ITERS 256
 
 /* Pinhole camera in the reference's split form: integer world origin plus a
  * fractional ray origin (GBuffer.h:79, CpuRenderer.cpp:447-448).  The ray of
@@ -276,11 +296,12 @@ typedef struct vrt_view {
     uint32_t world;     /* index into the batch's world list */
     uint32_t max_iters; /* 0 = VRT_DEFAULT_MAX_ITERS */
     uint32_t n_bounces; /* 0..15, exclusive with VRT_VIEW_SHADOW */
-    uint32_t flags;     /* VRT_VIEW_SHADOW */
+    uint32_t flags;     /* VRT_VIEW_SHADOW, VRT_VIEW_GLSL */
     float sun_dir[3];
 } vrt_view;
 
 #define VRT_VIEW_SHADOW 1u
+#define VRT_VIEW_GLSL 2u /* GLSL traversal mode (see VRT_CAST_GLSL); every view of a batch shares one mode */
 #define VRT_MAX_BOUNCES 15u
 
 /* One view with its secondary rays, one plain launch (thread per pixel, no

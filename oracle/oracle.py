@@ -56,9 +56,11 @@ def lib() -> C.CDLL:
         L.ora_world_allocated_bricks.argtypes = [_vp]
         L.ora_cast.argtypes = [_vp, _vp, C.c_uint64, C.POINTER(_CastParams), _vp, C.c_int, C.POINTER(Stats)]
         L.ora_camera_rays.argtypes = [_vp, _vp]
-        L.ora_render_view.argtypes = [_vp, _vp, C.c_uint32, _vp, C.c_int, C.POINTER(Stats)]
-        L.ora_render_view_shadow.argtypes = [_vp, _vp, _vp, C.c_uint32, _vp, _vp, C.c_int, C.POINTER(Stats)]
-        L.ora_render_view_bounces.argtypes = [_vp, _vp, C.c_uint32, C.c_uint32, _vp, C.c_int, C.POINTER(Stats)]
+        L.ora_render_view.argtypes = [_vp, _vp, C.c_uint32, C.c_uint32, _vp, C.c_int, C.POINTER(Stats)]
+        L.ora_render_view_shadow.argtypes = [_vp, _vp, _vp, C.c_uint32, C.c_uint32, _vp, _vp, C.c_int,
+                                             C.POINTER(Stats)]
+        L.ora_render_view_bounces.argtypes = [_vp, _vp, C.c_uint32, C.c_uint32, C.c_uint32, _vp, C.c_int,
+                                              C.POINTER(Stats)]
         L.ora_world_edit.argtypes = [_vp, _vp, C.c_uint32]
         L.ora_pick.argtypes = [_vp, _vp, C.c_uint64, C.c_uint32, _vp]
         _lib = L
@@ -126,39 +128,40 @@ class OracleWorld:
     def allocated_bricks(self) -> int:
         return lib().ora_world_allocated_bricks(self._h)
 
-    def cast(self, rays, world_origin=(0, 0, 0), max_iters=0, threads=0) -> np.ndarray:
+    def cast(self, rays, world_origin=(0, 0, 0), max_iters=0, threads=0, glsl=False) -> np.ndarray:
+        """glsl: the GPU renderer's rayCast (flag VRT_CAST_GLSL) instead of the CPU traversal."""
         rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
         hits = np.zeros(len(rays), HIT_DTYPE)
-        p = _CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), 0)
+        p = _CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), 1 if glsl else 0)
         s = Stats()
         _chk(lib().ora_cast(self._h, rays.ctypes.data, len(rays), C.byref(p), hits.ctypes.data, int(threads),
                             C.byref(s)))
         self.last_stats = _stats(s)
         return hits
 
-    def render_view(self, cam, max_iters=0, threads=0) -> np.ndarray:
+    def render_view(self, cam, max_iters=0, threads=0, glsl=False) -> np.ndarray:
         hits = np.zeros(cam.width * cam.height, HIT_DTYPE)
         s = Stats()
-        _chk(lib().ora_render_view(self._h, C.addressof(cam), int(max_iters), hits.ctypes.data, int(threads),
-                                   C.byref(s)))
+        _chk(lib().ora_render_view(self._h, C.addressof(cam), int(max_iters), int(glsl), hits.ctypes.data,
+                                   int(threads), C.byref(s)))
         self.last_stats = _stats(s)
         return hits
 
-    def render_view_shadow(self, cam, sun_dir, max_iters=0, threads=0):
+    def render_view_shadow(self, cam, sun_dir, max_iters=0, threads=0, glsl=False):
         n = cam.width * cam.height
         prim, shad = np.zeros(n, HIT_DTYPE), np.zeros(n, HIT_DTYPE)
         sd = np.ascontiguousarray(sun_dir, dtype=np.float32)
         s = Stats()
-        _chk(lib().ora_render_view_shadow(self._h, C.addressof(cam), sd.ctypes.data, int(max_iters),
+        _chk(lib().ora_render_view_shadow(self._h, C.addressof(cam), sd.ctypes.data, int(max_iters), int(glsl),
                                           prim.ctypes.data, shad.ctypes.data, int(threads), C.byref(s)))
         self.last_stats = _stats(s)
         return prim, shad
 
-    def render_view_bounces(self, cam, n_bounces, max_iters=0, threads=0) -> np.ndarray:
+    def render_view_bounces(self, cam, n_bounces, max_iters=0, threads=0, glsl=False) -> np.ndarray:
         n = cam.width * cam.height
         hits = np.zeros((n_bounces + 1) * n, HIT_DTYPE)
         s = Stats()
-        _chk(lib().ora_render_view_bounces(self._h, C.addressof(cam), int(n_bounces), int(max_iters),
+        _chk(lib().ora_render_view_bounces(self._h, C.addressof(cam), int(n_bounces), int(max_iters), int(glsl),
                                            hits.ctypes.data, int(threads), C.byref(s)))
         self.last_stats = _stats(s)
         return hits.reshape(n_bounces + 1, n)

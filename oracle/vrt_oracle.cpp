@@ -15,6 +15,13 @@
 //     iteration cap ran out (CpuRenderer.cpp:195 leaves relative coordinates in
 //     voxelPos in that case, a SIMD-lane artefact);
 //   * the step count mirrors GLSL hit.iters (VoxelTraversal.glsl:185,197).
+//
+// Mode VRT_CAST_GLSL / VRT_VIEW_GLSL restates instead the GPU renderer's rayCast
+// (VoxelTraversal.glsl:100-131 getStepPos, :162-204 rayCast) with anisotropic LODs
+// off: a 4th level of sector-group masks (GpuRenderer.cpp:139-149), cells of
+// isotropic size 1/2/4 x scale 1/8/32, a 256-iteration cap, the +5-ulp bias on tmin,
+// and side distances taken from the current voxel before each step, so the start
+// voxel itself is never tested.  Its parity is unpinned: the shader cannot run here.
 
 #include "vrt_oracle.h"
 
@@ -110,6 +117,8 @@ void parallel_for(uint64_t n, int threads, F&& fn) {
 
 struct Trace {
     bool hit;
+    bool glsl;      // traced in the GLSL mode (t, face and normal follow rayCast)
+    float tb;       // GLSL mode: the biased tmin of the hit step (hit.dist)
     uint16_t steps;
     uint8_t material;
     int32_t vp[3];
@@ -124,6 +133,20 @@ struct Trace {
 struct ora_world {
     uint32_t sx, sy, sz;
     std::vector<uint64_t> masks;
+    // GLSL mode 4th level: per group of 4^3 sectors, bit x | z<<2 | y<<4 set when that
+    // sector holds a brick (GpuRenderer.cpp:139-149), groups indexed x + z*GX + y*GX*GZ
+    std::vector<uint64_t> groups;
+    uint32_t gx() const { return (sx + 3) / 4; }
+    uint32_t gz() const { return (sz + 3) / 4; }
+    void refresh_groups() {
+        groups.assign((size_t)gx() * ((sy + 3) / 4) * gz(), 0);
+        for (uint32_t y = 0; y < sy; y++)
+            for (uint32_t z = 0; z < sz; z++)
+                for (uint32_t x = 0; x < sx; x++)
+                    if (masks[lin((int32_t)x, (int32_t)y, (int32_t)z)])
+                        groups[(x >> 2) + (z >> 2) * gx() + (y >> 2) * gx() * gz()] |=
+                            1ull << ((x & 3) | (z & 3) << 2 | (y & 3) << 4);
+    }
     std::vector<std::unique_ptr<SectorBlock>> data;
 
     uint32_t lin(int32_t x, int32_t y, int32_t z) const {
@@ -181,10 +204,118 @@ inline bool get_step_pos(const ora_world& w, int32_t vp[3], const float dir[3], 
     return false;
 }
 
+// getIsotropicLod (VoxelTraversal.glsl:24-34): cell size in units of the level's scale.
+inline int32_t iso_lod(uint64_t m, uint32_t idx) {
+    if (m == 0) return 4;
+    uint32_t half = (uint32_t)(idx < 32 ? m : m >> 32);
+    return ((half >> (idx & 0xA)) & 0x00330033u) == 0 ? 2 : 1;
+}
+
+// getStepPos (VoxelTraversal.glsl:100-131), coarse = false, anisotropic LODs off.
+// Returns true on a hit.
+inline bool get_step_pos_glsl(const ora_world& w, int32_t vp[3], const float dir[3], Trace& tr) {
+    const int32_t sx = vp[0] >> 5, sy = vp[1] >> 5, sz = vp[2] >> 5;
+    uint32_t s = w.lin(sx, sy, sz);
+    uint64_t m = w.masks[s];
+    uint32_t idx = ((vp[0] >> 3) & 3) | ((vp[2] >> 3) & 3) << 2 | ((vp[1] >> 3) & 3) << 4;
+    int32_t scale = 8;
+    tr.step_calls++;
+    if ((m >> idx) & 1) {
+        const SectorBlock* blk = w.data[s].get();
+        uint32_t brick = idx;
+        uint32_t cell = ((vp[0] >> 2) & 1) | ((vp[2] >> 2) & 1) << 1 | ((vp[1] >> 2) & 1) << 2;
+        m = blk->occ[brick * 8 + cell];
+        idx = (vp[0] & 3) | (vp[2] & 3) << 2 | (vp[1] & 3) << 4;
+        scale = 1;
+        tr.occ_fetches++;
+        if ((m >> idx) & 1) {
+            uint32_t vi = (vp[0] & 7) | (vp[2] & 7) << 3 | (vp[1] & 7) << 6;
+            tr.material = blk->vox[brick * 512 + vi];
+            return true;
+        }
+    } else if (m == 0) {
+        m = w.groups[(uint32_t)(sx >> 2) + (uint32_t)(sz >> 2) * w.gx() + (uint32_t)(sy >> 2) * w.gx() * w.gz()];
+        idx = (uint32_t)((sx & 3) | (sz & 3) << 2 | (sy & 3) << 4);
+        scale = 32;
+    }
+    int32_t cm = iso_lod(m, idx) * scale - 1;
+    for (int c = 0; c < 3; c++) vp[c] = dir[c] < 0.0f ? (vp[c] & ~cm) : (vp[c] | cm);
+    return false;
+}
+
+// The entry clip of VoxelTraversal.glsl:133-145 with bounds 1 - wo .. size - wo - 1
+// (:166): the start position (origin when the clip does not apply).
+void clip_start(const ora_world& w, const float o[3], const float d[3], const float inv[3], const int32_t wo[3],
+                float cur[3]) {
+    const int32_t size[3] = {(int32_t)w.sx * 32, (int32_t)w.sy * 32, (int32_t)w.sz * 32};
+    float lo[3], hi[3];
+    for (int c = 0; c < 3; c++) {
+        float bmin = (float)(1 - wo[c]);
+        float bmax = ((float)size[c] - (float)wo[c]) - 1.0f;
+        float t1 = (bmin - o[c]) * inv[c];
+        float t2 = (bmax - o[c]) * inv[c];
+        lo[c] = min_x86(t1, t2);
+        hi[c] = max_x86(t1, t2);
+    }
+    float tmin = max_x86(lo[0], max_x86(lo[1], lo[2]));
+    float tmax = min_x86(hi[0], min_x86(hi[1], hi[2]));
+    if (tmin > 0.0f && tmin < tmax) {
+        for (int c = 0; c < 3; c++) cur[c] = o[c] + d[c] * tmin;
+    } else {
+        for (int c = 0; c < 3; c++) cur[c] = o[c];
+    }
+}
+
+// rayCast (VoxelTraversal.glsl:162-204) for one ray: the voxel's side distances,
+// tmin + 5 ulp, the next position, bounds, getStepPos.
+void trace_ray_glsl(const ora_world& w, const float o[3], const float d[3], const int32_t wo[3],
+                    uint32_t max_iters, Trace& tr) {
+    tr.hit = false;
+    tr.glsl = true;
+    tr.tb = 0.0f;
+    tr.material = 0;
+    tr.step_calls = 0;
+    tr.occ_fetches = 0;
+    float inv[3], ts[3];
+    for (int c = 0; c < 3; c++) inv[c] = 1.0f / d[c];
+    for (int c = 0; c < 3; c++) ts[c] = ((d[c] < 0.0f ? 0.0f : 1.0f) - o[c]) * inv[c];
+    const int32_t size[3] = {(int32_t)w.sx * 32, (int32_t)w.sy * 32, (int32_t)w.sz * 32};
+    float* cur = tr.cur;
+    clip_start(w, o, d, inv, wo, cur);
+    int32_t* vp = tr.vp;
+    for (int c = 0; c < 3; c++) vp[c] = wadd(wo[c], floor2i(cur[c]));
+    float* side = tr.side;
+    for (uint32_t i = 0; i < max_iters; i++) {
+        for (int c = 0; c < 3; c++) side[c] = ts[c] + (float)wsub(vp[c], wo[c]) * inv[c];
+        float t = min_x86(min_x86(side[0], side[1]), side[2]);
+        if (t == t) {  // +5 ulp on the bits; a NaN stays NaN (its bits are platform-defined)
+            uint32_t bits;
+            std::memcpy(&bits, &t, 4);
+            bits += 5u;
+            std::memcpy(&t, &bits, 4);
+        }
+        for (int c = 0; c < 3; c++) cur[c] = o[c] + t * d[c];
+        for (int c = 0; c < 3; c++) vp[c] = wadd(wo[c], floor2i(cur[c]));
+        if (!((uint32_t)vp[0] < (uint32_t)size[0] && (uint32_t)vp[1] < (uint32_t)size[1] &&
+              (uint32_t)vp[2] < (uint32_t)size[2])) {
+            tr.steps = (uint16_t)i;
+            return;
+        }
+        if (get_step_pos_glsl(w, vp, d, tr)) {
+            tr.hit = true;
+            tr.tb = t;
+            tr.steps = (uint16_t)i;
+            return;
+        }
+    }
+    tr.steps = (uint16_t)max_iters;
+}
+
 // RayCast (CpuRenderer.cpp:172-224) for one lane, with the GLSL entry clip.
 void trace_ray(const ora_world& w, const float o[3], const float d[3], const int32_t wo[3],
                uint32_t max_iters, Trace& tr) {
     tr.hit = false;
+    tr.glsl = false;
     tr.material = 0;
     tr.step_calls = 0;
     tr.occ_fetches = 0;
@@ -245,9 +376,16 @@ void fill_hit(const Trace& tr, const float d[3], uint32_t tag, vrt_hit& h) {
         h.t = INFINITY;
         return;
     }
-    float t = min_x86(min_x86(tr.side[0], tr.side[1]), tr.side[2]);
-    uint32_t axis = tr.side[0] == t ? 0u : (tr.side[1] == t ? 1u : 2u);
-    h.t = t;
+    uint32_t axis;
+    if (tr.glsl) {
+        // hit.dist = biased tmin; the face is the first axis of sideMask = tmin >= sideDist
+        axis = tr.tb >= tr.side[0] ? 0u : (tr.tb >= tr.side[1] ? 1u : 2u);
+        h.t = tr.tb;
+    } else {
+        float t = min_x86(min_x86(tr.side[0], tr.side[1]), tr.side[2]);
+        axis = tr.side[0] == t ? 0u : (tr.side[1] == t ? 1u : 2u);
+        h.t = t;
+    }
     h.face = (uint8_t)(axis * 2 + (d[axis] < 0.0f ? 1 : 0));
     h.material = tr.material;
     h.voxel = (uint32_t)tr.vp[0] | (uint32_t)tr.vp[1] << 11 | (uint32_t)tr.vp[2] << 21;
@@ -265,6 +403,13 @@ void fill_no_ray(vrt_hit& h) {
 // HitResult.Normal (CpuRenderer.cpp:213-217): sideMaskX = sx==t, sideMaskY = sy==t,
 // sideMaskZ = neither; component = (sign bit of dir) ? +1 : -1.
 void hit_normal(const Trace& tr, const float d[3], float n[3]) {
+    if (tr.glsl) {
+        // hit.normal = mix(0, -sign(dir), tmin >= sideDist) (VoxelTraversal.glsl:190-192);
+        // sign(+-0) = 0
+        for (int c = 0; c < 3; c++)
+            n[c] = tr.tb >= tr.side[c] ? (d[c] > 0.0f ? -1.0f : (d[c] < 0.0f ? 1.0f : 0.0f)) : 0.0f;
+        return;
+    }
     float t = min_x86(min_x86(tr.side[0], tr.side[1]), tr.side[2]);
     bool mx = tr.side[0] == t, my = tr.side[1] == t, mz = !mx && !my;
     bool m[3] = {mx, my, mz};
@@ -331,6 +476,20 @@ void bounce_dir(uint32_t pixel, uint32_t bounce, const float n[3], float out[3])
     for (int c = 0; c < 3; c++) out[c] = n[c] / l;
 }
 
+// Traversal of one ray in the given mode.
+inline void trace_mode(const ora_world& w, bool glsl, const float o[3], const float d[3], const int32_t wo[3],
+                       uint32_t max_iters, Trace& tr) {
+    if (glsl)
+        trace_ray_glsl(w, o, d, wo, max_iters, tr);
+    else
+        trace_ray(w, o, d, wo, max_iters, tr);
+}
+
+uint32_t eff_iters_mode(uint32_t max_iters, bool glsl) {
+    if (max_iters == 0) return glsl ? VRT_GLSL_MAX_ITERS : VRT_DEFAULT_MAX_ITERS;
+    return max_iters > 65535u ? 65535u : max_iters;
+}
+
 uint32_t eff_iters(uint32_t max_iters) {
     if (max_iters == 0) return VRT_DEFAULT_MAX_ITERS;
     return max_iters > 65535 ? 65535 : max_iters;
@@ -375,6 +534,7 @@ ora_world* ora_world_create(uint32_t sx, uint32_t sy, uint32_t sz) {
     w->sz = sz;
     w->masks.assign((size_t)sx * sy * sz, 0);
     w->data.resize((size_t)sx * sy * sz);
+    w->refresh_groups();
     return w;
 }
 
@@ -413,6 +573,7 @@ int ora_world_sync(ora_world* w, uint32_t n, const int32_t* sector_idx, const ui
         }
         if (p) p += (size_t)popc64(dm) * 512;
     }
+    w->refresh_groups();
     return 0;
 }
 
@@ -468,12 +629,13 @@ uint64_t ora_world_allocated_bricks(const ora_world* w) {
 int ora_cast(const ora_world* w, const vrt_ray* rays, uint64_t n, const vrt_cast_params* params,
              vrt_hit* hits, int threads, ora_stats* stats) {
     if (!w || (n && (!rays || !hits)) || !params) return -1;
-    uint32_t iters = eff_iters(params->max_iters);
+    const bool glsl = (params->flags & VRT_CAST_GLSL) != 0;
+    uint32_t iters = eff_iters_mode(params->max_iters, glsl);
     StatAcc acc(threads);
     parallel_for(n, (int)acc.per.size(), [&](int tid, uint64_t b, uint64_t e) {
         Trace tr;
         for (uint64_t i = b; i < e; i++) {
-            trace_ray(*w, rays[i].origin, rays[i].dir, params->world_origin, iters, tr);
+            trace_mode(*w, glsl, rays[i].origin, rays[i].dir, params->world_origin, iters, tr);
             fill_hit(tr, rays[i].dir, rays[i].tag, hits[i]);
             acc.add(tid, tr);
         }
@@ -494,10 +656,11 @@ int ora_camera_rays(const vrt_camera* cam, vrt_ray* rays) {
     return 0;
 }
 
-int ora_render_view(const ora_world* w, const vrt_camera* cam, uint32_t max_iters, vrt_hit* hits,
+int ora_render_view(const ora_world* w, const vrt_camera* cam, uint32_t max_iters, uint32_t mode, vrt_hit* hits,
                     int threads, ora_stats* stats) {
     if (!w || !cam || !hits) return -1;
-    uint32_t iters = eff_iters(max_iters);
+    const bool glsl = mode != 0;
+    uint32_t iters = eff_iters_mode(max_iters, glsl);
     uint64_t n = (uint64_t)cam->width * cam->height;
     StatAcc acc(threads);
     parallel_for(n, (int)acc.per.size(), [&](int tid, uint64_t b, uint64_t e) {
@@ -505,7 +668,7 @@ int ora_render_view(const ora_world* w, const vrt_camera* cam, uint32_t max_iter
         float o[3], d[3];
         for (uint64_t i = b; i < e; i++) {
             camera_ray(*cam, (uint32_t)(i % cam->width), (uint32_t)(i / cam->width), o, d);
-            trace_ray(*w, o, d, cam->world_origin, iters, tr);
+            trace_mode(*w, glsl, o, d, cam->world_origin, iters, tr);
             fill_hit(tr, d, (uint32_t)i, hits[i]);
             acc.add(tid, tr);
         }
@@ -515,10 +678,11 @@ int ora_render_view(const ora_world* w, const vrt_camera* cam, uint32_t max_iter
 }
 
 int ora_render_view_shadow(const ora_world* w, const vrt_camera* cam, const float sun_dir[3],
-                           uint32_t max_iters, vrt_hit* primary, vrt_hit* shadow, int threads,
+                           uint32_t max_iters, uint32_t mode, vrt_hit* primary, vrt_hit* shadow, int threads,
                            ora_stats* stats) {
     if (!w || !cam || !sun_dir || !primary || !shadow) return -1;
-    uint32_t iters = eff_iters(max_iters);
+    const bool glsl = mode != 0;
+    uint32_t iters = eff_iters_mode(max_iters, glsl);
     uint64_t n = (uint64_t)cam->width * cam->height;
     StatAcc acc(threads);
     parallel_for(n, (int)acc.per.size(), [&](int tid, uint64_t b, uint64_t e) {
@@ -526,7 +690,7 @@ int ora_render_view_shadow(const ora_world* w, const vrt_camera* cam, const floa
         float o[3], d[3], nrm[3], so[3];
         for (uint64_t i = b; i < e; i++) {
             camera_ray(*cam, (uint32_t)(i % cam->width), (uint32_t)(i / cam->width), o, d);
-            trace_ray(*w, o, d, cam->world_origin, iters, tr);
+            trace_mode(*w, glsl, o, d, cam->world_origin, iters, tr);
             fill_hit(tr, d, (uint32_t)i, primary[i]);
             acc.add(tid, tr);
             if (!tr.hit) {
@@ -535,7 +699,7 @@ int ora_render_view_shadow(const ora_world* w, const vrt_camera* cam, const floa
             }
             hit_normal(tr, d, nrm);
             offset_origin(tr, nrm, so);
-            trace_ray(*w, so, sun_dir, cam->world_origin, iters, ts);
+            trace_mode(*w, glsl, so, sun_dir, cam->world_origin, iters, ts);
             fill_hit(ts, sun_dir, (uint32_t)i, shadow[i]);
             acc.add(tid, ts);
         }
@@ -545,9 +709,10 @@ int ora_render_view_shadow(const ora_world* w, const vrt_camera* cam, const floa
 }
 
 int ora_render_view_bounces(const ora_world* w, const vrt_camera* cam, uint32_t n_bounces,
-                            uint32_t max_iters, vrt_hit* hits, int threads, ora_stats* stats) {
+                            uint32_t max_iters, uint32_t mode, vrt_hit* hits, int threads, ora_stats* stats) {
     if (!w || !cam || !hits) return -1;
-    uint32_t iters = eff_iters(max_iters);
+    const bool glsl = mode != 0;
+    uint32_t iters = eff_iters_mode(max_iters, glsl);
     uint64_t n = (uint64_t)cam->width * cam->height;
     StatAcc acc(threads);
     parallel_for(n, (int)acc.per.size(), [&](int tid, uint64_t b, uint64_t e) {
@@ -567,7 +732,7 @@ int ora_render_view_bounces(const ora_world* w, const vrt_camera* cam, uint32_t 
                     offset_origin(tr, nrm, o);
                     bounce_dir((uint32_t)i, k, nrm, d);
                 }
-                trace_ray(*w, o, d, cam->world_origin, iters, tr);
+                trace_mode(*w, glsl, o, d, cam->world_origin, iters, tr);
                 fill_hit(tr, d, (uint32_t)i, h);
                 acc.add(tid, tr);
                 alive = tr.hit;
@@ -705,6 +870,7 @@ int ora_world_edit(ora_world* w, const vrt_edit* edits, uint32_t n) {
                     if (w->masks[s] == 0) w->data[s].reset();
                 }
     }
+    w->refresh_groups();
     return 0;
 }
 

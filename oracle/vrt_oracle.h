@@ -12,6 +12,9 @@
  * Edits follow VoxelMap::RegionDispatchSIMD + GC (src/VoxelRT/VoxelMap.h:222-263).
  * Parity is pinned against the reference's own RayCast compiled in place
  * (oracle/ref_pin/, x86 only) through the committed fixtures in tests/golden/.
+ * The GLSL mode (VRT_CAST_GLSL / VRT_VIEW_GLSL) restates the GPU renderer's rayCast
+ * (src/VoxelRT/Shaders/VoxelTraversal.glsl:100-204); its parity is unpinned, as the
+ * shader cannot run here.
  */
 #ifndef VRT_ORACLE_H_
 #define VRT_ORACLE_H_
@@ -51,13 +54,14 @@ int ora_cast(const ora_world* w, const vrt_ray* rays, uint64_t n, const vrt_cast
              vrt_hit* hits, int threads, ora_stats* stats);
 /* Camera rays of a view (the ray generation of vrt_camera). */
 int ora_camera_rays(const vrt_camera* cam, vrt_ray* rays);
-int ora_render_view(const ora_world* w, const vrt_camera* cam, uint32_t max_iters, vrt_hit* hits,
+/* mode: 0 = the reference CPU traversal, nonzero = the GLSL mode (VRT_VIEW_GLSL). */
+int ora_render_view(const ora_world* w, const vrt_camera* cam, uint32_t max_iters, uint32_t mode, vrt_hit* hits,
                     int threads, ora_stats* stats);
 /* Primary ray, then for every hit one shadow ray from hitPos + normal*0.01
  * (CpuRenderer.cpp:389) toward sun_dir.  shadow[i] for a primary miss is a miss
  * record with steps 0 and tag VRT_NO_RAY. */
 int ora_render_view_shadow(const ora_world* w, const vrt_camera* cam, const float sun_dir[3],
-                           uint32_t max_iters, vrt_hit* primary, vrt_hit* shadow, int threads,
+                           uint32_t max_iters, uint32_t mode, vrt_hit* primary, vrt_hit* shadow, int threads,
                            ora_stats* stats);
 /* Primary ray plus up to n_bounces diffuse bounces per pixel (CpuRenderer.cpp:342-393):
  * origin hitPos + normal*0.01, direction normalize(normal + s) with s uniform on the
@@ -66,7 +70,7 @@ int ora_render_view_shadow(const ora_world* w, const vrt_camera* cam, const floa
  * hits has (n_bounces+1)*width*height records, bounce-major; a path stops at its
  * first miss and later records are VRT_NO_RAY misses. */
 int ora_render_view_bounces(const ora_world* w, const vrt_camera* cam, uint32_t n_bounces,
-                            uint32_t max_iters, vrt_hit* hits, int threads, ora_stats* stats);
+                            uint32_t max_iters, uint32_t mode, vrt_hit* hits, int threads, ora_stats* stats);
 
 /* Picking ray cast (VoxelMap::RayCast, VoxelMap.cpp:125-170), double precision.
  * rays: 6 doubles each (origin, dir).  max_iters 0 = 1024. */

@@ -5,7 +5,7 @@
 // table and voxel codes, alignment, clipping, NaN handling) on every CPU test run,
 // without a GPU.
 //
-//   device_logic_test <world.bin> <rays.bin> <out.bin> <max_iters> <wox> <woy> <woz>
+//   device_logic_test <world.bin> <rays.bin> <out.bin> <max_iters> <wox> <woy> <woz> [glsl]
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -43,6 +43,11 @@ inline unsigned __float_as_uint(float f) {
     unsigned u;
     std::memcpy(&u, &f, 4);
     return u;
+}
+inline float __uint_as_float(unsigned u) {
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
 }
 inline int __popc(unsigned x) { return __builtin_popcount(x); }
 template <typename T>
@@ -85,15 +90,22 @@ int main(int argc, char** argv) {
     while (std::fread(&r, sizeof(r), 1, f) == 1) rays.push_back(r);
     std::fclose(f);
     const uint32_t max_iters = (uint32_t)std::atoi(argv[4]);
+    const bool glsl = argc > 8 && std::atoi(argv[8]) != 0;
     const int wo[3] = {std::atoi(argv[5]), std::atoi(argv[6]), std::atoi(argv[7])};
     std::vector<uint4> out(rays.size());
     for (size_t i = 0; i < rays.size(); i++) {
         TraceResult res;
         TraceCounters cnt{0, 0};
         const vrt_ray& q = rays[i];
-        trace_ray<false>(w, q.origin[0], q.origin[1], q.origin[2], q.dir[0], q.dir[1], q.dir[2], wo[0], wo[1], wo[2],
-                         max_iters, res, cnt);
-        out[i] = pack_hit(res, q.dir[0], q.dir[1], q.dir[2], q.tag);
+        if (glsl) {
+            trace_ray<false, true>(w, q.origin[0], q.origin[1], q.origin[2], q.dir[0], q.dir[1], q.dir[2], wo[0],
+                                   wo[1], wo[2], max_iters, res, cnt);
+            out[i] = pack_hit<true>(res, q.dir[0], q.dir[1], q.dir[2], q.tag);
+        } else {
+            trace_ray<false, false>(w, q.origin[0], q.origin[1], q.origin[2], q.dir[0], q.dir[1], q.dir[2], wo[0],
+                                    wo[1], wo[2], max_iters, res, cnt);
+            out[i] = pack_hit<false>(res, q.dir[0], q.dir[1], q.dir[2], q.tag);
+        }
     }
     f = std::fopen(argv[3], "wb");
     if (!f) return 9;

@@ -54,7 +54,18 @@ def device_layout(data: v.SectorData) -> bytes:
     up4 = lambda a: a.repeat(4, 0).repeat(4, 1).repeat(4, 2)
     up2 = lambda a: a.repeat(2, 0).repeat(2, 1).repeat(2, 2)
     level = np.where(~up4(sector_any), 31, np.where(~up2(group_any), 15, 7)).astype(np.uint32)
-    table = np.where(alloc, slot_of, np.uint32(0x80000000) | level).astype(np.uint32)
+    # GLSL mode (bits 8-15): where the sector is empty, the 4th level over groups of 4^3
+    # sectors: 127 when the whole group is empty, 63 when the aligned 2^3 block of
+    # sectors is, else 31; elsewhere the same mask as bits 0-7
+    py_, pz, px = (-sy) % 4, (-sz) % 4, (-sx) % 4
+    sa = np.pad(sector_any, ((0, py_), (0, pz), (0, px)))
+    gy, gz, gxx = sa.shape[0] // 4, sa.shape[1] // 4, sa.shape[2] // 4
+    g4 = sa.reshape(gy, 4, gz, 4, gxx, 4).any(axis=(1, 3, 5)).repeat(4, 0).repeat(4, 1).repeat(4, 2)
+    g2 = sa.reshape(gy * 2, 2, gz * 2, 2, gxx * 2, 2).any(axis=(1, 3, 5)).repeat(2, 0).repeat(2, 1).repeat(2, 2)
+    g4, g2 = g4[:sy, :sz, :sx], g2[:sy, :sz, :sx]
+    sector_level = np.where(~g4, 127, np.where(~g2, 63, 31)).astype(np.uint32)
+    glsl = np.where(~up4(sector_any), up4(sector_level), level).astype(np.uint32)
+    table = np.where(alloc, slot_of, np.uint32(0x80000000) | level | glsl << 8).astype(np.uint32)
     nb = data.n_bricks
     solid = data.bricks.reshape(nb, 8, 8, 8) != 0             # (n, y, z, x)
     cell_any = solid.reshape(nb, 2, 4, 2, 4, 2, 4).any(axis=(2, 4, 6))
@@ -67,11 +78,11 @@ def device_layout(data: v.SectorData) -> bytes:
     return head + table.tobytes() + words.tobytes() + data.bricks.tobytes()
 
 
-def run(exe, tmp_path, data, rays, max_iters=128, wo=(0, 0, 0)):
+def run(exe, tmp_path, data, rays, max_iters=128, wo=(0, 0, 0), glsl=False):
     (tmp_path / "w.bin").write_bytes(device_layout(data))
     np.ascontiguousarray(rays, v.RAY_DTYPE).tofile(tmp_path / "r.bin")
     subprocess.run([str(exe), str(tmp_path / "w.bin"), str(tmp_path / "r.bin"), str(tmp_path / "o.bin"),
-                    str(max_iters), *map(str, wo)], check=True)
+                    str(max_iters), *map(str, wo), "1" if glsl else "0"], check=True)
     return np.fromfile(tmp_path / "o.bin", v.HIT_DTYPE)
 
 
@@ -113,3 +124,27 @@ def test_mix_worlds_and_degenerate_rays(exe, tmp_path, seed):
         r["origin"] -= np.asarray(wo, np.float32)
         assert_hits_equal(run(exe, tmp_path, data, r, iters, wo), oracle_for(data).cast(r, world_origin=wo,
                                                                                           max_iters=iters))
+
+
+@pytest.mark.parametrize("seed", [5, 6])
+def test_glsl_mode_against_oracle(exe, tmp_path, seed):
+    """The GLSL-mode step (4th level from the brick table's bits 8-15, +5-ulp bias) on
+    sparse and mixed worlds, from camera-like frames and from the world frame."""
+    rng = np.random.default_rng(seed)
+    vol = np.zeros((128, 320, 288), np.uint8)
+    for _ in range(60):
+        y, z, x = rng.integers(0, (128, 320, 288))
+        vol[max(0, y - 5):y + 5, max(0, z - 5):z + 5, max(0, x - 5):x + 5] = rng.integers(1, 256)
+    for data in (dense_to_stream(vol), v.synth_mix(96, seed=seed)):
+        size = [s * 32 for s in data.sectors]
+        o = oracle_for(data)
+        eye = rng.uniform((0, 0, 0), size)
+        wo = tuple(int(c) for c in np.floor(eye))
+        d = rng.normal(size=(30_000, 3)).astype(np.float32)
+        d[rng.random(d.shape) < 0.02] = 0.0
+        rays = make_rays(np.tile((eye - np.floor(eye)).astype(np.float32), (30_000, 1)), d)
+        assert_hits_equal(run(exe, tmp_path, data, rays, 256, wo, glsl=True),
+                          o.cast(rays, world_origin=wo, max_iters=256, glsl=True))
+        world_rays = v.random_rays(size, seed=seed, n=20_000)
+        assert_hits_equal(run(exe, tmp_path, data, world_rays, 64, (0, 0, 0), glsl=True),
+                          o.cast(world_rays, max_iters=64, glsl=True))

@@ -1,0 +1,129 @@
+"""The GLSL traversal mode on the device against the oracle's restatement of the GPU
+renderer's rayCast (VoxelTraversal.glsl:100-204): casts, single-view paths, batches,
+edits that change the 4th-level group masks.  Parity unpinned: the shader itself
+cannot run here, so the oracle's restatement is the reference."""
+import numpy as np
+import pytest
+
+import voxelrt_gb300 as v
+from oracle.oracle import OracleWorld
+from tests.helpers import assert_hits_equal, both_worlds, cfg0_camera, cfg0_world, dense_to_stream, make_rays, \
+    oracle_view
+
+pytestmark = pytest.mark.gpu
+
+SUN = (0.3, 0.8, 0.5)
+
+
+def sparse_world(seed, shape=(128, 320, 288), blobs=60):
+    """(Y, Z, X) sector extents not multiples of 4, solid boxes far apart: long empty runs."""
+    rng = np.random.default_rng(seed)
+    vol = np.zeros(shape, np.uint8)
+    for _ in range(blobs):
+        y, z, x = rng.integers(0, shape)
+        vol[max(0, y - 5):y + 5, max(0, z - 5):z + 5, max(0, x - 5):x + 5] = rng.integers(1, 256)
+    return dense_to_stream(vol)
+
+
+def camera_frame_rays(rng, size, n, zero_frac=0.02):
+    eye = rng.uniform((0, 0, 0), size)
+    wo = tuple(int(c) for c in np.floor(eye))
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d[rng.random(d.shape) < zero_frac] = 0.0
+    return make_rays(np.tile((eye - np.floor(eye)).astype(np.float32), (n, 1)), d), wo
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_glsl_cast_matches_oracle(gpu, seed):
+    rng = np.random.default_rng(seed)
+    for data in (sparse_world(seed), v.synth_mix(96, seed=seed), cfg0_world()):
+        size = [s * 32 for s in data.sectors]
+        w, o = both_worlds(data)
+        for _ in range(3):
+            rays, wo = camera_frame_rays(rng, size, 40_000)
+            assert_hits_equal(w.cast(rays, world_origin=wo, glsl=True),
+                              o.cast(rays, world_origin=wo, glsl=True))
+        # world-frame rays, where the 5-ulp bias can stall a ray until the cap
+        rays = v.random_rays(size, seed=seed, n=30_000)
+        assert_hits_equal(w.cast(rays, max_iters=96, glsl=True), o.cast(rays, max_iters=96, glsl=True))
+        w.close()
+
+
+def test_glsl_mode_takes_fewer_steps_in_sparse_worlds(gpu):
+    data = sparse_world(7, shape=(256, 512, 512), blobs=30)
+    w, o = both_worlds(data)
+    rays, wo = camera_frame_rays(np.random.default_rng(7), [512, 256, 512], 50_000, zero_frac=0.0)
+    a = w.cast(rays, world_origin=wo)
+    b = w.cast(rays, world_origin=wo, glsl=True)
+    assert_hits_equal(b, o.cast(rays, world_origin=wo, glsl=True))
+    assert b["steps"].astype(np.int64).sum() < 0.8 * a["steps"].astype(np.int64).sum()
+    w.close()
+
+
+def test_glsl_render_paths_match_oracle(gpu):
+    data = cfg0_world()
+    w, o = both_worlds(data)
+    cam = cfg0_camera(160, 90)
+    for view in (v.make_view(cam, glsl=True), v.make_view(cam, shadow_dir=SUN, glsl=True),
+                 v.make_view(cam, n_bounces=3, max_iters=200, glsl=True)):
+        got = v.render_path(w, view)
+        want = oracle_view(o, view)
+        for k in range(want.shape[0]):
+            assert_hits_equal(got[k], want[k])
+    w.close()
+
+
+def test_glsl_batch_matches_oracle_and_per_view(gpu):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(11)
+    worlds, oracles, views = [], [], []
+    for i in range(5):
+        data = sparse_world(20 + i, shape=(96, 160, 128), blobs=20) if i % 2 else v.synth_mix(96, seed=30 + i)
+        w, o = both_worlds(data)
+        worlds.append(w)
+        oracles.append(o)
+        size = [s * 32 for s in data.sectors]
+        for k in range(3):
+            cam = v.look_at(rng.uniform(0, size), rng.uniform(0, size), 70.0, *[(64, 48), (33, 65), (80, 40)][k])
+            views.append(v.make_view(cam, world=i, glsl=True, **[{}, {"shadow_dir": SUN}, {"n_bounces": 2}][k]))
+    for cfg in (None, v.BatchConfig(8, 8, 1, 2, 0, 8, 4, 16), v.BatchConfig(32, 1, 0, 4, 0, 28, 1, 2)):
+        b = v.Batch(worlds, views, cfg)
+        hits = b.run()
+        for i, vw in enumerate(views):
+            got, want = b.view_hits(hits, i), oracle_view(oracles[vw.world], vw)
+            for k in range(want.shape[0]):
+                assert_hits_equal(got[k], want[k])
+        n = b.total_records
+        a = torch.empty(n * 16, dtype=torch.uint8, device="cuda")
+        c = torch.empty(n * 16, dtype=torch.uint8, device="cuda")
+        b.launch(a, graph=True)
+        b.launch_per_view(c)
+        torch.cuda.synchronize()
+        assert torch.equal(a, c)
+        b.close()
+    # one traversal mode per launch
+    with pytest.raises(v.VrtError):
+        v.Batch(worlds, views[:2] + [v.make_view(views[0].cam, world=0)])
+    for w in worlds:
+        w.close()
+
+
+def test_glsl_group_masks_follow_edits(gpu):
+    # carving whole sectors empty and filling empty ones changes the 4th-level masks
+    data = v.synth_mix(128, seed=9)
+    w, o = both_worlds(data)
+    rng = np.random.default_rng(9)
+    cam = v.look_at((64, 120, -20), (64, 40, 64), 80.0, 96, 64)
+    for step in range(3):
+        e = np.zeros(3, v.EDIT_DTYPE)
+        e["center"] = rng.integers(0, 128, (3, 3))
+        e["radius"] = [40, 25, 12]
+        e["material"] = [0, 7 + step, 0] if step != 1 else [5, 0, 9]
+        w.edit(e)
+        o.edit(e)
+        view = v.make_view(cam, glsl=True)
+        got = v.render_path(w, view)
+        assert_hits_equal(got[0], oracle_view(o, view)[0])
+        rays, wo = camera_frame_rays(rng, [128, 128, 128], 20_000)
+        assert_hits_equal(w.cast(rays, world_origin=wo, glsl=True), o.cast(rays, world_origin=wo, glsl=True))
+    w.close()

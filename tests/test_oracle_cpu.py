@@ -198,3 +198,82 @@ def test_edit_semantics_vs_dense_model(seed):
         for y in range(0, 64, 5):
             for z in range(0, 96, 3):
                 assert o.voxel(x, y, z) == vol[y, z, x]
+
+
+# ---- GLSL mode (VoxelTraversal.glsl rayCast); parity unpinned, so known answers and
+# properties against the default mode
+
+def _empty_world(sectors):
+    data = v.SectorData(sectors, np.zeros(0, np.int32), np.zeros(0, np.uint64), np.zeros((0, 512), np.uint8))
+    o = OracleWorld(data.sectors)
+    o.upload(data)
+    return o
+
+
+def test_glsl_mode_group_level_known_answer():
+    # empty 256^3 world = 2x2x2 groups of 4^3 sectors, all empty: iteration 0 leaves the
+    # start voxel (100 -> 101), getStepPos skips to the 128-voxel group cell's end (127),
+    # iteration 1 enters x = 128 and skips to 255, iteration 2 leaves the grid
+    o = _empty_world((8, 8, 8))
+    r = make_rays([[100.5, 100.5, 100.5]], [[1, 1e-4, 1e-4]])
+    h = o.cast(r, glsl=True)
+    assert h["steps"][0] == 2 and h["voxel"][0] == v.MISS_VOXEL
+    assert o.last_stats["step_calls"] == 2 and o.last_stats["occ_fetches"] == 0
+    # the default mode steps sector by sector: 101 -> 127 | 128 -> 159 | ... | 224 -> 255
+    h = o.cast(r)
+    assert h["steps"][0] == 5
+
+
+def test_glsl_mode_single_voxel_hit():
+    data = single_voxel_world((40, 20, 50), material=9, sectors=(8, 2, 8))
+    o = OracleWorld(data.sectors)
+    o.upload(data)
+    h = o.cast(make_rays([[40.5, 20.5, 200.25]], [[1e-4, 1e-4, -1]]), glsl=True)
+    assert h["voxel"][0] == 40 | 20 << 11 | 50 << 21 and h["material"][0] == 9
+    assert h["face"][0] == 5  # z axis, moving in -z
+    # t is the biased tmin of the hit step: the +z face at 51 is 149.25 away, plus 5 ulp
+    t = np.float32(149.25).view(np.uint32) + 5
+    assert h["t"][0].view(np.uint32) == t
+
+
+def test_glsl_mode_finds_the_same_first_voxel_in_sparse_worlds():
+    # the 4th level must never skip a non-empty sector: in a sparse world rays from empty
+    # space hit the same voxel as the default mode, except where the two biases (+5 ulp
+    # vs +0.001) enter a different voxel at an edge.  Rays start as camera rays do: in the
+    # frame of worldOrigin = floor(eye), origin = the fractional part (GBuffer.h:79); the
+    # 5-ulp bias of rayCast only moves the position off a cell boundary when positions
+    # scale with t like that, and rays in far-from-origin frames stall until the cap.
+    rng = np.random.default_rng(3)
+    vol = np.zeros((128, 256, 256), np.uint8)
+    for _ in range(150):
+        y, z, x = rng.integers(0, (128, 256, 256))
+        vol[max(0, y - 6):y + 6, max(0, z - 6):z + 6, max(0, x - 6):x + 6] = rng.integers(1, 256)
+    data = dense_to_stream(vol)
+    o = OracleWorld(data.sectors)
+    o.upload(data)
+    dense = data.dense()
+    same = hits = steps_a = steps_b = 0
+    for k in range(60):
+        eye = rng.uniform((0, 0, 0), (256, 128, 256))
+        if dense[int(eye[1]), int(eye[2]), int(eye[0])]:
+            continue
+        wo = np.floor(eye).astype(np.int32)
+        d = rng.normal(size=(500, 3)).astype(np.float32)
+        r = make_rays(np.tile((eye - wo).astype(np.float32), (500, 1)), d)
+        a, b = o.cast(r, world_origin=tuple(wo)), o.cast(r, world_origin=tuple(wo), glsl=True)
+        both = (a["voxel"] != v.MISS_VOXEL) & (b["voxel"] != v.MISS_VOXEL)
+        hits += both.sum()
+        same += (a["voxel"][both] == b["voxel"][both]).sum()
+        steps_a += a["steps"].astype(np.int64).sum()
+        steps_b += b["steps"].astype(np.int64).sum()
+    assert hits > 2000
+    assert same / hits > 0.99
+    # and it takes fewer iterations through the empty space
+    assert steps_b < steps_a
+
+
+def test_glsl_mode_iteration_cap_default_256():
+    o = _empty_world((64, 1, 64))
+    r = make_rays([[0.5, 16.5, 0.5]], [[1, 0, 1e-3]])  # zero y component: x86 min leaves NaN sides out
+    h = o.cast(r, glsl=True, max_iters=3)
+    assert h["steps"][0] <= 3

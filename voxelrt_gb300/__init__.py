@@ -17,11 +17,12 @@ import ctypes as C
 import numpy as np
 
 from . import capi
-from .capi import (EDIT_DTYPE, HIT_DTYPE, MISS_FACE, MISS_VOXEL, NO_RAY, RAY_DTYPE, VIEW_SHADOW, BatchConfig, Camera,
+from .capi import (CAST_GLSL, EDIT_DTYPE, HIT_DTYPE, MISS_FACE, MISS_VOXEL, NO_RAY, RAY_DTYPE, VIEW_GLSL, VIEW_SHADOW,
+                   BatchConfig, Camera,
                    CastParams, View, VrtError, check, lib, ptr)
 
 __all__ = ["Server", "PinnedHits", "view_records", "render_path", "cvox_read", "cvox_write", "World", "Camera", "View",
-           "make_view", "Batch", "BatchConfig", "VIEW_SHADOW", "look_at", "synth_terrain", "synth_mix", "random_rays", "SectorData", "VrtError",
+           "make_view", "Batch", "BatchConfig", "VIEW_SHADOW", "VIEW_GLSL", "CAST_GLSL", "look_at", "synth_terrain", "synth_mix", "random_rays", "SectorData", "VrtError",
            "RAY_DTYPE", "HIT_DTYPE", "EDIT_DTYPE", "MISS_VOXEL", "MISS_FACE", "NO_RAY", "unpack_voxel", "sector_index",
            "lib"]
 
@@ -219,15 +220,18 @@ class World:
         check(lib().vrt_world_read_sector(self._h, int(sector_idx), C.byref(mask), ptr(bricks), bricks.nbytes, None))
         return mask.value, bricks
 
-    def cast(self, rays: np.ndarray, world_origin=(0, 0, 0), max_iters: int = 0, stream=None) -> np.ndarray:
+    def cast(self, rays: np.ndarray, world_origin=(0, 0, 0), max_iters: int = 0, stream=None,
+             glsl: bool = False) -> np.ndarray:
+        """glsl: the GPU renderer's rayCast (VRT_CAST_GLSL) instead of the CPU traversal."""
         rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
         hits = np.zeros(len(rays), HIT_DTYPE)
-        p = CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), 0)
+        p = CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), CAST_GLSL if glsl else 0)
         check(lib().vrt_cast(self._h, ptr(rays), len(rays), C.byref(p), ptr(hits), _stream_ptr(stream)))
         return hits
 
-    def cast_device(self, rays, n: int, hits, world_origin=(0, 0, 0), max_iters: int = 0, stream=None) -> None:
-        p = CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), 0)
+    def cast_device(self, rays, n: int, hits, world_origin=(0, 0, 0), max_iters: int = 0, stream=None,
+                    glsl: bool = False) -> None:
+        p = CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), CAST_GLSL if glsl else 0)
         check(lib().vrt_cast_device(self._h, ptr(rays), int(n), C.byref(p), ptr(hits), _stream_ptr(stream)))
 
     def render_view(self, cam: Camera, max_iters: int = 0, stream=None) -> np.ndarray:
@@ -239,14 +243,16 @@ class World:
         check(lib().vrt_render_view_device(self._h, C.byref(cam), int(max_iters), ptr(hits), _stream_ptr(stream)))
 
 
-def make_view(cam: Camera, world: int = 0, max_iters: int = 0, n_bounces: int = 0, shadow_dir=None) -> View:
-    """A view: primary rays plus shadow rays toward shadow_dir, or n_bounces diffuse bounces."""
+def make_view(cam: Camera, world: int = 0, max_iters: int = 0, n_bounces: int = 0, shadow_dir=None,
+              glsl: bool = False) -> View:
+    """A view: primary rays plus shadow rays toward shadow_dir, or n_bounces diffuse bounces.
+    glsl: trace with the GPU renderer's rayCast (VRT_VIEW_GLSL) instead of the CPU traversal."""
     vw = View()
     vw.cam = cam
     vw.world = int(world)
     vw.max_iters = int(max_iters)
     vw.n_bounces = int(n_bounces)
-    vw.flags = VIEW_SHADOW if shadow_dir is not None else 0
+    vw.flags = (VIEW_SHADOW if shadow_dir is not None else 0) | (VIEW_GLSL if glsl else 0)
     if shadow_dir is not None:
         vw.sun_dir[:] = [float(c) for c in shadow_dir]
     return vw

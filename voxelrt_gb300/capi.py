@@ -71,6 +71,9 @@ class BatchStats(C.Structure):
 
 
 VIEW_SHADOW = 1
+VIEW_GLSL = 2        # the GPU renderer's rayCast (VoxelTraversal.glsl) instead of the CPU traversal
+CAST_GLSL = 1
+GLSL_MAX_ITERS = 256
 
 
 class ServerConfig(C.Structure):

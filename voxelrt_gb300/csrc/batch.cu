@@ -29,18 +29,18 @@ __device__ __forceinline__ uint32_t compact_even_bits(uint32_t k) {
     return k;
 }
 
-template <bool kCount>
+template <bool kCount, bool kGlsl>
 __device__ __forceinline__ bool run_ray(RayState& s, bool safe, const DevWorld& w, int32_t wox, int32_t woy,
                                         int32_t woz, uint32_t max_iters, uint32_t& steps, TraceCounters& cnt) {
     uint32_t st = kStepOut, i = 0;
     if (safe) {
         for (; i < max_iters; i++) {
-            st = ray_step<kCount, true>(s, w, wox, woy, woz, cnt);
+            st = ray_step<kCount, true, kGlsl>(s, w, wox, woy, woz, cnt);
             if (st != kStepContinue) break;
         }
     } else {
         for (; i < max_iters; i++) {
-            st = ray_step<kCount, false>(s, w, wox, woy, woz, cnt);
+            st = ray_step<kCount, false, kGlsl>(s, w, wox, woy, woz, cnt);
             if (st != kStepContinue) break;
         }
     }
@@ -49,6 +49,7 @@ __device__ __forceinline__ bool run_ray(RayState& s, bool safe, const DevWorld& 
 }
 
 // One thread per pixel, whole path (VoxelRender.comp:27-93 structure).
+template <bool kGlsl>
 __global__ void __launch_bounds__(64) view_path_kernel(DevWorld w, ViewDev v, uint4* __restrict__ out) {
     const uint32_t px = blockIdx.x * 8 + threadIdx.x;
     const uint32_t py = blockIdx.y * 8 + threadIdx.y;
@@ -60,25 +61,25 @@ __global__ void __launch_bounds__(64) view_path_kernel(DevWorld w, ViewDev v, ui
     float ox = v.cam.origin[0], oy = v.cam.origin[1], oz = v.cam.origin[2], dx, dy, dz;
     camera_ray(v.cam, px, py, dx, dy, dz);
     RayState s;
-    bool safe = ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
+    bool safe = ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
     uint32_t steps;
-    bool hit = run_ray<false>(s, safe, w, wox, woy, woz, v.max_iters, steps, cnt);
+    bool hit = run_ray<false, kGlsl>(s, safe, w, wox, woy, woz, v.max_iters, steps, cnt);
     uint4* o = out + v.out_base + pixel;
-    o[0] = pack_state(s, hit, steps, pixel);
+    o[0] = pack_state<kGlsl>(s, hit, steps, pixel);
     const uint32_t last = v.shadow ? 1u : v.n_bounces;
     for (uint32_t k = 1; k <= last; k++) {
         if (!hit) {
             o[k * plane] = no_ray_hit();
             continue;
         }
-        next_path_ray(s, v.shadow != 0, v.sun, pixel, k, ox, oy, oz, dx, dy, dz);
-        safe = ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
-        hit = run_ray<false>(s, safe, w, wox, woy, woz, v.max_iters, steps, cnt);
-        o[k * plane] = pack_state(s, hit, steps, pixel);
+        next_path_ray<kGlsl>(s, v.shadow != 0, v.sun, pixel, k, ox, oy, oz, dx, dy, dz);
+        safe = ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
+        hit = run_ray<false, kGlsl>(s, safe, w, wox, woy, woz, v.max_iters, steps, cnt);
+        o[k * plane] = pack_state<kGlsl>(s, hit, steps, pixel);
     }
 }
 
-template <bool kCount>
+template <bool kCount, bool kGlsl>
 __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt = (1u << lane) - 1u;
@@ -110,16 +111,16 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
             uint4* rec = p.out + __ldg(&v->out_base) + pixel;
             uint32_t kind = path & 0xFF;
             const uint32_t last_kind = (path >> 8) & 0xFF;
-            rec[(size_t)kind * plane] = pack_state(s, hit, iter, pixel);
+            rec[(size_t)kind * plane] = pack_state<kGlsl>(s, hit, iter, pixel);
             rays++;
             if (kCount && hit) hits++;
             if (hit && kind < last_kind) {
                 path++;
                 kind++;
                 float ox, oy, oz, dx, dy, dz;
-                next_path_ray(s, ((path >> 16) & 1u) != 0, v->sun, pixel, kind, ox, oy, oz, dx, dy, dz);
+                next_path_ray<kGlsl>(s, ((path >> 16) & 1u) != 0, v->sun, pixel, kind, ox, oy, oz, dx, dy, dz);
                 path &= ~kSafe;
-                if (ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz)) path |= kSafe;
+                if (ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz)) path |= kSafe;
                 iter = 0;
             } else {
                 for (uint32_t kk = kind + 1; kk <= last_kind; kk++) rec[(size_t)kk * plane] = no_ray_hit();
@@ -190,8 +191,8 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                         woz = __ldg(&v->cam.world_origin[2]);
                         float dx, dy, dz;
                         camera_ray(v->cam, px, py, dx, dy, dz);
-                        if (ray_init(s, w, __ldg(&v->cam.origin[0]), __ldg(&v->cam.origin[1]),
-                                     __ldg(&v->cam.origin[2]), dx, dy, dz, wox, woy, woz))
+                        if (ray_start<kGlsl>(s, w, __ldg(&v->cam.origin[0]), __ldg(&v->cam.origin[1]),
+                                             __ldg(&v->cam.origin[2]), dx, dy, dz, wox, woy, woz))
                             path |= kSafe;
                         active = true;
                     }
@@ -210,12 +211,12 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
             uint32_t k = 0, st = kStepContinue;
             if (all_safe) {
                 for (; k < kmax; k++) {
-                    st = ray_step<kCount, true>(s, w, wox, woy, woz, cnt);
+                    st = ray_step<kCount, true, kGlsl>(s, w, wox, woy, woz, cnt);
                     if (st != kStepContinue) break;
                 }
             } else {
                 for (; k < kmax; k++) {
-                    st = ray_step<kCount, false>(s, w, wox, woy, woz, cnt);
+                    st = ray_step<kCount, false, kGlsl>(s, w, wox, woy, woz, cnt);
                     if (st != kStepContinue) break;
                 }
             }
@@ -255,27 +256,42 @@ ViewDev make_view_dev(const vrt_view& v) {
     ViewDev d{};
     d.cam = v.cam;
     d.world = v.world;
-    d.max_iters = eff_iters(v.max_iters);
+    d.max_iters = eff_iters(v.max_iters, view_glsl(v));
     d.n_bounces = (v.flags & VRT_VIEW_SHADOW) ? 0 : v.n_bounces;
     d.shadow = (v.flags & VRT_VIEW_SHADOW) ? 1 : 0;
     for (int c = 0; c < 3; c++) d.sun[c] = v.sun_dir[c];
     return d;
 }
 
-vrt_status launch_view_path(vrt_world* w, const ViewDev& v, vrt_hit* hits, cudaStream_t stream) {
+vrt_status launch_view_path(vrt_world* w, const ViewDev& v, bool glsl, vrt_hit* hits, cudaStream_t stream) {
     dim3 block(8, 8), grid((v.cam.width + 7) / 8, (v.cam.height + 7) / 8);
-    view_path_kernel<<<grid, block, 0, stream>>>(w->dev(), v, reinterpret_cast<uint4*>(hits));
+    if (glsl)
+        view_path_kernel<true><<<grid, block, 0, stream>>>(w->dev(), v, reinterpret_cast<uint4*>(hits));
+    else
+        view_path_kernel<false><<<grid, block, 0, stream>>>(w->dev(), v, reinterpret_cast<uint4*>(hits));
     VRT_CUDA(cudaGetLastError());
     return VRT_OK;
 }
 
 }  // namespace
 
-uint32_t eff_iters(uint32_t m) { return m == 0 ? VRT_DEFAULT_MAX_ITERS : (m > 65535u ? 65535u : m); }
+uint32_t eff_iters(uint32_t m, bool glsl) {
+    if (m == 0) return glsl ? VRT_GLSL_MAX_ITERS : VRT_DEFAULT_MAX_ITERS;
+    return m > 65535u ? 65535u : m;
+}
+
+vrt_status check_same_mode(const vrt_view* views, uint32_t n) {
+    for (uint32_t i = 1; i < n; i++)
+        if (view_glsl(views[i]) != view_glsl(views[0])) {
+            set_error("the views of one launch must share one traversal mode (VRT_VIEW_GLSL)");
+            return VRT_ERR_INVALID_ARG;
+        }
+    return VRT_OK;
+}
 
 vrt_status check_view(const vrt_view* v) {
     if (!v || v->cam.width == 0 || v->cam.height == 0 || v->cam.width > 16384 || v->cam.height > 16384 ||
-        v->n_bounces > VRT_MAX_BOUNCES || (v->flags & ~VRT_VIEW_SHADOW) ||
+        v->n_bounces > VRT_MAX_BOUNCES || (v->flags & ~(VRT_VIEW_SHADOW | VRT_VIEW_GLSL)) ||
         ((v->flags & VRT_VIEW_SHADOW) && v->n_bounces) || !world_origin_ok(v->cam.world_origin)) {
         set_error("bad view: camera 1..16384 px, |world origin| <= 2^30, n_bounces <= 15, shadow and bounces "
                   "exclusive");
@@ -319,6 +335,8 @@ vrt_status plan_views(const vrt_view* views, uint32_t n, uint32_t n_worlds, cons
             return VRT_ERR_INVALID_ARG;
         }
     }
+    if ((st = check_same_mode(views, n)) != VRT_OK) return st;
+    plan.glsl = n > 0 && view_glsl(views[0]);
     plan.cfg = cfg;
     plan.tile_w_log2 = log2u(cfg.tile_w);
     plan.tile_size_log2 = log2u(cfg.tile_w * cfg.tile_h);
@@ -355,9 +373,9 @@ vrt_status persistent_grid(int device, const vrt_batch_config& cfg, bool count, 
     threads = (int)cfg.warps_per_block * 32;
     VRT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     if (count)
-        VRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<true>, threads, 0));
+        VRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<true, false>, threads, 0));
     else
-        VRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<false>, threads, 0));
+        VRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<false, false>, threads, 0));
     occ = std::max(occ, 1);
     const int per_sm = (!count && cfg.blocks_per_sm) ? std::min<int>((int)cfg.blocks_per_sm, occ) : occ;
     blocks = sms * per_sm;
@@ -382,16 +400,21 @@ BatchParams make_params(const LaunchPlan& plan, const DevWorld* worlds, const Vi
     p.chunk_rays = plan.cfg.chunk_tiles << plan.tile_size_log2;
     p.refill = plan.cfg.refill_threshold;
     p.inner = plan.cfg.inner_iters;
+    p.glsl = plan.glsl ? 1u : 0u;
     return p;
 }
 
 vrt_status launch_persistent(const BatchParams& p, int blocks, int threads, bool count, cudaStream_t stream,
                              bool reset_counters) {
     VRT_CUDA(cudaMemsetAsync(p.queue, 0, reset_counters ? 64 : 4, stream));
-    if (count)
-        persistent_kernel<true><<<blocks, threads, 0, stream>>>(p);
+    if (count && p.glsl)
+        persistent_kernel<true, true><<<blocks, threads, 0, stream>>>(p);
+    else if (count)
+        persistent_kernel<true, false><<<blocks, threads, 0, stream>>>(p);
+    else if (p.glsl)
+        persistent_kernel<false, true><<<blocks, threads, 0, stream>>>(p);
     else
-        persistent_kernel<false><<<blocks, threads, 0, stream>>>(p);
+        persistent_kernel<false, false><<<blocks, threads, 0, stream>>>(p);
     VRT_CUDA(cudaGetLastError());
     return VRT_OK;
 }
@@ -458,7 +481,7 @@ vrt_status vrt_render_path_device(vrt_world* w, const vrt_view* view, vrt_hit* h
     }
     ViewDev d = make_view_dev(*view);
     d.out_base = 0;
-    return launch_view_path(w, d, hits, (cudaStream_t)stream);
+    return launch_view_path(w, d, view_glsl(*view), hits, (cudaStream_t)stream);
 }
 
 vrt_status vrt_render_path(vrt_world* w, const vrt_view* view, vrt_hit* hits, void* stream_) {
@@ -473,7 +496,7 @@ vrt_status vrt_render_path(vrt_world* w, const vrt_view* view, vrt_hit* hits, vo
     const size_t hb = view_record_count(*view) * sizeof(vrt_hit);
     VRT_CUDA(w->d_io.reserve(hb));
     ViewDev d = make_view_dev(*view);
-    if ((st = launch_view_path(w, d, (vrt_hit*)w->d_io.ptr, stream)) != VRT_OK) return st;
+    if ((st = launch_view_path(w, d, view_glsl(*view), (vrt_hit*)w->d_io.ptr, stream)) != VRT_OK) return st;
     VRT_CUDA(cudaMemcpyAsync(hits, w->d_io.ptr, hb, cudaMemcpyDeviceToHost, stream));
     VRT_CUDA(cudaStreamSynchronize(stream));
     return VRT_OK;
@@ -629,7 +652,8 @@ vrt_status vrt_batch_launch_per_view(vrt_batch* b, vrt_hit* hits, void* stream_)
     VRT_CUDA(cudaSetDevice(b->device));
     cudaStream_t stream = (cudaStream_t)stream_;
     for (size_t i = 0; i < b->plan.views.size(); i++) {
-        vrt_status st = launch_view_path(b->worlds[b->plan.views[i].world], b->plan.views[i], hits, stream);
+        vrt_status st =
+            launch_view_path(b->worlds[b->plan.views[i].world], b->plan.views[i], b->plan.glsl, hits, stream);
         if (st != VRT_OK) return st;
     }
     b->last_stream = stream;

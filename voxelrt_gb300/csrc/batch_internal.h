@@ -45,6 +45,7 @@ struct BatchParams {
     uint32_t chunk_rays;
     uint32_t refill;
     uint32_t inner;
+    uint32_t glsl;  // traversal mode of every view (VRT_VIEW_GLSL)
 };
 
 // Views laid out behind one tile queue.
@@ -55,9 +56,14 @@ struct LaunchPlan {
     std::vector<uint32_t> chunk_base;  // n_views + 1
     uint64_t records = 0;
     uint32_t chunks = 0;
+    bool glsl = false;  // every view traces in the GLSL mode
 };
 
-uint32_t eff_iters(uint32_t max_iters);
+// Iteration cap of a view or cast: 0 = the mode's default, at most 65535.
+uint32_t eff_iters(uint32_t max_iters, bool glsl = false);
+inline bool view_glsl(const vrt_view& v) { return (v.flags & VRT_VIEW_GLSL) != 0; }
+// All views of one launch share a traversal mode (VRT_ERR_INVALID_ARG otherwise).
+vrt_status check_same_mode(const vrt_view* views, uint32_t n);
 uint64_t view_record_count(const vrt_view& v);
 vrt_status check_view(const vrt_view* v);
 // Fill defaults and validate a batch config.

@@ -89,6 +89,8 @@ extern "C" vrt_status vrt_render_views_static(vrt_world* const* worlds, uint32_t
             return VRT_ERR_INVALID_ARG;
         }
     }
+    if ((st = check_same_mode(views, n_views)) != VRT_OK) return st;
+    const bool glsl = n_views > 0 && view_glsl(views[0]);
     std::lock_guard<std::mutex> lock(g_state.mu);
     VRT_CUDA(cudaSetDevice(device));
     // first call on this device: look up the device address of the scratch array
@@ -107,7 +109,7 @@ extern "C" vrt_status vrt_render_views_static(vrt_world* const* worlds, uint32_t
         d = ViewDev{};
         d.cam = v.cam;
         d.world = v.world;
-        d.max_iters = eff_iters(v.max_iters);
+        d.max_iters = eff_iters(v.max_iters, glsl);
         d.n_bounces = (v.flags & VRT_VIEW_SHADOW) ? 0 : v.n_bounces;
         d.shadow = (v.flags & VRT_VIEW_SHADOW) ? 1 : 0;
         for (int c = 0; c < 3; c++) d.sun[c] = v.sun_dir[c];
@@ -152,6 +154,7 @@ extern "C" vrt_status vrt_render_views_static(vrt_world* const* worlds, uint32_t
     p.chunk_rays = cfg.chunk_tiles << ts_log2;
     p.refill = cfg.refill_threshold;
     p.inner = cfg.inner_iters;
+    p.glsl = glsl ? 1u : 0u;
     int blocks = 0, threads = 0;
     if ((st = persistent_grid(device, cfg, false, blocks, threads)) != VRT_OK) return st;
     // launch_persistent zeroes the queue counter and the launch counters first

@@ -248,6 +248,7 @@ void worker_main(vrt_server* sv) {
                 std::vector<Request*> rs;
                 while (!sv->queue.empty() && sv->queue.front()->kind == 0 && rs.size() < sv->cfg.max_batch_requests) {
                     Request* r = sv->queue.front();
+                    if (!rs.empty() && view_glsl(r->view) != view_glsl(rs[0]->view)) break;  // one mode per launch
                     const uint32_t base = sv->pages.realloc(0, 0, r->pages);
                     if (base == 0) break;  // budget full: wait for launches to retire
                     r->page_base = base;

@@ -15,8 +15,8 @@
 namespace vrt {
 namespace {
 
-uint32_t eff_iters(uint32_t max_iters) {
-    if (max_iters == 0) return VRT_DEFAULT_MAX_ITERS;
+uint32_t eff_iters(uint32_t max_iters, bool glsl = false) {
+    if (max_iters == 0) return glsl ? VRT_GLSL_MAX_ITERS : VRT_DEFAULT_MAX_ITERS;
     return max_iters > 65535u ? 65535u : max_iters;
 }
 
@@ -35,6 +35,7 @@ __global__ void __launch_bounds__(64) render_view_kernel(DevWorld w, vrt_camera 
     out[pix] = pack_hit(r, dx, dy, dz, pix);
 }
 
+template <bool kGlsl>
 __global__ void __launch_bounds__(256) cast_kernel(DevWorld w, const float4* __restrict__ rays, uint32_t n,
                                                   int32_t wox, int32_t woy, int32_t woz, uint32_t max_iters,
                                                   uint4* __restrict__ out) {
@@ -43,8 +44,8 @@ __global__ void __launch_bounds__(256) cast_kernel(DevWorld w, const float4* __r
     const float4 a = rays[2 * (size_t)i], b = rays[2 * (size_t)i + 1];
     TraceResult r;
     TraceCounters cnt;
-    trace_ray<false>(w, a.x, a.y, a.z, a.w, b.x, b.y, wox, woy, woz, max_iters, r, cnt);
-    out[i] = pack_hit(r, a.w, b.x, b.y, __float_as_uint(b.z));
+    trace_ray<false, kGlsl>(w, a.x, a.y, a.z, a.w, b.x, b.y, wox, woy, woz, max_iters, r, cnt);
+    out[i] = pack_hit<kGlsl>(r, a.w, b.x, b.y, __float_as_uint(b.z));
 }
 
 vrt_status check_camera(const vrt_camera* cam) {
@@ -69,16 +70,18 @@ vrt_status launch_render(vrt_world* w, const vrt_camera* cam, uint32_t max_iters
 vrt_status launch_cast(vrt_world* w, const vrt_ray* rays, uint32_t n, const vrt_cast_params* p, vrt_hit* hits,
                        cudaStream_t stream) {
     if (n == 0) return VRT_OK;
-    cast_kernel<<<(n + 255) / 256, 256, 0, stream>>>(w->dev(), reinterpret_cast<const float4*>(rays), n,
-                                                     p->world_origin[0], p->world_origin[1], p->world_origin[2],
-                                                     eff_iters(p->max_iters), reinterpret_cast<uint4*>(hits));
+    const bool glsl = (p->flags & VRT_CAST_GLSL) != 0;
+    auto kernel = glsl ? cast_kernel<true> : cast_kernel<false>;
+    kernel<<<(n + 255) / 256, 256, 0, stream>>>(w->dev(), reinterpret_cast<const float4*>(rays), n,
+                                                p->world_origin[0], p->world_origin[1], p->world_origin[2],
+                                                eff_iters(p->max_iters, glsl), reinterpret_cast<uint4*>(hits));
     VRT_CUDA(cudaGetLastError());
     return VRT_OK;
 }
 
 vrt_status check_params(const vrt_cast_params* p) {
-    if (!p || p->flags != 0 || !world_origin_ok(p->world_origin)) {
-        set_error("cast params missing, flags not 0 or |world origin| > 2^30");
+    if (!p || (p->flags & ~VRT_CAST_GLSL) != 0 || !world_origin_ok(p->world_origin)) {
+        set_error("cast params missing, flags other than VRT_CAST_GLSL, or |world origin| > 2^30");
         return VRT_ERR_INVALID_ARG;
     }
     return VRT_OK;

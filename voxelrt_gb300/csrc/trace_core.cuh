@@ -28,6 +28,7 @@ __device__ __forceinline__ int32_t wsub(int32_t a, int32_t b) { return (int32_t)
 struct TraceResult {
     float cx, cy, cz;  // final position (HitResult.Pos)
     float sx, sy, sz;  // final side distances
+    float tb;          // GLSL mode: biased tmin of the last step (hit.dist)
     int32_t vx, vy, vz;
     uint32_t steps;
     uint32_t material;
@@ -60,6 +61,7 @@ struct RayState {
     float tsx, tsy, tsz;  // tStart
     float cx, cy, cz;     // currPos
     float sx, sy, sz;     // sideDist
+    float tb;             // GLSL mode: biased tmin of the last step
     int32_t vx, vy, vz;   // voxel of the last step (hit voxel on a hit)
     int32_t gx, gy, gz;   // -1 where dir < 0, else 0 (cell alignment side)
     uint32_t material;
@@ -123,15 +125,47 @@ __device__ __forceinline__ bool ray_init(RayState& s, const DevWorld& w, float o
            fabsf(s.ix) < kSafeInvDir && fabsf(s.iy) < kSafeInvDir && fabsf(s.iz) < kSafeInvDir;
 }
 
+// GLSL mode (VoxelTraversal.glsl rayCast): the start voxel worldOrigin + floor(start),
+// from which iteration 0 takes its side distances (:164-167).
+template <bool kGlsl>
+__device__ __forceinline__ bool ray_start(RayState& s, const DevWorld& w, float ox, float oy, float oz, float dx,
+                                          float dy, float dz, int32_t wox, int32_t woy, int32_t woz) {
+    const bool safe = ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
+    if (kGlsl) {
+        s.vx = wadd(wox, floor2i(s.cx));
+        s.vy = wadd(woy, floor2i(s.cy));
+        s.vz = wadd(woz, floor2i(s.cz));
+        s.tb = 0.0f;
+    }
+    return safe;
+}
+
 enum : uint32_t { kStepContinue = 0, kStepHit = 1, kStepOut = 2 };
 
 // One iteration of RayCast (CpuRenderer.cpp:186-201) with GetStepPos (:135-171).
 // kSafe: the ray passed the bounds of ray_init, so no NaN can occur; the NaN test
 // is skipped and min uses fminf, which equals the minps rule on non-NaN operands up
 // to the sign of a zero result, which the +0.001 bias removes.
-template <bool kCount, bool kSafe = false>
+// kGlsl: one iteration of rayCast (VoxelTraversal.glsl:170-199) instead: side
+// distances of the current voxel, tmin + 5 ulp (kept as the hit distance, so min
+// keeps the minps rule), position, bounds, then getStepPos (:100-131) whose empty
+// sectors take the 4th-level mask from the brick table.
+template <bool kCount, bool kSafe = false, bool kGlsl = false>
 __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int32_t wox, int32_t woy, int32_t woz,
                                              TraceCounters& cnt) {
+    if (kGlsl) {
+        s.sx = __fadd_rn(s.tsx, __fmul_rn(__int2float_rn(wsub(s.vx, wox)), s.ix));
+        s.sy = __fadd_rn(s.tsy, __fmul_rn(__int2float_rn(wsub(s.vy, woy)), s.iy));
+        s.sz = __fadd_rn(s.tsz, __fmul_rn(__int2float_rn(wsub(s.vz, woz)), s.iz));
+        // +5 ulp as an integer add on the bits; a NaN tmin stays NaN (its bit pattern
+        // differs between platforms: the GPU's 0x7FFFFFFF would wrap to a denormal)
+        const float m = min_x86(min_x86(s.sx, s.sy), s.sz);
+        const float t = (!kSafe && m != m) ? m : __uint_as_float(__float_as_uint(m) + 5u);
+        s.tb = t;
+        s.cx = __fadd_rn(s.ox, __fmul_rn(t, s.dx));
+        s.cy = __fadd_rn(s.oy, __fmul_rn(t, s.dy));
+        s.cz = __fadd_rn(s.oz, __fmul_rn(t, s.dz));
+    }
     // floor2i: a NaN coordinate converts to INT32_MIN on x86 and leaves the grid;
     // cvt.rmi saturates infinities and out-of-range values, which leave the grid
     // too (|world origin| <= 2^30 is enforced at the API), so only NaN needs a test
@@ -174,7 +208,7 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
         }
         m = (int32_t)code;
     } else {
-        m = (int32_t)(e & 31u);
+        m = kGlsl ? (int32_t)((e >> 8) & 127u) : (int32_t)(e & 31u);
     }
     // dir < 0 ? pos & ~m : pos | m, as (pos | m) ^ (g & m) with g = -1 for dir < 0
     vx = (vx | m) ^ (s.gx & m);
@@ -183,6 +217,7 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
     s.vx = vx;
     s.vy = vy;
     s.vz = vz;
+    if (kGlsl) return kStepContinue;
     s.sx = __fadd_rn(s.tsx, __fmul_rn(__int2float_rn(wsub(vx, wox)), s.ix));
     s.sy = __fadd_rn(s.tsy, __fmul_rn(__int2float_rn(wsub(vy, woy)), s.iy));
     s.sz = __fadd_rn(s.tsz, __fmul_rn(__int2float_rn(wsub(vz, woz)), s.iz));
@@ -194,22 +229,22 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
     return kStepContinue;
 }
 
-// Whole RayCast for one ray.
-template <bool kCount>
+// Whole RayCast (or rayCast, kGlsl) for one ray.
+template <bool kCount, bool kGlsl = false>
 __device__ __forceinline__ void trace_ray(const DevWorld& w, float ox, float oy, float oz, float dx, float dy,
                                           float dz, int32_t wox, int32_t woy, int32_t woz, uint32_t max_iters,
                                           TraceResult& r, TraceCounters& cnt) {
     RayState s;
-    const bool safe = ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
+    const bool safe = ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
     uint32_t st = kStepOut, i = 0;
     if (safe) {
         for (; i < max_iters; i++) {
-            st = ray_step<kCount, true>(s, w, wox, woy, woz, cnt);
+            st = ray_step<kCount, true, kGlsl>(s, w, wox, woy, woz, cnt);
             if (st != kStepContinue) break;
         }
     } else {
         for (; i < max_iters; i++) {
-            st = ray_step<kCount, false>(s, w, wox, woy, woz, cnt);
+            st = ray_step<kCount, false, kGlsl>(s, w, wox, woy, woz, cnt);
             if (st != kStepContinue) break;
         }
     }
@@ -219,6 +254,7 @@ __device__ __forceinline__ void trace_ray(const DevWorld& w, float ox, float oy,
     r.sx = s.sx;
     r.sy = s.sy;
     r.sz = s.sz;
+    r.tb = s.tb;
     r.vx = s.vx;
     r.vy = s.vy;
     r.vz = s.vz;
@@ -227,17 +263,30 @@ __device__ __forceinline__ void trace_ray(const DevWorld& w, float ox, float oy,
     r.hit = st == kStepHit && i < max_iters;
 }
 
-// The 16-byte vrt_hit record as one vector store.
+// The 16-byte vrt_hit record as one vector store.  kGlsl: t is the biased tmin and
+// the face the first axis with tmin >= side (hit.normal's sideMask, VoxelTraversal.glsl:190).
+template <bool kGlsl = false>
 __device__ __forceinline__ uint4 pack_hit(const TraceResult& r, float dx, float dy, float dz, uint32_t tag) {
     if (!r.hit) return make_uint4(VRT_MISS_VOXEL, VRT_MISS_FACE | (r.steps << 16), 0x7F800000u, tag);
-    const float t = min_x86(min_x86(r.sx, r.sy), r.sz);
+    float t;
     uint32_t face;
-    if (r.sx == t)
-        face = dx < 0.0f ? 1u : 0u;
-    else if (r.sy == t)
-        face = dy < 0.0f ? 3u : 2u;
-    else
-        face = dz < 0.0f ? 5u : 4u;
+    if (kGlsl) {
+        t = r.tb;
+        if (t >= r.sx)
+            face = dx < 0.0f ? 1u : 0u;
+        else if (t >= r.sy)
+            face = dy < 0.0f ? 3u : 2u;
+        else
+            face = dz < 0.0f ? 5u : 4u;
+    } else {
+        t = min_x86(min_x86(r.sx, r.sy), r.sz);
+        if (r.sx == t)
+            face = dx < 0.0f ? 1u : 0u;
+        else if (r.sy == t)
+            face = dy < 0.0f ? 3u : 2u;
+        else
+            face = dz < 0.0f ? 5u : 4u;
+    }
     const uint32_t voxel = (uint32_t)r.vx | (uint32_t)r.vy << 11 | (uint32_t)r.vz << 21;
     return make_uint4(voxel, face | r.material << 8 | r.steps << 16, __float_as_uint(t), tag);
 }
@@ -247,13 +296,22 @@ __device__ __forceinline__ uint4 no_ray_hit() {
 }
 
 // HitResult.Normal (CpuRenderer.cpp:213-217) and origin = Pos + Normal*0.01 (:389).
+// kGlsl: hit.normal = mix(0, -sign(dir), tmin >= sideDist) (VoxelTraversal.glsl:190-192),
+// every axis within the bias, sign(+-0) = 0.
+template <bool kGlsl = false>
 __device__ __forceinline__ void secondary_origin(const TraceResult& r, float dx, float dy, float dz, float& ox,
                                                  float& oy, float& oz, float& nx, float& ny, float& nz) {
-    const float t = min_x86(min_x86(r.sx, r.sy), r.sz);
-    const bool mx = r.sx == t, my = r.sy == t, mz = !mx && !my;
-    nx = mx ? (signbit(dx) ? 1.0f : -1.0f) : 0.0f;
-    ny = my ? (signbit(dy) ? 1.0f : -1.0f) : 0.0f;
-    nz = mz ? (signbit(dz) ? 1.0f : -1.0f) : 0.0f;
+    if (kGlsl) {
+        nx = r.tb >= r.sx ? (dx > 0.0f ? -1.0f : (dx < 0.0f ? 1.0f : 0.0f)) : 0.0f;
+        ny = r.tb >= r.sy ? (dy > 0.0f ? -1.0f : (dy < 0.0f ? 1.0f : 0.0f)) : 0.0f;
+        nz = r.tb >= r.sz ? (dz > 0.0f ? -1.0f : (dz < 0.0f ? 1.0f : 0.0f)) : 0.0f;
+    } else {
+        const float t = min_x86(min_x86(r.sx, r.sy), r.sz);
+        const bool mx = r.sx == t, my = r.sy == t, mz = !mx && !my;
+        nx = mx ? (signbit(dx) ? 1.0f : -1.0f) : 0.0f;
+        ny = my ? (signbit(dy) ? 1.0f : -1.0f) : 0.0f;
+        nz = mz ? (signbit(dz) ? 1.0f : -1.0f) : 0.0f;
+    }
     ox = __fadd_rn(r.cx, __fmul_rn(nx, 0.01f));
     oy = __fadd_rn(r.cy, __fmul_rn(ny, 0.01f));
     oz = __fadd_rn(r.cz, __fmul_rn(nz, 0.01f));
@@ -315,22 +373,25 @@ __device__ __forceinline__ void bounce_dir(uint32_t pixel, uint32_t bounce, floa
 }
 
 // Hit record from a finished RayState (steps = iteration index at exit).
+template <bool kGlsl = false>
 __device__ __forceinline__ uint4 pack_state(const RayState& s, bool hit, uint32_t steps, uint32_t tag) {
     TraceResult r;
     r.sx = s.sx;
     r.sy = s.sy;
     r.sz = s.sz;
+    r.tb = s.tb;
     r.vx = s.vx;
     r.vy = s.vy;
     r.vz = s.vz;
     r.steps = steps;
     r.material = s.material;
     r.hit = hit;
-    return pack_hit(r, s.dx, s.dy, s.dz, tag);
+    return pack_hit<kGlsl>(r, s.dx, s.dy, s.dz, tag);
 }
 
 // Origin and direction of the next ray of a path after a hit: the shadow ray
 // (kind 1 with shadows) or bounce `bounce` (1-based).
+template <bool kGlsl = false>
 __device__ __forceinline__ void next_path_ray(const RayState& s, bool shadow, const float* sun, uint32_t pixel,
                                               uint32_t bounce, float& ox, float& oy, float& oz, float& dx, float& dy,
                                               float& dz) {
@@ -341,8 +402,9 @@ __device__ __forceinline__ void next_path_ray(const RayState& s, bool shadow, co
     r.sx = s.sx;
     r.sy = s.sy;
     r.sz = s.sz;
+    r.tb = s.tb;
     float nx, ny, nz;
-    secondary_origin(r, s.dx, s.dy, s.dz, ox, oy, oz, nx, ny, nz);
+    secondary_origin<kGlsl>(r, s.dx, s.dy, s.dz, ox, oy, oz, nx, ny, nz);
     if (shadow) {
         dx = sun[0];
         dy = sun[1];

@@ -9,7 +9,11 @@
 //            world, index bx + bz*BX + by*BX*BZ (BX = 4*SX, BZ = 4*SZ): the brick's
 //            slot when its bit is set in the sector mask, else kBrickEmpty | the
 //            alignment mask (1 << level) - 1 of the level GetStepPos reaches there,
-//            level = 3 + skip_levels of the sector mask (CpuRenderer.cpp:139-167);
+//            level = 3 + skip_levels of the sector mask (CpuRenderer.cpp:139-167),
+//            in bits 0-7, and in bits 8-15 the mask of the GLSL mode's getStepPos
+//            (VoxelTraversal.glsl:100-131): the same where the sector holds a brick,
+//            else (32 << skip_levels of the sector-group mask) - 1, cells of 32, 64
+//            or 128 voxels;
 //   codes    2-bit voxel codes, 32 u32 words (128 B) per brick slot; voxel
 //            v = x | z<<3 | y<<6 sits in word v>>4 at bit 2*(v&15): kCodeSolid, or
 //            for an empty voxel the alignment mask (1 << level) - 1 (0, 1 or 3) of

@@ -104,9 +104,30 @@ __global__ void __launch_bounds__(kOpsWarps * 32)
     }
 }
 
+// Sector-group masks of the GLSL mode's 4th level (VoxelTraversal.glsl:114-118): per
+// group of 4^3 sectors, bit x | z<<2 | y<<4 set when that sector holds a brick
+// (GpuRenderer.cpp:139-149); groups indexed x + z*GX + y*GX*GZ, one thread each.
+__global__ void group_masks_kernel(const SectorRec* __restrict__ sectors, uint32_t sx, uint32_t sy, uint32_t sz,
+                                   unsigned long long* __restrict__ groups) {
+    const uint32_t gx = (sx + 3) / 4, gy = (sy + 3) / 4, gz = (sz + 3) / 4;
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= gx * gy * gz) return;
+    const uint32_t x0 = (g % gx) * 4, z0 = ((g / gx) % gz) * 4, y0 = (g / (gx * gz)) * 4;
+    unsigned long long m = 0;
+    for (uint32_t b = 0; b < 64; b++) {
+        const uint32_t x = x0 + (b & 3), z = z0 + ((b >> 2) & 3), y = y0 + (b >> 4);
+        if (x < sx && y < sy && z < sz) {
+            const SectorRec r = sectors[x + z * sx + y * sx * sz];
+            if ((r.mask_lo | r.mask_hi) != 0) m |= 1ull << b;
+        }
+    }
+    groups[g] = m;
+}
+
 // Brick-table entries of sectors [s_lo, s_hi), one thread per brick position.
-__global__ void brick_table_kernel(const SectorRec* __restrict__ sectors, uint32_t s_lo, uint32_t s_hi, uint32_t sx,
-                                   uint32_t sz, uint32_t* __restrict__ bricks) {
+__global__ void brick_table_kernel(const SectorRec* __restrict__ sectors, const unsigned long long* __restrict__ groups,
+                                   uint32_t s_lo, uint32_t s_hi, uint32_t sx, uint32_t sz,
+                                   uint32_t* __restrict__ bricks) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (s_hi - s_lo) * 64u) return;
     const uint32_t s = s_lo + (i >> 6), b = i & 63;
@@ -119,7 +140,15 @@ __global__ void brick_table_kernel(const SectorRec* __restrict__ sectors, uint32
         const uint32_t below = (1u << (b & 31)) - 1u;
         e = rec.base + (b < 32 ? __popc(lo & below) : __popc(lo) + __popc(hi & below));
     } else {
-        e = kBrickEmpty | ((8u << skip_levels(lo, hi, b)) - 1u);
+        const uint32_t cpu_m = (8u << skip_levels(lo, hi, b)) - 1u;
+        uint32_t glsl_m = cpu_m;
+        if ((lo | hi) == 0) {
+            const uint32_t gx = (sx + 3) / 4, gz = (sz + 3) / 4;
+            const unsigned long long g = groups[(x >> 2) + (z >> 2) * gx + (y >> 2) * gx * gz];
+            const uint32_t si = (x & 3) | (z & 3) << 2 | (y & 3) << 4;
+            glsl_m = (32u << skip_levels((uint32_t)g, (uint32_t)(g >> 32), si)) - 1u;
+        }
+        e = kBrickEmpty | cpu_m | glsl_m << 8;
     }
     bricks[bx + bz * (sx * 4) + by * (sx * 4) * (sz * 4)] = e;
 }
@@ -209,10 +238,15 @@ vrt_status plan_sector(vrt_world* w, SyncBatch& b, uint32_t s, uint64_t am, uint
     return VRT_OK;
 }
 
-// Re-derive the brick-table entries of sectors [lo, hi) from the device sector table.
-cudaError_t rebuild_brick_table(vrt_world* w, uint32_t lo, uint32_t hi, cudaStream_t stream) {
-    const uint32_t n = (hi - lo) * 64;
-    brick_table_kernel<<<(n + 255) / 256, 256, 0, stream>>>(w->d_sectors, lo, hi, w->sx, w->sz, w->d_bricks);
+// Re-derive the sector-group masks and the whole brick table from the device sector
+// table (a sector's emptiness changes the GLSL-mode entries of its whole group).
+cudaError_t rebuild_brick_table(vrt_world* w, cudaStream_t stream) {
+    const uint32_t ng = w->num_groups();
+    group_masks_kernel<<<(ng + 127) / 128, 128, 0, stream>>>(w->d_sectors, w->sx, w->sy, w->sz,
+                                                           (unsigned long long*)w->d_groups);
+    const uint32_t ns = w->num_sectors(), n = ns * 64;
+    brick_table_kernel<<<(n + 255) / 256, 256, 0, stream>>>(w->d_sectors, (const unsigned long long*)w->d_groups, 0,
+                                                           ns, w->sx, w->sz, w->d_bricks);
     return cudaGetLastError();
 }
 
@@ -255,7 +289,7 @@ vrt_status run_batch(vrt_world* w, SyncBatch& b, cudaStream_t stream) {
         const uint32_t lo = *mm.first, hi = *mm.second + 1;
         VRT_CUDA(cudaMemcpyAsync(w->d_sectors + lo, w->h_table.data() + lo, (size_t)(hi - lo) * sizeof(SectorRec),
                                  cudaMemcpyHostToDevice, stream));
-        VRT_CUDA(rebuild_brick_table(w, lo, hi, stream));
+        VRT_CUDA(rebuild_brick_table(w, stream));
     }
     VRT_CUDA(cudaStreamSynchronize(stream));
     b = SyncBatch();
@@ -324,7 +358,8 @@ vrt_status vrt_world_create(const vrt_world_desc* desc, vrt_world** out) {
         e = cudaMalloc(&w->d_sectors, (size_t)w->num_sectors() * sizeof(SectorRec));
         if (e == cudaSuccess) e = cudaMemset(w->d_sectors, 0, (size_t)w->num_sectors() * sizeof(SectorRec));
         if (e == cudaSuccess) e = cudaMalloc(&w->d_bricks, w->num_brick_positions() * sizeof(uint32_t));
-        if (e == cudaSuccess) e = rebuild_brick_table(w, 0, w->num_sectors(), 0);
+        if (e == cudaSuccess) e = cudaMalloc(&w->d_groups, (size_t)w->num_groups() * sizeof(uint64_t));
+        if (e == cudaSuccess) e = rebuild_brick_table(w, 0);
         if (e == cudaSuccess) e = cudaStreamSynchronize(0);
         if (e != cudaSuccess) st = cuda_fail(e, "allocate sector table");
     }
@@ -343,6 +378,7 @@ vrt_status vrt_world_destroy(vrt_world* w) {
     cudaDeviceSynchronize();
     if (w->d_sectors) cudaFree(w->d_sectors);
     if (w->d_bricks) cudaFree(w->d_bricks);
+    if (w->d_groups) cudaFree(w->d_groups);
     if (w->d_codes) cudaFree(w->d_codes);
     if (w->d_payload) cudaFree(w->d_payload);
     w->d_stage.release();

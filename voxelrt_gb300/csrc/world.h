@@ -60,6 +60,7 @@ struct vrt_world {
     // device storage
     vrt::SectorRec* d_sectors = nullptr;
     uint32_t* d_bricks = nullptr;  // brick table, derived from the sector table on the device
+    uint64_t* d_groups = nullptr;  // sector-group masks of the GLSL mode's 4th level
     uint32_t* d_codes = nullptr;   // 2-bit voxel codes, 128 B per slot
     uint8_t* d_payload = nullptr;
     uint32_t capacity = 0;  // brick slots in the device pools
@@ -73,6 +74,7 @@ struct vrt_world {
 
     uint32_t num_sectors() const { return sx * sy * sz; }
     size_t num_brick_positions() const { return (size_t)num_sectors() * 64; }
+    uint32_t num_groups() const { return ((sx + 3) / 4) * ((sy + 3) / 4) * ((sz + 3) / 4); }
     uint32_t lin(int32_t x, int32_t y, int32_t z) const {
         return (uint32_t)x + (uint32_t)z * sx + (uint32_t)y * sx * sz;
     }
