@@ -498,11 +498,27 @@ def run_serving(args, dev):
                     o.edit(e)
             o.close()
     srv.close()
+    # edit latency on its own: sphere edits (radius 4..32, carve or fill at surface points)
+    # applied one at a time to the largest resident world through vrt_world_edit
+    big = int(np.argmax(edges))
+    rng = np.random.default_rng(77)
+    edit_ms = []
+    for k in range(200):
+        e = np.zeros(1, v.EDIT_DTYPE)
+        e["center"] = surf[big][int(rng.integers(0, len(surf[big])))]
+        e["radius"] = int(rng.integers(4, 33))
+        e["material"] = 0 if k % 2 else int(rng.integers(1, 256))
+        t0 = time.perf_counter()
+        worlds[big].edit(e)
+        edit_ms.append((time.perf_counter() - t0) * 1e3)
+    edit_lat = {"edits": len(edit_ms), "world_edge": edges[big], "p50_ms": float(np.percentile(edit_ms, 50)),
+                "p99_ms": float(np.percentile(edit_ms, 99)), "api": "vrt_world_edit, host call to completion"}
     for b in bufs:
         b.close()
     for w in worlds:
         w.close()
     return {"worlds": len(datas), "max_edge": max(edges), "world_bytes": int(sum(d.n_bricks for d in datas) * 640),
+            "edit_latency": edit_lat,
             "resolutions": "256^2 / 1280x720 / 1920x1080 at p 0.5 / 0.3 / 0.2", "edits_per_s": 100,
             "seconds_per_rate": args.serve_seconds, "rates": out, "oracle_replay": replay,
             "latency": "submit to records in pinned host memory, server clock"}

@@ -158,3 +158,41 @@ def test_rays_near_the_grid_corner_and_brick_edges(gpu):
     want = o.render_view_bounces(cam, 3)
     for k in range(4):
         assert_hits_equal(got[k], want[k])
+
+
+def sparse_voxels_world(voxels, sectors):
+    """SectorData holding the given (x, y, z, material) voxels."""
+    by_sector = {}
+    for x, y, z, m in voxels:
+        s = (x >> 5, y >> 5, z >> 5)
+        b = ((x >> 3) & 3) | ((z >> 3) & 3) << 2 | ((y >> 3) & 3) << 4
+        by_sector.setdefault(s, {}).setdefault(b, np.zeros(512, np.uint8))[(x & 7) | (z & 7) << 3 | (y & 7) << 6] = m
+    idx, masks, bricks = [], [], []
+    for (sx, sy, sz), bs in sorted(by_sector.items()):
+        idx.append(v.sector_index(sx, sy, sz))
+        masks.append(sum(1 << b for b in bs))
+        bricks += [bs[b] for b in sorted(bs)]
+    return v.SectorData(sectors, np.array(idx, np.int32), np.array(masks, np.uint64), np.stack(bricks))
+
+
+@pytest.mark.parametrize("glsl", [False, True])
+def test_maximum_world_extent(gpu, glsl):
+    """64 x 32 x 64 sectors = 2048 x 1024 x 2048 voxels, the largest world the 11/10/11-bit
+    hit packing allows, with voxels at both far corners and scattered between."""
+    rng = np.random.default_rng(17)
+    vox = [(2047, 1023, 2047, 200), (0, 0, 0, 3), (2047, 0, 0, 4), (0, 1023, 2047, 5)]
+    vox += [tuple(int(c) for c in rng.integers(0, (2048, 1024, 2048))) + (int(rng.integers(1, 256)),)
+            for _ in range(3000)]
+    data = sparse_voxels_world(vox, (64, 32, 64))
+    w, o = both_worlds(data)
+    # rays at the far corner from inside the world, camera-like frame
+    eye = np.array([2040.3, 1015.6, 2041.1])
+    wo = tuple(int(c) for c in np.floor(eye))
+    d = (np.array([2047.5, 1023.5, 2047.5]) - eye + rng.normal(0, 0.05, (2000, 3))).astype(np.float32)
+    r = make_rays(np.tile((eye - np.floor(eye)).astype(np.float32), (2000, 1)), d)
+    got = w.cast(r, world_origin=wo, glsl=glsl)
+    assert_hits_equal(got, o.cast(r, world_origin=wo, glsl=glsl))
+    assert (got["voxel"] == (2047 | 1023 << 11 | 2047 << 21)).mean() > 0.5
+    rays = v.random_rays((2048, 1024, 2048), seed=17, n=60_000)
+    assert_hits_equal(w.cast(rays, max_iters=400, glsl=glsl), o.cast(rays, max_iters=400, glsl=glsl))
+    w.close()

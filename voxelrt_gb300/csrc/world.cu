@@ -106,22 +106,26 @@ __global__ void __launch_bounds__(kOpsWarps * 32)
 
 // Sector-group masks of the GLSL mode's 4th level (VoxelTraversal.glsl:114-118): per
 // group of 4^3 sectors, bit x | z<<2 | y<<4 set when that sector holds a brick
-// (GpuRenderer.cpp:139-149); groups indexed x + z*GX + y*GX*GZ, one thread each.
+// (GpuRenderer.cpp:139-149); groups indexed x + z*GX + y*GX*GZ, one warp each (lane l
+// tests sectors l and l + 32 of the group, a ballot gathers each half).
 __global__ void group_masks_kernel(const SectorRec* __restrict__ sectors, uint32_t sx, uint32_t sy, uint32_t sz,
                                    unsigned long long* __restrict__ groups) {
     const uint32_t gx = (sx + 3) / 4, gy = (sy + 3) / 4, gz = (sz + 3) / 4;
-    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= gx * gy * gz) return;
+    const uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (g >= gx * gy * gz) return;  // whole warps leave together
     const uint32_t x0 = (g % gx) * 4, z0 = ((g / gx) % gz) * 4, y0 = (g / (gx * gz)) * 4;
-    unsigned long long m = 0;
-    for (uint32_t b = 0; b < 64; b++) {
+    uint32_t half[2];
+    for (uint32_t h = 0; h < 2; h++) {
+        const uint32_t b = lane + 32 * h;
         const uint32_t x = x0 + (b & 3), z = z0 + ((b >> 2) & 3), y = y0 + (b >> 4);
+        bool nonempty = false;
         if (x < sx && y < sy && z < sz) {
             const SectorRec r = sectors[x + z * sx + y * sx * sz];
-            if ((r.mask_lo | r.mask_hi) != 0) m |= 1ull << b;
+            nonempty = (r.mask_lo | r.mask_hi) != 0;
         }
+        half[h] = __ballot_sync(0xffffffffu, nonempty);
     }
-    groups[g] = m;
+    if (lane == 0) groups[g] = (unsigned long long)half[0] | (unsigned long long)half[1] << 32;
 }
 
 // Brick-table entries of sectors [s_lo, s_hi), one thread per brick position.
@@ -242,8 +246,8 @@ vrt_status plan_sector(vrt_world* w, SyncBatch& b, uint32_t s, uint64_t am, uint
 // table (a sector's emptiness changes the GLSL-mode entries of its whole group).
 cudaError_t rebuild_brick_table(vrt_world* w, cudaStream_t stream) {
     const uint32_t ng = w->num_groups();
-    group_masks_kernel<<<(ng + 127) / 128, 128, 0, stream>>>(w->d_sectors, w->sx, w->sy, w->sz,
-                                                           (unsigned long long*)w->d_groups);
+    group_masks_kernel<<<(ng + 3) / 4, 128, 0, stream>>>(w->d_sectors, w->sx, w->sy, w->sz,
+                                                       (unsigned long long*)w->d_groups);
     const uint32_t ns = w->num_sectors(), n = ns * 64;
     brick_table_kernel<<<(n + 255) / 256, 256, 0, stream>>>(w->d_sectors, (const unsigned long long*)w->d_groups, 0,
                                                            ns, w->sx, w->sz, w->d_bricks);
