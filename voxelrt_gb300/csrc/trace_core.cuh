@@ -25,6 +25,24 @@ __device__ __forceinline__ int32_t floor2i(float x) {
 __device__ __forceinline__ int32_t wadd(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
 __device__ __forceinline__ int32_t wsub(int32_t a, int32_t b) { return (int32_t)((uint32_t)a - (uint32_t)b); }
 
+// a * b + c (mod 2^32) on the integer multiply-add unit.  The step loop is bound by
+// the ALU pipe (bit ops, compares, shifts) while the FMA pipe, which also executes
+// integer multiply-add, has room; inline PTX keeps the compiler from folding these
+// back into masks and adds (x - 8*(x >> 3) would become x & 7).
+__device__ __forceinline__ uint32_t imad(uint32_t a, uint32_t b, uint32_t c) {
+#ifdef __CUDA_ARCH__
+    uint32_t r;
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+    return r;
+#else
+    return a * b + c;
+#endif
+}
+// v - worldOrigin (wrapping), the ray-frame coordinate of a voxel
+__device__ __forceinline__ float rel_voxel(int32_t v, int32_t wo) {
+    return __int2float_rn((int32_t)imad((uint32_t)wo, 0xFFFFFFFFu, (uint32_t)v));
+}
+
 struct TraceResult {
     float cx, cy, cz;  // final position (HitResult.Pos)
     float sx, sy, sz;  // final side distances
@@ -154,9 +172,9 @@ template <bool kCount, bool kSafe = false, bool kGlsl = false>
 __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int32_t wox, int32_t woy, int32_t woz,
                                              TraceCounters& cnt) {
     if (kGlsl) {
-        s.sx = __fadd_rn(s.tsx, __fmul_rn(__int2float_rn(wsub(s.vx, wox)), s.ix));
-        s.sy = __fadd_rn(s.tsy, __fmul_rn(__int2float_rn(wsub(s.vy, woy)), s.iy));
-        s.sz = __fadd_rn(s.tsz, __fmul_rn(__int2float_rn(wsub(s.vz, woz)), s.iz));
+        s.sx = __fadd_rn(s.tsx, __fmul_rn(rel_voxel(s.vx, wox), s.ix));
+        s.sy = __fadd_rn(s.tsy, __fmul_rn(rel_voxel(s.vy, woy), s.iy));
+        s.sz = __fadd_rn(s.tsz, __fmul_rn(rel_voxel(s.vz, woz), s.iz));
         // +5 ulp as an integer add on the bits; a NaN tmin stays NaN (its bit pattern
         // differs between platforms: the GPU's 0x7FFFFFFF would wrap to a denormal)
         const float m = min_x86(min_x86(s.sx, s.sy), s.sz);
@@ -177,9 +195,9 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
             return kStepOut;
         }
     }
-    int32_t vx = wadd(wox, __float2int_rd(s.cx));
-    int32_t vy = wadd(woy, __float2int_rd(s.cy));
-    int32_t vz = wadd(woz, __float2int_rd(s.cz));
+    int32_t vx = (int32_t)imad((uint32_t)__float2int_rd(s.cx), 1u, (uint32_t)wox);
+    int32_t vy = (int32_t)imad((uint32_t)__float2int_rd(s.cy), 1u, (uint32_t)woy);
+    int32_t vz = (int32_t)imad((uint32_t)__float2int_rd(s.cz), 1u, (uint32_t)woz);
     if (!((uint32_t)vx < w.size_x && (uint32_t)vy < w.size_y && (uint32_t)vz < w.size_z)) {
         s.vx = vx;
         s.vy = vy;
@@ -192,13 +210,17 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
     // (3 + skip_levels).  An allocated brick's voxel code is kCodeSolid (the hit) or
     // the alignment mask of the skip level of the voxel's 4^3 cell; both replace the
     // two mask fetches of the reference with their precomputed outcome.
-    const uint32_t e =
-        __ldg(w.bricks + ((uint32_t)vx >> 3) + ((uint32_t)vz >> 3) * w.bsx + ((uint32_t)vy >> 3) * w.bsxz);
+    const uint32_t bx = (uint32_t)vx >> 3, by = (uint32_t)vy >> 3, bz = (uint32_t)vz >> 3;
+    const uint32_t e = __ldg(w.bricks + bx + bz * w.bsx + by * w.bsxz);
     int32_t m;
     if (e < kBrickEmpty) {
         if (kCount) cnt.occ_fetches++;
-        const uint32_t vi = (uint32_t)((vx & 7) | (vz & 7) << 3 | (vy & 7) << 6);
-        const uint32_t code = (__ldg(w.codes + (size_t)e * 32 + (vi >> 4)) >> ((vi & 15) * 2)) & 3u;
+        // voxel in brick v = x | z<<3 | y<<6 from v - 8*(v >> 3) per axis, word v >> 4, 2-bit field v & 15
+        const uint32_t lx = imad(bx, 0xFFFFFFF8u, (uint32_t)vx), ly = imad(by, 0xFFFFFFF8u, (uint32_t)vy),
+                       lz = imad(bz, 0xFFFFFFF8u, (uint32_t)vz);
+        const uint32_t vi = imad(ly, 64u, imad(lz, 8u, lx));
+        const uint32_t wd = vi >> 4;
+        const uint32_t code = (__ldg(w.codes + (size_t)e * 32 + wd) >> (imad(wd, 0xFFFFFFF0u, vi) * 2)) & 3u;
         if (code == kCodeSolid) {
             s.material = __ldg(w.payload + (size_t)e * 512 + vi);
             s.vx = vx;
@@ -218,9 +240,9 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
     s.vy = vy;
     s.vz = vz;
     if (kGlsl) return kStepContinue;
-    s.sx = __fadd_rn(s.tsx, __fmul_rn(__int2float_rn(wsub(vx, wox)), s.ix));
-    s.sy = __fadd_rn(s.tsy, __fmul_rn(__int2float_rn(wsub(vy, woy)), s.iy));
-    s.sz = __fadd_rn(s.tsz, __fmul_rn(__int2float_rn(wsub(vz, woz)), s.iz));
+    s.sx = __fadd_rn(s.tsx, __fmul_rn(rel_voxel(vx, wox), s.ix));
+    s.sy = __fadd_rn(s.tsy, __fmul_rn(rel_voxel(vy, woy), s.iy));
+    s.sz = __fadd_rn(s.tsz, __fmul_rn(rel_voxel(vz, woz), s.iz));
     const float t = kSafe ? __fadd_rn(fminf(fminf(s.sx, s.sy), s.sz), 0.001f)
                           : __fadd_rn(min_x86(min_x86(s.sx, s.sy), s.sz), 0.001f);
     s.cx = __fadd_rn(s.ox, __fmul_rn(t, s.dx));
