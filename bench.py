@@ -400,14 +400,7 @@ def surface_points(w, edge, n, seed):
     return vox if len(vox) else np.array([[edge // 2, edge // 2, edge // 2]])
 
 
-def run_serving(args, dev):
-    """Poisson render arrivals (+100 edits/s) against the request server, per arrival rate."""
-    import collections
-
-    import voxelrt_gb300 as v
-    from oracle.oracle import OracleWorld
-    from voxelrt_gb300 import workloads as W
-    datas = W.serving_worlds(n_worlds=args.serve_worlds, max_edge=args.serve_max_edge)
+def load_serving_worlds(v, datas, dev):
     worlds, edges, surf = [], [], []
     for i, d in enumerate(datas):
         w = v.World(d.sectors, brick_capacity=d.n_bricks + 4096, device=dev)
@@ -415,7 +408,40 @@ def run_serving(args, dev):
         worlds.append(w)
         edges.append(d.sectors[0] * 32)
         surf.append(surface_points(w, edges[-1], 256, seed=i))
-    srv = v.Server(worlds, max_inflight=3)
+    return worlds, edges, surf
+
+
+def run_serving(args, dev):
+    """Poisson render arrivals (+100 edits/s) against the request server, per arrival rate,
+    in both scheduling modes (a launch per batch of queued requests; one resident launch
+    taking requests while it runs), each on freshly uploaded worlds."""
+    import voxelrt_gb300 as v
+    from voxelrt_gb300 import workloads as W
+    datas = W.serving_worlds(n_worlds=args.serve_worlds, max_edge=args.serve_max_edge)
+    modes = {}
+    for name, resident in (("launches", False), ("resident", True)):
+        worlds, edges, surf = load_serving_worlds(v, datas, dev)
+        modes[name] = serve_sweep(args, v, datas, worlds, edges, surf, resident)
+        if name != "resident":
+            for w in worlds:
+                w.close()
+    edit_lat = edit_latency(v, worlds, edges, surf)
+    for w in worlds:
+        w.close()
+    return {"worlds": len(datas), "max_edge": max(edges), "world_bytes": int(sum(d.n_bricks for d in datas) * 640),
+            "edit_latency": edit_lat, "resolutions": "256^2 / 1280x720 / 1920x1080 at p 0.5 / 0.3 / 0.2",
+            "edits_per_s": 100, "seconds_per_rate": args.serve_seconds,
+            "rates": modes["launches"]["rates"], "oracle_replay": modes["launches"]["oracle_replay"],
+            "resident": modes["resident"],
+            "latency": "submit to records in pinned host memory, server clock"}
+
+
+def serve_sweep(args, v, datas, worlds, edges, surf, resident):
+    import collections
+
+    from oracle.oracle import OracleWorld
+    from voxelrt_gb300 import workloads as W
+    srv = v.Server(worlds, max_inflight=3, resident=resident)
     max_rec = 1920 * 1080
     bufs = [v.PinnedHits(max_rec) for _ in range(24)]
     out = []
@@ -498,8 +524,14 @@ def run_serving(args, dev):
                     o.edit(e)
             o.close()
     srv.close()
-    # edit latency on its own: sphere edits (radius 4..32, carve or fill at surface points)
-    # applied one at a time to the largest resident world through vrt_world_edit
+    for b in bufs:
+        b.close()
+    return {"rates": out, "oracle_replay": replay, "launches": sum(r["launches"] for r in out)}
+
+
+def edit_latency(v, worlds, edges, surf):
+    """Sphere edits (radius 4..32, carve or fill at surface points) applied one at a time to
+    the largest resident world through vrt_world_edit."""
     big = int(np.argmax(edges))
     rng = np.random.default_rng(77)
     edit_ms = []
@@ -513,15 +545,7 @@ def run_serving(args, dev):
         edit_ms.append((time.perf_counter() - t0) * 1e3)
     edit_lat = {"edits": len(edit_ms), "world_edge": edges[big], "p50_ms": float(np.percentile(edit_ms, 50)),
                 "p99_ms": float(np.percentile(edit_ms, 99)), "api": "vrt_world_edit, host call to completion"}
-    for b in bufs:
-        b.close()
-    for w in worlds:
-        w.close()
-    return {"worlds": len(datas), "max_edge": max(edges), "world_bytes": int(sum(d.n_bricks for d in datas) * 640),
-            "edit_latency": edit_lat,
-            "resolutions": "256^2 / 1280x720 / 1920x1080 at p 0.5 / 0.3 / 0.2", "edits_per_s": 100,
-            "seconds_per_rate": args.serve_seconds, "rates": out, "oracle_replay": replay,
-            "latency": "submit to records in pinned host memory, server clock"}
+    return edit_lat
 
 
 def parity_sample(wl, batch, hits, stream, max_views=3):

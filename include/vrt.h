@@ -387,11 +387,24 @@ vrt_status vrt_host_free(void* ptr);
 typedef struct vrt_server vrt_server;
 
 typedef struct vrt_server_config {
-    uint32_t max_inflight;          /* concurrent launches (0 = 2) */
-    uint32_t max_batch_requests;    /* requests per launch at most (0 = 256) */
+    uint32_t max_inflight;          /* concurrent launches (0 = 2); launch mode only */
+    uint32_t max_batch_requests;    /* requests per launch / per publish at most (0 = 256) */
     uint64_t hbm_budget_bytes;      /* output records in flight (0 = 1/4 of free HBM at creation) */
     vrt_batch_config batch;         /* persistent launch configuration */
+    uint32_t flags;                 /* VRT_SERVE_RESIDENT */
+    uint32_t idle_us;               /* resident mode: how long an idle launch waits for work (0 = 500) */
 } vrt_server_config;
+
+/* Resident mode: one persistent launch stays on the device and takes the ray tiles of
+ * requests published while it runs (through a mailbox word in mapped host memory that
+ * the scheduler and the kernel update with system-scope atomics); a request is done
+ * when the last of its pixels is finished (a per-view counter, then a flag in host
+ * memory) and its records are copied back.  The launch ends when it has been idle for
+ * idle_us, or is closed before an edit or a change of traversal mode.  Needs a device
+ * with host-native atomics (GB300's coherent host link has them); VRT_ERR_INVALID_ARG
+ * otherwise.  Without the flag each batch of queued requests is its own launch, up to
+ * max_inflight of them overlapping on separate streams. */
+#define VRT_SERVE_RESIDENT 1u
 
 #define VRT_REQ_QUEUED 0u
 #define VRT_REQ_RUNNING 1u

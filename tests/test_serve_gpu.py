@@ -1,4 +1,6 @@
-"""Request server: continuous batching, edits between frames, HBM admission.
+"""Request server: continuous batching, edits between frames, HBM admission, in both
+scheduling modes (a launch per batch of queued requests, and one resident launch that
+takes requests while it runs).
 
 The key property: a request's records are the same whether it runs alone or inside
 a mix of concurrent requests (bit-exact, t within 1e-6 relative), and they equal
@@ -59,10 +61,14 @@ def setup(gpu):
         w.close()
 
 
-def test_alone_equals_mix_equals_oracle(setup):
+MODES = [pytest.param(False, id="launches"), pytest.param(True, id="resident")]
+
+
+@pytest.mark.parametrize("resident", MODES)
+def test_alone_equals_mix_equals_oracle(setup, resident):
     datas, worlds, oracles = setup
     rng = np.random.default_rng(1)
-    srv = v.Server(worlds, max_inflight=3)
+    srv = v.Server(worlds, max_inflight=3, resident=resident)
     views = [random_view(rng, i % 4, datas[i % 4].sectors[0] * 32) for i in range(40)]
     probe = views[7]
     # alone
@@ -91,7 +97,8 @@ def test_alone_equals_mix_equals_oracle(setup):
     srv.close()
 
 
-def test_edits_apply_between_frames_in_order(gpu):
+@pytest.mark.parametrize("resident", MODES)
+def test_edits_apply_between_frames_in_order(gpu, resident):
     datas, worlds = make_worlds(2, seed=3)
     oracles = []
     for d in datas:
@@ -99,7 +106,7 @@ def test_edits_apply_between_frames_in_order(gpu):
         o.upload(d)
         oracles.append(o)
     rng = np.random.default_rng(2)
-    srv = v.Server(worlds, max_inflight=2)
+    srv = v.Server(worlds, max_inflight=2, resident=resident)
     log = []  # replayed on the oracle in submission order
     outs = []
     for step in range(30):
@@ -130,11 +137,12 @@ def test_edits_apply_between_frames_in_order(gpu):
         w.close()
 
 
-def test_admission_by_budget(setup):
+@pytest.mark.parametrize("resident", MODES)
+def test_admission_by_budget(setup, resident):
     datas, worlds, oracles = setup
     rng = np.random.default_rng(4)
     # budget of 4 pages (256 KiB): one 160x90 request needs 225 KiB
-    srv = v.Server(worlds, max_inflight=2, hbm_budget_bytes=4 * 65536)
+    srv = v.Server(worlds, max_inflight=2, hbm_budget_bytes=4 * 65536, resident=resident)
     views = [random_view(rng, 0, 64, res=(160, 90)) for _ in range(6)]
     views = [v.make_view(vw.cam, world=0) for vw in views]
     outs = [v.PinnedHits(v.view_records(vw)) for vw in views]
@@ -157,4 +165,40 @@ def test_wait_timeout_and_unknown_ticket(setup):
     with pytest.raises(v.VrtError) as ei:
         srv.wait(12345, timeout_ms=1)
     assert ei.value.status == v.capi.VRT_ERR_NOT_FOUND
+    srv.close()
+
+
+def test_resident_mode_switches_and_idle_restart(setup):
+    """Requests in the GLSL traversal mode close the running launch and start one in
+    their mode; an idle launch closes itself and the next request starts a new one."""
+    import time
+    datas, worlds, oracles = setup
+    rng = np.random.default_rng(6)
+    srv = v.Server(worlds, resident=True, idle_us=200)
+    views = []
+    for i in range(24):
+        vw = random_view(rng, i % 4, datas[i % 4].sectors[0] * 32)
+        if (i // 6) % 2:
+            vw.flags |= v.VIEW_GLSL
+        views.append(vw)
+    outs = [v.PinnedHits(v.view_records(vw)) for vw in views]
+    ts = [srv.submit_render(vw, o.array) for vw, o in zip(views, outs)]
+    for t in ts:
+        srv.wait(t)
+    time.sleep(0.05)  # the launch has been idle for well over 200 us: it ends
+    late = v.make_view(views[0].cam, world=views[0].world)
+    lo = v.PinnedHits(v.view_records(late))
+    srv.wait(srv.submit_render(late, lo.array))
+    for vw, o in zip(views, outs):
+        glsl = bool(vw.flags & v.VIEW_GLSL)
+        o_ = oracles[vw.world]
+        if vw.flags & v.VIEW_SHADOW:
+            want = np.concatenate(o_.render_view_shadow(vw.cam, np.array(vw.sun_dir[:], np.float32), glsl=glsl))
+        elif vw.n_bounces:
+            want = o_.render_view_bounces(vw.cam, vw.n_bounces, glsl=glsl).reshape(-1)
+        else:
+            want = o_.render_view(vw.cam, glsl=glsl)
+        assert_hits_equal(o.array, want)
+    assert_hits_equal(lo.array, oracle_records(oracles[late.world], late))
+    assert srv.stats()["launches"] >= 4  # 4 mode changes, then a restart after the idle end
     srv.close()

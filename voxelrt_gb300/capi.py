@@ -78,7 +78,10 @@ GLSL_MAX_ITERS = 256
 
 class ServerConfig(C.Structure):
     _fields_ = [("max_inflight", C.c_uint32), ("max_batch_requests", C.c_uint32), ("hbm_budget_bytes", C.c_uint64),
-                ("batch", BatchConfig)]
+                ("batch", BatchConfig), ("flags", C.c_uint32), ("idle_us", C.c_uint32)]
+
+
+SERVE_RESIDENT = 1
 
 
 class RequestInfo(C.Structure):

@@ -11,6 +11,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cuda/atomic>
+
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -79,7 +81,69 @@ __global__ void __launch_bounds__(64) view_path_kernel(DevWorld w, ViewDev v, ui
     }
 }
 
-template <bool kCount, bool kGlsl>
+// View-table loads: read-only through the non-coherent path, or at L2 (coherent with
+// the host's copies) for a resident launch, whose table grows while it runs.
+template <bool kResident, typename T>
+__device__ __forceinline__ T ldv(const T* p) {
+    if (kResident) return __ldcg(p);
+    return __ldg(p);
+}
+
+constexpr uint32_t kClaimEmpty = 0xFFFFFFFFu, kClaimStop = 0xFFFFFFFEu;
+
+constexpr uint32_t kNoChunk = 0xFFFFFFFFu;
+
+// Resident launch, lane 0: the next chunk to trace.  Chunk numbers come from one
+// atomicAdd (no retries under contention); a number the host has not published yet
+// stays reserved in `pend` until it is (kClaimEmpty meanwhile), or until the mailbox
+// is closed below it (kClaimStop: a closed word's chunk count is final, nothing is
+// published after a close).  Published counts come from the device copy of the
+// mailbox word (the hint): it is never ahead of the mailbox, and the host writes it
+// only after the views it counts are uploaded, so the warps never read host memory
+// to claim (thousands of them reading one host word at once would queue on the host
+// link).  pub_chunks / pub_views cache the last word read.
+__device__ __forceinline__ uint32_t resident_claim(const BatchParams& p, uint32_t& pub_chunks, uint32_t& pub_views,
+                                                   uint32_t& pend) {
+    const uint32_t n = pend != kNoChunk ? pend : atomicAdd(p.next_chunk, 1u);
+    if (n >= pub_chunks) {
+        const unsigned long long h =
+            cuda::atomic_ref<const unsigned long long, cuda::thread_scope_device>(*p.hint).load(
+                cuda::memory_order_acquire);
+        pub_chunks = (uint32_t)h;
+        pub_views = (uint32_t)(h >> 32) & 0x7FFFFFFFu;
+        if (n >= pub_chunks) {
+            if (h & kMailboxClosed) {
+                pend = kNoChunk;
+                return kClaimStop;
+            }
+            pend = n;
+            return kClaimEmpty;
+        }
+    }
+    pend = kNoChunk;
+    return n;
+}
+
+// Resident launch, lane 0 of an idle warp that has claimed every chunk it saw
+// published: close the mailbox unless more work was published since the hint word
+// in pub_chunks / pub_views.  True when the mailbox is closed with nothing left to
+// claim.  On a failed close nothing is adopted from the mailbox word: it can count
+// views whose uploads are still in flight, so published counts come from the hint
+// alone (the next claim re-reads it).
+__device__ __forceinline__ bool resident_try_close(const BatchParams& p, uint32_t pub_chunks, uint32_t pub_views) {
+    const unsigned long long seen = mailbox_word(pub_chunks, pub_views);
+    unsigned long long expected = seen;
+    cuda::atomic_ref<unsigned long long, cuda::thread_scope_system> mb(*p.mailbox);
+    if (mb.compare_exchange_strong(expected, seen | kMailboxClosed, cuda::memory_order_acq_rel)) {
+        // the other warps learn of the close from the hint (same value the host would write)
+        cuda::atomic_ref<unsigned long long, cuda::thread_scope_device>(*const_cast<unsigned long long*>(p.hint))
+            .store(seen | kMailboxClosed, cuda::memory_order_relaxed);
+        return true;
+    }
+    return expected == (seen | kMailboxClosed);  // closed by the host with no new work
+}
+
+template <bool kCount, bool kGlsl, bool kResident = false>
 __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt = (1u << lane) - 1u;
@@ -99,8 +163,11 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
     RayState s;
     uint32_t rays = 0, hits = 0;
     TraceCounters cnt{0, 0};
+    // resident launches: last mailbox word seen (lane 0), sleep while idle, claim backoff
+    uint32_t pub_chunks = 0, pub_views = 0, idle_ns = 0, sleep_ns = 1000, claim_backoff = 0, pend = kNoChunk;
 
     for (;;) {
+        bool finished = false;  // a pixel's path ended this round (resident completion)
         // Rays that ended during the last DDA round are retired together here, so the
         // record store and the next ray of the path run once per round for all of
         // them instead of once per lane that happens to end on a given step.
@@ -108,7 +175,7 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
             const bool hit = (path & kHit) != 0;
             path &= ~(kEnded | kHit | kSafe);
             const ViewDev* v = p.views + vidx;
-            uint4* rec = p.out + __ldg(&v->out_base) + pixel;
+            uint4* rec = p.out + ldv<kResident>(&v->out_base) + pixel;
             uint32_t kind = path & 0xFF;
             const uint32_t last_kind = (path >> 8) & 0xFF;
             rec[(size_t)kind * plane] = pack_state<kGlsl>(s, hit, iter, pixel);
@@ -118,39 +185,83 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                 path++;
                 kind++;
                 float ox, oy, oz, dx, dy, dz;
-                next_path_ray<kGlsl>(s, ((path >> 16) & 1u) != 0, v->sun, pixel, kind, ox, oy, oz, dx, dy, dz);
+                const float sun[3] = {ldv<kResident>(&v->sun[0]), ldv<kResident>(&v->sun[1]),
+                                      ldv<kResident>(&v->sun[2])};
+                next_path_ray<kGlsl>(s, ((path >> 16) & 1u) != 0, sun, pixel, kind, ox, oy, oz, dx, dy, dz);
                 path &= ~kSafe;
                 if (ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz)) path |= kSafe;
                 iter = 0;
             } else {
                 for (uint32_t kk = kind + 1; kk <= last_kind; kk++) rec[(size_t)kk * plane] = no_ray_hit();
                 active = false;
+                finished = true;
+            }
+        }
+        if (kResident) {
+            // pixels whose path ended: one decrement per view and warp; the last one
+            // raises the view's done flag (records stored before, fences in between)
+            const uint32_t fm = __ballot_sync(0xffffffffu, finished);
+            if (finished) {
+                const uint32_t peers = __match_any_sync(fm, vidx);
+                if (lane == (uint32_t)__ffs(peers) - 1u) {
+                    const uint32_t n = (uint32_t)__popc(peers);
+                    __threadfence();
+                    if (atomicSub(p.remaining + vidx, n) == n) {
+                        __threadfence_system();
+                        *reinterpret_cast<volatile uint32_t*>(p.done_flags + vidx) = 1u;
+                    }
+                }
             }
         }
         const uint32_t act = __ballot_sync(0xffffffffu, active);
+        bool q_wait = false;  // resident: nothing published right now
         if ((uint32_t)__popc(act) < p.refill && !q_empty) {
             uint32_t idle = ~act;
             while (idle) {
                 if (q_next >= q_end) {
-                    uint32_t c = 0;
-                    if (lane == 0) c = atomicAdd(p.queue, 1u);
-                    c = __shfl_sync(0xffffffffu, c, 0);
-                    if (c >= p.total_chunks) {
-                        q_empty = true;
-                        break;
+                    uint32_t c = 0, nv = p.n_views;
+                    if (kResident) {
+                        // while lanes still trace, an empty mailbox is re-read every 8 rounds
+                        if (claim_backoff > 0 && act != 0) {
+                            claim_backoff--;
+                            q_wait = true;
+                            break;
+                        }
+                        if (lane == 0) {
+                            c = resident_claim(p, pub_chunks, pub_views, pend);
+                            nv = pub_views;
+                        }
+                        c = __shfl_sync(0xffffffffu, c, 0);
+                        nv = __shfl_sync(0xffffffffu, nv, 0);
+                        if (c == kClaimStop) {
+                            q_empty = true;
+                            break;
+                        }
+                        if (c == kClaimEmpty) {
+                            q_wait = true;
+                            claim_backoff = 8;
+                            break;
+                        }
+                    } else {
+                        if (lane == 0) c = atomicAdd(p.queue, 1u);
+                        c = __shfl_sync(0xffffffffu, c, 0);
+                        if (c >= p.total_chunks) {
+                            q_empty = true;
+                            break;
+                        }
+                        c += p.chunk_first;
                     }
-                    c += p.chunk_first;
-                    uint32_t lo = 0, hi = p.n_views;
+                    uint32_t lo = 0, hi = nv;
                     while (hi - lo > 1) {
                         const uint32_t mid = (lo + hi) >> 1;
-                        if (__ldg(p.chunk_base + mid) <= c)
+                        if (ldv<kResident>(p.chunk_base + mid) <= c)
                             lo = mid;
                         else
                             hi = mid;
                     }
                     q_view = lo;
-                    q_next = (c - __ldg(p.chunk_base + lo)) * p.chunk_rays;
-                    q_end = min(q_next + p.chunk_rays, __ldg(&p.views[lo].n_rays));
+                    q_next = (c - ldv<kResident>(p.chunk_base + lo)) * p.chunk_rays;
+                    q_end = min(q_next + p.chunk_rays, ldv<kResident>(&p.views[lo].n_rays));
                     continue;
                 }
                 const uint32_t take = min(q_end - q_next, (uint32_t)__popc(idle));
@@ -161,7 +272,7 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                     const ViewDev* v = p.views + q_view;
                     const uint32_t r = q_next + rank;
                     const uint32_t t = r >> p.tile_size_log2, k = r & ((1u << p.tile_size_log2) - 1u);
-                    const uint32_t tiles_x = __ldg(&v->tiles_x);
+                    const uint32_t tiles_x = ldv<kResident>(&v->tiles_x);
                     uint32_t kx, ky;
                     if (p.morton) {
                         kx = compact_even_bits(k);
@@ -172,27 +283,44 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                     }
                     const uint32_t tw = 1u << p.tile_w_log2, th = 1u << (p.tile_size_log2 - p.tile_w_log2);
                     // t / tiles_x by multiply-high: the estimate is the quotient or one more
-                    const uint32_t magic = __ldg(&v->tiles_x_magic);
+                    const uint32_t magic = ldv<kResident>(&v->tiles_x_magic);
                     uint32_t trow = magic ? __umulhi(t, magic) : t;
                     if (trow * tiles_x > t) trow--;
                     const uint32_t px = (t - trow * tiles_x) * tw + kx, py = trow * th + ky;
-                    const uint32_t width = __ldg(&v->cam.width), height = __ldg(&v->cam.height);
-                    if (px < width && py < height) {
+                    const uint32_t width = ldv<kResident>(&v->cam.width), height = ldv<kResident>(&v->cam.height);
+                    bool valid = px < width && py < height;
+                    if (kResident && valid) {
+                        // a resident launch's views arrive while it runs: check what the
+                        // ray would index (its world, its records) before touching it
+                        const uint32_t kinds =
+                            1u + (ldv<kResident>(&v->shadow) ? 1u : ldv<kResident>(&v->n_bounces));
+                        valid = ldv<kResident>(&v->world) < p.n_worlds &&
+                                ldv<kResident>(&v->out_base) + (unsigned long long)width * height * kinds <=
+                                    p.out_records;
+                    }
+                    if (valid) {
                         vidx = q_view;
                         pixel = py * width + px;
                         plane = width * height;
                         iter = 0;
-                        max_iters = __ldg(&v->max_iters);
-                        const uint32_t shadow = __ldg(&v->shadow);
-                        path = (shadow ? 1u : __ldg(&v->n_bounces)) << 8 | shadow << 16;
-                        w = p.worlds[__ldg(&v->world)];
-                        wox = __ldg(&v->cam.world_origin[0]);
-                        woy = __ldg(&v->cam.world_origin[1]);
-                        woz = __ldg(&v->cam.world_origin[2]);
+                        max_iters = ldv<kResident>(&v->max_iters);
+                        const uint32_t shadow = ldv<kResident>(&v->shadow);
+                        path = (shadow ? 1u : ldv<kResident>(&v->n_bounces)) << 8 | shadow << 16;
+                        w = p.worlds[ldv<kResident>(&v->world)];
+                        wox = ldv<kResident>(&v->cam.world_origin[0]);
+                        woy = ldv<kResident>(&v->cam.world_origin[1]);
+                        woz = ldv<kResident>(&v->cam.world_origin[2]);
+                        float d0[3], du[3], dv[3];
+                        for (int c = 0; c < 3; c++) {
+                            d0[c] = ldv<kResident>(&v->cam.d0[c]);
+                            du[c] = ldv<kResident>(&v->cam.du[c]);
+                            dv[c] = ldv<kResident>(&v->cam.dv[c]);
+                        }
                         float dx, dy, dz;
-                        camera_ray(v->cam, px, py, dx, dy, dz);
-                        if (ray_start<kGlsl>(s, w, __ldg(&v->cam.origin[0]), __ldg(&v->cam.origin[1]),
-                                             __ldg(&v->cam.origin[2]), dx, dy, dz, wox, woy, woz))
+                        camera_ray(d0, du, dv, px, py, dx, dy, dz);
+                        if (ray_start<kGlsl>(s, w, ldv<kResident>(&v->cam.origin[0]),
+                                             ldv<kResident>(&v->cam.origin[1]), ldv<kResident>(&v->cam.origin[2]),
+                                             dx, dy, dz, wox, woy, woz))
                             path |= kSafe;
                         active = true;
                     }
@@ -201,7 +329,29 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                 q_next += take;
             }
         }
-        if (__ballot_sync(0xffffffffu, active) == 0 && q_empty) break;
+        if (__ballot_sync(0xffffffffu, active) == 0) {
+            if (q_empty) break;
+            if (kResident) {
+                // nothing to trace and nothing published: wait for the host, sleeping
+                // 1, 2, 4, 8 us between polls so thousands of idle warps do not crowd
+                // the queue's cache lines, and after p.idle_us of sleep close the mailbox
+                // unless new work arrived; every wait here is bounded
+                if (idle_ns >= p.idle_us * 1000u) {
+                    bool closed = false;
+                    if (lane == 0) closed = resident_try_close(p, pub_chunks, pub_views);
+                    if (__shfl_sync(0xffffffffu, closed ? 1u : 0u, 0)) q_empty = true;
+                    idle_ns = 0;
+                    sleep_ns = 1000;
+                } else if (q_wait) {
+                    __nanosleep(sleep_ns);
+                    idle_ns += sleep_ns;
+                    sleep_ns = min(sleep_ns * 2u, 8000u);
+                }
+                continue;
+            }
+        }
+        idle_ns = 0;
+        sleep_ns = 1000;
         // one DDA round: up to p.inner steps, fewer when the iteration cap comes first
         // (an active lane always has iter < max_iters); the fast step when every
         // tracing lane of the warp is safe
@@ -402,6 +552,15 @@ BatchParams make_params(const LaunchPlan& plan, const DevWorld* worlds, const Vi
     p.inner = plan.cfg.inner_iters;
     p.glsl = plan.glsl ? 1u : 0u;
     return p;
+}
+
+vrt_status launch_resident(const BatchParams& p, int blocks, int threads, cudaStream_t stream) {
+    if (p.glsl)
+        persistent_kernel<false, true, true><<<blocks, threads, 0, stream>>>(p);
+    else
+        persistent_kernel<false, false, true><<<blocks, threads, 0, stream>>>(p);
+    VRT_CUDA(cudaGetLastError());
+    return VRT_OK;
 }
 
 vrt_status launch_persistent(const BatchParams& p, int blocks, int threads, bool count, cudaStream_t stream,

@@ -46,7 +46,23 @@ struct BatchParams {
     uint32_t refill;
     uint32_t inner;
     uint32_t glsl;  // traversal mode of every view (VRT_VIEW_GLSL)
+    // resident launches (request server): views are published while the kernel runs
+    unsigned long long* mailbox;  // host-mapped: published chunks | published views << 32 | closed << 63
+    uint32_t* next_chunk;         // device: next chunk to claim
+    const unsigned long long* hint;  // device copy of the mailbox word the host writes after each change
+                                     // (never ahead of it): idle warps poll it instead of host memory
+    uint32_t* remaining;          // device, per view: pixels whose path is not finished
+    uint32_t* done_flags;         // host-mapped, per view: 1 once every record of the view is stored
+    uint32_t idle_us;             // sleep an idle warp accumulates before it closes the mailbox
+    uint32_t n_worlds;            // bounds the kernel checks views of a resident launch against:
+    unsigned long long out_records;  // a bad entry is skipped, never accessed
 };
+
+// Mailbox word of a resident launch.
+constexpr unsigned long long kMailboxClosed = 1ull << 63;
+VRT_HD inline unsigned long long mailbox_word(uint32_t chunks, uint32_t views) {
+    return (unsigned long long)chunks | (unsigned long long)(views & 0x7FFFFFFFu) << 32;
+}
 
 // Views laid out behind one tile queue.
 struct LaunchPlan {
@@ -79,5 +95,12 @@ BatchParams make_params(const LaunchPlan& plan, const DevWorld* worlds, const Vi
 // bytes at params.queue) + persistent kernel launch.
 vrt_status launch_persistent(const BatchParams& p, int blocks, int threads, bool count, cudaStream_t stream,
                              bool reset_counters = true);
+// A resident launch: the kernel claims chunks the host publishes through p.mailbox
+// while it runs, and exits once the mailbox is closed and its work is done.  The
+// caller zeroes the block at p.queue (claim counter and launch counters in the first
+// 64 bytes, the hint on its own line at kResidentHintOffset) before publishing the
+// first views.
+constexpr size_t kResidentHintOffset = 128;
+vrt_status launch_resident(const BatchParams& p, int blocks, int threads, cudaStream_t stream);
 
 }  // namespace vrt

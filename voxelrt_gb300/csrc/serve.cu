@@ -67,6 +67,34 @@ struct Slot {
     struct vrt_server* server = nullptr;
 };
 
+// One resident launch (VRT_SERVE_RESIDENT): the persistent kernel claims the views the
+// scheduler publishes through `mailbox` while it runs.  View slots are not reused
+// within a launch; a launch takes at most `cap` views.
+struct Resident {
+    cudaStream_t stream = nullptr;  // the launch
+    cudaStream_t ctl = nullptr;     // view uploads
+    cudaStream_t copy = nullptr;    // records to the host
+    cudaEvent_t ended = nullptr;
+    DevBuf views, chunk_base, remaining, queue;
+    unsigned long long* mailbox = nullptr;  // pinned, mapped: the word, then the done flags
+    uint32_t* done = nullptr;
+    unsigned long long* d_mailbox = nullptr;
+    uint32_t* d_done = nullptr;
+    ViewDev* h_views = nullptr;  // pinned staging
+    uint32_t* h_cb = nullptr;
+    uint32_t* h_rem = nullptr;
+    unsigned long long* h_hint = nullptr;  // pinned staging of the hint words, one per publish or close
+    uint32_t n_hints = 0;                  // staging entries used by the current launch
+    uint32_t cap = 0;
+    bool live = false, closing = false, glsl = false;
+    uint32_t n_views = 0, n_chunks = 0;
+    std::vector<Request*> req;     // per view slot
+    std::vector<uint8_t> state;    // per slot: 0 tracing, 1 copy issued, 2 finished
+    std::vector<cudaEvent_t> copy_ev;
+    BatchParams params{};
+};
+constexpr uint32_t kResidentViews = 4096;
+
 double now_us(std::chrono::steady_clock::time_point t0) {
     return std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - t0).count();
 }
@@ -87,6 +115,7 @@ struct vrt_server {
     FreeList pages;
     cudaStream_t edit_stream = nullptr;
     std::vector<std::unique_ptr<Slot>> slots;
+    Resident res;
     std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
 
     std::mutex mu;  // queue, requests, stats
@@ -290,6 +319,346 @@ void worker_main(vrt_server* sv) {
     }
 }
 
+// ---- resident mode -----------------------------------------------------------------
+
+// Launch configuration of resident launches: one tile per queue chunk, so a single
+// request spreads over as many warps as it has tiles.
+vrt_batch_config resident_config(const vrt_server* sv) {
+    vrt_batch_config cfg = sv->bcfg;
+    cfg.chunk_tiles = 1;
+    return cfg;
+}
+
+bool resident_done_flag(const Resident& R, uint32_t slot) {
+    return __atomic_load_n(R.done + slot, __ATOMIC_ACQUIRE) != 0;
+}
+
+// The device copy of the mailbox word (8 bytes into the queue block), after a change.
+// Stream-ordered behind the view uploads of the same publish, so it lands after them;
+// each change stages its own word (no staging memory is reused within a launch, so
+// nothing waits for the copies).
+void resident_hint(Resident& R, unsigned long long word) {
+    unsigned long long* h = R.h_hint + std::min<uint32_t>(R.n_hints++, 2 * R.cap);
+    *h = word;
+    cudaMemcpyAsync((uint8_t*)R.queue.ptr + kResidentHintOffset, h, 8, cudaMemcpyHostToDevice, R.ctl);
+}
+
+// Close the launch's mailbox from the host (the kernel may have closed it already).
+void resident_close(Resident& R) {
+    unsigned long long cur = __atomic_load_n(R.mailbox, __ATOMIC_ACQUIRE);
+    while (!(cur & kMailboxClosed))
+        if (__atomic_compare_exchange_n(R.mailbox, &cur, cur | kMailboxClosed, false, __ATOMIC_SEQ_CST,
+                                        __ATOMIC_SEQ_CST))
+            break;
+    R.closing = true;
+    if (R.live) resident_hint(R, cur | kMailboxClosed);
+}
+
+// Lay out `rs` behind the views already published and publish them: advance the
+// mailbox word with one CAS, then enqueue the uploads of the view entries, chunk
+// bases and pixel counts and, behind them on the same stream, the device hint the
+// warps claim from.  Returns false (nothing published) when the launch was closed
+// meanwhile.  No host wait: staging entries belong to their view slot.
+bool resident_publish(vrt_server* sv, const std::vector<Request*>& rs, vrt_status& st) {
+    Resident& R = sv->res;
+    std::vector<vrt_view> views(rs.size());
+    for (size_t i = 0; i < rs.size(); i++) views[i] = rs[i]->view;
+    LaunchPlan plan;
+    st = plan_views(views.data(), (uint32_t)views.size(), (uint32_t)sv->worlds.size(), resident_config(sv), plan);
+    if (st != VRT_OK) return false;
+    if ((uint64_t)R.n_chunks + plan.chunks >= 0x7fffffffull) {
+        resident_close(R);
+        return false;
+    }
+    const uint32_t base = R.n_views, n = (uint32_t)rs.size();
+    unsigned long long expected = mailbox_word(R.n_chunks, R.n_views);
+    if (!__atomic_compare_exchange_n(R.mailbox, &expected, mailbox_word(R.n_chunks + plan.chunks, base + n), false,
+                                     __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST)) {
+        R.closing = true;  // a warp closed the launch: these requests go to the next one
+        return false;
+    }
+    for (uint32_t i = 0; i < n; i++) {
+        ViewDev d = plan.views[i];
+        d.chunk_base += R.n_chunks;
+        d.out_base = (uint64_t)(rs[i]->page_base - 1) * kPageRecords;
+        R.h_views[base + i] = d;
+        R.h_cb[base + i] = d.chunk_base;
+        R.h_rem[base + i] = d.cam.width * d.cam.height;
+        __atomic_store_n(R.done + base + i, 0u, __ATOMIC_RELAXED);
+    }
+    cudaError_t e = cudaMemcpyAsync((ViewDev*)R.views.ptr + base, R.h_views + base, n * sizeof(ViewDev),
+                                    cudaMemcpyHostToDevice, R.ctl);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync((uint32_t*)R.chunk_base.ptr + base, R.h_cb + base, n * sizeof(uint32_t),
+                            cudaMemcpyHostToDevice, R.ctl);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync((uint32_t*)R.remaining.ptr + base, R.h_rem + base, n * sizeof(uint32_t),
+                            cudaMemcpyHostToDevice, R.ctl);
+    if (e != cudaSuccess) {
+        // counted in the mailbox but not uploaded: the warps claim from the hint, so
+        // close the hint at the count before this publish (no warp reaches these
+        // chunks) and the mailbox itself; the requests fail
+        st = cuda_fail(e, "resident publish");
+        resident_hint(R, mailbox_word(R.n_chunks, R.n_views) | kMailboxClosed);
+        unsigned long long cur = __atomic_load_n(R.mailbox, __ATOMIC_ACQUIRE);
+        while (!(cur & kMailboxClosed) && !__atomic_compare_exchange_n(R.mailbox, &cur, cur | kMailboxClosed, false,
+                                                                      __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST)) {
+        }
+        R.closing = true;
+        return false;
+    }
+    for (uint32_t i = 0; i < n; i++) {
+        R.req[base + i] = rs[i];
+        R.state[base + i] = 0;
+    }
+    R.n_views = base + n;
+    R.n_chunks += plan.chunks;
+    resident_hint(R, mailbox_word(R.n_chunks, R.n_views));
+    return true;
+}
+
+vrt_status resident_start(vrt_server* sv, bool glsl) {
+    Resident& R = sv->res;
+    R.n_views = R.n_chunks = 0;
+    R.closing = false;
+    R.glsl = glsl;
+    R.n_hints = 0;
+    VRT_CUDA(cudaStreamSynchronize(R.ctl));  // staging of the last launch is free again
+    __atomic_store_n(R.mailbox, 0ull, __ATOMIC_SEQ_CST);
+    VRT_CUDA(cudaMemsetAsync(R.queue.ptr, 0, kResidentHintOffset + 8, R.ctl));  // claim counter, counters, hint
+    LaunchPlan plan;
+    vrt_batch_config cfg = resident_config(sv);
+    plan.cfg = cfg;
+    uint32_t r = 0;
+    while ((1u << r) < cfg.tile_w) r++;
+    plan.tile_w_log2 = r;
+    r = 0;
+    while ((1u << r) < cfg.tile_w * cfg.tile_h) r++;
+    plan.tile_size_log2 = r;
+    plan.glsl = glsl;
+    BatchParams p = make_params(plan, sv->d_worlds, (const ViewDev*)R.views.ptr, (const uint32_t*)R.chunk_base.ptr,
+                                (uint32_t*)R.queue.ptr, (vrt_hit*)sv->arena);
+    p.mailbox = R.d_mailbox;
+    p.next_chunk = (uint32_t*)R.queue.ptr;
+    p.hint = (const unsigned long long*)((uint8_t*)R.queue.ptr + kResidentHintOffset);
+    p.remaining = (uint32_t*)R.remaining.ptr;
+    p.done_flags = R.d_done;
+    p.idle_us = sv->cfg.idle_us;
+    p.n_worlds = (uint32_t)sv->worlds.size();
+    p.out_records = (unsigned long long)sv->pages.capacity() * kPageRecords;
+    R.params = p;
+    return VRT_OK;
+}
+
+vrt_status resident_launch(vrt_server* sv) {
+    Resident& R = sv->res;
+    vrt_status st = launch_resident(R.params, sv->blocks, sv->threads, R.stream);
+    if (st != VRT_OK) return st;
+    VRT_CUDA(cudaEventRecord(R.ended, R.stream));
+    R.live = true;
+    sv->launches++;
+    return VRT_OK;
+}
+
+// Copies of finished views, completed copies, the end of the launch.  True if any
+// request changed state.
+bool resident_poll(vrt_server* sv) {
+    Resident& R = sv->res;
+    bool progressed = false;
+    for (uint32_t s = 0; s < R.n_views; s++) {
+        if (R.state[s] == 0 && resident_done_flag(R, s)) {
+            Request* r = R.req[s];
+            cudaError_t e = cudaMemcpyAsync(r->host_out, sv->arena + (uint64_t)(r->page_base - 1) * kPageBytes,
+                                            r->records * sizeof(vrt_hit), cudaMemcpyDeviceToHost, R.copy);
+            if (e == cudaSuccess) e = cudaEventRecord(R.copy_ev[s], R.copy);
+            if (e != cudaSuccess) {
+                finish(sv, r, cuda_fail(e, "resident copy"), now_us(sv->t0));
+                R.state[s] = 2;
+                progressed = true;
+                continue;
+            }
+            R.state[s] = 1;
+        }
+        if (R.state[s] == 1) {
+            const cudaError_t e = cudaEventQuery(R.copy_ev[s]);
+            if (e == cudaErrorNotReady) continue;
+            finish(sv, R.req[s], e == cudaSuccess ? VRT_OK : cuda_fail(e, "resident copy"), now_us(sv->t0));
+            R.state[s] = 2;
+            progressed = true;
+        }
+    }
+    if (R.live) {
+        const cudaError_t e = cudaEventQuery(R.ended);
+        if (e != cudaErrorNotReady) {
+            R.live = false;
+            R.closing = true;
+            // every published view must be finished once the launch has ended
+            for (uint32_t s = 0; s < R.n_views; s++)
+                if (R.state[s] == 0 && !resident_done_flag(R, s)) {
+                    if (e != cudaSuccess) cuda_fail(e, "resident launch");
+                    else set_error("resident launch ended before a published view finished");
+                    finish(sv, R.req[s], e == cudaSuccess ? VRT_ERR_DEVICE : VRT_ERR_DEVICE, now_us(sv->t0));
+                    R.state[s] = 2;
+                    progressed = true;
+                }
+        }
+    }
+    return progressed;
+}
+
+bool resident_idle(const Resident& R) {
+    if (R.live) return false;
+    for (uint32_t s = 0; s < R.n_views; s++)
+        if (R.state[s] != 2) return false;
+    return true;
+}
+
+void worker_resident(vrt_server* sv) {
+    cudaSetDevice(sv->device);
+    Resident& R = sv->res;
+    uint64_t seen = 0;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    for (;;) {
+        if (resident_poll(sv)) sv->done_cv.notify_all();
+        if (sv->stop && sv->queue.empty()) {
+            if (resident_idle(R)) break;
+            if (R.live && !R.closing) resident_close(R);  // shutting down: no more work will come
+        }
+        if (!sv->queue.empty() && sv->queue.front()->kind == 1) {
+            // an edit runs between frames: close the launch and wait for its end
+            if (R.live) {
+                if (!R.closing) resident_close(R);
+            } else if (resident_idle(R)) {
+                Request* r = sv->queue.front();
+                sv->queue.pop_front();
+                r->state = VRT_REQ_RUNNING;
+                r->start_us = now_us(sv->t0);
+                lk.unlock();
+                vrt_status st = vrt_world_edit(sv->worlds[r->world], r->edits.data(), (uint32_t)r->edits.size(),
+                                               sv->edit_stream);
+                if (st == VRT_OK) st = refresh_world_table(sv);
+                lk.lock();
+                finish(sv, r, st, now_us(sv->t0));
+                sv->done_cv.notify_all();
+                continue;
+            }
+        } else if (!sv->queue.empty()) {
+            const bool glsl = view_glsl(sv->queue.front()->view);
+            if (R.live && (R.closing || glsl != R.glsl || R.n_views >= R.cap)) {
+                if (!R.closing) resident_close(R);  // a new launch takes the next requests
+            } else if (R.live || resident_idle(R)) {
+                std::vector<Request*> rs;
+                const uint32_t room = R.live ? R.cap - R.n_views : R.cap;
+                for (Request* r : sv->queue) {
+                    if (r->kind != 0 || view_glsl(r->view) != glsl || rs.size() >= sv->cfg.max_batch_requests ||
+                        rs.size() >= room)
+                        break;
+                    const uint32_t base = sv->pages.realloc(0, 0, r->pages);
+                    if (base == 0) break;  // budget full: wait for requests to finish
+                    r->page_base = base;
+                    rs.push_back(r);
+                }
+                if (!rs.empty()) {
+                    const bool fresh = !R.live;
+                    vrt_status st = fresh ? resident_start(sv, glsl) : VRT_OK;
+                    bool ok = st == VRT_OK && resident_publish(sv, rs, st);
+                    if (ok && fresh) st = resident_launch(sv);
+                    if (ok && st == VRT_OK) {
+                        const double ts = now_us(sv->t0);
+                        for (Request* r : rs) {
+                            sv->queue.pop_front();
+                            r->state = VRT_REQ_RUNNING;
+                            r->start_us = ts;
+                            r->batch_size = (uint32_t)rs.size();
+                        }
+                        continue;
+                    }
+                    for (Request* r : rs) {  // not published: pages back, requests stay queued
+                        sv->pages.free(r->page_base, r->pages);
+                        r->page_base = 0;
+                    }
+                    if (st != VRT_OK) {  // a device or planning error fails these requests
+                        for (Request* r : rs) {
+                            sv->queue.pop_front();
+                            finish(sv, r, st, now_us(sv->t0));
+                        }
+                        sv->done_cv.notify_all();
+                        continue;
+                    }
+                }
+            }
+        }
+        // with work on the device, poll for finished views; otherwise sleep until signalled
+        lk.unlock();
+        if (R.live || !resident_idle(R)) {
+            std::this_thread::yield();
+        } else {
+            std::unique_lock<std::mutex> g(sv->sig_mu);
+            sv->sig_cv.wait_for(g, std::chrono::milliseconds(1), [&] { return sv->signals != seen; });
+            seen = sv->signals;
+        }
+        lk.lock();
+    }
+}
+
+vrt_status resident_init(vrt_server* sv) {
+    Resident& R = sv->res;
+    int native = 0;
+    VRT_CUDA(cudaDeviceGetAttribute(&native, cudaDevAttrHostNativeAtomicSupported, sv->device));
+    if (!native) {
+        set_error("resident serving needs host-native atomics between the device and host memory");
+        return VRT_ERR_INVALID_ARG;
+    }
+    R.cap = kResidentViews;
+    VRT_CUDA(cudaStreamCreateWithFlags(&R.stream, cudaStreamNonBlocking));
+    VRT_CUDA(cudaStreamCreateWithFlags(&R.ctl, cudaStreamNonBlocking));
+    VRT_CUDA(cudaStreamCreateWithFlags(&R.copy, cudaStreamNonBlocking));
+    VRT_CUDA(cudaEventCreateWithFlags(&R.ended, cudaEventDisableTiming));
+    VRT_CUDA(R.views.reserve((size_t)R.cap * sizeof(ViewDev)));
+    VRT_CUDA(R.chunk_base.reserve((size_t)R.cap * sizeof(uint32_t)));
+    VRT_CUDA(R.remaining.reserve((size_t)R.cap * sizeof(uint32_t)));
+    VRT_CUDA(R.queue.reserve(256));
+    void* mb = nullptr;
+    VRT_CUDA(cudaHostAlloc(&mb, 64 + (size_t)R.cap * sizeof(uint32_t), cudaHostAllocMapped | cudaHostAllocPortable));
+    std::memset(mb, 0, 64 + (size_t)R.cap * sizeof(uint32_t));
+    R.mailbox = static_cast<unsigned long long*>(mb);
+    R.done = reinterpret_cast<uint32_t*>(static_cast<uint8_t*>(mb) + 64);
+    void* dmb = nullptr;
+    VRT_CUDA(cudaHostGetDevicePointer(&dmb, mb, 0));
+    R.d_mailbox = static_cast<unsigned long long*>(dmb);
+    R.d_done = reinterpret_cast<uint32_t*>(static_cast<uint8_t*>(dmb) + 64);
+    VRT_CUDA(cudaHostAlloc(&R.h_views, (size_t)R.cap * sizeof(ViewDev), cudaHostAllocDefault));
+    VRT_CUDA(cudaHostAlloc(&R.h_cb, (size_t)R.cap * sizeof(uint32_t), cudaHostAllocDefault));
+    VRT_CUDA(cudaHostAlloc(&R.h_rem, (size_t)R.cap * sizeof(uint32_t), cudaHostAllocDefault));
+    VRT_CUDA(cudaHostAlloc(&R.h_hint, (2 * (size_t)R.cap + 1) * sizeof(unsigned long long), cudaHostAllocDefault));
+    R.req.assign(R.cap, nullptr);
+    R.state.assign(R.cap, 2);
+    R.copy_ev.assign(R.cap, nullptr);
+    for (auto& ev : R.copy_ev) VRT_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    return VRT_OK;
+}
+
+void resident_release(vrt_server* sv) {
+    Resident& R = sv->res;
+    if (R.stream) cudaStreamSynchronize(R.stream);
+    if (R.copy) cudaStreamSynchronize(R.copy);
+    for (cudaEvent_t ev : R.copy_ev)
+        if (ev) cudaEventDestroy(ev);
+    R.copy_ev.clear();
+    if (R.ended) cudaEventDestroy(R.ended);
+    for (cudaStream_t* s : {&R.stream, &R.ctl, &R.copy})
+        if (*s) cudaStreamDestroy(*s);
+    R.views.release();
+    R.chunk_base.release();
+    R.remaining.release();
+    R.queue.release();
+    if (R.mailbox) cudaFreeHost(R.mailbox);
+    if (R.h_views) cudaFreeHost(R.h_views);
+    if (R.h_cb) cudaFreeHost(R.h_cb);
+    if (R.h_rem) cudaFreeHost(R.h_rem);
+    if (R.h_hint) cudaFreeHost(R.h_hint);
+}
+
 }  // namespace
 
 extern "C" {
@@ -369,7 +738,11 @@ vrt_status vrt_server_create(vrt_world* const* worlds, uint32_t n_worlds, const 
         }
         sv->slots.push_back(std::move(s));
     }
-    sv->worker = std::thread(worker_main, sv);
+    if (sv->cfg.flags & ~VRT_SERVE_RESIDENT) return fail((set_error("unknown server flags"), VRT_ERR_INVALID_ARG));
+    if (sv->cfg.idle_us == 0) sv->cfg.idle_us = 500;
+    const bool resident = (sv->cfg.flags & VRT_SERVE_RESIDENT) != 0;
+    if (resident && (st = resident_init(sv)) != VRT_OK) return fail(st);
+    sv->worker = resident ? std::thread(worker_resident, sv) : std::thread(worker_main, sv);
     *out = sv;
     return VRT_OK;
 }
@@ -405,6 +778,7 @@ vrt_status vrt_server_destroy(vrt_server* sv, uint32_t timeout_ms) {
         if (s->h_views) cudaFreeHost(s->h_views);
         if (s->h_cb) cudaFreeHost(s->h_cb);
     }
+    resident_release(sv);
     if (sv->edit_stream) cudaStreamDestroy(sv->edit_stream);
     if (sv->arena) cudaFree(sv->arena);
     if (sv->d_worlds) cudaFree(sv->d_worlds);

@@ -58,18 +58,23 @@ struct TraceCounters {
     uint32_t occ_fetches;
 };
 
-// Ray entry point of a camera pixel (the ray generation of vrt_camera).
-__device__ __forceinline__ void camera_ray(const vrt_camera& cam, uint32_t px, uint32_t py, float& dx,
-                                           float& dy, float& dz) {
+// Ray entry point of a camera pixel (the ray generation of vrt_camera) from the
+// camera's d0, du, dv vectors.
+__device__ __forceinline__ void camera_ray(const float* d0, const float* du, const float* dv, uint32_t px,
+                                           uint32_t py, float& dx, float& dy, float& dz) {
     float u = __fadd_rn(__uint2float_rn(px), 0.5f);
     float v = __fadd_rn(__uint2float_rn(py), 0.5f);
-    float x = __fadd_rn(__fadd_rn(cam.d0[0], __fmul_rn(u, cam.du[0])), __fmul_rn(v, cam.dv[0]));
-    float y = __fadd_rn(__fadd_rn(cam.d0[1], __fmul_rn(u, cam.du[1])), __fmul_rn(v, cam.dv[1]));
-    float z = __fadd_rn(__fadd_rn(cam.d0[2], __fmul_rn(u, cam.du[2])), __fmul_rn(v, cam.dv[2]));
+    float x = __fadd_rn(__fadd_rn(d0[0], __fmul_rn(u, du[0])), __fmul_rn(v, dv[0]));
+    float y = __fadd_rn(__fadd_rn(d0[1], __fmul_rn(u, du[1])), __fmul_rn(v, dv[1]));
+    float z = __fadd_rn(__fadd_rn(d0[2], __fmul_rn(u, du[2])), __fmul_rn(v, dv[2]));
     float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
     dx = __fdiv_rn(x, len);
     dy = __fdiv_rn(y, len);
     dz = __fdiv_rn(z, len);
+}
+__device__ __forceinline__ void camera_ray(const vrt_camera& cam, uint32_t px, uint32_t py, float& dx,
+                                           float& dy, float& dz) {
+    camera_ray(cam.d0, cam.du, cam.dv, px, py, dx, dy, dz);
 }
 
 // Per-ray traversal state: RayCast's loop-carried values (CpuRenderer.cpp:173-184).
