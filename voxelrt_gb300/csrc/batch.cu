@@ -89,9 +89,30 @@ __device__ __forceinline__ T ldv(const T* p) {
     return __ldg(p);
 }
 
+// A view-table field: from the warp's shared copy (`shared`, resident launches only),
+// else from global memory.
+template <bool kResident, typename T>
+__device__ __forceinline__ T vget(const T* a, bool shared) {
+    if (!kResident) return __ldg(a);
+    return shared ? *a : __ldcg(a);
+}
+
 constexpr uint32_t kClaimEmpty = 0xFFFFFFFFu, kClaimStop = 0xFFFFFFFEu;
 
 constexpr uint32_t kNoChunk = 0xFFFFFFFFu;
+
+// Resident launch: per-warp state of the mailbox protocol, kept in shared memory and
+// used by lane 0 alone (warp-uniform values in registers would cost every lane a
+// register in the traversal loop).
+struct ResidentWarp {
+    uint32_t pub_chunks, pub_views;  // last hint word read
+    uint32_t pend;                   // reserved chunk number not yet published, or kNoChunk
+    uint32_t backoff;                // rounds until an empty mailbox is re-read
+    uint32_t idle_ns, sleep_ns;      // sleep while idle
+    uint32_t acc_view, acc_n;        // finished pixels of view acc_view not yet subtracted
+    uint32_t cached_view;            // view held in the warp's shared copy of the table entry
+};
+constexpr uint32_t kNoView = 0xFFFFFFFFu;
 
 // Resident launch, lane 0: the next chunk to trace.  Chunk numbers come from one
 // atomicAdd (no retries under contention); a number the host has not published yet
@@ -101,26 +122,31 @@ constexpr uint32_t kNoChunk = 0xFFFFFFFFu;
 // mailbox word (the hint): it is never ahead of the mailbox, and the host writes it
 // only after the views it counts are uploaded, so the warps never read host memory
 // to claim (thousands of them reading one host word at once would queue on the host
-// link).  pub_chunks / pub_views cache the last word read.
-__device__ __forceinline__ uint32_t resident_claim(const BatchParams& p, uint32_t& pub_chunks, uint32_t& pub_views,
-                                                   uint32_t& pend) {
-    const uint32_t n = pend != kNoChunk ? pend : atomicAdd(p.next_chunk, 1u);
-    if (n >= pub_chunks) {
+// link).  While the warp still has lanes tracing (`busy`), an empty mailbox is
+// re-read only every 8 rounds.
+__device__ __forceinline__ uint32_t resident_claim(const BatchParams& p, ResidentWarp& rw, bool busy) {
+    if (busy && rw.backoff > 0) {
+        rw.backoff--;
+        return kClaimEmpty;
+    }
+    const uint32_t n = rw.pend != kNoChunk ? rw.pend : atomicAdd(p.next_chunk, 1u);
+    if (n >= rw.pub_chunks) {
         const unsigned long long h =
             cuda::atomic_ref<const unsigned long long, cuda::thread_scope_device>(*p.hint).load(
                 cuda::memory_order_acquire);
-        pub_chunks = (uint32_t)h;
-        pub_views = (uint32_t)(h >> 32) & 0x7FFFFFFFu;
-        if (n >= pub_chunks) {
+        rw.pub_chunks = (uint32_t)h;
+        rw.pub_views = (uint32_t)(h >> 32) & 0x7FFFFFFFu;
+        if (n >= rw.pub_chunks) {
             if (h & kMailboxClosed) {
-                pend = kNoChunk;
+                rw.pend = kNoChunk;
                 return kClaimStop;
             }
-            pend = n;
+            rw.pend = n;
+            rw.backoff = 8;
             return kClaimEmpty;
         }
     }
-    pend = kNoChunk;
+    rw.pend = kNoChunk;
     return n;
 }
 
@@ -143,6 +169,36 @@ __device__ __forceinline__ bool resident_try_close(const BatchParams& p, uint32_
     return expected == (seen | kMailboxClosed);  // closed by the host with no new work
 }
 
+// Resident launch, lane 0 of a warp with nothing to trace: sleep 1, 2, 4, 8 us between
+// polls (`waiting`: the last claim found nothing) so thousands of idle warps do not
+// crowd the queue's cache lines, and after p.idle_us of sleep close the mailbox unless
+// new work arrived.  True when the warp is to stop; every wait here is bounded.
+__device__ __forceinline__ bool resident_wait(const BatchParams& p, ResidentWarp& rw, bool waiting) {
+    if (rw.idle_ns >= p.idle_us * 1000u) {
+        rw.idle_ns = 0;
+        rw.sleep_ns = 1000;
+        return resident_try_close(p, rw.pub_chunks, rw.pub_views);
+    }
+    if (waiting) {
+        __nanosleep(rw.sleep_ns);
+        rw.idle_ns += rw.sleep_ns;
+        rw.sleep_ns = min(rw.sleep_ns * 2u, 8000u);
+    }
+    return false;
+}
+
+// Resident launch: `n` pixels of view `view` have stored all their records.  The
+// caller's warp has synchronised after the stores; this lane's fence orders them (and,
+// cumulatively, the other lanes') before the decrement, and the decrement that empties
+// the count raises the view's done flag in host memory.
+__device__ __forceinline__ void resident_pixels_done(const BatchParams& p, uint32_t view, uint32_t n) {
+    __threadfence();
+    if (atomicSub(p.remaining + view, n) == n) {
+        __threadfence_system();
+        *reinterpret_cast<volatile uint32_t*>(p.done_flags + view) = 1u;
+    }
+}
+
 template <bool kCount, bool kGlsl, bool kResident = false>
 __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
     const uint32_t lane = threadIdx.x & 31;
@@ -163,8 +219,15 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
     RayState s;
     uint32_t rays = 0, hits = 0;
     TraceCounters cnt{0, 0};
-    // resident launches: last mailbox word seen (lane 0), sleep while idle, claim backoff
-    uint32_t pub_chunks = 0, pub_views = 0, idle_ns = 0, sleep_ns = 1000, claim_backoff = 0, pend = kNoChunk;
+    // resident launches: the warp's mailbox state and its count of finished pixels not
+    // yet subtracted (lane 0)
+    __shared__ ResidentWarp s_resident[16];  // warps_per_block <= 16 (checked when planning)
+    ResidentWarp& rw = s_resident[threadIdx.x >> 5];
+    if (kResident && lane == 0) rw = ResidentWarp{0, 0, kNoChunk, 0, 0, 1000, kNoView, 0, kNoView};
+    // resident launches: the entry of the view the warp takes rays from (q_view), so
+    // that ray setup reads shared memory instead of making L2 round trips
+    __shared__ ViewDev s_views[16];
+    ViewDev& sview = s_views[threadIdx.x >> 5];
 
     for (;;) {
         bool finished = false;  // a pixel's path ended this round (resident completion)
@@ -175,7 +238,9 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
             const bool hit = (path & kHit) != 0;
             path &= ~(kEnded | kHit | kSafe);
             const ViewDev* v = p.views + vidx;
-            uint4* rec = p.out + ldv<kResident>(&v->out_base) + pixel;
+            const bool vs = kResident && vidx == rw.cached_view;
+            if (vs) v = &sview;
+            uint4* rec = p.out + vget<kResident>(&v->out_base, vs) + pixel;
             uint32_t kind = path & 0xFF;
             const uint32_t last_kind = (path >> 8) & 0xFF;
             rec[(size_t)kind * plane] = pack_state<kGlsl>(s, hit, iter, pixel);
@@ -185,8 +250,8 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                 path++;
                 kind++;
                 float ox, oy, oz, dx, dy, dz;
-                const float sun[3] = {ldv<kResident>(&v->sun[0]), ldv<kResident>(&v->sun[1]),
-                                      ldv<kResident>(&v->sun[2])};
+                const float sun[3] = {vget<kResident>(&v->sun[0], vs), vget<kResident>(&v->sun[1], vs),
+                                      vget<kResident>(&v->sun[2], vs)};
                 next_path_ray<kGlsl>(s, ((path >> 16) & 1u) != 0, sun, pixel, kind, ox, oy, oz, dx, dy, dz);
                 path &= ~kSafe;
                 if (ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz)) path |= kSafe;
@@ -198,18 +263,38 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
             }
         }
         if (kResident) {
-            // pixels whose path ended: one decrement per view and warp; the last one
-            // raises the view's done flag (records stored before, fences in between)
+            // Finished pixels are counted per warp (rw.acc_n, of view rw.acc_view) and
+            // subtracted from the view's remaining count once no lane of the warp
+            // traces that view any more: one atomic per warp and stretch of a view,
+            // not one per round (a large view would otherwise queue hundreds of
+            // thousands of atomics on one counter).  Pixels of another view that end
+            // meanwhile are subtracted at once.
             const uint32_t fm = __ballot_sync(0xffffffffu, finished);
-            if (finished) {
-                const uint32_t peers = __match_any_sync(fm, vidx);
-                if (lane == (uint32_t)__ffs(peers) - 1u) {
-                    const uint32_t n = (uint32_t)__popc(peers);
-                    __threadfence();
-                    if (atomicSub(p.remaining + vidx, n) == n) {
-                        __threadfence_system();
-                        *reinterpret_cast<volatile uint32_t*>(p.done_flags + vidx) = 1u;
+            if (fm) {
+                const uint32_t first = __shfl_sync(0xffffffffu, vidx, __ffs(fm) - 1);
+                uint32_t av = 0;
+                if (lane == 0) {
+                    if (rw.acc_view == kNoView) rw.acc_view = first;
+                    av = rw.acc_view;
+                }
+                av = __shfl_sync(0xffffffffu, av, 0);
+                const uint32_t same = __ballot_sync(0xffffffffu, finished && vidx == av);
+                if (lane == 0) rw.acc_n += (uint32_t)__popc(same);
+                if (fm & ~same) {
+                    __syncwarp();  // the records of every lane before the leader's fence
+                    if (finished && vidx != av) {
+                        const uint32_t peers = __match_any_sync(fm & ~same, vidx);
+                        if (lane == (uint32_t)__ffs(peers) - 1u) resident_pixels_done(p, vidx, __popc(peers));
                     }
+                }
+            }
+            const uint32_t av = __shfl_sync(0xffffffffu, lane == 0 ? rw.acc_view : 0u, 0);
+            if (av != kNoView && !__any_sync(0xffffffffu, active && vidx == av)) {
+                __syncwarp();
+                if (lane == 0) {
+                    resident_pixels_done(p, av, rw.acc_n);
+                    rw.acc_view = kNoView;
+                    rw.acc_n = 0;
                 }
             }
         }
@@ -221,15 +306,9 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                 if (q_next >= q_end) {
                     uint32_t c = 0, nv = p.n_views;
                     if (kResident) {
-                        // while lanes still trace, an empty mailbox is re-read every 8 rounds
-                        if (claim_backoff > 0 && act != 0) {
-                            claim_backoff--;
-                            q_wait = true;
-                            break;
-                        }
                         if (lane == 0) {
-                            c = resident_claim(p, pub_chunks, pub_views, pend);
-                            nv = pub_views;
+                            c = resident_claim(p, rw, act != 0);
+                            nv = rw.pub_views;
                         }
                         c = __shfl_sync(0xffffffffu, c, 0);
                         nv = __shfl_sync(0xffffffffu, nv, 0);
@@ -239,7 +318,6 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                         }
                         if (c == kClaimEmpty) {
                             q_wait = true;
-                            claim_backoff = 8;
                             break;
                         }
                     } else {
@@ -251,7 +329,13 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                         }
                         c += p.chunk_first;
                     }
-                    uint32_t lo = 0, hi = nv;
+                    // a warp's claims only grow, so the chunk lies in view q_view or a
+                    // later one: test the next view's start before searching
+                    uint32_t lo = q_view, hi = nv;
+                    if (lo + 1 < hi && ldv<kResident>(p.chunk_base + lo + 1) <= c)
+                        lo++;
+                    else
+                        hi = lo + 1;
                     while (hi - lo > 1) {
                         const uint32_t mid = (lo + hi) >> 1;
                         if (ldv<kResident>(p.chunk_base + mid) <= c)
@@ -261,7 +345,18 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                     }
                     q_view = lo;
                     q_next = (c - ldv<kResident>(p.chunk_base + lo)) * p.chunk_rays;
-                    q_end = min(q_next + p.chunk_rays, ldv<kResident>(&p.views[lo].n_rays));
+                    if (kResident && lo != rw.cached_view) {
+                        // every lane is done with the old copy, and the loads below are
+                        // ordered after lane 0's acquire of the hint that published lo
+                        __syncwarp();
+                        if (lane < sizeof(ViewDev) / 4)
+                            reinterpret_cast<uint32_t*>(&sview)[lane] =
+                                __ldcg(reinterpret_cast<const uint32_t*>(p.views + lo) + lane);
+                        if (lane == 0) rw.cached_view = lo;
+                        __syncwarp();
+                    }
+                    const ViewDev* qv = kResident ? &sview : p.views + lo;
+                    q_end = min(q_next + p.chunk_rays, vget<kResident>(&qv->n_rays, true));
                     continue;
                 }
                 const uint32_t take = min(q_end - q_next, (uint32_t)__popc(idle));
@@ -269,10 +364,10 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                 const bool mine = ((idle >> lane) & 1u) && rank < take;
                 const uint32_t assigned = __ballot_sync(0xffffffffu, mine);
                 if (mine) {
-                    const ViewDev* v = p.views + q_view;
+                    const ViewDev* v = kResident ? &sview : p.views + q_view;
                     const uint32_t r = q_next + rank;
                     const uint32_t t = r >> p.tile_size_log2, k = r & ((1u << p.tile_size_log2) - 1u);
-                    const uint32_t tiles_x = ldv<kResident>(&v->tiles_x);
+                    const uint32_t tiles_x = vget<kResident>(&v->tiles_x, true);
                     uint32_t kx, ky;
                     if (p.morton) {
                         kx = compact_even_bits(k);
@@ -283,19 +378,19 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                     }
                     const uint32_t tw = 1u << p.tile_w_log2, th = 1u << (p.tile_size_log2 - p.tile_w_log2);
                     // t / tiles_x by multiply-high: the estimate is the quotient or one more
-                    const uint32_t magic = ldv<kResident>(&v->tiles_x_magic);
+                    const uint32_t magic = vget<kResident>(&v->tiles_x_magic, true);
                     uint32_t trow = magic ? __umulhi(t, magic) : t;
                     if (trow * tiles_x > t) trow--;
                     const uint32_t px = (t - trow * tiles_x) * tw + kx, py = trow * th + ky;
-                    const uint32_t width = ldv<kResident>(&v->cam.width), height = ldv<kResident>(&v->cam.height);
+                    const uint32_t width = vget<kResident>(&v->cam.width, true), height = vget<kResident>(&v->cam.height, true);
                     bool valid = px < width && py < height;
                     if (kResident && valid) {
                         // a resident launch's views arrive while it runs: check what the
                         // ray would index (its world, its records) before touching it
                         const uint32_t kinds =
-                            1u + (ldv<kResident>(&v->shadow) ? 1u : ldv<kResident>(&v->n_bounces));
-                        valid = ldv<kResident>(&v->world) < p.n_worlds &&
-                                ldv<kResident>(&v->out_base) + (unsigned long long)width * height * kinds <=
+                            1u + (vget<kResident>(&v->shadow, true) ? 1u : vget<kResident>(&v->n_bounces, true));
+                        valid = vget<kResident>(&v->world, true) < p.n_worlds &&
+                                vget<kResident>(&v->out_base, true) + (unsigned long long)width * height * kinds <=
                                     p.out_records;
                     }
                     if (valid) {
@@ -303,23 +398,23 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                         pixel = py * width + px;
                         plane = width * height;
                         iter = 0;
-                        max_iters = ldv<kResident>(&v->max_iters);
-                        const uint32_t shadow = ldv<kResident>(&v->shadow);
-                        path = (shadow ? 1u : ldv<kResident>(&v->n_bounces)) << 8 | shadow << 16;
-                        w = p.worlds[ldv<kResident>(&v->world)];
-                        wox = ldv<kResident>(&v->cam.world_origin[0]);
-                        woy = ldv<kResident>(&v->cam.world_origin[1]);
-                        woz = ldv<kResident>(&v->cam.world_origin[2]);
+                        max_iters = vget<kResident>(&v->max_iters, true);
+                        const uint32_t shadow = vget<kResident>(&v->shadow, true);
+                        path = (shadow ? 1u : vget<kResident>(&v->n_bounces, true)) << 8 | shadow << 16;
+                        w = p.worlds[vget<kResident>(&v->world, true)];
+                        wox = vget<kResident>(&v->cam.world_origin[0], true);
+                        woy = vget<kResident>(&v->cam.world_origin[1], true);
+                        woz = vget<kResident>(&v->cam.world_origin[2], true);
                         float d0[3], du[3], dv[3];
                         for (int c = 0; c < 3; c++) {
-                            d0[c] = ldv<kResident>(&v->cam.d0[c]);
-                            du[c] = ldv<kResident>(&v->cam.du[c]);
-                            dv[c] = ldv<kResident>(&v->cam.dv[c]);
+                            d0[c] = vget<kResident>(&v->cam.d0[c], true);
+                            du[c] = vget<kResident>(&v->cam.du[c], true);
+                            dv[c] = vget<kResident>(&v->cam.dv[c], true);
                         }
                         float dx, dy, dz;
                         camera_ray(d0, du, dv, px, py, dx, dy, dz);
-                        if (ray_start<kGlsl>(s, w, ldv<kResident>(&v->cam.origin[0]),
-                                             ldv<kResident>(&v->cam.origin[1]), ldv<kResident>(&v->cam.origin[2]),
+                        if (ray_start<kGlsl>(s, w, vget<kResident>(&v->cam.origin[0], true),
+                                             vget<kResident>(&v->cam.origin[1], true), vget<kResident>(&v->cam.origin[2], true),
                                              dx, dy, dz, wox, woy, woz))
                             path |= kSafe;
                         active = true;
@@ -332,26 +427,17 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
         if (__ballot_sync(0xffffffffu, active) == 0) {
             if (q_empty) break;
             if (kResident) {
-                // nothing to trace and nothing published: wait for the host, sleeping
-                // 1, 2, 4, 8 us between polls so thousands of idle warps do not crowd
-                // the queue's cache lines, and after p.idle_us of sleep close the mailbox
-                // unless new work arrived; every wait here is bounded
-                if (idle_ns >= p.idle_us * 1000u) {
-                    bool closed = false;
-                    if (lane == 0) closed = resident_try_close(p, pub_chunks, pub_views);
-                    if (__shfl_sync(0xffffffffu, closed ? 1u : 0u, 0)) q_empty = true;
-                    idle_ns = 0;
-                    sleep_ns = 1000;
-                } else if (q_wait) {
-                    __nanosleep(sleep_ns);
-                    idle_ns += sleep_ns;
-                    sleep_ns = min(sleep_ns * 2u, 8000u);
-                }
+                // nothing to trace and nothing published: wait for the host
+                bool stop = false;
+                if (lane == 0) stop = resident_wait(p, rw, q_wait);
+                if (__shfl_sync(0xffffffffu, stop ? 1u : 0u, 0)) q_empty = true;
                 continue;
             }
         }
-        idle_ns = 0;
-        sleep_ns = 1000;
+        if (kResident && lane == 0 && rw.idle_ns) {
+            rw.idle_ns = 0;
+            rw.sleep_ns = 1000;
+        }
         // one DDA round: up to p.inner steps, fewer when the iteration cap comes first
         // (an active lane always has iter < max_iters); the fast step when every
         // tracing lane of the warp is safe

@@ -73,7 +73,9 @@ struct Slot {
 struct Resident {
     cudaStream_t stream = nullptr;  // the launch
     cudaStream_t ctl = nullptr;     // view uploads
-    cudaStream_t copy = nullptr;    // records to the host
+    // records to the host, slot s on copy[s % 4], so that a small view's copy need not
+    // queue behind a large one (they share the link's bandwidth)
+    cudaStream_t copy[4] = {};
     cudaEvent_t ended = nullptr;
     DevBuf views, chunk_base, remaining, queue;
     unsigned long long* mailbox = nullptr;  // pinned, mapped: the word, then the done flags
@@ -88,12 +90,21 @@ struct Resident {
     uint32_t cap = 0;
     bool live = false, closing = false, glsl = false;
     uint32_t n_views = 0, n_chunks = 0;
+    uint32_t first_open = 0;       // slots below it are all finished
     std::vector<Request*> req;     // per view slot
     std::vector<uint8_t> state;    // per slot: 0 tracing, 1 copy issued, 2 finished
     std::vector<cudaEvent_t> copy_ev;
     BatchParams params{};
 };
 constexpr uint32_t kResidentViews = 4096;
+
+// A request the resident scheduler saw finish, collected before it takes the server lock.
+struct Finished {
+    Request* r;
+    vrt_status status;
+    double t;
+    std::string error;
+};
 
 double now_us(std::chrono::steady_clock::time_point t0) {
     return std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - t0).count();
@@ -129,7 +140,7 @@ struct vrt_server {
 
     std::mutex sig_mu;  // worker wake-ups (submissions, completions)
     std::condition_variable sig_cv;
-    uint64_t signals = 0;
+    std::atomic<uint64_t> signals{0};
 
     // stats
     std::vector<double> lat;
@@ -419,7 +430,7 @@ bool resident_publish(vrt_server* sv, const std::vector<Request*>& rs, vrt_statu
 
 vrt_status resident_start(vrt_server* sv, bool glsl) {
     Resident& R = sv->res;
-    R.n_views = R.n_chunks = 0;
+    R.n_views = R.n_chunks = R.first_open = 0;
     R.closing = false;
     R.glsl = glsl;
     R.n_hints = 0;
@@ -462,19 +473,24 @@ vrt_status resident_launch(vrt_server* sv) {
 
 // Copies of finished views, completed copies, the end of the launch.  True if any
 // request changed state.
-bool resident_poll(vrt_server* sv) {
+// Collects into `out` the views whose records reached host memory, or that failed,
+// without the server lock: slot state belongs to the scheduler thread.  Returns true
+// when the launch was seen to end.
+bool resident_poll(vrt_server* sv, std::vector<Finished>& out) {
     Resident& R = sv->res;
-    bool progressed = false;
-    for (uint32_t s = 0; s < R.n_views; s++) {
+    auto fail = [&](uint32_t s, vrt_status st) {
+        out.push_back({R.req[s], st, now_us(sv->t0), last_error_cstr()});
+        R.state[s] = 2;
+    };
+    while (R.first_open < R.n_views && R.state[R.first_open] == 2) R.first_open++;
+    for (uint32_t s = R.first_open; s < R.n_views; s++) {
         if (R.state[s] == 0 && resident_done_flag(R, s)) {
-            Request* r = R.req[s];
+            const Request* r = R.req[s];
             cudaError_t e = cudaMemcpyAsync(r->host_out, sv->arena + (uint64_t)(r->page_base - 1) * kPageBytes,
-                                            r->records * sizeof(vrt_hit), cudaMemcpyDeviceToHost, R.copy);
-            if (e == cudaSuccess) e = cudaEventRecord(R.copy_ev[s], R.copy);
+                                            r->records * sizeof(vrt_hit), cudaMemcpyDeviceToHost, R.copy[s % 4]);
+            if (e == cudaSuccess) e = cudaEventRecord(R.copy_ev[s], R.copy[s % 4]);
             if (e != cudaSuccess) {
-                finish(sv, r, cuda_fail(e, "resident copy"), now_us(sv->t0));
-                R.state[s] = 2;
-                progressed = true;
+                fail(s, cuda_fail(e, "resident copy"));
                 continue;
             }
             R.state[s] = 1;
@@ -482,28 +498,27 @@ bool resident_poll(vrt_server* sv) {
         if (R.state[s] == 1) {
             const cudaError_t e = cudaEventQuery(R.copy_ev[s]);
             if (e == cudaErrorNotReady) continue;
-            finish(sv, R.req[s], e == cudaSuccess ? VRT_OK : cuda_fail(e, "resident copy"), now_us(sv->t0));
-            R.state[s] = 2;
-            progressed = true;
+            if (e == cudaSuccess) {
+                out.push_back({R.req[s], VRT_OK, now_us(sv->t0), {}});
+                R.state[s] = 2;
+            } else {
+                fail(s, cuda_fail(e, "resident copy"));
+            }
         }
     }
-    if (R.live) {
-        const cudaError_t e = cudaEventQuery(R.ended);
-        if (e != cudaErrorNotReady) {
-            R.live = false;
-            R.closing = true;
-            // every published view must be finished once the launch has ended
-            for (uint32_t s = 0; s < R.n_views; s++)
-                if (R.state[s] == 0 && !resident_done_flag(R, s)) {
-                    if (e != cudaSuccess) cuda_fail(e, "resident launch");
-                    else set_error("resident launch ended before a published view finished");
-                    finish(sv, R.req[s], e == cudaSuccess ? VRT_ERR_DEVICE : VRT_ERR_DEVICE, now_us(sv->t0));
-                    R.state[s] = 2;
-                    progressed = true;
-                }
+    if (!R.live) return false;
+    const cudaError_t e = cudaEventQuery(R.ended);
+    if (e == cudaErrorNotReady) return false;
+    R.live = false;
+    R.closing = true;
+    // every published view must be finished once the launch has ended
+    for (uint32_t s = R.first_open; s < R.n_views; s++)
+        if (R.state[s] == 0 && !resident_done_flag(R, s)) {
+            if (e != cudaSuccess) cuda_fail(e, "resident launch");
+            else set_error("resident launch ended before a published view finished");
+            fail(s, VRT_ERR_DEVICE);
         }
-    }
-    return progressed;
+    return true;
 }
 
 bool resident_idle(const Resident& R) {
@@ -513,91 +528,114 @@ bool resident_idle(const Resident& R) {
     return true;
 }
 
+// One pass of the resident scheduler over the queue, with sv->mu held by `lk`.  Returns
+// true when it made progress and another pass may make more.
+bool resident_schedule(vrt_server* sv, std::unique_lock<std::mutex>& lk) {
+    Resident& R = sv->res;
+    if (sv->queue.empty()) {
+        if (sv->stop && R.live && !R.closing) resident_close(R);  // shutting down: no more work will come
+        return false;
+    }
+    Request* front = sv->queue.front();
+    if (front->kind == 1) {
+        // an edit runs between frames: close the launch and wait for its end
+        if (R.live) {
+            if (!R.closing) resident_close(R);
+            return false;
+        }
+        if (!resident_idle(R)) return false;
+        sv->queue.pop_front();
+        front->state = VRT_REQ_RUNNING;
+        front->start_us = now_us(sv->t0);
+        lk.unlock();
+        vrt_status st = vrt_world_edit(sv->worlds[front->world], front->edits.data(),
+                                       (uint32_t)front->edits.size(), sv->edit_stream);
+        if (st == VRT_OK) st = refresh_world_table(sv);
+        lk.lock();
+        finish(sv, front, st, now_us(sv->t0));
+        sv->done_cv.notify_all();
+        return true;
+    }
+    const bool glsl = view_glsl(front->view);
+    if (R.live && (R.closing || glsl != R.glsl || R.n_views >= R.cap)) {
+        if (!R.closing) resident_close(R);  // a new launch takes the next requests
+        return false;
+    }
+    if (!R.live && !resident_idle(R)) return false;  // the last launch's records are still copying
+    std::vector<Request*> rs;
+    const uint32_t room = R.live ? R.cap - R.n_views : R.cap;
+    for (Request* r : sv->queue) {
+        if (r->kind != 0 || view_glsl(r->view) != glsl || rs.size() >= sv->cfg.max_batch_requests ||
+            rs.size() >= room)
+            break;
+        const uint32_t base = sv->pages.realloc(0, 0, r->pages);
+        if (base == 0) break;  // budget full: wait for requests to finish
+        r->page_base = base;
+        rs.push_back(r);
+    }
+    if (rs.empty()) return false;
+    const bool fresh = !R.live;
+    vrt_status st = fresh ? resident_start(sv, glsl) : VRT_OK;
+    const bool ok = st == VRT_OK && resident_publish(sv, rs, st);
+    if (ok && fresh) st = resident_launch(sv);
+    if (ok && st == VRT_OK) {
+        const double ts = now_us(sv->t0);
+        for (Request* r : rs) {
+            sv->queue.pop_front();
+            r->state = VRT_REQ_RUNNING;
+            r->start_us = ts;
+            r->batch_size = (uint32_t)rs.size();
+        }
+        return true;
+    }
+    for (Request* r : rs) {  // not published: pages back, requests stay queued
+        sv->pages.free(r->page_base, r->pages);
+        r->page_base = 0;
+    }
+    if (st == VRT_OK) return false;  // the launch closed itself first: the next one takes them
+    for (Request* r : rs) {          // a device or planning error fails these requests
+        sv->queue.pop_front();
+        finish(sv, r, st, now_us(sv->t0));
+    }
+    sv->done_cv.notify_all();
+    return true;
+}
+
+// The scheduler thread of resident mode.  It polls the done flags and copy events
+// without the server lock (a spinning thread that held it would starve submitters and
+// waiters) and takes the lock only when a request finished, the launch ended, a
+// submission or stop was signalled, or the last pass made progress.
 void worker_resident(vrt_server* sv) {
     cudaSetDevice(sv->device);
     Resident& R = sv->res;
-    uint64_t seen = 0;
-    std::unique_lock<std::mutex> lk(sv->mu);
+    uint64_t seen = ~0ull;
+    bool again = true;
+    std::vector<Finished> fin;
     for (;;) {
-        if (resident_poll(sv)) sv->done_cv.notify_all();
-        if (sv->stop && sv->queue.empty()) {
-            if (resident_idle(R)) break;
-            if (R.live && !R.closing) resident_close(R);  // shutting down: no more work will come
-        }
-        if (!sv->queue.empty() && sv->queue.front()->kind == 1) {
-            // an edit runs between frames: close the launch and wait for its end
-            if (R.live) {
-                if (!R.closing) resident_close(R);
-            } else if (resident_idle(R)) {
-                Request* r = sv->queue.front();
-                sv->queue.pop_front();
-                r->state = VRT_REQ_RUNNING;
-                r->start_us = now_us(sv->t0);
-                lk.unlock();
-                vrt_status st = vrt_world_edit(sv->worlds[r->world], r->edits.data(), (uint32_t)r->edits.size(),
-                                               sv->edit_stream);
-                if (st == VRT_OK) st = refresh_world_table(sv);
-                lk.lock();
-                finish(sv, r, st, now_us(sv->t0));
+        const bool ended = resident_poll(sv, fin);
+        const uint64_t sig = sv->signals.load(std::memory_order_acquire);
+        if (again || ended || !fin.empty() || sig != seen) {
+            seen = sig;
+            std::unique_lock<std::mutex> lk(sv->mu);
+            if (!fin.empty()) {
+                for (Finished& f : fin) {
+                    finish(sv, f.r, f.status, f.t);
+                    if (f.status != VRT_OK) f.r->error = f.error;
+                }
+                fin.clear();
                 sv->done_cv.notify_all();
-                continue;
             }
-        } else if (!sv->queue.empty()) {
-            const bool glsl = view_glsl(sv->queue.front()->view);
-            if (R.live && (R.closing || glsl != R.glsl || R.n_views >= R.cap)) {
-                if (!R.closing) resident_close(R);  // a new launch takes the next requests
-            } else if (R.live || resident_idle(R)) {
-                std::vector<Request*> rs;
-                const uint32_t room = R.live ? R.cap - R.n_views : R.cap;
-                for (Request* r : sv->queue) {
-                    if (r->kind != 0 || view_glsl(r->view) != glsl || rs.size() >= sv->cfg.max_batch_requests ||
-                        rs.size() >= room)
-                        break;
-                    const uint32_t base = sv->pages.realloc(0, 0, r->pages);
-                    if (base == 0) break;  // budget full: wait for requests to finish
-                    r->page_base = base;
-                    rs.push_back(r);
-                }
-                if (!rs.empty()) {
-                    const bool fresh = !R.live;
-                    vrt_status st = fresh ? resident_start(sv, glsl) : VRT_OK;
-                    bool ok = st == VRT_OK && resident_publish(sv, rs, st);
-                    if (ok && fresh) st = resident_launch(sv);
-                    if (ok && st == VRT_OK) {
-                        const double ts = now_us(sv->t0);
-                        for (Request* r : rs) {
-                            sv->queue.pop_front();
-                            r->state = VRT_REQ_RUNNING;
-                            r->start_us = ts;
-                            r->batch_size = (uint32_t)rs.size();
-                        }
-                        continue;
-                    }
-                    for (Request* r : rs) {  // not published: pages back, requests stay queued
-                        sv->pages.free(r->page_base, r->pages);
-                        r->page_base = 0;
-                    }
-                    if (st != VRT_OK) {  // a device or planning error fails these requests
-                        for (Request* r : rs) {
-                            sv->queue.pop_front();
-                            finish(sv, r, st, now_us(sv->t0));
-                        }
-                        sv->done_cv.notify_all();
-                        continue;
-                    }
-                }
-            }
+            if (sv->stop && sv->queue.empty() && resident_idle(R)) break;
+            again = resident_schedule(sv, lk);
+            if (again) continue;
         }
         // with work on the device, poll for finished views; otherwise sleep until signalled
-        lk.unlock();
         if (R.live || !resident_idle(R)) {
             std::this_thread::yield();
         } else {
             std::unique_lock<std::mutex> g(sv->sig_mu);
-            sv->sig_cv.wait_for(g, std::chrono::milliseconds(1), [&] { return sv->signals != seen; });
-            seen = sv->signals;
+            sv->sig_cv.wait_for(g, std::chrono::milliseconds(1), [&] { return sv->signals.load() != seen; });
         }
-        lk.lock();
     }
 }
 
@@ -612,7 +650,7 @@ vrt_status resident_init(vrt_server* sv) {
     R.cap = kResidentViews;
     VRT_CUDA(cudaStreamCreateWithFlags(&R.stream, cudaStreamNonBlocking));
     VRT_CUDA(cudaStreamCreateWithFlags(&R.ctl, cudaStreamNonBlocking));
-    VRT_CUDA(cudaStreamCreateWithFlags(&R.copy, cudaStreamNonBlocking));
+    for (cudaStream_t& c : R.copy) VRT_CUDA(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
     VRT_CUDA(cudaEventCreateWithFlags(&R.ended, cudaEventDisableTiming));
     VRT_CUDA(R.views.reserve((size_t)R.cap * sizeof(ViewDev)));
     VRT_CUDA(R.chunk_base.reserve((size_t)R.cap * sizeof(uint32_t)));
@@ -641,12 +679,13 @@ vrt_status resident_init(vrt_server* sv) {
 void resident_release(vrt_server* sv) {
     Resident& R = sv->res;
     if (R.stream) cudaStreamSynchronize(R.stream);
-    if (R.copy) cudaStreamSynchronize(R.copy);
+    for (cudaStream_t c : R.copy)
+        if (c) cudaStreamSynchronize(c);
     for (cudaEvent_t ev : R.copy_ev)
         if (ev) cudaEventDestroy(ev);
     R.copy_ev.clear();
     if (R.ended) cudaEventDestroy(R.ended);
-    for (cudaStream_t* s : {&R.stream, &R.ctl, &R.copy})
+    for (cudaStream_t* s : {&R.stream, &R.ctl, &R.copy[0], &R.copy[1], &R.copy[2], &R.copy[3]})
         if (*s) cudaStreamDestroy(*s);
     R.views.release();
     R.chunk_base.release();
