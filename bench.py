@@ -322,7 +322,8 @@ def run_ours(args):
                     "kernel": "view_path_kernel, 8x8 blocks, thread per pixel"}
 
     # end to end through the host-buffer API: new cameras in (H2D), all records out to
-    # pinned host memory from vrt_host_alloc (the kernel stores them there directly)
+    # pinned host memory from vrt_host_alloc (the copies of finished parts overlap the
+    # traversal of later ones)
     host = v.PinnedHits(n_rec)
     host_np = host.array
     cams = [vw.cam for vw in wl.views]
@@ -338,6 +339,9 @@ def run_ours(args):
     e2e = {"value": job_rays / e2e_s / 1e9, "unit": "Grays/s", "ms_per_step": e2e_s * 1e3,
            "h2d_bytes_per_step": 120 * len(wl.views), "d2h_bytes_per_step": n_rec * HIT_BYTES,
            "api": "vrt_batch_update_cameras + vrt_batch_run (pinned host records)"}
+    link = d2h_link_gbs(torch, stream)
+    e2e["d2h_link_gbs"] = link
+    e2e["d2h_link_frac"] = n_rec * HIT_BYTES / e2e_s / 1e9 / link
 
     peak, peak_src = peak_hbm()
     achieved = alg_bytes / (ms * 1e-3) / 1e9
@@ -434,6 +438,22 @@ def run_serving(args, dev):
             "rates": modes["launches"]["rates"], "oracle_replay": modes["launches"]["oracle_replay"],
             "resident": modes["resident"],
             "latency": "submit to records in pinned host memory, server clock"}
+
+
+def d2h_link_gbs(torch, stream, nbytes=1 << 30, reps=3):
+    """Device-to-host copy bandwidth into pinned memory (GB/s): the bound of the end-to-end
+    leg, whose records all cross this link."""
+    dev = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    with torch.cuda.stream(stream):
+        host.copy_(dev, non_blocking=True)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            host.copy_(dev, non_blocking=True)
+        b.record(stream)
+    b.synchronize()
+    return reps * nbytes / (a.elapsed_time(b) * 1e-3) / 1e9
 
 
 def serve_sweep(args, v, datas, worlds, edges, surf, resident):
