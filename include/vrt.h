@@ -125,8 +125,11 @@ typedef struct vrt_cast_params {
 /* Pinhole camera in the reference's split form: integer world origin plus a
  * fractional ray origin (GBuffer.h:79, CpuRenderer.cpp:447-448).  The ray of
  * pixel (px, py), u = px + 0.5, v = py + 0.5, has unnormalised direction
- * d0 + u*du + v*dv (each op rounded separately), normalised with an IEEE sqrt
- * and divisions.  Build one with vrt_camera_look_at(). */
+ * d0 + u*du + v*dv (each op rounded separately), multiplied per component by
+ * r = 1/sqrt(l2), l2 = (x*x + y*y) + z*z, computed as: r = bits 0x5F3759DF -
+ * (bits(l2) >> 1), then three times r = r * fma(-(0.5*l2), r*r, 1.5) (every op IEEE
+ * round-to-nearest, so any machine reproduces the direction bit for bit; within 3 ulp
+ * of unit length).  Build one with vrt_camera_look_at(). */
 typedef struct vrt_camera {
     int32_t world_origin[3];
     float origin[3];

@@ -421,15 +421,30 @@ void offset_origin(const Trace& tr, const float n[3], float o[3]) {
     for (int c = 0; c < 3; c++) o[c] = tr.cur[c] + n[c] * 0.01f;
 }
 
+// 1/sqrt(l2): integer first estimate 0x5F3759DF - (bits >> 1) (Lomont 2003), then three
+// Newton steps r * fma(-l2/2, r*r, 1.5); the vrt_camera contract of include/vrt.h.
+float camera_rsqrt(float l2) {
+    const float h = 0.5f * l2;
+    uint32_t b;
+    std::memcpy(&b, &l2, 4);
+    b = 0x5F3759DFu - (b >> 1);
+    float r;
+    std::memcpy(&r, &b, 4);
+    for (int i = 0; i < 3; i++) r = r * std::fmaf(-h, r * r, 1.5f);
+    return r;
+}
+
+// The ray of pixel (px, py) of a vrt_camera: d0 + u*du + v*dv, u = px + 0.5, v = py + 0.5,
+// times camera_rsqrt of its squared length.
 void camera_ray(const vrt_camera& cam, uint32_t px, uint32_t py, float o[3], float d[3]) {
     float u = (float)px + 0.5f, v = (float)py + 0.5f;
     float x = (cam.d0[0] + u * cam.du[0]) + v * cam.dv[0];
     float y = (cam.d0[1] + u * cam.du[1]) + v * cam.dv[1];
     float z = (cam.d0[2] + u * cam.du[2]) + v * cam.dv[2];
-    float len = std::sqrt((x * x + y * y) + z * z);
-    d[0] = x / len;
-    d[1] = y / len;
-    d[2] = z / len;
+    const float r = camera_rsqrt((x * x + y * y) + z * z);
+    d[0] = x * r;
+    d[1] = y * r;
+    d[2] = z * r;
     for (int c = 0; c < 3; c++) o[c] = cam.origin[c];
 }
 

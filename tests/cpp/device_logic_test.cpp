@@ -29,6 +29,7 @@ inline float __fmul_rn(float a, float b) { return a * b; }
 inline float __fdiv_rn(float a, float b) { return a / b; }
 inline float __frcp_rn(float a) { return 1.0f / a; }
 inline float __fsqrt_rn(float a) { return std::sqrt(a); }
+inline float __fmaf_rn(float a, float b, float c) { return std::fmaf(a, b, c); }
 inline float __int2float_rn(int a) { return (float)a; }
 inline float __uint2float_rn(unsigned a) { return (float)a; }
 // cvt.rmi.s32.f32: floor, saturating, NaN -> 0

@@ -111,6 +111,7 @@ struct ResidentWarp {
     uint32_t idle_ns, sleep_ns;      // sleep while idle
     uint32_t acc_view, acc_n;        // finished pixels of view acc_view not yet subtracted
     uint32_t cached_view;            // view held in the warp's shared copy of the table entry
+    uint32_t q_inside;               // origin_inside_safe() for that view's camera
 };
 constexpr uint32_t kNoView = 0xFFFFFFFFu;
 
@@ -205,7 +206,7 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
     const uint32_t lt = (1u << lane) - 1u;
     // warp-uniform queue state: rays [q_next, q_end) of view q_view
     uint32_t q_view = 0, q_next = 0, q_end = 0;
-    bool q_empty = false;
+    bool q_empty = false, q_inside = false;  // q_inside: origin_inside_safe() for q_view's camera
     // lane state
     bool active = false;
     // path: kind of the current ray (0 primary, then shadow or bounce number) in bits
@@ -223,7 +224,7 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
     // yet subtracted (lane 0)
     __shared__ ResidentWarp s_resident[16];  // warps_per_block <= 16 (checked when planning)
     ResidentWarp& rw = s_resident[threadIdx.x >> 5];
-    if (kResident && lane == 0) rw = ResidentWarp{0, 0, kNoChunk, 0, 0, 1000, kNoView, 0, kNoView};
+    if (kResident && lane == 0) rw = ResidentWarp{0, 0, kNoChunk, 0, 0, 1000, kNoView, 0, kNoView, 0};
     // resident launches: the entry of the view the warp takes rays from (q_view), so
     // that ray setup reads shared memory instead of making L2 round trips
     __shared__ ViewDev s_views[16];
@@ -357,6 +358,22 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                     }
                     const ViewDev* qv = kResident ? &sview : p.views + lo;
                     q_end = min(q_next + p.chunk_rays, vget<kResident>(&qv->n_rays, true));
+                    // the view's camera origin, shared by its rays: inside the clip box?
+                    // (a resident view's world index is checked before it is used)
+                    const uint32_t qworld = vget<kResident>(&qv->world, true);
+                    const bool inside = (!kResident || qworld < p.n_worlds) &&
+                                        origin_inside_safe(p.worlds[qworld], vget<kResident>(&qv->cam.origin[0], true),
+                                                           vget<kResident>(&qv->cam.origin[1], true),
+                                                           vget<kResident>(&qv->cam.origin[2], true),
+                                                           vget<kResident>(&qv->cam.world_origin[0], true),
+                                                           vget<kResident>(&qv->cam.world_origin[1], true),
+                                                           vget<kResident>(&qv->cam.world_origin[2], true));
+                    if (kResident) {  // kept with the warp's other shared state (registers are short)
+                        if (lane == 0) rw.q_inside = inside ? 1u : 0u;
+                        __syncwarp();
+                    } else {
+                        q_inside = inside;
+                    }
                     continue;
                 }
                 const uint32_t take = min(q_end - q_next, (uint32_t)__popc(idle));
@@ -415,7 +432,7 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                         camera_ray(d0, du, dv, px, py, dx, dy, dz);
                         if (ray_start<kGlsl>(s, w, vget<kResident>(&v->cam.origin[0], true),
                                              vget<kResident>(&v->cam.origin[1], true), vget<kResident>(&v->cam.origin[2], true),
-                                             dx, dy, dz, wox, woy, woz))
+                                             dx, dy, dz, wox, woy, woz, kResident ? rw.q_inside != 0 : q_inside))
                             path |= kSafe;
                         active = true;
                     }

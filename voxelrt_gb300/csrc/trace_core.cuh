@@ -58,6 +58,20 @@ struct TraceCounters {
     uint32_t occ_fetches;
 };
 
+// 1/sqrt(l2) for the normalisation of camera rays: the integer first estimate
+// 0x5F3759DF - (bits(l2) >> 1) (C. Lomont, "Fast Inverse Square Root", 2003), then
+// three Newton steps r <- r * (1.5 - (l2/2) * r*r), each one exactly rounded multiply,
+// one fused multiply-add and one multiply, so any IEEE machine gets the same bits.
+// For l2 in [2^-126, 2^126] the result is within 2.5 ulp of 1/sqrt(l2); the reference
+// normalises with a 14-bit hardware estimate (SIMD.h normalize, rsqrt14).
+__device__ __forceinline__ float camera_rsqrt(float l2) {
+    const float h = __fmul_rn(0.5f, l2);
+    float r = __uint_as_float(0x5F3759DFu - (__float_as_uint(l2) >> 1));
+#pragma unroll
+    for (int i = 0; i < 3; i++) r = __fmul_rn(r, __fmaf_rn(-h, __fmul_rn(r, r), 1.5f));
+    return r;
+}
+
 // Ray entry point of a camera pixel (the ray generation of vrt_camera) from the
 // camera's d0, du, dv vectors.
 __device__ __forceinline__ void camera_ray(const float* d0, const float* du, const float* dv, uint32_t px,
@@ -67,10 +81,10 @@ __device__ __forceinline__ void camera_ray(const float* d0, const float* du, con
     float x = __fadd_rn(__fadd_rn(d0[0], __fmul_rn(u, du[0])), __fmul_rn(v, dv[0]));
     float y = __fadd_rn(__fadd_rn(d0[1], __fmul_rn(u, du[1])), __fmul_rn(v, dv[1]));
     float z = __fadd_rn(__fadd_rn(d0[2], __fmul_rn(u, du[2])), __fmul_rn(v, dv[2]));
-    float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
-    dx = __fdiv_rn(x, len);
-    dy = __fdiv_rn(y, len);
-    dz = __fdiv_rn(z, len);
+    const float r = camera_rsqrt(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
+    dx = __fmul_rn(x, r);
+    dy = __fmul_rn(y, r);
+    dz = __fmul_rn(z, r);
 }
 __device__ __forceinline__ void camera_ray(const vrt_camera& cam, uint32_t px, uint32_t py, float& dx,
                                            float& dy, float& dz) {
@@ -96,10 +110,26 @@ struct RayState {
 // and the position o + t*dir is finite or an infinity (never NaN) that leaves the grid.
 constexpr float kSafeOrigin = 0x1p30f, kSafeInvDir = 0x1p95f;
 
+// The clip box [1 - worldOrigin, size - 1 - worldOrigin] (VoxelTraversal.glsl:166) holds
+// the origin strictly inside, and the origin is within the safe bound: ray_init then
+// needs neither the slab test nor the origin's bound check.  Camera rays of a view
+// share their origin, so the persistent kernel evaluates this once per queue chunk.
+__device__ __forceinline__ bool origin_inside_safe(const DevWorld& w, float ox, float oy, float oz, int32_t wox,
+                                                   int32_t woy, int32_t woz) {
+    const float lx = __int2float_rn(1 - wox), ly = __int2float_rn(1 - woy), lz = __int2float_rn(1 - woz);
+    const float hx = __fsub_rn(__fsub_rn(__uint2float_rn(w.size_x), __int2float_rn(wox)), 1.0f);
+    const float hy = __fsub_rn(__fsub_rn(__uint2float_rn(w.size_y), __int2float_rn(woy)), 1.0f);
+    const float hz = __fsub_rn(__fsub_rn(__uint2float_rn(w.size_z), __int2float_rn(woz)), 1.0f);
+    return lx < ox && ox < hx && ly < oy && oy < hy && lz < oz && oz < hz && fabsf(ox) < kSafeOrigin &&
+           fabsf(oy) < kSafeOrigin && fabsf(oz) < kSafeOrigin;
+}
+
 // invDir, tStart and the clipped start position (VoxelTraversal.glsl:133-145,163-167).
 // Returns whether the ray is safe in the sense above (ray_step<kCount, true> applies).
+// inside_safe: origin_inside_safe() is known to hold for this origin.
 __device__ __forceinline__ bool ray_init(RayState& s, const DevWorld& w, float ox, float oy, float oz, float dx,
-                                         float dy, float dz, int32_t wox, int32_t woy, int32_t woz) {
+                                         float dy, float dz, int32_t wox, int32_t woy, int32_t woz,
+                                         bool inside_safe = false) {
     s.ox = ox;
     s.oy = oy;
     s.oz = oz;
@@ -113,18 +143,19 @@ __device__ __forceinline__ bool ray_init(RayState& s, const DevWorld& w, float o
     s.tsx = __fmul_rn(__fsub_rn(dx < 0.0f ? 0.0f : 1.0f, ox), s.ix);
     s.tsy = __fmul_rn(__fsub_rn(dy < 0.0f ? 0.0f : 1.0f, oy), s.iy);
     s.tsz = __fmul_rn(__fsub_rn(dz < 0.0f ? 0.0f : 1.0f, oz), s.iz);
-    // clip box [1 - worldOrigin, size - 1 - worldOrigin] (VoxelTraversal.glsl:166)
-    const float lx = __int2float_rn(1 - wox), ly = __int2float_rn(1 - woy), lz = __int2float_rn(1 - woz);
-    const float hx = __fsub_rn(__fsub_rn(__uint2float_rn(w.size_x), __int2float_rn(wox)), 1.0f);
-    const float hy = __fsub_rn(__fsub_rn(__uint2float_rn(w.size_y), __int2float_rn(woy)), 1.0f);
-    const float hz = __fsub_rn(__fsub_rn(__uint2float_rn(w.size_z), __int2float_rn(woz)), 1.0f);
-    // An origin strictly inside the box never clips: per axis l - o < 0 < h - o, so
-    // min(t1, t2) is negative (or -inf, or NaN when dir is NaN, which minps/maxps drop)
-    // and tmin <= 0 on every path.  Camera rays of a view share the origin, so the
-    // slab test below runs only for views from outside the world.
+    // An origin strictly inside the clip box never clips: per axis l - o < 0 < h - o,
+    // so min(t1, t2) is negative (or -inf, or NaN when dir is NaN, which minps/maxps
+    // drop) and tmin <= 0 on every path.  Camera rays of a view share the origin, so
+    // the slab test below runs only for views from outside the world.
     bool clip = false;
     float tmin = 0.0f;
-    if (!(lx < ox && ox < hx && ly < oy && oy < hy && lz < oz && oz < hz)) {
+    bool origin_ok = true;
+    if (!inside_safe && !origin_inside_safe(w, ox, oy, oz, wox, woy, woz)) {
+        // clip box [1 - worldOrigin, size - 1 - worldOrigin] (VoxelTraversal.glsl:166)
+        const float lx = __int2float_rn(1 - wox), ly = __int2float_rn(1 - woy), lz = __int2float_rn(1 - woz);
+        const float hx = __fsub_rn(__fsub_rn(__uint2float_rn(w.size_x), __int2float_rn(wox)), 1.0f);
+        const float hy = __fsub_rn(__fsub_rn(__uint2float_rn(w.size_y), __int2float_rn(woy)), 1.0f);
+        const float hz = __fsub_rn(__fsub_rn(__uint2float_rn(w.size_z), __int2float_rn(woz)), 1.0f);
         const float t1x = __fmul_rn(__fsub_rn(lx, ox), s.ix);
         const float t1y = __fmul_rn(__fsub_rn(ly, oy), s.iy);
         const float t1z = __fmul_rn(__fsub_rn(lz, oz), s.iz);
@@ -134,6 +165,7 @@ __device__ __forceinline__ bool ray_init(RayState& s, const DevWorld& w, float o
         tmin = max_x86(min_x86(t1x, t2x), max_x86(min_x86(t1y, t2y), min_x86(t1z, t2z)));
         const float tmax = min_x86(max_x86(t1x, t2x), min_x86(max_x86(t1y, t2y), max_x86(t1z, t2z)));
         clip = tmin > 0.0f && tmin < tmax;
+        origin_ok = fabsf(ox) < kSafeOrigin && fabsf(oy) < kSafeOrigin && fabsf(oz) < kSafeOrigin;
     }
     s.cx = clip ? __fadd_rn(ox, __fmul_rn(dx, tmin)) : ox;
     s.cy = clip ? __fadd_rn(oy, __fmul_rn(dy, tmin)) : oy;
@@ -144,16 +176,16 @@ __device__ __forceinline__ bool ray_init(RayState& s, const DevWorld& w, float o
     s.gy = dy < 0.0f ? -1 : 0;
     s.gz = dz < 0.0f ? -1 : 0;
     s.material = 0;
-    return fabsf(ox) < kSafeOrigin && fabsf(oy) < kSafeOrigin && fabsf(oz) < kSafeOrigin &&
-           fabsf(s.ix) < kSafeInvDir && fabsf(s.iy) < kSafeInvDir && fabsf(s.iz) < kSafeInvDir;
+    return origin_ok && fabsf(s.ix) < kSafeInvDir && fabsf(s.iy) < kSafeInvDir && fabsf(s.iz) < kSafeInvDir;
 }
 
 // GLSL mode (VoxelTraversal.glsl rayCast): the start voxel worldOrigin + floor(start),
 // from which iteration 0 takes its side distances (:164-167).
 template <bool kGlsl>
 __device__ __forceinline__ bool ray_start(RayState& s, const DevWorld& w, float ox, float oy, float oz, float dx,
-                                          float dy, float dz, int32_t wox, int32_t woy, int32_t woz) {
-    const bool safe = ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
+                                          float dy, float dz, int32_t wox, int32_t woy, int32_t woz,
+                                          bool inside_safe = false) {
+    const bool safe = ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz, inside_safe);
     if (kGlsl) {
         s.vx = wadd(wox, floor2i(s.cx));
         s.vy = wadd(woy, floor2i(s.cy));
