@@ -337,7 +337,7 @@ def run_ours(args):
         batch.run(host_np, stream)
     e2e_s = max_over_ranks(pg, (time.perf_counter() - t0) / ke)
     e2e = {"value": job_rays / e2e_s / 1e9, "unit": "Grays/s", "ms_per_step": e2e_s * 1e3,
-           "h2d_bytes_per_step": 120 * len(wl.views), "d2h_bytes_per_step": n_rec * HIT_BYTES,
+           "h2d_bytes_per_step": 128 * len(wl.views), "d2h_bytes_per_step": n_rec * HIT_BYTES,
            "api": "vrt_batch_update_cameras + vrt_batch_run (pinned host records)"}
     link = d2h_link_gbs(torch, stream)
     e2e["d2h_link_gbs"] = link

@@ -363,7 +363,7 @@ vrt_status vrt_batch_measure(vrt_batch* batch, vrt_hit* hits_device, void* strea
  * no memory: no counterpart in the reference.  For callers that cannot call
  * cudaMalloc once their frame loop runs (it may synchronise the device) or whose
  * host application owns all device memory.  The launch scratch (world table, view
- * table, tile-queue counter) lives in one fixed 140.5 KiB device array that every GPU
+ * table, tile-queue counter) lives in one fixed 148.5 KiB device array that every GPU
  * loading the library holds until the process exits, so a call takes at most 256
  * worlds and 1024 views (VRT_ERR_INVALID_ARG beyond).  The first call on a device
  * looks up that array's address; make it before any stream capture.  All calls

@@ -55,26 +55,26 @@ template <bool kGlsl>
 __global__ void __launch_bounds__(64) view_path_kernel(DevWorld w, ViewDev v, uint4* __restrict__ out) {
     const uint32_t px = blockIdx.x * 8 + threadIdx.x;
     const uint32_t py = blockIdx.y * 8 + threadIdx.y;
-    if (px >= v.cam.width || py >= v.cam.height) return;
-    const uint32_t pixel = py * v.cam.width + px;
-    const uint64_t plane = (uint64_t)v.cam.width * v.cam.height;
-    const int32_t wox = v.cam.world_origin[0], woy = v.cam.world_origin[1], woz = v.cam.world_origin[2];
+    if (px >= v.width || py >= v.height) return;
+    const uint32_t pixel = py * v.width + px;
+    const uint64_t plane = (uint64_t)v.width * v.height;
+    const int32_t wox = v.wo[0], woy = v.wo[1], woz = v.wo[2];
     TraceCounters cnt{0, 0};
-    float ox = v.cam.origin[0], oy = v.cam.origin[1], oz = v.cam.origin[2], dx, dy, dz;
-    camera_ray(v.cam, px, py, dx, dy, dz);
+    float ox = v.ox, oy = v.oy, oz = v.oz, dx, dy, dz;
+    camera_ray(v.d0, v.du, v.dv, px, py, dx, dy, dz);
     RayState s;
     bool safe = ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
     uint32_t steps;
     bool hit = run_ray<false, kGlsl>(s, safe, w, wox, woy, woz, v.max_iters, steps, cnt);
     uint4* o = out + v.out_base + pixel;
     o[0] = pack_state<kGlsl>(s, hit, steps, pixel);
-    const uint32_t last = v.shadow ? 1u : v.n_bounces;
+    const uint32_t last = v.last_kind();
     for (uint32_t k = 1; k <= last; k++) {
         if (!hit) {
             o[k * plane] = no_ray_hit();
             continue;
         }
-        next_path_ray<kGlsl>(s, v.shadow != 0, v.sun, pixel, k, ox, oy, oz, dx, dy, dz);
+        next_path_ray<kGlsl>(s, v.shadow() != 0, v.sun, pixel, k, ox, oy, oz, dx, dy, dz);
         safe = ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
         hit = run_ray<false, kGlsl>(s, safe, w, wox, woy, woz, v.max_iters, steps, cnt);
         o[k * plane] = pack_state<kGlsl>(s, hit, steps, pixel);
@@ -95,6 +95,14 @@ template <bool kResident, typename T>
 __device__ __forceinline__ T vget(const T* a, bool shared) {
     if (!kResident) return __ldg(a);
     return shared ? *a : __ldcg(a);
+}
+
+// A 16-byte (or 8-byte) group of view-table fields: from global memory through the
+// read-only path, or from the warp's shared copy (resident launches).
+template <bool kResident, typename V>
+__device__ __forceinline__ V vget4(const V* a) {
+    if (!kResident) return __ldg(a);
+    return *a;
 }
 
 constexpr uint32_t kClaimEmpty = 0xFFFFFFFFu, kClaimStop = 0xFFFFFFFEu;
@@ -360,14 +368,11 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                     q_end = min(q_next + p.chunk_rays, vget<kResident>(&qv->n_rays, true));
                     // the view's camera origin, shared by its rays: inside the clip box?
                     // (a resident view's world index is checked before it is used)
-                    const uint32_t qworld = vget<kResident>(&qv->world, true);
-                    const bool inside = (!kResident || qworld < p.n_worlds) &&
-                                        origin_inside_safe(p.worlds[qworld], vget<kResident>(&qv->cam.origin[0], true),
-                                                           vget<kResident>(&qv->cam.origin[1], true),
-                                                           vget<kResident>(&qv->cam.origin[2], true),
-                                                           vget<kResident>(&qv->cam.world_origin[0], true),
-                                                           vget<kResident>(&qv->cam.world_origin[1], true),
-                                                           vget<kResident>(&qv->cam.world_origin[2], true));
+                    const int4 qwv = vget4<kResident>(reinterpret_cast<const int4*>(qv->wo));  // origin xyz, world
+                    const bool inside = (!kResident || (uint32_t)qwv.w < p.n_worlds) &&
+                                        origin_inside_safe(p.worlds[qwv.w], vget<kResident>(&qv->ox, true),
+                                                           vget<kResident>(&qv->oy, true), vget<kResident>(&qv->oz, true),
+                                                           qwv.x, qwv.y, qwv.z);
                     if (kResident) {  // kept with the warp's other shared state (registers are short)
                         if (lane == 0) rw.q_inside = inside ? 1u : 0u;
                         __syncwarp();
@@ -382,9 +387,10 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                 const uint32_t assigned = __ballot_sync(0xffffffffu, mine);
                 if (mine) {
                     const ViewDev* v = kResident ? &sview : p.views + q_view;
+                    // width, height, tiles_x, tiles_x_magic
+                    const uint4 geo = vget4<kResident>(reinterpret_cast<const uint4*>(&v->width));
                     const uint32_t r = q_next + rank;
                     const uint32_t t = r >> p.tile_size_log2, k = r & ((1u << p.tile_size_log2) - 1u);
-                    const uint32_t tiles_x = vget<kResident>(&v->tiles_x, true);
                     uint32_t kx, ky;
                     if (p.morton) {
                         kx = compact_even_bits(k);
@@ -395,18 +401,18 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                     }
                     const uint32_t tw = 1u << p.tile_w_log2, th = 1u << (p.tile_size_log2 - p.tile_w_log2);
                     // t / tiles_x by multiply-high: the estimate is the quotient or one more
-                    const uint32_t magic = vget<kResident>(&v->tiles_x_magic, true);
-                    uint32_t trow = magic ? __umulhi(t, magic) : t;
-                    if (trow * tiles_x > t) trow--;
-                    const uint32_t px = (t - trow * tiles_x) * tw + kx, py = trow * th + ky;
-                    const uint32_t width = vget<kResident>(&v->cam.width, true), height = vget<kResident>(&v->cam.height, true);
+                    uint32_t trow = geo.w ? __umulhi(t, geo.w) : t;
+                    if (trow * geo.z > t) trow--;
+                    const uint32_t px = (t - trow * geo.z) * tw + kx, py = trow * th + ky;
+                    const uint32_t width = geo.x, height = geo.y;
                     bool valid = px < width && py < height;
+                    const int4 wv = vget4<kResident>(reinterpret_cast<const int4*>(v->wo));  // origin xyz, world
+                    const uint2 mp = vget4<kResident>(reinterpret_cast<const uint2*>(&v->max_iters));  // cap, path
                     if (kResident && valid) {
                         // a resident launch's views arrive while it runs: check what the
                         // ray would index (its world, its records) before touching it
-                        const uint32_t kinds =
-                            1u + (vget<kResident>(&v->shadow, true) ? 1u : vget<kResident>(&v->n_bounces, true));
-                        valid = vget<kResident>(&v->world, true) < p.n_worlds &&
+                        const uint32_t kinds = 1u + ((mp.y >> 8) & 0xFFu);
+                        valid = (uint32_t)wv.w < p.n_worlds &&
                                 vget<kResident>(&v->out_base, true) + (unsigned long long)width * height * kinds <=
                                     p.out_records;
                     }
@@ -415,24 +421,21 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                         pixel = py * width + px;
                         plane = width * height;
                         iter = 0;
-                        max_iters = vget<kResident>(&v->max_iters, true);
-                        const uint32_t shadow = vget<kResident>(&v->shadow, true);
-                        path = (shadow ? 1u : vget<kResident>(&v->n_bounces, true)) << 8 | shadow << 16;
-                        w = p.worlds[vget<kResident>(&v->world, true)];
-                        wox = vget<kResident>(&v->cam.world_origin[0], true);
-                        woy = vget<kResident>(&v->cam.world_origin[1], true);
-                        woz = vget<kResident>(&v->cam.world_origin[2], true);
-                        float d0[3], du[3], dv[3];
-                        for (int c = 0; c < 3; c++) {
-                            d0[c] = vget<kResident>(&v->cam.d0[c], true);
-                            du[c] = vget<kResident>(&v->cam.du[c], true);
-                            dv[c] = vget<kResident>(&v->cam.dv[c], true);
-                        }
+                        max_iters = mp.x;
+                        path = mp.y;
+                        w = p.worlds[wv.w];
+                        wox = wv.x;
+                        woy = wv.y;
+                        woz = wv.z;
+                        // d0, du, dv with the camera origin in the fourth lanes
+                        const float4 g0 = vget4<kResident>(reinterpret_cast<const float4*>(v->d0));
+                        const float4 g1 = vget4<kResident>(reinterpret_cast<const float4*>(v->du));
+                        const float4 g2 = vget4<kResident>(reinterpret_cast<const float4*>(v->dv));
+                        const float d0[3] = {g0.x, g0.y, g0.z}, du[3] = {g1.x, g1.y, g1.z}, dv[3] = {g2.x, g2.y, g2.z};
                         float dx, dy, dz;
                         camera_ray(d0, du, dv, px, py, dx, dy, dz);
-                        if (ray_start<kGlsl>(s, w, vget<kResident>(&v->cam.origin[0], true),
-                                             vget<kResident>(&v->cam.origin[1], true), vget<kResident>(&v->cam.origin[2], true),
-                                             dx, dy, dz, wox, woy, woz, kResident ? rw.q_inside != 0 : q_inside))
+                        if (ray_start<kGlsl>(s, w, g0.w, g1.w, g2.w, dx, dy, dz, wox, woy, woz,
+                                             kResident ? rw.q_inside != 0 : q_inside))
                             path |= kSafe;
                         active = true;
                     }
@@ -505,19 +508,37 @@ uint32_t log2u(uint32_t v) {
     return r;
 }
 
+}  // namespace
+
+void set_view_camera(ViewDev& d, const vrt_camera& c) {
+    for (int k = 0; k < 3; k++) {
+        d.d0[k] = c.d0[k];
+        d.du[k] = c.du[k];
+        d.dv[k] = c.dv[k];
+        d.wo[k] = c.world_origin[k];
+    }
+    d.ox = c.origin[0];
+    d.oy = c.origin[1];
+    d.oz = c.origin[2];
+    d.width = c.width;
+    d.height = c.height;
+}
+
 ViewDev make_view_dev(const vrt_view& v) {
     ViewDev d{};
-    d.cam = v.cam;
+    set_view_camera(d, v.cam);
     d.world = v.world;
     d.max_iters = eff_iters(v.max_iters, view_glsl(v));
-    d.n_bounces = (v.flags & VRT_VIEW_SHADOW) ? 0 : v.n_bounces;
-    d.shadow = (v.flags & VRT_VIEW_SHADOW) ? 1 : 0;
+    const uint32_t shadow = (v.flags & VRT_VIEW_SHADOW) ? 1u : 0u;
+    d.path = (shadow ? 1u : v.n_bounces) << 8 | shadow << 16;
     for (int c = 0; c < 3; c++) d.sun[c] = v.sun_dir[c];
     return d;
 }
 
+namespace {
+
 vrt_status launch_view_path(vrt_world* w, const ViewDev& v, bool glsl, vrt_hit* hits, cudaStream_t stream) {
-    dim3 block(8, 8), grid((v.cam.width + 7) / 8, (v.cam.height + 7) / 8);
+    dim3 block(8, 8), grid((v.width + 7) / 8, (v.height + 7) / 8);
     if (glsl)
         view_path_kernel<true><<<grid, block, 0, stream>>>(w->dev(), v, reinterpret_cast<uint4*>(hits));
     else
@@ -598,8 +619,8 @@ vrt_status plan_views(const vrt_view* views, uint32_t n, uint32_t n_worlds, cons
     uint64_t chunks = 0, records = 0;
     for (uint32_t i = 0; i < n; i++) {
         ViewDev d = make_view_dev(views[i]);
-        const uint32_t tx = (d.cam.width + cfg.tile_w - 1) / cfg.tile_w;
-        const uint32_t ty = (d.cam.height + cfg.tile_h - 1) / cfg.tile_h;
+        const uint32_t tx = (d.width + cfg.tile_w - 1) / cfg.tile_w;
+        const uint32_t ty = (d.height + cfg.tile_h - 1) / cfg.tile_h;
         const uint64_t tiles = (uint64_t)tx * ty;
         d.tiles_x = tx;
         d.tiles_x_magic = div_magic(tx);
@@ -842,14 +863,19 @@ vrt_status vrt_batch_update_cameras(vrt_batch* b, const vrt_camera* cams, void* 
         set_error("null argument");
         return VRT_ERR_INVALID_ARG;
     }
-    for (size_t i = 0; i < b->plan.views.size(); i++)
-        if (cams[i].width != b->plan.views[i].cam.width || cams[i].height != b->plan.views[i].cam.height) {
+    for (size_t i = 0; i < b->plan.views.size(); i++) {
+        if (cams[i].width != b->plan.views[i].width || cams[i].height != b->plan.views[i].height) {
             set_error("camera resolution differs from the batch's view");
             return VRT_ERR_INVALID_ARG;
         }
+        if (!world_origin_ok(cams[i].world_origin)) {
+            set_error("camera world origin outside +-2^30");
+            return VRT_ERR_INVALID_ARG;
+        }
+    }
     VRT_CUDA(cudaSetDevice(b->device));
     for (size_t i = 0; i < b->plan.views.size(); i++) {
-        b->plan.views[i].cam = cams[i];
+        set_view_camera(b->plan.views[i], cams[i]);
         b->views[i].cam = cams[i];
     }
     cudaStream_t stream = (cudaStream_t)stream_;

@@ -10,21 +10,35 @@
 
 namespace vrt {
 
-// Device view-table entry of the persistent kernel.
-struct ViewDev {
-    vrt_camera cam;
+// Device view-table entry of the persistent kernel: 128 bytes, 16-byte aligned, so ray
+// setup reads it with 128-bit loads (the camera's ray generation in the first three
+// vectors, world origin and world index in the fourth, the tile geometry in the fifth).
+struct alignas(16) ViewDev {
+    float d0[3], ox;          // camera: d0 and origin.x
+    float du[3], oy;          // du and origin.y
+    float dv[3], oz;          // dv and origin.z
+    int32_t wo[3];            // camera world origin
     uint32_t world;
-    uint32_t max_iters;
-    uint32_t n_bounces;
-    uint32_t shadow;
-    float sun[3];
+    uint32_t width, height;
     uint32_t tiles_x;
-    uint32_t tiles_x_magic;  // ceil(2^32 / tiles_x): tile row by a multiply-high
-    uint32_t n_rays;         // tile-padded ray space of the view
-    uint32_t chunk_base;     // first queue chunk of the view
-    uint64_t out_base;       // first record of the view
+    uint32_t tiles_x_magic;   // ceil(2^32 / tiles_x): tile row by a multiply-high
+    uint32_t max_iters;
+    uint32_t path;            // last kind of a pixel's path << 8 | shadow << 16
+    uint32_t n_rays;          // tile-padded ray space of the view
+    uint32_t chunk_base;      // first queue chunk of the view
+    uint64_t out_base;        // first record of the view
+    float sun[3];
+    uint32_t pad[3];
+    VRT_HD uint32_t shadow() const { return (path >> 16) & 1u; }
+    VRT_HD uint32_t last_kind() const { return (path >> 8) & 0xFFu; }
 };
-static_assert(sizeof(ViewDev) == 120, "view table entry is 120 bytes (copied per camera update)");
+static_assert(sizeof(ViewDev) == 128, "view table entry is 128 bytes (copied per camera update)");
+
+// The camera fields of a view-table entry.
+void set_view_camera(ViewDev& d, const vrt_camera& c);
+// A view-table entry for view `v` (camera, world, path, iteration cap, sun); the
+// planner adds the tile and queue fields.
+ViewDev make_view_dev(const vrt_view& v);
 
 // ceil(2^32 / d) for 2 <= d < 2^32; 0 marks d == 1 (the quotient is the numerator).
 inline uint32_t div_magic(uint32_t d) {

@@ -106,13 +106,7 @@ extern "C" vrt_status vrt_render_views_static(vrt_world* const* worlds, uint32_t
     for (uint32_t i = 0; i < n_views; i++) {
         const vrt_view& v = views[i];
         ViewDev& d = g_state.views[i];
-        d = ViewDev{};
-        d.cam = v.cam;
-        d.world = v.world;
-        d.max_iters = eff_iters(v.max_iters, glsl);
-        d.n_bounces = (v.flags & VRT_VIEW_SHADOW) ? 0 : v.n_bounces;
-        d.shadow = (v.flags & VRT_VIEW_SHADOW) ? 1 : 0;
-        for (int c = 0; c < 3; c++) d.sun[c] = v.sun_dir[c];
+        d = make_view_dev(v);
         const uint32_t tx = (v.cam.width + cfg.tile_w - 1) / cfg.tile_w;
         const uint32_t ty = (v.cam.height + cfg.tile_h - 1) / cfg.tile_h;
         const uint64_t tiles = (uint64_t)tx * ty;

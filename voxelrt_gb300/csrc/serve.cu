@@ -394,7 +394,7 @@ bool resident_publish(vrt_server* sv, const std::vector<Request*>& rs, vrt_statu
         d.out_base = (uint64_t)(rs[i]->page_base - 1) * kPageRecords;
         R.h_views[base + i] = d;
         R.h_cb[base + i] = d.chunk_base;
-        R.h_rem[base + i] = d.cam.width * d.cam.height;
+        R.h_rem[base + i] = d.width * d.height;
         __atomic_store_n(R.done + base + i, 0u, __ATOMIC_RELAXED);
     }
     cudaError_t e = cudaMemcpyAsync((ViewDev*)R.views.ptr + base, R.h_views + base, n * sizeof(ViewDev),

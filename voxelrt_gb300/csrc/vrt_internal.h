@@ -60,7 +60,7 @@ VRT_HD inline uint32_t skip_levels(uint32_t lo, uint32_t hi, uint32_t idx) {
 }
 
 // Kernel-side view of one world (passed by value or stored in a world table).
-struct DevWorld {
+struct alignas(16) DevWorld {
     const uint32_t* bricks;
     const uint32_t* codes;
     const uint8_t* payload;
