@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-per-view", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the request-server run")
+    ap.add_argument("--no-stress", action="store_true", help="incoherent: skip the 2^26 stress rays")
     ap.add_argument("--serve-rates", default="50,200,1000,2000", help="render requests per second to sweep")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="duration of each arrival-rate run")
     ap.add_argument("--serve-worlds", type=int, default=32)
@@ -358,6 +359,10 @@ def run_ours(args):
                "sample": f"{nv} smallest views of the workload, {r} rays, CPU oracle (scalar restatement of "
                          f"CpuRenderer.cpp RayCast) on all host threads"}
 
+    stress = None
+    if rank == 0 and args.workload == "incoherent" and not args.no_stress:
+        stress = run_stress(v, worlds[0], wl.worlds[0], args, stream)
+
     serving = None
     if rank == 0 and not args.no_serving and args.workload == "uneven_batch":
         del hits, host_np, host, batch
@@ -383,6 +388,7 @@ def run_ours(args):
             "batched_over_per_view": (value / per_view["value"]) if per_view else None,
             "parity_sample": parity,
             "serving": serving,
+            "stress": stress,
             "traversal": {"step_calls": meas["step_calls"], "occ_fetches": meas["occ_fetches"],
                           "hits": meas["hits"], "mean_steps_per_ray": meas["step_calls"] / max(rays_per_step, 1)},
         }
@@ -568,6 +574,49 @@ def edit_latency(v, worlds, edges, surf):
     return edit_lat
 
 
+def hits_match(got, want) -> bool:
+    """Integer fields bit-exact, t within 1e-6 relative (the parity bar)."""
+    ok = True
+    for f in ("voxel", "face", "material", "steps", "tag"):
+        ok &= bool(np.array_equal(got[f], want[f]))
+    fin = np.isfinite(want["t"])
+    ok &= bool(np.array_equal(np.isfinite(got["t"]), fin))
+    ok &= bool(np.allclose(got["t"][fin], want["t"][fin], rtol=1e-6, atol=0))
+    return ok
+
+
+def run_stress(v, world, data, args, stream, n=1 << 26, steps=3):
+    """The incoherent workload's stress set: 2^26 rays with origins uniform in the world box and
+    directions uniform on the sphere, cast with vrt_cast_device (thread per ray) from device
+    memory; 64 Ki of them are checked against the CPU oracle."""
+    import torch
+
+    from oracle.oracle import OracleWorld
+    size = [c * 32 for c in data.sectors]
+    rays = v.random_rays(size, seed=9, n=n)
+    d_rays = torch.from_numpy(rays.view(np.uint8)).cuda()
+    d_hits = torch.empty(n * HIT_BYTES, dtype=torch.uint8, device="cuda")
+    with torch.cuda.stream(stream):
+        world.cast_device(d_rays, n, d_hits, stream=stream)
+        world.cast_device(d_rays, n, d_hits, stream=stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            world.cast_device(d_rays, n, d_hits, stream=stream)
+        e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    sub = rays[: 1 << 16]
+    got = d_hits[: sub.size * HIT_BYTES].cpu().numpy().view(v.HIT_DTYPE)
+    o = OracleWorld(data.sectors)
+    o.upload(data)
+    ok = hits_match(got, o.cast(sub))
+    o.close()
+    return {"rays": n, "ms": ms, "value": n / (ms * 1e-3) / 1e9, "unit": "Grays/s",
+            "api": "vrt_cast_device, rays and records in device memory", "checked_rays": int(sub.size),
+            "bit_exact": ok}
+
+
 def parity_sample(wl, batch, hits, stream, max_views=3):
     """Compare a few views of one batch launch with the CPU oracle."""
     import voxelrt_gb300 as v
@@ -588,11 +637,7 @@ def parity_sample(wl, batch, hits, stream, max_views=3):
             want = o.render_view(vw.cam, vw.max_iters)[None]
         a, b = int(batch.offsets[i]), int(batch.offsets[i + 1])
         got = hits[a * HIT_BYTES:b * HIT_BYTES].cpu().numpy().view(v.HIT_DTYPE).reshape(want.shape)
-        for f in ("voxel", "face", "material", "steps", "tag"):
-            ok &= bool(np.array_equal(got[f], want[f]))
-        fin = np.isfinite(want["t"])
-        ok &= bool(np.array_equal(np.isfinite(got["t"]), fin))
-        ok &= bool(np.allclose(got["t"][fin], want["t"][fin], rtol=1e-6, atol=0))
+        ok &= hits_match(got, want)
         rays += want.size
         o.close()
     return {"views": len(order), "records": rays, "bit_exact": ok}

@@ -196,3 +196,26 @@ def test_maximum_world_extent(gpu, glsl):
     rays = v.random_rays((2048, 1024, 2048), seed=17, n=60_000)
     assert_hits_equal(w.cast(rays, max_iters=400, glsl=glsl), o.cast(rays, max_iters=400, glsl=glsl))
     w.close()
+
+
+@pytest.mark.parametrize("glsl", [False, True])
+@pytest.mark.parametrize("max_iters", [0, 5])
+def test_large_casts_take_the_persistent_kernel(cfg0, glsl, max_iters):
+    """Casts of 2^18 rays and more run the persistent cast kernel (lanes refilled as rays
+    end): a ragged count, random and degenerate directions, rays from inside solid, a
+    non-zero world origin, iteration caps."""
+    _, w, o = cfg0
+    rng = np.random.default_rng(17 + glsl + max_iters)
+    n = (1 << 18) + 37
+    rays = v.random_rays((256, 256, 256), seed=21, n=n)
+    d = rays["dir"].copy()
+    zero = rng.random(d.shape) < 0.05
+    d[zero] = np.where(rng.random(zero.sum()) < 0.5, 0.0, -0.0)
+    d[(d == 0).all(1)] = [0, -1, 0]
+    rays["dir"] = d
+    rays["tag"] = rng.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32)
+    for wo in ((0, 0, 0), (-40, 12, 300)):
+        r = rays.copy()
+        r["origin"] -= np.array(wo, np.float32)
+        assert_hits_equal(w.cast(r, world_origin=wo, max_iters=max_iters, glsl=glsl),
+                          o.cast(r, world_origin=wo, max_iters=max_iters, glsl=glsl))

@@ -7,6 +7,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 
 #include "trace_core.cuh"
@@ -48,6 +49,84 @@ __global__ void __launch_bounds__(256) cast_kernel(DevWorld w, const float4* __r
     out[i] = pack_hit<kGlsl>(r, a.w, b.x, b.y, __float_as_uint(b.z));
 }
 
+// Explicit rays whose lengths vary widely (random origins and directions: some hit at
+// once, others run to the iteration cap) leave most lanes of a thread-per-ray warp idle
+// behind its longest ray.  Here each warp walks its own grid-strided sequence of 32-ray
+// chunks (warp g takes rays [32 (g + k G), +32) for k = 0, 1, ...), traces in rounds
+// of `inner` DDA steps, and between rounds stores the records of the rays that ended
+// and refills those lanes from its chunks once fewer than `refill` lanes trace.  No
+// device queue: calls on different streams stay independent.  Same records as
+// cast_kernel: a lane's steps continue from where its ray left off, and a ray's record
+// is packed from the state at its exit.
+template <bool kGlsl>
+__global__ void __launch_bounds__(128) cast_persistent_kernel(DevWorld w, const float4* __restrict__ rays, uint32_t n,
+                                                             int32_t wox, int32_t woy, int32_t woz, uint32_t max_iters,
+                                                             uint32_t inner, uint32_t refill, uint4* __restrict__ out) {
+    const uint32_t lane = threadIdx.x & 31, lt = (1u << lane) - 1u;
+    const uint32_t stride = (gridDim.x * blockDim.x) & ~31u;  // rays between a warp's chunks
+    uint32_t next = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;  // first ray of the warp's next chunk
+    uint32_t q_next = 0, q_end = 0;
+    bool active = false, ended = false, hit = false, safe = false;
+    uint32_t ri = 0, iter = 0, tag = 0;
+    RayState s;
+    TraceCounters cnt{0, 0};
+    for (;;) {
+        if (ended) {
+            out[ri] = pack_state<kGlsl>(s, hit, iter, tag);
+            ended = false;
+            active = false;
+        }
+        const uint32_t act = __ballot_sync(0xffffffffu, active);
+        if ((uint32_t)__popc(act) < refill) {
+            uint32_t idle = ~act;
+            while (idle) {
+                if (q_next >= q_end) {
+                    if (next >= n) break;
+                    q_next = next;
+                    q_end = min(next + 32u, n);
+                    next = next + stride < next ? n : next + stride;  // no wrap past 2^32
+                }
+                const uint32_t take = min(q_end - q_next, (uint32_t)__popc(idle));
+                const uint32_t rank = __popc(idle & lt);
+                const bool mine = ((idle >> lane) & 1u) && rank < take;
+                const uint32_t assigned = __ballot_sync(0xffffffffu, mine);
+                if (mine) {
+                    ri = q_next + rank;
+                    const float4 a = __ldg(rays + 2 * (size_t)ri), b = __ldg(rays + 2 * (size_t)ri + 1);
+                    tag = __float_as_uint(b.z);
+                    safe = ray_start<kGlsl>(s, w, a.x, a.y, a.z, a.w, b.x, b.y, wox, woy, woz);
+                    iter = 0;
+                    active = true;
+                }
+                idle &= ~assigned;
+                q_next += take;
+            }
+        }
+        if (__ballot_sync(0xffffffffu, active) == 0) break;
+        const bool all_safe = __all_sync(0xffffffffu, !active || safe);
+        if (active) {
+            const uint32_t kmax = min(inner, max_iters - iter);
+            uint32_t k = 0, st = kStepContinue;
+            if (all_safe) {
+                for (; k < kmax; k++) {
+                    st = ray_step<false, true, kGlsl>(s, w, wox, woy, woz, cnt);
+                    if (st != kStepContinue) break;
+                }
+            } else {
+                for (; k < kmax; k++) {
+                    st = ray_step<false, false, kGlsl>(s, w, wox, woy, woz, cnt);
+                    if (st != kStepContinue) break;
+                }
+            }
+            iter += k;
+            if (st != kStepContinue || iter >= max_iters) {
+                ended = true;
+                hit = st == kStepHit;
+            }
+        }
+    }
+}
+
 vrt_status check_camera(const vrt_camera* cam) {
     if (!cam || cam->width == 0 || cam->height == 0 || cam->width > 16384 || cam->height > 16384 ||
         !world_origin_ok(cam->world_origin)) {
@@ -67,14 +146,34 @@ vrt_status launch_render(vrt_world* w, const vrt_camera* cam, uint32_t max_iters
     return VRT_OK;
 }
 
+// Launch shape of cast_persistent_kernel: measured on GB300 with the 2^26 random rays
+// of the incoherent workload.
+constexpr uint32_t kCastThreads = 128, kCastInner = 12, kCastRefill = 28;
+// Below this many rays the thread-per-ray kernel is used (too few rays to fill the
+// persistent grid's lanes twice).
+constexpr uint32_t kCastPersistentMin = 1u << 18;
+
 vrt_status launch_cast(vrt_world* w, const vrt_ray* rays, uint32_t n, const vrt_cast_params* p, vrt_hit* hits,
                        cudaStream_t stream) {
     if (n == 0) return VRT_OK;
     const bool glsl = (p->flags & VRT_CAST_GLSL) != 0;
-    auto kernel = glsl ? cast_kernel<true> : cast_kernel<false>;
-    kernel<<<(n + 255) / 256, 256, 0, stream>>>(w->dev(), reinterpret_cast<const float4*>(rays), n,
-                                                p->world_origin[0], p->world_origin[1], p->world_origin[2],
-                                                eff_iters(p->max_iters, glsl), reinterpret_cast<uint4*>(hits));
+    const float4* r4 = reinterpret_cast<const float4*>(rays);
+    uint4* o4 = reinterpret_cast<uint4*>(hits);
+    const uint32_t iters = eff_iters(p->max_iters, glsl);
+    if (n < kCastPersistentMin) {
+        auto kernel = glsl ? cast_kernel<true> : cast_kernel<false>;
+        kernel<<<(n + 255) / 256, 256, 0, stream>>>(w->dev(), r4, n, p->world_origin[0], p->world_origin[1],
+                                                    p->world_origin[2], iters, o4);
+    } else {
+        auto kernel = glsl ? cast_persistent_kernel<true> : cast_persistent_kernel<false>;
+        int dev = 0, sms = 0, occ = 0;
+        VRT_CUDA(cudaGetDevice(&dev));
+        VRT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        VRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kCastThreads, 0));
+        const uint32_t blocks = (uint32_t)(sms * std::max(occ, 1));
+        kernel<<<blocks, kCastThreads, 0, stream>>>(w->dev(), r4, n, p->world_origin[0], p->world_origin[1],
+                                                    p->world_origin[2], iters, kCastInner, kCastRefill, o4);
+    }
     VRT_CUDA(cudaGetLastError());
     return VRT_OK;
 }
