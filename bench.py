@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--no-per-view", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the request-server run")
     ap.add_argument("--no-stress", action="store_true", help="incoherent: skip the 2^26 stress rays")
+    ap.add_argument("--glsl", action="store_true",
+                    help="trace every view in the GLSL mode (the GPU renderer's rayCast) instead of the CPU traversal")
     ap.add_argument("--serve-rates", default="50,200,1000,2000", help="render requests per second to sweep")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="duration of each arrival-rate run")
     ap.add_argument("--serve-worlds", type=int, default=32)
@@ -89,7 +91,18 @@ def sum_over_ranks(pg, x: float) -> float:
 
 def build_workload(name: str, rank: int, args=None, world_size: int = 1):
     """The rank's workload: its own seeded batch (weak scaling) or its share, by world, of
-    the one batch (strong scaling, uneven_batch only)."""
+    the one batch (strong scaling, uneven_batch only).  With --glsl every view traces in
+    the GLSL mode (the GPU renderer's rayCast)."""
+    wl = _build_workload(name, rank, args, world_size)
+    if args is not None and getattr(args, "glsl", False):
+        from voxelrt_gb300 import capi
+        for vw in wl.views:
+            vw.flags |= capi.VIEW_GLSL
+        wl.description += ", GLSL traversal mode"
+    return wl
+
+
+def _build_workload(name: str, rank: int, args=None, world_size: int = 1):
     from voxelrt_gb300 import shard
     from voxelrt_gb300 import workloads as W
     if name == "uneven_batch":
@@ -190,6 +203,11 @@ def host_cores() -> int:
         return os.cpu_count() or 1
 
 
+def view_is_glsl(vw) -> bool:
+    from voxelrt_gb300 import capi
+    return bool(vw.flags & capi.VIEW_GLSL)
+
+
 def cpu_oracle_sample(wl, seconds: float, threads: int = 0):
     """Time the CPU oracle on whole views of the workload until `seconds` of work."""
     from oracle.oracle import OracleWorld
@@ -204,13 +222,14 @@ def cpu_oracle_sample(wl, seconds: float, threads: int = 0):
             o.upload(wl.worlds[vw.world])
             cache[vw.world] = o
         o = cache[vw.world]
+        glsl = view_is_glsl(vw)
         t0 = time.perf_counter()
         if vw.flags & 1:
-            o.render_view_shadow(vw.cam, np.array(vw.sun_dir[:], np.float32), vw.max_iters, threads)
+            o.render_view_shadow(vw.cam, np.array(vw.sun_dir[:], np.float32), vw.max_iters, threads, glsl=glsl)
         elif vw.n_bounces:
-            o.render_view_bounces(vw.cam, vw.n_bounces, vw.max_iters, threads)
+            o.render_view_bounces(vw.cam, vw.n_bounces, vw.max_iters, threads, glsl=glsl)
         else:
-            o.render_view(vw.cam, vw.max_iters, threads)
+            o.render_view(vw.cam, vw.max_iters, threads, glsl=glsl)
         elapsed += time.perf_counter() - t0
         rays += o.last_stats["rays"]
         nviews += 1
@@ -238,13 +257,15 @@ def run_reference(args):
         tot_rays += r
         tot_t += t
     value = tot_rays / tot_t / 1e9
+    algo = ("VoxelTraversal.glsl rayCast" if args.glsl else "CpuRenderer.cpp RayCast")
     sample = (f"{nv} smallest views of the {wl.name} workload per step ({tot_rays // max(args.steps, 1)} rays), "
-              f"scalar C++ restatement of CpuRenderer.cpp RayCast, all {cores} host threads")
+              f"scalar C++ restatement of {algo}, all {cores} host threads")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Grays/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / max(args.steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": wl.name, "description": wl.description},
+        "config": {"workload": wl.name, "description": wl.description,
+                   "traversal": "glsl" if args.glsl else "cpu"},
         "cpu_baseline": {"value": value, "unit": "Grays/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "Grays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -382,7 +403,8 @@ def run_ours(args):
                        "world_bytes": int(sum(d.n_bricks for d in wl.worlds) * 640),
                        "l2": "inputs larger than L2 (brick pools of all worlds)",
                        "batch_config": autotune.describe(cfg), "batch_config_source": cfg_src,
-                       "launch": "persistent kernel + queue reset, CUDA graph replay"},
+                       "launch": "persistent kernel + queue reset, CUDA graph replay",
+                       "traversal": "glsl" if args.glsl else "cpu"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
             "clocks": clk.summary(), "per_view": per_view,
             "batched_over_per_view": (value / per_view["value"]) if per_view else None,
@@ -629,12 +651,14 @@ def parity_sample(wl, batch, hits, stream, max_views=3):
         vw = wl.views[i]
         o = OracleWorld(wl.worlds[vw.world].sectors)
         o.upload(wl.worlds[vw.world])
+        glsl = view_is_glsl(vw)
         if vw.flags & 1:
-            want = np.stack(o.render_view_shadow(vw.cam, np.array(vw.sun_dir[:], np.float32), vw.max_iters))
+            want = np.stack(o.render_view_shadow(vw.cam, np.array(vw.sun_dir[:], np.float32), vw.max_iters,
+                                                 glsl=glsl))
         elif vw.n_bounces:
-            want = o.render_view_bounces(vw.cam, vw.n_bounces, vw.max_iters)
+            want = o.render_view_bounces(vw.cam, vw.n_bounces, vw.max_iters, glsl=glsl)
         else:
-            want = o.render_view(vw.cam, vw.max_iters)[None]
+            want = o.render_view(vw.cam, vw.max_iters, glsl=glsl)[None]
         a, b = int(batch.offsets[i]), int(batch.offsets[i + 1])
         got = hits[a * HIT_BYTES:b * HIT_BYTES].cpu().numpy().view(v.HIT_DTYPE).reshape(want.shape)
         ok &= hits_match(got, want)
