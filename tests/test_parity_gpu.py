@@ -219,3 +219,27 @@ def test_large_casts_take_the_persistent_kernel(cfg0, glsl, max_iters):
         r["origin"] -= np.array(wo, np.float32)
         assert_hits_equal(w.cast(r, world_origin=wo, max_iters=max_iters, glsl=glsl),
                           o.cast(r, world_origin=wo, max_iters=max_iters, glsl=glsl))
+
+
+def test_concurrent_large_casts_on_two_streams(cfg0):
+    """The persistent cast kernel keeps no device queue: two large casts on one world, on
+    two streams at once, give the records of the same casts run one after the other."""
+    torch = pytest.importorskip("torch")
+    _, w, o = cfg0
+    n = 1 << 19
+    rays = [v.random_rays((256, 256, 256), seed=s, n=n) for s in (31, 32)]
+    d_rays = [torch.from_numpy(r.view(np.uint8)).cuda() for r in rays]
+    alone = [torch.empty(n * 16, dtype=torch.uint8, device="cuda") for _ in rays]
+    for r, h in zip(d_rays, alone):
+        w.cast_device(r, n, h)
+    torch.cuda.synchronize()
+    streams = [torch.cuda.Stream() for _ in rays]
+    mixed = [torch.empty(n * 16, dtype=torch.uint8, device="cuda") for _ in rays]
+    for _ in range(3):
+        for r, h, s in zip(d_rays, mixed, streams):
+            w.cast_device(r, n, h, stream=s)
+        torch.cuda.synchronize()
+        for a, b in zip(alone, mixed):
+            assert torch.equal(a, b)
+    sub = rays[1][:1 << 16]
+    assert_hits_equal(mixed[1][:sub.size * 16].cpu().numpy().view(v.HIT_DTYPE), o.cast(sub))
