@@ -445,8 +445,9 @@ def load_serving_worlds(v, datas, dev):
 
 def run_serving(args, dev):
     """Poisson render arrivals (+100 edits/s) against the request server, per arrival rate,
-    in both scheduling modes (a launch per batch of queued requests; one resident launch
-    taking requests while it runs), each on freshly uploaded worlds."""
+    in both scheduling modes, each on freshly uploaded worlds: the default, one resident
+    launch taking requests while it runs (top-level rates), and a launch per batch of
+    queued requests ("launches")."""
     import voxelrt_gb300 as v
     from voxelrt_gb300 import workloads as W
     datas = W.serving_worlds(n_worlds=args.serve_worlds, max_edge=args.serve_max_edge)
@@ -463,8 +464,8 @@ def run_serving(args, dev):
     return {"worlds": len(datas), "max_edge": max(edges), "world_bytes": int(sum(d.n_bricks for d in datas) * 640),
             "edit_latency": edit_lat, "resolutions": "256^2 / 1280x720 / 1920x1080 at p 0.5 / 0.3 / 0.2",
             "edits_per_s": 100, "seconds_per_rate": args.serve_seconds,
-            "rates": modes["launches"]["rates"], "oracle_replay": modes["launches"]["oracle_replay"],
-            "resident": modes["resident"],
+            "mode": "resident", "rates": modes["resident"]["rates"],
+            "oracle_replay": modes["resident"]["oracle_replay"], "launches": modes["launches"],
             "latency": "submit to records in pinned host memory, server clock"}
 
 

@@ -394,7 +394,7 @@ typedef struct vrt_server_config {
     uint32_t max_batch_requests;    /* requests per launch / per publish at most (0 = 256) */
     uint64_t hbm_budget_bytes;      /* output records in flight (0 = 1/4 of free HBM at creation) */
     vrt_batch_config batch;         /* persistent launch configuration */
-    uint32_t flags;                 /* VRT_SERVE_RESIDENT */
+    uint32_t flags;                 /* VRT_SERVE_RESIDENT or VRT_SERVE_LAUNCHES (0: see below) */
     uint32_t idle_us;               /* resident mode: how long an idle launch waits for work (0 = 500) */
 } vrt_server_config;
 
@@ -405,9 +405,13 @@ typedef struct vrt_server_config {
  * memory) and its records are copied back.  The launch ends when it has been idle for
  * idle_us, or is closed before an edit or a change of traversal mode.  Needs a device
  * with host-native atomics (GB300's coherent host link has them); VRT_ERR_INVALID_ARG
- * otherwise.  Without the flag each batch of queued requests is its own launch, up to
- * max_inflight of them overlapping on separate streams. */
+ * otherwise.
+ * Launch mode (VRT_SERVE_LAUNCHES): each batch of queued requests is its own launch, up
+ * to max_inflight of them overlapping on separate streams.
+ * With neither flag the server runs in resident mode where the device has host-native
+ * atomics and in launch mode elsewhere (vrt_server_stats.resident says which). */
 #define VRT_SERVE_RESIDENT 1u
+#define VRT_SERVE_LAUNCHES 2u
 
 #define VRT_REQ_QUEUED 0u
 #define VRT_REQ_RUNNING 1u
@@ -428,6 +432,8 @@ typedef struct vrt_server_stats {
     uint64_t records;
     double p50_us, p99_us, p999_us, max_us; /* render latency, submit -> records in host memory */
     double busy_seconds;                    /* wall time with at least one launch in flight */
+    uint32_t resident;                      /* 1 in resident mode, 0 in launch mode */
+    uint32_t reserved;
 } vrt_server_stats;
 
 vrt_status vrt_server_create(vrt_world* const* worlds, uint32_t n_worlds, const vrt_server_config* cfg,

@@ -203,3 +203,25 @@ def test_resident_mode_switches_and_idle_restart(setup):
     assert_hits_equal(lo.array, oracle_records(oracles[late.world], late))
     assert srv.stats()["launches"] >= 4  # 4 mode changes, then a restart after the idle end
     srv.close()
+
+
+def test_default_mode_and_mode_flags(setup):
+    """With no mode flag the server runs resident on a device with host-native atomics
+    (GB300), and launch mode when asked; asking for both modes is refused."""
+    import ctypes as C
+
+    from voxelrt_gb300 import capi
+    datas, worlds, oracles = setup
+    srv = v.Server(worlds)
+    assert srv.stats()["resident"] == 1
+    vw = random_view(np.random.default_rng(8), 0, datas[0].sectors[0] * 32)
+    out = v.PinnedHits(v.view_records(vw))
+    srv.wait(srv.submit_render(vw, out.array))
+    srv.close()
+    srv = v.Server(worlds, resident=False)
+    assert srv.stats()["resident"] == 0
+    srv.close()
+    cfg = capi.ServerConfig(2, 0, 0, v.BatchConfig(), capi.SERVE_RESIDENT | capi.SERVE_LAUNCHES, 0)
+    wh = (C.c_void_p * len(worlds))(*[w.handle.value for w in worlds])
+    h = C.c_void_p()
+    assert capi.lib().vrt_server_create(wh, len(worlds), C.byref(cfg), C.byref(h)) == capi.VRT_ERR_INVALID_ARG

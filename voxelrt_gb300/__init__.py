@@ -359,13 +359,15 @@ class Server:
     """Request server with continuous batching over resident worlds (vrt_server)."""
 
     def __init__(self, worlds, max_inflight: int = 2, max_batch_requests: int = 0, hbm_budget_bytes: int = 0,
-                 batch: BatchConfig | None = None, resident: bool = False, idle_us: int = 0):
-        """resident: one persistent launch takes requests while it runs (VRT_SERVE_RESIDENT);
-        otherwise each batch of queued requests is its own launch, max_inflight at a time."""
+                 batch: BatchConfig | None = None, resident: bool | None = None, idle_us: int = 0):
+        """resident=True: one persistent launch takes requests while it runs (VRT_SERVE_RESIDENT);
+        False: each batch of queued requests is its own launch, max_inflight at a time
+        (VRT_SERVE_LAUNCHES); None: resident where the device supports it."""
         self.worlds = list(worlds)
         cfg = capi.ServerConfig(int(max_inflight), int(max_batch_requests), int(hbm_budget_bytes),
                                 batch if batch is not None else BatchConfig(),
-                                capi.SERVE_RESIDENT if resident else 0, int(idle_us))
+                                {None: 0, True: capi.SERVE_RESIDENT, False: capi.SERVE_LAUNCHES}[resident],
+                                int(idle_us))
         wh = (C.c_void_p * len(self.worlds))(*[w.handle.value for w in self.worlds])
         h = C.c_void_p()
         check(lib().vrt_server_create(wh, len(self.worlds), C.byref(cfg), C.byref(h)))

@@ -82,6 +82,7 @@ class ServerConfig(C.Structure):
 
 
 SERVE_RESIDENT = 1
+SERVE_LAUNCHES = 2
 
 
 class RequestInfo(C.Structure):
@@ -92,7 +93,8 @@ class RequestInfo(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("renders_done", C.c_uint64), ("edits_done", C.c_uint64), ("rejected", C.c_uint64),
                 ("launches", C.c_uint64), ("records", C.c_uint64), ("p50_us", C.c_double), ("p99_us", C.c_double),
-                ("p999_us", C.c_double), ("max_us", C.c_double), ("busy_seconds", C.c_double)]
+                ("p999_us", C.c_double), ("max_us", C.c_double), ("busy_seconds", C.c_double),
+                ("resident", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3

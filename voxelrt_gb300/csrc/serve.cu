@@ -136,6 +136,7 @@ struct vrt_server {
     uint64_t next_id = 1;
     uint64_t outstanding = 0;
     bool stop = false;
+    bool resident = false;  // scheduling mode (VRT_SERVE_RESIDENT)
     std::thread worker;
 
     std::mutex sig_mu;  // worker wake-ups (submissions, completions)
@@ -777,9 +778,18 @@ vrt_status vrt_server_create(vrt_world* const* worlds, uint32_t n_worlds, const 
         }
         sv->slots.push_back(std::move(s));
     }
-    if (sv->cfg.flags & ~VRT_SERVE_RESIDENT) return fail((set_error("unknown server flags"), VRT_ERR_INVALID_ARG));
+    const uint32_t modes = VRT_SERVE_RESIDENT | VRT_SERVE_LAUNCHES;
+    if ((sv->cfg.flags & ~modes) || (sv->cfg.flags & modes) == modes)
+        return fail((set_error("unknown server flags, or both modes asked for"), VRT_ERR_INVALID_ARG));
     if (sv->cfg.idle_us == 0) sv->cfg.idle_us = 500;
-    const bool resident = (sv->cfg.flags & VRT_SERVE_RESIDENT) != 0;
+    bool resident = (sv->cfg.flags & VRT_SERVE_RESIDENT) != 0;
+    if (!(sv->cfg.flags & modes)) {  // default: resident where the device supports it
+        int native = 0;
+        if ((e = cudaDeviceGetAttribute(&native, cudaDevAttrHostNativeAtomicSupported, sv->device)) != cudaSuccess)
+            return fail(cuda_fail(e, "device attribute"));
+        resident = native != 0;
+    }
+    sv->resident = resident;
     if (resident && (st = resident_init(sv)) != VRT_OK) return fail(st);
     sv->worker = resident ? std::thread(worker_resident, sv) : std::thread(worker_main, sv);
     *out = sv;
@@ -952,6 +962,7 @@ vrt_status vrt_server_get_stats(vrt_server* sv, int reset, vrt_server_stats* out
     out->rejected = sv->rejected;
     out->launches = sv->launches;
     out->records = sv->records_done;
+    out->resident = sv->resident ? 1u : 0u;
     double busy = sv->busy_total;
     if (sv->busy_since >= 0) busy += now_us(sv->t0) - sv->busy_since;
     out->busy_seconds = busy * 1e-6;
