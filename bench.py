@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--no-per-view", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the request-server run")
     ap.add_argument("--no-stress", action="store_true", help="incoherent: skip the 2^26 stress rays")
+    ap.add_argument("--stress-rays", type=int, default=1 << 26, help="incoherent: number of stress rays")
     ap.add_argument("--glsl", action="store_true",
                     help="trace every view in the GLSL mode (the GPU renderer's rayCast) instead of the CPU traversal")
     ap.add_argument("--serve-rates", default="50,200,1000,2000", help="render requests per second to sweep")
@@ -382,7 +383,7 @@ def run_ours(args):
 
     stress = None
     if rank == 0 and args.workload == "incoherent" and not args.no_stress:
-        stress = run_stress(v, worlds[0], wl.worlds[0], args, stream)
+        stress = run_stress(v, worlds[0], wl.worlds[0], args, stream, n=args.stress_rays)
 
     serving = None
     if rank == 0 and not args.no_serving and args.workload == "uneven_batch":
@@ -610,8 +611,8 @@ def hits_match(got, want) -> bool:
 
 def run_stress(v, world, data, args, stream, n=1 << 26, steps=3):
     """The incoherent workload's stress set: 2^26 rays with origins uniform in the world box and
-    directions uniform on the sphere, cast with vrt_cast_device (thread per ray) from device
-    memory; 64 Ki of them are checked against the CPU oracle."""
+    directions uniform on the sphere, cast with vrt_cast_device from device memory; 64 Ki
+    of them are checked against the CPU oracle."""
     import torch
 
     from oracle.oracle import OracleWorld
