@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(256) cast_kernel(DevWorld w, const float4* __r
 // cast_kernel: a lane's steps continue from where its ray left off, and a ray's record
 // is packed from the state at its exit.
 template <bool kGlsl>
-__global__ void __launch_bounds__(128) cast_persistent_kernel(DevWorld w, const float4* __restrict__ rays, uint32_t n,
+__global__ void __maxnreg__(48) cast_persistent_kernel(DevWorld w, const float4* __restrict__ rays, uint32_t n,
                                                              int32_t wox, int32_t woy, int32_t woz, uint32_t max_iters,
                                                              uint32_t inner, uint32_t refill, uint4* __restrict__ out) {
     const uint32_t lane = threadIdx.x & 31, lt = (1u << lane) - 1u;
@@ -146,7 +146,8 @@ vrt_status launch_render(vrt_world* w, const vrt_camera* cam, uint32_t max_iters
     return VRT_OK;
 }
 
-// Launch shape of cast_persistent_kernel: measured on GB300 with the 2^26 random rays
+// Launch shape of cast_persistent_kernel (also capped at 48 registers, for more warps to hide
+// L2 latency): measured on GB300 with the 2^26 random rays
 // of the incoherent workload.
 constexpr uint32_t kCastThreads = 128, kCastInner = 12, kCastRefill = 28;
 // Below this many rays the thread-per-ray kernel is used (too few rays to fill the
