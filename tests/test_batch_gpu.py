@@ -143,6 +143,17 @@ def test_batch_rejects_bad_input(mix):
     both = v.make_view(cfg0_camera(8, 8), n_bounces=1, shadow_dir=SUN)
     with pytest.raises(v.VrtError):
         v.Batch(worlds, [both])
+    # camera updates keep each view's resolution and a world origin within +-2^30
+    b = v.Batch(worlds, views)
+    cams = [v.Camera.from_buffer_copy(vw.cam) for vw in views]
+    cams[0].width += 1
+    with pytest.raises(v.VrtError):
+        b.update_cameras(cams)
+    cams = [v.Camera.from_buffer_copy(vw.cam) for vw in views]
+    cams[-1].world_origin[1] = (1 << 30) + 1
+    with pytest.raises(v.VrtError):
+        b.update_cameras(cams)
+    b.close()
 
 
 def test_run_into_pinned_buffers_matches_pageable(mix):
