@@ -401,7 +401,7 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": wl.name, "description": wl.description, "worlds": len(wl.worlds),
                        "views": len(wl.views), "rays_per_step": rays_per_step, "records_per_step": n_rec,
-                       "world_bytes": int(sum(d.n_bricks for d in wl.worlds) * 640),
+                       "world_bytes": int(sum(d.n_bricks for d in wl.worlds) * 1024),
                        "l2": "inputs larger than L2 (brick pools of all worlds)",
                        "batch_config": autotune.describe(cfg), "batch_config_source": cfg_src,
                        "launch": "persistent kernel + queue reset, CUDA graph replay",
@@ -462,7 +462,7 @@ def run_serving(args, dev):
     edit_lat = edit_latency(v, worlds, edges, surf)
     for w in worlds:
         w.close()
-    return {"worlds": len(datas), "max_edge": max(edges), "world_bytes": int(sum(d.n_bricks for d in datas) * 640),
+    return {"worlds": len(datas), "max_edge": max(edges), "world_bytes": int(sum(d.n_bricks for d in datas) * 1024),
             "edit_latency": edit_lat, "resolutions": "256^2 / 1280x720 / 1920x1080 at p 0.5 / 0.3 / 0.2",
             "edits_per_s": 100, "seconds_per_rate": args.serve_seconds,
             "mode": "resident", "rates": modes["resident"]["rates"],

@@ -69,10 +69,10 @@ int main(int argc, char** argv) {
     if (std::fread(dims, 4, 3, f) != 3 || std::fread(&nslots, 4, 1, f) != 1) return 4;
     const size_t npos = (size_t)dims[0] * dims[1] * dims[2] * 64;
     std::vector<uint32_t> bricks(npos);
-    std::vector<uint32_t> codes((size_t)nslots * 32);
+    std::vector<uint8_t> codes((size_t)nslots * 512);
     std::vector<uint8_t> payload((size_t)nslots * 512);
     if (std::fread(bricks.data(), 4, npos, f) != npos) return 5;
-    if (std::fread(codes.data(), 4, codes.size(), f) != codes.size()) return 6;
+    if (std::fread(codes.data(), 1, codes.size(), f) != codes.size()) return 6;
     if (std::fread(payload.data(), 1, payload.size(), f) != payload.size()) return 7;
     std::fclose(f);
     DevWorld w{};

@@ -71,11 +71,10 @@ def device_layout(data: v.SectorData) -> bytes:
     cell_any = solid.reshape(nb, 2, 4, 2, 4, 2, 4).any(axis=(2, 4, 6))
     block_any = solid.reshape(nb, 4, 2, 4, 2, 4, 2).any(axis=(2, 4, 6))
     up = lambda a, k: a.repeat(k, 1).repeat(k, 2).repeat(k, 3)
-    code = np.where(solid, 2, np.where(~up(cell_any, 4), 3, np.where(~up(block_any, 2), 1, 0))).astype(np.uint32)
-    code = code.reshape(nb, 32, 16)                          # voxel x | z<<3 | y<<6 -> word, position
-    words = (code << (2 * np.arange(16, dtype=np.uint32))).sum(axis=2, dtype=np.uint64).astype(np.uint32)
+    code = np.where(solid, 2, np.where(~up(cell_any, 4), 3, np.where(~up(block_any, 2), 1, 0))).astype(np.uint8)
     head = np.array([sx, sy, sz, nb], np.uint32).tobytes()
-    return head + table.tobytes() + words.tobytes() + data.bricks.tobytes()
+    # one code byte per voxel, x | z<<3 | y<<6 within the slot (the payload's order)
+    return head + table.tobytes() + code.tobytes() + data.bricks.tobytes()
 
 
 def run(exe, tmp_path, data, rays, max_iters=128, wo=(0, 0, 0), glsl=False):

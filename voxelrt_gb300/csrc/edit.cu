@@ -46,7 +46,7 @@ constexpr int kEditWarps = 8;
 
 __global__ void __launch_bounds__(kEditWarps * 32)
     edit_bricks_kernel(const TouchedBrick* __restrict__ bricks, uint32_t n, const EditDev* __restrict__ edits,
-                       uint32_t n_edits, uint8_t* __restrict__ payload, uint32_t* __restrict__ codes,
+                       uint32_t n_edits, uint8_t* __restrict__ payload, uint4* __restrict__ codes,
                        uint8_t* __restrict__ empty) {
     __shared__ __align__(16) uint8_t sb[kEditWarps][512];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;

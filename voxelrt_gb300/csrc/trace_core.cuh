@@ -252,12 +252,11 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
     int32_t m;
     if (e < kBrickEmpty) {
         if (kCount) cnt.occ_fetches++;
-        // voxel in brick v = x | z<<3 | y<<6 from v - 8*(v >> 3) per axis, word v >> 4, 2-bit field v & 15
+        // voxel in brick v = x | z<<3 | y<<6 from v - 8*(v >> 3) per axis; its code byte
         const uint32_t lx = imad(bx, 0xFFFFFFF8u, (uint32_t)vx), ly = imad(by, 0xFFFFFFF8u, (uint32_t)vy),
                        lz = imad(bz, 0xFFFFFFF8u, (uint32_t)vz);
         const uint32_t vi = imad(ly, 64u, imad(lz, 8u, lx));
-        const uint32_t wd = vi >> 4;
-        const uint32_t code = (__ldg(w.codes + (size_t)e * 32 + wd) >> (imad(wd, 0xFFFFFFF0u, vi) * 2)) & 3u;
+        const uint32_t code = __ldg(w.codes + (size_t)e * 512 + vi);
         if (code == kCodeSolid) {
             s.material = __ldg(w.payload + (size_t)e * 512 + vi);
             s.vx = vx;

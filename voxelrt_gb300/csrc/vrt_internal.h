@@ -14,8 +14,8 @@
 //            (VoxelTraversal.glsl:100-131): the same where the sector holds a brick,
 //            else (32 << skip_levels of the sector-group mask) - 1, cells of 32, 64
 //            or 128 voxels;
-//   codes    2-bit voxel codes, 32 u32 words (128 B) per brick slot; voxel
-//            v = x | z<<3 | y<<6 sits in word v>>4 at bit 2*(v&15): kCodeSolid, or
+//   codes    voxel codes, one byte per voxel (512 B per brick slot), voxel
+//            v = x | z<<3 | y<<6 at byte v (as the payload): kCodeSolid, or
 //            for an empty voxel the alignment mask (1 << level) - 1 (0, 1 or 3) of
 //            level = skip_levels of its 4^3 cell's occupancy mask (cell
 //            cx | cz<<1 | cy<<2, bit vx + vz*4 + vy*16: UpdateOccupancy,
@@ -23,7 +23,7 @@
 //   payload  512 B of u8 voxel ids per brick slot, voxel x | z<<3 | y<<6.
 // A brick's slot is base + popcount(mask & ((1<<b)-1)) (VoxelMap.glsl:45-64,
 // BrickSlotAllocator.h:37-41).  The traversal reads bricks, codes and payload
-// only: one 4-byte load per step, one more on an allocated brick.
+// only: one 4-byte load per step, one byte more on an allocated brick.
 #pragma once
 
 #include <cstdint>
@@ -62,7 +62,7 @@ VRT_HD inline uint32_t skip_levels(uint32_t lo, uint32_t hi, uint32_t idx) {
 // Kernel-side view of one world (passed by value or stored in a world table).
 struct alignas(16) DevWorld {
     const uint32_t* bricks;
-    const uint32_t* codes;
+    const uint8_t* codes;
     const uint8_t* payload;
     const SectorRec* sectors;
     uint32_t bsx, bsxz;               // brick-table strides: 4*SX, 4*SX * 4*SZ

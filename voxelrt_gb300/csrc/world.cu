@@ -59,8 +59,8 @@ struct BrickOp {
 constexpr int kOpsWarps = 8;
 
 __global__ void gather_bricks_kernel(const uint32_t* __restrict__ src_slots, uint32_t n,
-                                     const uint8_t* __restrict__ payload, const uint32_t* __restrict__ codes,
-                                     uint8_t* __restrict__ scratch_payload, uint32_t* __restrict__ scratch_codes) {
+                                     const uint8_t* __restrict__ payload, const uint4* __restrict__ codes,
+                                     uint8_t* __restrict__ scratch_payload, uint4* __restrict__ scratch_codes) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -74,8 +74,8 @@ __global__ void gather_bricks_kernel(const uint32_t* __restrict__ src_slots, uin
 
 __global__ void __launch_bounds__(kOpsWarps * 32)
     brick_ops_kernel(const BrickOp* __restrict__ ops, uint32_t n, const uint8_t* __restrict__ stage,
-                     const uint8_t* __restrict__ scratch_payload, const uint32_t* __restrict__ scratch_codes,
-                     uint8_t* __restrict__ payload, uint32_t* __restrict__ codes) {
+                     const uint8_t* __restrict__ scratch_payload, const uint4* __restrict__ scratch_codes,
+                     uint8_t* __restrict__ payload, uint4* __restrict__ codes) {
     __shared__ __align__(16) uint8_t sbrick[kOpsWarps][512];
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t wib = threadIdx.x >> 5;
@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(kOpsWarps * 32)
             codes[d * 32 + lane] = scratch_codes[(size_t)si * 32 + lane];
         } else if (kind == kOpZero) {
             reinterpret_cast<uint4*>(payload + d * 512)[lane] = make_uint4(0, 0, 0, 0);
-            codes[d * 32 + lane] = kEmptyBrickCodes;
+            codes[d * 32 + lane] = empty_brick_codes();
         } else {
             const uint4 v = reinterpret_cast<const uint4*>(stage + (size_t)si * 512)[lane];
             reinterpret_cast<uint4*>(payload + d * 512)[lane] = v;
@@ -174,9 +174,9 @@ vrt_status grow_pool(vrt_world* w, uint32_t min_capacity, cudaStream_t stream) {
         return VRT_ERR_SLOTS_EXHAUSTED;
     }
     uint32_t cap = (uint32_t)want;
-    uint32_t* codes = nullptr;
+    uint4* codes = nullptr;
     uint8_t* payload = nullptr;
-    cudaError_t e = cudaMalloc(&codes, (size_t)cap * 128);
+    cudaError_t e = cudaMalloc(&codes, (size_t)cap * 512);
     if (e == cudaSuccess) e = cudaMalloc(&payload, (size_t)cap * 512);
     if (e != cudaSuccess) {
         if (codes) cudaFree(codes);
@@ -184,7 +184,7 @@ vrt_status grow_pool(vrt_world* w, uint32_t min_capacity, cudaStream_t stream) {
         return cuda_fail(e, "grow brick pool");
     }
     if (w->capacity) {
-        VRT_CUDA(cudaMemcpyAsync(codes, w->d_codes, (size_t)w->capacity * 128, cudaMemcpyDeviceToDevice, stream));
+        VRT_CUDA(cudaMemcpyAsync(codes, w->d_codes, (size_t)w->capacity * 512, cudaMemcpyDeviceToDevice, stream));
         VRT_CUDA(cudaMemcpyAsync(payload, w->d_payload, (size_t)w->capacity * 512, cudaMemcpyDeviceToDevice, stream));
         VRT_CUDA(cudaStreamSynchronize(stream));
     }
@@ -272,16 +272,16 @@ vrt_status run_batch(vrt_world* w, SyncBatch& b, cudaStream_t stream) {
     }
     const size_t ng = b.gathers.size();
     if (ng) {
-        VRT_CUDA(w->d_scratch.reserve(ng * 640));
+        VRT_CUDA(w->d_scratch.reserve(ng * 1024));
         uint8_t* sp = (uint8_t*)w->d_scratch.ptr;
-        uint32_t* sc = (uint32_t*)(sp + ng * 512);
+        uint4* sc = (uint4*)(sp + ng * 512);
         gather_bricks_kernel<<<ops_grid((uint32_t)ng), kOpsWarps * 32, 0, stream>>>(
             (const uint32_t*)w->d_ops.ptr, (uint32_t)ng, w->d_payload, w->d_codes, sp, sc);
         VRT_CUDA(cudaGetLastError());
     }
     if (!b.ops.empty()) {
         uint8_t* sp = (uint8_t*)w->d_scratch.ptr;
-        uint32_t* sc = sp ? (uint32_t*)(sp + ng * 512) : nullptr;
+        uint4* sc = sp ? (uint4*)(sp + ng * 512) : nullptr;
         brick_ops_kernel<<<ops_grid((uint32_t)b.ops.size()), kOpsWarps * 32, 0, stream>>>(
             (const BrickOp*)((uint8_t*)w->d_ops.ptr + ooff), (uint32_t)b.ops.size(), (const uint8_t*)w->d_stage.ptr,
             sp, sc, w->d_payload, w->d_codes);

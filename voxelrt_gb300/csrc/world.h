@@ -61,7 +61,7 @@ struct vrt_world {
     vrt::SectorRec* d_sectors = nullptr;
     uint32_t* d_bricks = nullptr;  // brick table, derived from the sector table on the device
     uint64_t* d_groups = nullptr;  // sector-group masks of the GLSL mode's 4th level
-    uint32_t* d_codes = nullptr;   // 2-bit voxel codes, 128 B per slot
+    uint4* d_codes = nullptr;      // byte voxel codes, 512 B (32 x 16 B) per slot
     uint8_t* d_payload = nullptr;
     uint32_t capacity = 0;  // brick slots in the device pools
 
@@ -84,7 +84,7 @@ struct vrt_world {
     vrt::DevWorld dev() const {
         vrt::DevWorld w;
         w.bricks = d_bricks;
-        w.codes = d_codes;
+        w.codes = reinterpret_cast<const uint8_t*>(d_codes);
         w.payload = d_payload;
         w.sectors = d_sectors;
         w.bsx = sx * 4;
