@@ -272,10 +272,14 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
     vx = (vx | m) ^ (s.gx & m);
     vy = (vy | m) ^ (s.gy & m);
     vz = (vz | m) ^ (s.gz & m);
-    s.vx = vx;
-    s.vy = vy;
-    s.vz = vz;
-    if (kGlsl) return kStepContinue;
+    if (kGlsl) {  // the next GLSL iteration starts from this voxel
+        s.vx = vx;
+        s.vy = vy;
+        s.vz = vz;
+        return kStepContinue;
+    }
+    // (the CPU loop needs the voxel only in the record of a hit or of a ray that left the
+    // grid, whose paths above set it)
     s.sx = __fadd_rn(s.tsx, __fmul_rn(rel_voxel(vx, wox), s.ix));
     s.sy = __fadd_rn(s.tsy, __fmul_rn(rel_voxel(vy, woy), s.iy));
     s.sz = __fadd_rn(s.tsz, __fmul_rn(rel_voxel(vz, woz), s.iz));
