@@ -964,7 +964,7 @@ vrt_status vrt_batch_run(vrt_batch* b, vrt_hit* hits_host, void* stream_) {
     // All parts are launched first, one after another on `stream`; the copy of a
     // part's records (one contiguous range) waits for that part only, so the host
     // transfer of finished parts overlaps the traversal of the later ones.
-    constexpr uint64_t kParts = 8;
+    constexpr uint64_t kParts = 32;  // measured on GB300: 8 parts 30.99 ms, 32 parts 30.02, 128 parts 35.30
     std::vector<size_t> cut{0};
     for (size_t i = 1; i < nv; i++)
         if (plan.views[i].out_base * kParts >= plan.records * cut.size()) cut.push_back(i);
