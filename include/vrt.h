@@ -99,7 +99,7 @@ typedef struct vrt_hit {
 typedef struct vrt_cast_params {
     int32_t world_origin[3]; /* FrameConstants::WorldOrigin (CpuRenderer.cpp:447) */
     uint32_t max_iters;      /* 0 = VRT_DEFAULT_MAX_ITERS (VRT_GLSL_MAX_ITERS in GLSL mode); at most 65535 */
-    uint32_t flags;          /* 0 or VRT_CAST_GLSL */
+    uint32_t flags;          /* 0, VRT_CAST_GLSL or VRT_CAST_GLSL | VRT_CAST_GLSL_COARSE */
 } vrt_cast_params;
 
 /* Traversal modes.  The default is the reference CPU traversal (CpuRenderer.cpp:135-224,
@@ -117,10 +117,21 @@ typedef struct vrt_cast_params {
  *     secondary rays start at pos + normal*0.01 with normal = -sign(dir) on every such
  *     axis (sign(0) = 0);
  *   - the iteration cap defaults to VRT_GLSL_MAX_ITERS.
+ * The GPU renderer casts shadow and bounce rays with rayCastCoarse instead
+ * (VoxelTraversal.glsl:206-240, VoxelRender.comp:56,74,81), and so do the secondary
+ * rays of VRT_VIEW_GLSL views and casts with VRT_CAST_GLSL_COARSE:
+ *   - tmin = min(sides) + 0.001 instead of + 5 ulp;
+ *   - from iteration 31 on, an empty voxel whose 4^3 cell holds a solid voxel ends
+ *     the ray as a hit on the cell's first solid voxel in mask order (x, then z, then
+ *     y; getStepPos with coarse, findAnyOccupiedPos): that voxel and its material are
+ *     reported;
+ *   - the iteration cap is VRT_GLSL_COARSE_MAX_ITERS (or a smaller max_iters).
  * Entry clip, bounds (per axis, the world's extent) and the x86 min/floor rules are
  * shared with the default mode. */
 #define VRT_CAST_GLSL 1u
+#define VRT_CAST_GLSL_COARSE 2u
 #define VRT_GLSL_MAX_ITERS 256
+#define VRT_GLSL_COARSE_MAX_ITERS 96
 
 /* Pinhole camera in the reference's split form: integer world origin plus a
  * fractional ray origin (GBuffer.h:79, CpuRenderer.cpp:447-448).  The ray of

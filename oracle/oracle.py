@@ -128,11 +128,12 @@ class OracleWorld:
     def allocated_bricks(self) -> int:
         return lib().ora_world_allocated_bricks(self._h)
 
-    def cast(self, rays, world_origin=(0, 0, 0), max_iters=0, threads=0, glsl=False) -> np.ndarray:
-        """glsl: the GPU renderer's rayCast (flag VRT_CAST_GLSL) instead of the CPU traversal."""
+    def cast(self, rays, world_origin=(0, 0, 0), max_iters=0, threads=0, glsl=False, coarse=False) -> np.ndarray:
+        """glsl: the GPU renderer's rayCast (flag VRT_CAST_GLSL) instead of the CPU traversal;
+        with coarse also its rayCastCoarse (VRT_CAST_GLSL_COARSE)."""
         rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
         hits = np.zeros(len(rays), HIT_DTYPE)
-        p = _CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), 1 if glsl else 0)
+        p = _CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), (1 if glsl else 0) | (2 if coarse else 0))
         s = Stats()
         _chk(lib().ora_cast(self._h, rays.ctypes.data, len(rays), C.byref(p), hits.ctypes.data, int(threads),
                             C.byref(s)))

@@ -21,11 +21,14 @@
 // off: a 4th level of sector-group masks (GpuRenderer.cpp:139-149), cells of
 // isotropic size 1/2/4 x scale 1/8/32, a 256-iteration cap, the +5-ulp bias on tmin,
 // and side distances taken from the current voxel before each step, so the start
-// voxel itself is never tested.  Its parity is unpinned: the shader cannot run here.
+// voxel itself is never tested; shadow and bounce rays (and casts with
+// VRT_CAST_GLSL_COARSE) follow rayCastCoarse (:206-240) as the GPU renderer's do.  Its
+// parity is unpinned: the shader cannot run here.
 
 #include "vrt_oracle.h"
 
 #include <atomic>
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -211,9 +214,12 @@ inline int32_t iso_lod(uint64_t m, uint32_t idx) {
     return ((half >> (idx & 0xA)) & 0x00330033u) == 0 ? 2 : 1;
 }
 
-// getStepPos (VoxelTraversal.glsl:100-131), coarse = false, anisotropic LODs off.
-// Returns true on a hit.
-inline bool get_step_pos_glsl(const ora_world& w, int32_t vp[3], const float dir[3], Trace& tr) {
+// getStepPos (VoxelTraversal.glsl:100-131), anisotropic LODs off.  With coarse
+// (rayCastCoarse from iteration 31, :218), an empty voxel whose 4^3 cell mask is not
+// empty (lod < 4, :125) is a hit on the cell's first solid voxel, the lowest set bit of
+// the mask (findAnyOccupiedPos, :41-53).  Returns true on a hit.
+inline bool get_step_pos_glsl(const ora_world& w, int32_t vp[3], const float dir[3], Trace& tr,
+                              bool coarse = false) {
     const int32_t sx = vp[0] >> 5, sy = vp[1] >> 5, sz = vp[2] >> 5;
     uint32_t s = w.lin(sx, sy, sz);
     uint64_t m = w.masks[s];
@@ -229,6 +235,16 @@ inline bool get_step_pos_glsl(const ora_world& w, int32_t vp[3], const float dir
         scale = 1;
         tr.occ_fetches++;
         if ((m >> idx) & 1) {
+            uint32_t vi = (vp[0] & 7) | (vp[2] & 7) << 3 | (vp[1] & 7) << 6;
+            tr.material = blk->vox[brick * 512 + vi];
+            return true;
+        }
+        if (coarse && m != 0) {
+            uint32_t b = 0;
+            while (!((m >> b) & 1)) b++;
+            vp[0] = (vp[0] & ~3) | (int32_t)(b & 3);
+            vp[1] = (vp[1] & ~3) | (int32_t)(b >> 4);
+            vp[2] = (vp[2] & ~3) | (int32_t)((b >> 2) & 3);
             uint32_t vi = (vp[0] & 7) | (vp[2] & 7) << 3 | (vp[1] & 7) << 6;
             tr.material = blk->vox[brick * 512 + vi];
             return true;
@@ -267,9 +283,10 @@ void clip_start(const ora_world& w, const float o[3], const float d[3], const fl
 }
 
 // rayCast (VoxelTraversal.glsl:162-204) for one ray: the voxel's side distances,
-// tmin + 5 ulp, the next position, bounds, getStepPos.
+// tmin + 5 ulp, the next position, bounds, getStepPos.  coarse: rayCastCoarse
+// (:206-240) instead, tmin + 0.001 and coarse steps from iteration 31.
 void trace_ray_glsl(const ora_world& w, const float o[3], const float d[3], const int32_t wo[3],
-                    uint32_t max_iters, Trace& tr) {
+                    uint32_t max_iters, Trace& tr, bool coarse = false) {
     tr.hit = false;
     tr.glsl = true;
     tr.tb = 0.0f;
@@ -288,7 +305,9 @@ void trace_ray_glsl(const ora_world& w, const float o[3], const float d[3], cons
     for (uint32_t i = 0; i < max_iters; i++) {
         for (int c = 0; c < 3; c++) side[c] = ts[c] + (float)wsub(vp[c], wo[c]) * inv[c];
         float t = min_x86(min_x86(side[0], side[1]), side[2]);
-        if (t == t) {  // +5 ulp on the bits; a NaN stays NaN (its bits are platform-defined)
+        if (coarse) {
+            t = t + 0.001f;
+        } else if (t == t) {  // +5 ulp on the bits; a NaN stays NaN (its bits are platform-defined)
             uint32_t bits;
             std::memcpy(&bits, &t, 4);
             bits += 5u;
@@ -301,7 +320,7 @@ void trace_ray_glsl(const ora_world& w, const float o[3], const float d[3], cons
             tr.steps = (uint16_t)i;
             return;
         }
-        if (get_step_pos_glsl(w, vp, d, tr)) {
+        if (get_step_pos_glsl(w, vp, d, tr, coarse && i >= 31)) {
             tr.hit = true;
             tr.tb = t;
             tr.steps = (uint16_t)i;
@@ -491,10 +510,13 @@ void bounce_dir(uint32_t pixel, uint32_t bounce, const float n[3], float out[3])
     for (int c = 0; c < 3; c++) out[c] = n[c] / l;
 }
 
-// Traversal of one ray in the given mode.
+// Traversal of one ray in the given mode.  secondary: a shadow or bounce ray, which the
+// GPU renderer casts with rayCastCoarse (VoxelRender.comp:56,74,81; cap 96).
 inline void trace_mode(const ora_world& w, bool glsl, const float o[3], const float d[3], const int32_t wo[3],
-                       uint32_t max_iters, Trace& tr) {
-    if (glsl)
+                       uint32_t max_iters, Trace& tr, bool secondary = false) {
+    if (glsl && secondary)
+        trace_ray_glsl(w, o, d, wo, std::min<uint32_t>(max_iters, VRT_GLSL_COARSE_MAX_ITERS), tr, true);
+    else if (glsl)
         trace_ray_glsl(w, o, d, wo, max_iters, tr);
     else
         trace_ray(w, o, d, wo, max_iters, tr);
@@ -645,12 +667,13 @@ int ora_cast(const ora_world* w, const vrt_ray* rays, uint64_t n, const vrt_cast
              vrt_hit* hits, int threads, ora_stats* stats) {
     if (!w || (n && (!rays || !hits)) || !params) return -1;
     const bool glsl = (params->flags & VRT_CAST_GLSL) != 0;
+    const bool coarse = glsl && (params->flags & VRT_CAST_GLSL_COARSE) != 0;
     uint32_t iters = eff_iters_mode(params->max_iters, glsl);
     StatAcc acc(threads);
     parallel_for(n, (int)acc.per.size(), [&](int tid, uint64_t b, uint64_t e) {
         Trace tr;
         for (uint64_t i = b; i < e; i++) {
-            trace_mode(*w, glsl, rays[i].origin, rays[i].dir, params->world_origin, iters, tr);
+            trace_mode(*w, glsl, rays[i].origin, rays[i].dir, params->world_origin, iters, tr, coarse);
             fill_hit(tr, rays[i].dir, rays[i].tag, hits[i]);
             acc.add(tid, tr);
         }
@@ -714,7 +737,7 @@ int ora_render_view_shadow(const ora_world* w, const vrt_camera* cam, const floa
             }
             hit_normal(tr, d, nrm);
             offset_origin(tr, nrm, so);
-            trace_mode(*w, glsl, so, sun_dir, cam->world_origin, iters, ts);
+            trace_mode(*w, glsl, so, sun_dir, cam->world_origin, iters, ts, true);
             fill_hit(ts, sun_dir, (uint32_t)i, shadow[i]);
             acc.add(tid, ts);
         }
@@ -747,7 +770,7 @@ int ora_render_view_bounces(const ora_world* w, const vrt_camera* cam, uint32_t 
                     offset_origin(tr, nrm, o);
                     bounce_dir((uint32_t)i, k, nrm, d);
                 }
-                trace_mode(*w, glsl, o, d, cam->world_origin, iters, tr);
+                trace_mode(*w, glsl, o, d, cam->world_origin, iters, tr, k > 0);
                 fill_hit(tr, d, (uint32_t)i, h);
                 acc.add(tid, tr);
                 alive = tr.hit;

@@ -92,6 +92,7 @@ int main(int argc, char** argv) {
     std::fclose(f);
     const uint32_t max_iters = (uint32_t)std::atoi(argv[4]);
     const bool glsl = argc > 8 && std::atoi(argv[8]) != 0;
+    const bool coarse = argc > 9 && std::atoi(argv[9]) != 0;
     const int wo[3] = {std::atoi(argv[5]), std::atoi(argv[6]), std::atoi(argv[7])};
     std::vector<uint4> out(rays.size());
     for (size_t i = 0; i < rays.size(); i++) {
@@ -100,7 +101,7 @@ int main(int argc, char** argv) {
         const vrt_ray& q = rays[i];
         if (glsl) {
             trace_ray<false, true>(w, q.origin[0], q.origin[1], q.origin[2], q.dir[0], q.dir[1], q.dir[2], wo[0],
-                                   wo[1], wo[2], max_iters, res, cnt);
+                                   wo[1], wo[2], max_iters, res, cnt, coarse);
             out[i] = pack_hit<true>(res, q.dir[0], q.dir[1], q.dir[2], q.tag);
         } else {
             trace_ray<false, false>(w, q.origin[0], q.origin[1], q.origin[2], q.dir[0], q.dir[1], q.dir[2], wo[0],

@@ -91,3 +91,11 @@ def oracle_view(o: OracleWorld, view) -> np.ndarray:
     if view.n_bounces:
         return o.render_view_bounces(view.cam, view.n_bounces, view.max_iters, glsl=glsl)
     return o.render_view(view.cam, view.max_iters, glsl=glsl)[None]
+
+
+def cell_corner_world(shape=(32, 32, 128), material=7) -> v.SectorData:
+    """(Y, Z, X) world with one solid voxel at offset (3, 3, 3) of every 4^3 cell: every
+    brick is allocated, every cell non-empty, every 2^3 block at the cell origin empty."""
+    vol = np.zeros(shape, np.uint8)
+    vol[3::4, 3::4, 3::4] = material
+    return dense_to_stream(vol)

@@ -13,7 +13,7 @@ import pytest
 
 import voxelrt_gb300 as v
 from oracle.oracle import OracleWorld
-from tests.helpers import assert_hits_equal, cfg0_world, dense_to_stream, make_rays
+from tests.helpers import assert_hits_equal, cell_corner_world, cfg0_world, dense_to_stream, make_rays
 
 ROOT = Path(__file__).resolve().parent.parent
 SRC = ROOT / "tests" / "cpp" / "device_logic_test.cpp"
@@ -77,11 +77,11 @@ def device_layout(data: v.SectorData) -> bytes:
     return head + table.tobytes() + code.tobytes() + data.bricks.tobytes()
 
 
-def run(exe, tmp_path, data, rays, max_iters=128, wo=(0, 0, 0), glsl=False):
+def run(exe, tmp_path, data, rays, max_iters=128, wo=(0, 0, 0), glsl=False, coarse=False):
     (tmp_path / "w.bin").write_bytes(device_layout(data))
     np.ascontiguousarray(rays, v.RAY_DTYPE).tofile(tmp_path / "r.bin")
     subprocess.run([str(exe), str(tmp_path / "w.bin"), str(tmp_path / "r.bin"), str(tmp_path / "o.bin"),
-                    str(max_iters), *map(str, wo), "1" if glsl else "0"], check=True)
+                    str(max_iters), *map(str, wo), "1" if glsl else "0", "1" if coarse else "0"], check=True)
     return np.fromfile(tmp_path / "o.bin", v.HIT_DTYPE)
 
 
@@ -147,3 +147,16 @@ def test_glsl_mode_against_oracle(exe, tmp_path, seed):
         world_rays = v.random_rays(size, seed=seed, n=20_000)
         assert_hits_equal(run(exe, tmp_path, data, world_rays, 64, (0, 0, 0), glsl=True),
                           o.cast(world_rays, max_iters=64, glsl=True))
+        # rayCastCoarse (the GPU renderer's shadow and bounce rays): 0.001 bias, coarse
+        # hits from iteration 31, cap 96
+        assert_hits_equal(run(exe, tmp_path, data, rays, 96, wo, glsl=True, coarse=True),
+                          o.cast(rays, world_origin=wo, max_iters=96, glsl=True, coarse=True))
+
+
+def test_glsl_coarse_known_answer(exe, tmp_path):
+    data = cell_corner_world()
+    d = np.array([1.0, 1e-3, 1e-3], np.float32)
+    rays = make_rays([[1.5, 0.5, 0.5], [1.5, 1.5, 0.5]], [d / np.linalg.norm(d)] * 2)
+    got = run(exe, tmp_path, data, rays, 96, (0, 0, 0), glsl=True, coarse=True)
+    assert_hits_equal(got, oracle_for(data).cast(rays, max_iters=96, glsl=True, coarse=True))
+    assert tuple(v.unpack_voxel(got["voxel"][:1])[0]) == (67, 3, 3)

@@ -7,8 +7,8 @@ import pytest
 
 import voxelrt_gb300 as v
 from oracle.oracle import OracleWorld
-from tests.helpers import assert_hits_equal, both_worlds, cfg0_camera, cfg0_world, dense_to_stream, make_rays, \
-    oracle_view
+from tests.helpers import assert_hits_equal, both_worlds, cell_corner_world, cfg0_camera, cfg0_world, dense_to_stream, \
+    make_rays, oracle_view
 
 pytestmark = pytest.mark.gpu
 
@@ -126,4 +126,29 @@ def test_glsl_group_masks_follow_edits(gpu):
         assert_hits_equal(got[0], oracle_view(o, view)[0])
         rays, wo = camera_frame_rays(rng, [128, 128, 128], 20_000)
         assert_hits_equal(w.cast(rays, world_origin=wo, glsl=True), o.cast(rays, world_origin=wo, glsl=True))
+    w.close()
+
+
+def test_glsl_coarse_casts_match_oracle(gpu):
+    """rayCastCoarse (VRT_CAST_GLSL_COARSE): 0.001 bias, coarse hits from iteration 31,
+    cap 96; through the thread-per-ray kernel and, from 2^18 rays, the persistent one."""
+    rng = np.random.default_rng(13)
+    for data in (sparse_world(13), v.synth_mix(96, seed=13), cell_corner_world()):
+        size = [s * 32 for s in data.sectors]
+        w, o = both_worlds(data)
+        for n in (30_000, (1 << 18) + 5):
+            rays, wo = camera_frame_rays(rng, size, n)
+            got = w.cast(rays, world_origin=wo, glsl=True, coarse=True)
+            assert_hits_equal(got, o.cast(rays, world_origin=wo, glsl=True, coarse=True))
+            assert int(got["steps"].max()) <= 96
+        w.close()
+    # the known answer: the coarse step at iteration 31 stops on the cell's solid voxel
+    data = cell_corner_world()
+    w, _ = both_worlds(data)
+    d = np.array([1.0, 1e-3, 1e-3], np.float32)
+    h = w.cast(make_rays([[1.5, 0.5, 0.5]], [d / np.linalg.norm(d)]), glsl=True, coarse=True)[0]
+    assert int(h["steps"]) == 31 and tuple(v.unpack_voxel(np.array([h["voxel"]]))[0]) == (67, 3, 3)
+    with pytest.raises(v.VrtError):  # coarse without the GLSL mode
+        p = v.capi.CastParams((v.C.c_int32 * 3)(0, 0, 0), 0, v.capi.CAST_GLSL_COARSE)
+        v.check(v.lib().vrt_cast(w.handle, None, 0, v.C.byref(p), None, None))
     w.close()

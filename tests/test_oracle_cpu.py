@@ -10,7 +10,7 @@ import pytest
 
 import voxelrt_gb300 as v
 from oracle.oracle import OracleWorld
-from tests.helpers import cfg0_camera, cfg0_world, dense_to_stream, make_rays, single_voxel_world
+from tests.helpers import cell_corner_world, cfg0_camera, cfg0_world, dense_to_stream, make_rays, single_voxel_world
 
 
 def occupancy_numpy(brick: np.ndarray) -> np.ndarray:
@@ -277,3 +277,27 @@ def test_glsl_mode_iteration_cap_default_256():
     r = make_rays([[0.5, 16.5, 0.5]], [[1, 0, 1e-3]])  # zero y component: x86 min leaves NaN sides out
     h = o.cast(r, glsl=True, max_iters=3)
     assert h["steps"][0] <= 3
+
+
+def test_glsl_coarse_rays_stop_at_the_first_solid_voxel_of_a_cell():
+    """rayCastCoarse (VoxelTraversal.glsl:206-240): in a world with one solid voxel at
+    offset (3,3,3) of every 4^3 cell, a ray along +x near y = z = 0 steps two voxels
+    per iteration (its 2^3 blocks are empty) and lands on x = 2 + 2i; from iteration
+    31 (x = 64) the non-empty cell ends it at that cell's solid voxel (67, 3, 3).
+    rayCast, with no coarse steps, runs to the edge of the world."""
+    data = cell_corner_world()
+    o = OracleWorld(data.sectors)
+    o.upload(data)
+    d = np.array([1.0, 1e-3, 1e-3], np.float32)
+    rays = make_rays([[1.5, 0.5, 0.5]], [d / np.linalg.norm(d)])
+    h = o.cast(rays, glsl=True, coarse=True)[0]
+    assert int(h["steps"]) == 31
+    assert tuple(v.unpack_voxel(np.array([h["voxel"]]))[0]) == (67, 3, 3)
+    assert int(h["material"]) == 7
+    assert 62.5 < float(h["t"]) < 62.51  # the biased tmin of the step onto x = 64 from x = 1.5
+    plain = o.cast(rays, glsl=True)[0]
+    assert int(plain["voxel"]) == v.MISS_VOXEL
+    # before iteration 31 a coarse ray is a rayCast ray with the CPU bias: capped at 20
+    # iterations it misses where it stood
+    capped = o.cast(rays, glsl=True, coarse=True, max_iters=20)[0]
+    assert int(capped["voxel"]) == v.MISS_VOXEL and int(capped["steps"]) == 20

@@ -137,6 +137,10 @@ def random_rays(size, seed: int, n: int, first: int = 0, threads: int = 0) -> np
     return rays
 
 
+def cast_flags(glsl: bool, coarse: bool) -> int:
+    return (CAST_GLSL if glsl or coarse else 0) | (capi.CAST_GLSL_COARSE if coarse else 0)
+
+
 def _stream_ptr(stream) -> int | None:
     if stream is None:
         return None
@@ -221,17 +225,18 @@ class World:
         return mask.value, bricks
 
     def cast(self, rays: np.ndarray, world_origin=(0, 0, 0), max_iters: int = 0, stream=None,
-             glsl: bool = False) -> np.ndarray:
-        """glsl: the GPU renderer's rayCast (VRT_CAST_GLSL) instead of the CPU traversal."""
+             glsl: bool = False, coarse: bool = False) -> np.ndarray:
+        """glsl: the GPU renderer's rayCast (VRT_CAST_GLSL) instead of the CPU traversal;
+        coarse: its rayCastCoarse (VRT_CAST_GLSL_COARSE, with glsl)."""
         rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
         hits = np.zeros(len(rays), HIT_DTYPE)
-        p = CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), CAST_GLSL if glsl else 0)
+        p = CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), cast_flags(glsl, coarse))
         check(lib().vrt_cast(self._h, ptr(rays), len(rays), C.byref(p), ptr(hits), _stream_ptr(stream)))
         return hits
 
     def cast_device(self, rays, n: int, hits, world_origin=(0, 0, 0), max_iters: int = 0, stream=None,
-                    glsl: bool = False) -> None:
-        p = CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), CAST_GLSL if glsl else 0)
+                    glsl: bool = False, coarse: bool = False) -> None:
+        p = CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), cast_flags(glsl, coarse))
         check(lib().vrt_cast_device(self._h, ptr(rays), int(n), C.byref(p), ptr(hits), _stream_ptr(stream)))
 
     def render_view(self, cam: Camera, max_iters: int = 0, stream=None) -> np.ndarray:

@@ -73,6 +73,7 @@ class BatchStats(C.Structure):
 VIEW_SHADOW = 1
 VIEW_GLSL = 2        # the GPU renderer's rayCast (VoxelTraversal.glsl) instead of the CPU traversal
 CAST_GLSL = 1
+CAST_GLSL_COARSE = 2
 GLSL_MAX_ITERS = 256
 
 

@@ -33,16 +33,17 @@ __device__ __forceinline__ uint32_t compact_even_bits(uint32_t k) {
 
 template <bool kCount, bool kGlsl>
 __device__ __forceinline__ bool run_ray(RayState& s, bool safe, const DevWorld& w, int32_t wox, int32_t woy,
-                                        int32_t woz, uint32_t max_iters, uint32_t& steps, TraceCounters& cnt) {
+                                        int32_t woz, uint32_t max_iters, uint32_t& steps, TraceCounters& cnt,
+                                        bool coarse_ray = false) {
     uint32_t st = kStepOut, i = 0;
     if (safe) {
         for (; i < max_iters; i++) {
-            st = ray_step<kCount, true, kGlsl>(s, w, wox, woy, woz, cnt);
+            st = ray_step<kCount, true, kGlsl>(s, w, wox, woy, woz, cnt, kGlsl ? coarse_bits(coarse_ray, i) : 0u);
             if (st != kStepContinue) break;
         }
     } else {
         for (; i < max_iters; i++) {
-            st = ray_step<kCount, false, kGlsl>(s, w, wox, woy, woz, cnt);
+            st = ray_step<kCount, false, kGlsl>(s, w, wox, woy, woz, cnt, kGlsl ? coarse_bits(coarse_ray, i) : 0u);
             if (st != kStepContinue) break;
         }
     }
@@ -76,7 +77,9 @@ __global__ void __launch_bounds__(64) view_path_kernel(DevWorld w, ViewDev v, ui
         }
         next_path_ray<kGlsl>(s, v.shadow() != 0, v.sun, pixel, k, ox, oy, oz, dx, dy, dz);
         safe = ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
-        hit = run_ray<false, kGlsl>(s, safe, w, wox, woy, woz, v.max_iters, steps, cnt);
+        // GLSL mode: shadow and bounce rays are rayCastCoarse's (VoxelRender.comp:56,74)
+        hit = run_ray<false, kGlsl>(s, safe, w, wox, woy, woz, kGlsl ? min(v.max_iters, kCoarseMaxIters) : v.max_iters,
+                                    steps, cnt, kGlsl);
         o[k * plane] = pack_state<kGlsl>(s, hit, steps, pixel);
     }
 }
@@ -265,6 +268,7 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                 path &= ~kSafe;
                 if (ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz)) path |= kSafe;
                 iter = 0;
+                if (kGlsl) max_iters = min(max_iters, kCoarseMaxIters);  // rayCastCoarse's cap
             } else {
                 for (uint32_t kk = kind + 1; kk <= last_kind; kk++) rec[(size_t)kk * plane] = no_ray_hit();
                 active = false;
@@ -465,14 +469,18 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
         if (active) {
             const uint32_t kmax = min(p.inner, max_iters - iter);
             uint32_t k = 0, st = kStepContinue;
+            // GLSL mode: a pixel's shadow and bounce rays are rayCastCoarse's
+            const bool coarse_ray = kGlsl && (path & 0xFFu) != 0;
             if (all_safe) {
                 for (; k < kmax; k++) {
-                    st = ray_step<kCount, true, kGlsl>(s, w, wox, woy, woz, cnt);
+                    st = ray_step<kCount, true, kGlsl>(s, w, wox, woy, woz, cnt,
+                                                       kGlsl ? coarse_bits(coarse_ray, iter + k) : 0u);
                     if (st != kStepContinue) break;
                 }
             } else {
                 for (; k < kmax; k++) {
-                    st = ray_step<kCount, false, kGlsl>(s, w, wox, woy, woz, cnt);
+                    st = ray_step<kCount, false, kGlsl>(s, w, wox, woy, woz, cnt,
+                                                        kGlsl ? coarse_bits(coarse_ray, iter + k) : 0u);
                     if (st != kStepContinue) break;
                 }
             }

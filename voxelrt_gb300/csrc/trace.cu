@@ -39,13 +39,13 @@ __global__ void __launch_bounds__(64) render_view_kernel(DevWorld w, vrt_camera 
 template <bool kGlsl>
 __global__ void __launch_bounds__(256) cast_kernel(DevWorld w, const float4* __restrict__ rays, uint32_t n,
                                                   int32_t wox, int32_t woy, int32_t woz, uint32_t max_iters,
-                                                  uint4* __restrict__ out) {
+                                                  uint4* __restrict__ out, bool coarse) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 a = rays[2 * (size_t)i], b = rays[2 * (size_t)i + 1];
     TraceResult r;
     TraceCounters cnt;
-    trace_ray<false, kGlsl>(w, a.x, a.y, a.z, a.w, b.x, b.y, wox, woy, woz, max_iters, r, cnt);
+    trace_ray<false, kGlsl>(w, a.x, a.y, a.z, a.w, b.x, b.y, wox, woy, woz, max_iters, r, cnt, coarse);
     out[i] = pack_hit<kGlsl>(r, a.w, b.x, b.y, __float_as_uint(b.z));
 }
 
@@ -61,7 +61,8 @@ __global__ void __launch_bounds__(256) cast_kernel(DevWorld w, const float4* __r
 template <bool kGlsl>
 __global__ void __maxnreg__(48) cast_persistent_kernel(DevWorld w, const float4* __restrict__ rays, uint32_t n,
                                                              int32_t wox, int32_t woy, int32_t woz, uint32_t max_iters,
-                                                             uint32_t inner, uint32_t refill, uint4* __restrict__ out) {
+                                                             uint32_t inner, uint32_t refill, uint4* __restrict__ out,
+                                                             bool coarse) {
     const uint32_t lane = threadIdx.x & 31, lt = (1u << lane) - 1u;
     const uint32_t stride = (gridDim.x * blockDim.x) & ~31u;  // rays between a warp's chunks
     uint32_t next = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;  // first ray of the warp's next chunk
@@ -109,12 +110,14 @@ __global__ void __maxnreg__(48) cast_persistent_kernel(DevWorld w, const float4*
             uint32_t k = 0, st = kStepContinue;
             if (all_safe) {
                 for (; k < kmax; k++) {
-                    st = ray_step<false, true, kGlsl>(s, w, wox, woy, woz, cnt);
+                    st = ray_step<false, true, kGlsl>(s, w, wox, woy, woz, cnt,
+                                                      kGlsl ? coarse_bits(coarse, iter + k) : 0u);
                     if (st != kStepContinue) break;
                 }
             } else {
                 for (; k < kmax; k++) {
-                    st = ray_step<false, false, kGlsl>(s, w, wox, woy, woz, cnt);
+                    st = ray_step<false, false, kGlsl>(s, w, wox, woy, woz, cnt,
+                                                       kGlsl ? coarse_bits(coarse, iter + k) : 0u);
                     if (st != kStepContinue) break;
                 }
             }
@@ -157,14 +160,15 @@ constexpr uint32_t kCastPersistentMin = 1u << 18;
 vrt_status launch_cast(vrt_world* w, const vrt_ray* rays, uint32_t n, const vrt_cast_params* p, vrt_hit* hits,
                        cudaStream_t stream) {
     if (n == 0) return VRT_OK;
-    const bool glsl = (p->flags & VRT_CAST_GLSL) != 0;
+    const bool glsl = (p->flags & VRT_CAST_GLSL) != 0, coarse = (p->flags & VRT_CAST_GLSL_COARSE) != 0;
     const float4* r4 = reinterpret_cast<const float4*>(rays);
     uint4* o4 = reinterpret_cast<uint4*>(hits);
-    const uint32_t iters = eff_iters(p->max_iters, glsl);
+    uint32_t iters = eff_iters(p->max_iters, glsl);
+    if (coarse) iters = std::min<uint32_t>(iters, VRT_GLSL_COARSE_MAX_ITERS);
     if (n < kCastPersistentMin) {
         auto kernel = glsl ? cast_kernel<true> : cast_kernel<false>;
         kernel<<<(n + 255) / 256, 256, 0, stream>>>(w->dev(), r4, n, p->world_origin[0], p->world_origin[1],
-                                                    p->world_origin[2], iters, o4);
+                                                    p->world_origin[2], iters, o4, coarse);
     } else {
         auto kernel = glsl ? cast_persistent_kernel<true> : cast_persistent_kernel<false>;
         int dev = 0, sms = 0, occ = 0;
@@ -173,15 +177,17 @@ vrt_status launch_cast(vrt_world* w, const vrt_ray* rays, uint32_t n, const vrt_
         VRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kCastThreads, 0));
         const uint32_t blocks = (uint32_t)(sms * std::max(occ, 1));
         kernel<<<blocks, kCastThreads, 0, stream>>>(w->dev(), r4, n, p->world_origin[0], p->world_origin[1],
-                                                    p->world_origin[2], iters, kCastInner, kCastRefill, o4);
+                                                    p->world_origin[2], iters, kCastInner, kCastRefill, o4, coarse);
     }
     VRT_CUDA(cudaGetLastError());
     return VRT_OK;
 }
 
 vrt_status check_params(const vrt_cast_params* p) {
-    if (!p || (p->flags & ~VRT_CAST_GLSL) != 0 || !world_origin_ok(p->world_origin)) {
-        set_error("cast params missing, flags other than VRT_CAST_GLSL, or |world origin| > 2^30");
+    if (!p || (p->flags & ~(VRT_CAST_GLSL | VRT_CAST_GLSL_COARSE)) != 0 ||
+        (p->flags & (VRT_CAST_GLSL | VRT_CAST_GLSL_COARSE)) == VRT_CAST_GLSL_COARSE || !world_origin_ok(p->world_origin)) {
+        set_error("cast params missing, flags other than VRT_CAST_GLSL [| VRT_CAST_GLSL_COARSE], or "
+                  "|world origin| > 2^30");
         return VRT_ERR_INVALID_ARG;
     }
     return VRT_OK;

@@ -197,6 +197,15 @@ __device__ __forceinline__ bool ray_start(RayState& s, const DevWorld& w, float 
 
 enum : uint32_t { kStepContinue = 0, kStepHit = 1, kStepOut = 2 };
 
+// GLSL mode: rayCastCoarse (VoxelTraversal.glsl:206-240), the GPU renderer's shadow and
+// bounce rays (VoxelRender.comp:56,74,81): kCoarseRay for every step of such a ray,
+// kCoarseNow from its iteration 31 on (`coarse = i > 30`, :218).
+enum : uint32_t { kCoarseRay = 1, kCoarseNow = 2 };
+constexpr uint32_t kCoarseFrom = 31, kCoarseMaxIters = 96;
+__device__ __forceinline__ uint32_t coarse_bits(bool coarse_ray, uint32_t i) {
+    return coarse_ray ? (kCoarseRay | (i >= kCoarseFrom ? kCoarseNow : 0u)) : 0u;
+}
+
 // One iteration of RayCast (CpuRenderer.cpp:186-201) with GetStepPos (:135-171).
 // kSafe: the ray passed the bounds of ray_init, so no NaN can occur; the NaN test
 // is skipped and min uses fminf, which equals the minps rule on non-NaN operands up
@@ -204,10 +213,14 @@ enum : uint32_t { kStepContinue = 0, kStepHit = 1, kStepOut = 2 };
 // kGlsl: one iteration of rayCast (VoxelTraversal.glsl:170-199) instead: side
 // distances of the current voxel, tmin + 5 ulp (kept as the hit distance, so min
 // keeps the minps rule), position, bounds, then getStepPos (:100-131) whose empty
-// sectors take the 4th-level mask from the brick table.
+// sectors take the 4th-level mask from the brick table.  coarse (kGlsl only,
+// coarse_bits): rayCastCoarse's iteration instead, tmin + 0.001 (:213), and from
+// iteration 31 an empty voxel whose 4^3 cell holds a solid voxel stops the ray at the
+// cell's first solid voxel in mask order (getStepPos with coarse, :125-128, and
+// findAnyOccupiedPos, :41-53).
 template <bool kCount, bool kSafe = false, bool kGlsl = false>
 __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int32_t wox, int32_t woy, int32_t woz,
-                                             TraceCounters& cnt) {
+                                             TraceCounters& cnt, uint32_t coarse = 0) {
     if (kGlsl) {
         s.sx = __fadd_rn(s.tsx, __fmul_rn(rel_voxel(s.vx, wox), s.ix));
         s.sy = __fadd_rn(s.tsy, __fmul_rn(rel_voxel(s.vy, woy), s.iy));
@@ -215,7 +228,9 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
         // +5 ulp as an integer add on the bits; a NaN tmin stays NaN (its bit pattern
         // differs between platforms: the GPU's 0x7FFFFFFF would wrap to a denormal)
         const float m = min_x86(min_x86(s.sx, s.sy), s.sz);
-        const float t = (!kSafe && m != m) ? m : __uint_as_float(__float_as_uint(m) + 5u);
+        const float t = (coarse & kCoarseRay) ? __fadd_rn(m, 0.001f)
+                        : (!kSafe && m != m) ? m
+                                             : __uint_as_float(__float_as_uint(m) + 5u);
         s.tb = t;
         s.cx = __fadd_rn(s.ox, __fmul_rn(t, s.dx));
         s.cy = __fadd_rn(s.oy, __fmul_rn(t, s.dy));
@@ -264,6 +279,21 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
             s.vz = vz;
             return kStepHit;
         }
+        if (kGlsl && (coarse & kCoarseNow) && code != 3u) {
+            // the cell's mask is not empty (lod < 4): its first solid voxel, bit
+            // x + z*4 + y*16 of the cell mask, is the hit (mask-order scan of the payload)
+            const uint8_t* cell = w.payload + (size_t)e * 512 + ((lx & 4u) | (lz & 4u) << 3 | (ly & 4u) << 6);
+            for (uint32_t j = 0; j < 64; j++) {
+                const uint32_t mat = __ldg(cell + ((j & 3u) | ((j >> 2) & 3u) << 3 | (j >> 4) << 6));
+                if (mat) {
+                    s.material = mat;
+                    s.vx = (vx & ~3) | (int32_t)(j & 3u);
+                    s.vy = (vy & ~3) | (int32_t)(j >> 4);
+                    s.vz = (vz & ~3) | (int32_t)((j >> 2) & 3u);
+                    return kStepHit;
+                }
+            }
+        }
         m = (int32_t)code;
     } else {
         m = kGlsl ? (int32_t)((e >> 8) & 127u) : (int32_t)(e & 31u);
@@ -295,18 +325,18 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
 template <bool kCount, bool kGlsl = false>
 __device__ __forceinline__ void trace_ray(const DevWorld& w, float ox, float oy, float oz, float dx, float dy,
                                           float dz, int32_t wox, int32_t woy, int32_t woz, uint32_t max_iters,
-                                          TraceResult& r, TraceCounters& cnt) {
+                                          TraceResult& r, TraceCounters& cnt, bool coarse_ray = false) {
     RayState s;
     const bool safe = ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
     uint32_t st = kStepOut, i = 0;
     if (safe) {
         for (; i < max_iters; i++) {
-            st = ray_step<kCount, true, kGlsl>(s, w, wox, woy, woz, cnt);
+            st = ray_step<kCount, true, kGlsl>(s, w, wox, woy, woz, cnt, kGlsl ? coarse_bits(coarse_ray, i) : 0u);
             if (st != kStepContinue) break;
         }
     } else {
         for (; i < max_iters; i++) {
-            st = ray_step<kCount, false, kGlsl>(s, w, wox, woy, woz, cnt);
+            st = ray_step<kCount, false, kGlsl>(s, w, wox, woy, woz, cnt, kGlsl ? coarse_bits(coarse_ray, i) : 0u);
             if (st != kStepContinue) break;
         }
     }
