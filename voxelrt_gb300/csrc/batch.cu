@@ -36,14 +36,20 @@ __device__ __forceinline__ bool run_ray(RayState& s, bool safe, const DevWorld& 
                                         int32_t woz, uint32_t max_iters, uint32_t& steps, TraceCounters& cnt,
                                         bool coarse_ray = false) {
     uint32_t st = kStepOut, i = 0;
-    if (safe) {
+    if (kGlsl && coarse_ray) {
         for (; i < max_iters; i++) {
-            st = ray_step<kCount, true, kGlsl>(s, w, wox, woy, woz, cnt, kGlsl ? coarse_bits(coarse_ray, i) : 0u);
+            st = safe ? ray_step<kCount, true, kGlsl, true>(s, w, wox, woy, woz, cnt, coarse_bits(true, i))
+                      : ray_step<kCount, false, kGlsl, true>(s, w, wox, woy, woz, cnt, coarse_bits(true, i));
+            if (st != kStepContinue) break;
+        }
+    } else if (safe) {
+        for (; i < max_iters; i++) {
+            st = ray_step<kCount, true, kGlsl>(s, w, wox, woy, woz, cnt);
             if (st != kStepContinue) break;
         }
     } else {
         for (; i < max_iters; i++) {
-            st = ray_step<kCount, false, kGlsl>(s, w, wox, woy, woz, cnt, kGlsl ? coarse_bits(coarse_ray, i) : 0u);
+            st = ray_step<kCount, false, kGlsl>(s, w, wox, woy, woz, cnt);
             if (st != kStepContinue) break;
         }
     }
@@ -466,21 +472,29 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
         // (an active lane always has iter < max_iters); the fast step when every
         // tracing lane of the warp is safe
         const bool all_safe = __all_sync(0xffffffffu, !active || (path & kSafe) != 0);
+        // GLSL mode: does any lane trace a shadow or bounce ray (rayCastCoarse's)?
+        const bool any_coarse = kGlsl && __any_sync(0xffffffffu, active && (path & 0xFFu) != 0);
         if (active) {
             const uint32_t kmax = min(p.inner, max_iters - iter);
             uint32_t k = 0, st = kStepContinue;
-            // GLSL mode: a pixel's shadow and bounce rays are rayCastCoarse's
-            const bool coarse_ray = kGlsl && (path & 0xFFu) != 0;
-            if (all_safe) {
+            if (any_coarse) {
+                // GLSL mode, some lane traces a shadow or bounce ray: rayCastCoarse's
+                const bool coarse_ray = (path & 0xFFu) != 0;
                 for (; k < kmax; k++) {
-                    st = ray_step<kCount, true, kGlsl>(s, w, wox, woy, woz, cnt,
-                                                       kGlsl ? coarse_bits(coarse_ray, iter + k) : 0u);
+                    st = all_safe ? ray_step<kCount, true, kGlsl, true>(s, w, wox, woy, woz, cnt,
+                                                                        coarse_bits(coarse_ray, iter + k))
+                                  : ray_step<kCount, false, kGlsl, true>(s, w, wox, woy, woz, cnt,
+                                                                         coarse_bits(coarse_ray, iter + k));
+                    if (st != kStepContinue) break;
+                }
+            } else if (all_safe) {
+                for (; k < kmax; k++) {
+                    st = ray_step<kCount, true, kGlsl>(s, w, wox, woy, woz, cnt);
                     if (st != kStepContinue) break;
                 }
             } else {
                 for (; k < kmax; k++) {
-                    st = ray_step<kCount, false, kGlsl>(s, w, wox, woy, woz, cnt,
-                                                        kGlsl ? coarse_bits(coarse_ray, iter + k) : 0u);
+                    st = ray_step<kCount, false, kGlsl>(s, w, wox, woy, woz, cnt);
                     if (st != kStepContinue) break;
                 }
             }

@@ -108,16 +108,22 @@ __global__ void __maxnreg__(48) cast_persistent_kernel(DevWorld w, const float4*
         if (active) {
             const uint32_t kmax = min(inner, max_iters - iter);
             uint32_t k = 0, st = kStepContinue;
-            if (all_safe) {
+            if (kGlsl && coarse) {  // rayCastCoarse rays (uniform over the launch)
                 for (; k < kmax; k++) {
-                    st = ray_step<false, true, kGlsl>(s, w, wox, woy, woz, cnt,
-                                                      kGlsl ? coarse_bits(coarse, iter + k) : 0u);
+                    st = all_safe ? ray_step<false, true, kGlsl, true>(s, w, wox, woy, woz, cnt,
+                                                                       coarse_bits(true, iter + k))
+                                  : ray_step<false, false, kGlsl, true>(s, w, wox, woy, woz, cnt,
+                                                                        coarse_bits(true, iter + k));
+                    if (st != kStepContinue) break;
+                }
+            } else if (all_safe) {
+                for (; k < kmax; k++) {
+                    st = ray_step<false, true, kGlsl>(s, w, wox, woy, woz, cnt);
                     if (st != kStepContinue) break;
                 }
             } else {
                 for (; k < kmax; k++) {
-                    st = ray_step<false, false, kGlsl>(s, w, wox, woy, woz, cnt,
-                                                       kGlsl ? coarse_bits(coarse, iter + k) : 0u);
+                    st = ray_step<false, false, kGlsl>(s, w, wox, woy, woz, cnt);
                     if (st != kStepContinue) break;
                 }
             }

@@ -213,12 +213,12 @@ __device__ __forceinline__ uint32_t coarse_bits(bool coarse_ray, uint32_t i) {
 // kGlsl: one iteration of rayCast (VoxelTraversal.glsl:170-199) instead: side
 // distances of the current voxel, tmin + 5 ulp (kept as the hit distance, so min
 // keeps the minps rule), position, bounds, then getStepPos (:100-131) whose empty
-// sectors take the 4th-level mask from the brick table.  coarse (kGlsl only,
-// coarse_bits): rayCastCoarse's iteration instead, tmin + 0.001 (:213), and from
-// iteration 31 an empty voxel whose 4^3 cell holds a solid voxel stops the ray at the
-// cell's first solid voxel in mask order (getStepPos with coarse, :125-128, and
-// findAnyOccupiedPos, :41-53).
-template <bool kCount, bool kSafe = false, bool kGlsl = false>
+// sectors take the 4th-level mask from the brick table.  kCoarse (with kGlsl): the
+// step may belong to a rayCastCoarse ray, as `coarse` (coarse_bits) says: tmin + 0.001
+// (:213) instead, and from iteration 31 an empty voxel whose 4^3 cell holds a solid
+// voxel stops the ray at the cell's first solid voxel in mask order (getStepPos with
+// coarse, :125-128, and findAnyOccupiedPos, :41-53).  Without kCoarse `coarse` is 0.
+template <bool kCount, bool kSafe = false, bool kGlsl = false, bool kCoarse = false>
 __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int32_t wox, int32_t woy, int32_t woz,
                                              TraceCounters& cnt, uint32_t coarse = 0) {
     if (kGlsl) {
@@ -228,7 +228,7 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
         // +5 ulp as an integer add on the bits; a NaN tmin stays NaN (its bit pattern
         // differs between platforms: the GPU's 0x7FFFFFFF would wrap to a denormal)
         const float m = min_x86(min_x86(s.sx, s.sy), s.sz);
-        const float t = (coarse & kCoarseRay) ? __fadd_rn(m, 0.001f)
+        const float t = (kCoarse && (coarse & kCoarseRay)) ? __fadd_rn(m, 0.001f)
                         : (!kSafe && m != m) ? m
                                              : __uint_as_float(__float_as_uint(m) + 5u);
         s.tb = t;
@@ -279,7 +279,7 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
             s.vz = vz;
             return kStepHit;
         }
-        if (kGlsl && (coarse & kCoarseNow) && code != 3u) {
+        if (kGlsl && kCoarse && (coarse & kCoarseNow) && code != 3u) {
             // the cell's mask is not empty (lod < 4): its first solid voxel, bit
             // x + z*4 + y*16 of the cell mask, is the hit (mask-order scan of the payload)
             const uint8_t* cell = w.payload + (size_t)e * 512 + ((lx & 4u) | (lz & 4u) << 3 | (ly & 4u) << 6);
@@ -329,14 +329,20 @@ __device__ __forceinline__ void trace_ray(const DevWorld& w, float ox, float oy,
     RayState s;
     const bool safe = ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
     uint32_t st = kStepOut, i = 0;
-    if (safe) {
+    if (kGlsl && coarse_ray) {
         for (; i < max_iters; i++) {
-            st = ray_step<kCount, true, kGlsl>(s, w, wox, woy, woz, cnt, kGlsl ? coarse_bits(coarse_ray, i) : 0u);
+            st = safe ? ray_step<kCount, true, kGlsl, true>(s, w, wox, woy, woz, cnt, coarse_bits(true, i))
+                      : ray_step<kCount, false, kGlsl, true>(s, w, wox, woy, woz, cnt, coarse_bits(true, i));
+            if (st != kStepContinue) break;
+        }
+    } else if (safe) {
+        for (; i < max_iters; i++) {
+            st = ray_step<kCount, true, kGlsl>(s, w, wox, woy, woz, cnt);
             if (st != kStepContinue) break;
         }
     } else {
         for (; i < max_iters; i++) {
-            st = ray_step<kCount, false, kGlsl>(s, w, wox, woy, woz, cnt, kGlsl ? coarse_bits(coarse_ray, i) : 0u);
+            st = ray_step<kCount, false, kGlsl>(s, w, wox, woy, woz, cnt);
             if (st != kStepContinue) break;
         }
     }
