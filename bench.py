@@ -51,7 +51,9 @@ def parse():
     ap.add_argument("--glsl", action="store_true",
                     help="trace every view in the GLSL mode (the GPU renderer's rayCast) instead of the CPU traversal")
     ap.add_argument("--serve-rates", default="50,200,1000,2000", help="render requests per second to sweep")
-    ap.add_argument("--serve-seconds", type=float, default=2.0, help="duration of each arrival-rate run")
+    ap.add_argument("--serve-seconds", type=float, default=2.0, help="duration of each arrival-rate run, at least")
+    ap.add_argument("--serve-min-requests", type=int, default=400,
+                    help="renders per arrival rate, at least (longer runs at low rates)")
     ap.add_argument("--serve-worlds", type=int, default=32)
     ap.add_argument("--serve-max-edge", type=int, default=1024)
     ap.add_argument("--worlds", type=int, default=128, help="uneven_batch: number of worlds")
@@ -464,7 +466,9 @@ def run_serving(args, dev):
         w.close()
     return {"worlds": len(datas), "max_edge": max(edges), "world_bytes": int(sum(d.n_bricks for d in datas) * 1024),
             "edit_latency": edit_lat, "resolutions": "256^2 / 1280x720 / 1920x1080 at p 0.5 / 0.3 / 0.2",
-            "edits_per_s": 100, "seconds_per_rate": args.serve_seconds,
+            "edits_per_s": 100,
+            "seconds_per_rate": f"max({args.serve_seconds}, {args.serve_min_requests} / rate): at least "
+                                f"{args.serve_min_requests} renders per rate for the p99",
             "mode": "resident", "rates": modes["resident"]["rates"],
             "oracle_replay": modes["resident"]["oracle_replay"], "launches": modes["launches"],
             "latency": "submit to records in pinned host memory, server clock"}
@@ -498,7 +502,8 @@ def serve_sweep(args, v, datas, worlds, edges, surf, resident):
     check_world = int(np.argmin(edges))
     replay = {"renders": 0, "bit_exact": True}
     for ri, lam in enumerate(float(x) for x in args.serve_rates.split(",")):
-        sched = W.serving_schedule(lam, args.serve_seconds, len(worlds), edges, seed=100 + ri)
+        seconds = max(args.serve_seconds, args.serve_min_requests / lam)
+        sched = W.serving_schedule(lam, seconds, len(worlds), edges, seed=100 + ri)
         srv.stats(reset=True)
         free = list(range(len(bufs)))
         inflight = collections.deque()
