@@ -30,6 +30,8 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
+# device bytes per brick slot: 512 payload + 512 voxel codes + 64 cell masks
+SLOT_BYTES = 512 + 512 + 64
 METRIC = "Grays/s batched vs per-view launch (bit-exact hits); p50/p99 request latency"
 HIT_BYTES = 16
 
@@ -50,6 +52,7 @@ def parse():
     ap.add_argument("--stress-rays", type=int, default=1 << 26, help="incoherent: number of stress rays")
     ap.add_argument("--glsl", action="store_true",
                     help="trace every view in the GLSL mode (the GPU renderer's rayCast) instead of the CPU traversal")
+    ap.add_argument("--aniso", action="store_true", help="the GLSL mode with anisotropic LODs (implies --glsl)")
     ap.add_argument("--serve-rates", default="50,200,1000,2000", help="render requests per second to sweep")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="duration of each arrival-rate run, at least")
     ap.add_argument("--serve-min-requests", type=int, default=400,
@@ -97,11 +100,12 @@ def build_workload(name: str, rank: int, args=None, world_size: int = 1):
     the one batch (strong scaling, uneven_batch only).  With --glsl every view traces in
     the GLSL mode (the GPU renderer's rayCast)."""
     wl = _build_workload(name, rank, args, world_size)
-    if args is not None and getattr(args, "glsl", False):
+    if args is not None and (getattr(args, "glsl", False) or getattr(args, "aniso", False)):
         from voxelrt_gb300 import capi
+        aniso = getattr(args, "aniso", False)
         for vw in wl.views:
-            vw.flags |= capi.VIEW_GLSL
-        wl.description += ", GLSL traversal mode"
+            vw.flags |= capi.VIEW_GLSL | (capi.VIEW_GLSL_ANISO if aniso else 0)
+        wl.description += ", GLSL traversal mode" + (" with anisotropic LODs" if aniso else "")
     return wl
 
 
@@ -206,9 +210,18 @@ def host_cores() -> int:
         return os.cpu_count() or 1
 
 
+def traversal_name(args) -> str:
+    return "glsl_aniso" if args.aniso else "glsl" if args.glsl else "cpu"
+
+
 def view_is_glsl(vw) -> bool:
     from voxelrt_gb300 import capi
     return bool(vw.flags & capi.VIEW_GLSL)
+
+
+def view_is_aniso(vw) -> bool:
+    from voxelrt_gb300 import capi
+    return bool(vw.flags & capi.VIEW_GLSL_ANISO)
 
 
 def cpu_oracle_sample(wl, seconds: float, threads: int = 0):
@@ -225,14 +238,15 @@ def cpu_oracle_sample(wl, seconds: float, threads: int = 0):
             o.upload(wl.worlds[vw.world])
             cache[vw.world] = o
         o = cache[vw.world]
-        glsl = view_is_glsl(vw)
+        glsl, aniso = view_is_glsl(vw), view_is_aniso(vw)
         t0 = time.perf_counter()
         if vw.flags & 1:
-            o.render_view_shadow(vw.cam, np.array(vw.sun_dir[:], np.float32), vw.max_iters, threads, glsl=glsl)
+            o.render_view_shadow(vw.cam, np.array(vw.sun_dir[:], np.float32), vw.max_iters, threads, glsl=glsl,
+                                 aniso=aniso)
         elif vw.n_bounces:
-            o.render_view_bounces(vw.cam, vw.n_bounces, vw.max_iters, threads, glsl=glsl)
+            o.render_view_bounces(vw.cam, vw.n_bounces, vw.max_iters, threads, glsl=glsl, aniso=aniso)
         else:
-            o.render_view(vw.cam, vw.max_iters, threads, glsl=glsl)
+            o.render_view(vw.cam, vw.max_iters, threads, glsl=glsl, aniso=aniso)
         elapsed += time.perf_counter() - t0
         rays += o.last_stats["rays"]
         nviews += 1
@@ -260,7 +274,8 @@ def run_reference(args):
         tot_rays += r
         tot_t += t
     value = tot_rays / tot_t / 1e9
-    algo = ("VoxelTraversal.glsl rayCast" if args.glsl else "CpuRenderer.cpp RayCast")
+    algo = ("VoxelTraversal.glsl rayCast" + (" with anisotropic LODs" if args.aniso else "")
+            if args.glsl or args.aniso else "CpuRenderer.cpp RayCast")
     sample = (f"{nv} smallest views of the {wl.name} workload per step ({tot_rays // max(args.steps, 1)} rays), "
               f"scalar C++ restatement of {algo}, all {cores} host threads")
     line = {
@@ -268,7 +283,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / max(args.steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": wl.name, "description": wl.description,
-                   "traversal": "glsl" if args.glsl else "cpu"},
+                   "traversal": traversal_name(args)},
         "cpu_baseline": {"value": value, "unit": "Grays/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "Grays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -403,11 +418,11 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": wl.name, "description": wl.description, "worlds": len(wl.worlds),
                        "views": len(wl.views), "rays_per_step": rays_per_step, "records_per_step": n_rec,
-                       "world_bytes": int(sum(d.n_bricks for d in wl.worlds) * 1024),
+                       "world_bytes": int(sum(d.n_bricks for d in wl.worlds) * SLOT_BYTES),
                        "l2": "inputs larger than L2 (brick pools of all worlds)",
                        "batch_config": autotune.describe(cfg), "batch_config_source": cfg_src,
                        "launch": "persistent kernel + queue reset, CUDA graph replay",
-                       "traversal": "glsl" if args.glsl else "cpu"},
+                       "traversal": traversal_name(args)},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
             "clocks": clk.summary(), "per_view": per_view,
             "batched_over_per_view": (value / per_view["value"]) if per_view else None,
@@ -464,7 +479,7 @@ def run_serving(args, dev):
     edit_lat = edit_latency(v, worlds, edges, surf)
     for w in worlds:
         w.close()
-    return {"worlds": len(datas), "max_edge": max(edges), "world_bytes": int(sum(d.n_bricks for d in datas) * 1024),
+    return {"worlds": len(datas), "max_edge": max(edges), "world_bytes": int(sum(d.n_bricks for d in datas) * SLOT_BYTES),
             "edit_latency": edit_lat, "resolutions": "256^2 / 1280x720 / 1920x1080 at p 0.5 / 0.3 / 0.2",
             "edits_per_s": 100,
             "seconds_per_rate": f"max({args.serve_seconds}, {args.serve_min_requests} / rate): at least "
@@ -658,14 +673,14 @@ def parity_sample(wl, batch, hits, stream, max_views=3):
         vw = wl.views[i]
         o = OracleWorld(wl.worlds[vw.world].sectors)
         o.upload(wl.worlds[vw.world])
-        glsl = view_is_glsl(vw)
+        glsl, aniso = view_is_glsl(vw), view_is_aniso(vw)
         if vw.flags & 1:
             want = np.stack(o.render_view_shadow(vw.cam, np.array(vw.sun_dir[:], np.float32), vw.max_iters,
-                                                 glsl=glsl))
+                                                 glsl=glsl, aniso=aniso))
         elif vw.n_bounces:
-            want = o.render_view_bounces(vw.cam, vw.n_bounces, vw.max_iters, glsl=glsl)
+            want = o.render_view_bounces(vw.cam, vw.n_bounces, vw.max_iters, glsl=glsl, aniso=aniso)
         else:
-            want = o.render_view(vw.cam, vw.max_iters, glsl=glsl)[None]
+            want = o.render_view(vw.cam, vw.max_iters, glsl=glsl, aniso=aniso)[None]
         a, b = int(batch.offsets[i]), int(batch.offsets[i + 1])
         got = hits[a * HIT_BYTES:b * HIT_BYTES].cpu().numpy().view(v.HIT_DTYPE).reshape(want.shape)
         ok &= hits_match(got, want)

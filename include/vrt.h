@@ -99,7 +99,7 @@ typedef struct vrt_hit {
 typedef struct vrt_cast_params {
     int32_t world_origin[3]; /* FrameConstants::WorldOrigin (CpuRenderer.cpp:447) */
     uint32_t max_iters;      /* 0 = VRT_DEFAULT_MAX_ITERS (VRT_GLSL_MAX_ITERS in GLSL mode); at most 65535 */
-    uint32_t flags;          /* 0, VRT_CAST_GLSL or VRT_CAST_GLSL | VRT_CAST_GLSL_COARSE */
+    uint32_t flags;          /* 0, or VRT_CAST_GLSL with VRT_CAST_GLSL_COARSE and/or VRT_CAST_GLSL_ANISO */
 } vrt_cast_params;
 
 /* Traversal modes.  The default is the reference CPU traversal (CpuRenderer.cpp:135-224,
@@ -130,6 +130,12 @@ typedef struct vrt_cast_params {
  * shared with the default mode. */
 #define VRT_CAST_GLSL 1u
 #define VRT_CAST_GLSL_COARSE 2u
+/* With VRT_CAST_GLSL (or on a view, VRT_VIEW_GLSL_ANISO with VRT_VIEW_GLSL): the GPU
+ * renderer's anisotropic LODs (u_UseAnisotropicLods, off by default there;
+ * VoxelTraversal.glsl:116-121): getStepPos restricts the occupancy mask of the level it
+ * reads (4^3 cell, sector or sector group) to the cells ahead of the ray in its octant
+ * (RayCellInteractionMaskLUT, GpuRenderer.cpp:193-210) before taking its LOD. */
+#define VRT_CAST_GLSL_ANISO 4u
 #define VRT_GLSL_MAX_ITERS 256
 #define VRT_GLSL_COARSE_MAX_ITERS 96
 
@@ -310,12 +316,13 @@ typedef struct vrt_view {
     uint32_t world;     /* index into the batch's world list */
     uint32_t max_iters; /* 0 = VRT_DEFAULT_MAX_ITERS */
     uint32_t n_bounces; /* 0..15, exclusive with VRT_VIEW_SHADOW */
-    uint32_t flags;     /* VRT_VIEW_SHADOW, VRT_VIEW_GLSL */
+    uint32_t flags;     /* VRT_VIEW_SHADOW, VRT_VIEW_GLSL, VRT_VIEW_GLSL_ANISO */
     float sun_dir[3];
 } vrt_view;
 
 #define VRT_VIEW_SHADOW 1u
 #define VRT_VIEW_GLSL 2u /* GLSL traversal mode (see VRT_CAST_GLSL); every view of a batch shares one mode */
+#define VRT_VIEW_GLSL_ANISO 4u /* with VRT_VIEW_GLSL: anisotropic LODs (see VRT_CAST_GLSL_ANISO) */
 #define VRT_MAX_BOUNCES 15u
 
 /* One view with its secondary rays, one plain launch (thread per pixel, no
@@ -374,7 +381,7 @@ vrt_status vrt_batch_measure(vrt_batch* batch, vrt_hit* hits_device, void* strea
  * no memory: no counterpart in the reference.  For callers that cannot call
  * cudaMalloc once their frame loop runs (it may synchronise the device) or whose
  * host application owns all device memory.  The launch scratch (world table, view
- * table, tile-queue counter) lives in one fixed 148.5 KiB device array that every GPU
+ * table, tile-queue counter) lives in one fixed 152.5 KiB device array that every GPU
  * loading the library holds until the process exits, so a call takes at most 256
  * worlds and 1024 views (VRT_ERR_INVALID_ARG beyond).  The first call on a device
  * looks up that array's address; make it before any stream capture.  All calls

@@ -55,6 +55,7 @@ def lib() -> C.CDLL:
         L.ora_world_allocated_bricks.restype = C.c_uint64
         L.ora_world_allocated_bricks.argtypes = [_vp]
         L.ora_cast.argtypes = [_vp, _vp, C.c_uint64, C.POINTER(_CastParams), _vp, C.c_int, C.POINTER(Stats)]
+        L.ora_ray_cell_lut.argtypes = [_vp]
         L.ora_camera_rays.argtypes = [_vp, _vp]
         L.ora_render_view.argtypes = [_vp, _vp, C.c_uint32, C.c_uint32, _vp, C.c_int, C.POINTER(Stats)]
         L.ora_render_view_shadow.argtypes = [_vp, _vp, _vp, C.c_uint32, C.c_uint32, _vp, _vp, C.c_int,
@@ -74,6 +75,18 @@ def _chk(rc: int) -> None:
 
 def _stats(s: Stats) -> dict:
     return {f: getattr(s, f) for f, _ in s._fields_}
+
+
+def ray_cell_lut() -> np.ndarray:
+    """The oracle's RayCellInteractionMaskLUT: 512 u64 masks, entry idx + octant*64."""
+    out = np.zeros(512, np.uint64)
+    _chk(lib().ora_ray_cell_lut(out.ctypes.data))
+    return out
+
+
+def _mode(glsl: bool, aniso: bool) -> int:
+    """Traversal mode of the render calls: 0 CPU, 1 GLSL, 3 GLSL with anisotropic LODs."""
+    return (1 if glsl or aniso else 0) | (2 if aniso else 0)
 
 
 class OracleWorld:
@@ -128,41 +141,43 @@ class OracleWorld:
     def allocated_bricks(self) -> int:
         return lib().ora_world_allocated_bricks(self._h)
 
-    def cast(self, rays, world_origin=(0, 0, 0), max_iters=0, threads=0, glsl=False, coarse=False) -> np.ndarray:
+    def cast(self, rays, world_origin=(0, 0, 0), max_iters=0, threads=0, glsl=False, coarse=False,
+             aniso=False) -> np.ndarray:
         """glsl: the GPU renderer's rayCast (flag VRT_CAST_GLSL) instead of the CPU traversal;
-        with coarse also its rayCastCoarse (VRT_CAST_GLSL_COARSE)."""
+        with coarse its rayCastCoarse (VRT_CAST_GLSL_COARSE), with aniso its anisotropic
+        LODs (VRT_CAST_GLSL_ANISO)."""
         rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
         hits = np.zeros(len(rays), HIT_DTYPE)
-        p = _CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), (1 if glsl else 0) | (2 if coarse else 0))
+        p = _CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), (1 if glsl else 0) | (2 if coarse else 0) | (4 if aniso else 0))
         s = Stats()
         _chk(lib().ora_cast(self._h, rays.ctypes.data, len(rays), C.byref(p), hits.ctypes.data, int(threads),
                             C.byref(s)))
         self.last_stats = _stats(s)
         return hits
 
-    def render_view(self, cam, max_iters=0, threads=0, glsl=False) -> np.ndarray:
+    def render_view(self, cam, max_iters=0, threads=0, glsl=False, aniso=False) -> np.ndarray:
         hits = np.zeros(cam.width * cam.height, HIT_DTYPE)
         s = Stats()
-        _chk(lib().ora_render_view(self._h, C.addressof(cam), int(max_iters), int(glsl), hits.ctypes.data,
+        _chk(lib().ora_render_view(self._h, C.addressof(cam), int(max_iters), _mode(glsl, aniso), hits.ctypes.data,
                                    int(threads), C.byref(s)))
         self.last_stats = _stats(s)
         return hits
 
-    def render_view_shadow(self, cam, sun_dir, max_iters=0, threads=0, glsl=False):
+    def render_view_shadow(self, cam, sun_dir, max_iters=0, threads=0, glsl=False, aniso=False):
         n = cam.width * cam.height
         prim, shad = np.zeros(n, HIT_DTYPE), np.zeros(n, HIT_DTYPE)
         sd = np.ascontiguousarray(sun_dir, dtype=np.float32)
         s = Stats()
-        _chk(lib().ora_render_view_shadow(self._h, C.addressof(cam), sd.ctypes.data, int(max_iters), int(glsl),
+        _chk(lib().ora_render_view_shadow(self._h, C.addressof(cam), sd.ctypes.data, int(max_iters), _mode(glsl, aniso),
                                           prim.ctypes.data, shad.ctypes.data, int(threads), C.byref(s)))
         self.last_stats = _stats(s)
         return prim, shad
 
-    def render_view_bounces(self, cam, n_bounces, max_iters=0, threads=0, glsl=False) -> np.ndarray:
+    def render_view_bounces(self, cam, n_bounces, max_iters=0, threads=0, glsl=False, aniso=False) -> np.ndarray:
         n = cam.width * cam.height
         hits = np.zeros((n_bounces + 1) * n, HIT_DTYPE)
         s = Stats()
-        _chk(lib().ora_render_view_bounces(self._h, C.addressof(cam), int(n_bounces), int(max_iters), int(glsl),
+        _chk(lib().ora_render_view_bounces(self._h, C.addressof(cam), int(n_bounces), int(max_iters), _mode(glsl, aniso),
                                            hits.ctypes.data, int(threads), C.byref(s)))
         self.last_stats = _stats(s)
         return hits.reshape(n_bounces + 1, n)

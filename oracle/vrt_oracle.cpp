@@ -214,21 +214,57 @@ inline int32_t iso_lod(uint64_t m, uint32_t idx) {
     return ((half >> (idx & 0xA)) & 0x00330033u) == 0 ? 2 : 1;
 }
 
-// getStepPos (VoxelTraversal.glsl:100-131), anisotropic LODs off.  With coarse
-// (rayCastCoarse from iteration 31, :218), an empty voxel whose 4^3 cell mask is not
-// empty (lod < 4, :125) is a hit on the cell's first solid voxel, the lowest set bit of
-// the mask (findAnyOccupiedPos, :41-53).  Returns true on a hit.
+// RayCellInteractionMaskLUT (GenerateRayCellInteractionMaskLUT, GpuRenderer.cpp:193-210):
+// for octant o (axis a stepping +1 when bit a of o is set, else -1) and cell origin i of
+// a 4^3 mask, the cells origin + j*dir for the 64 offsets j that stay inside the block.
+struct RayCellLut {
+    uint64_t m[512];
+    RayCellLut() {
+        for (uint32_t oct = 0; oct < 8; oct++) {
+            const int32_t dir[3] = {(int32_t)(oct & 1) * 2 - 1, (int32_t)((oct >> 1) & 1) * 2 - 1,
+                                    (int32_t)((oct >> 2) & 1) * 2 - 1};
+            for (uint32_t o = 0; o < 64; o++) {
+                const int32_t op[3] = {(int32_t)(o & 3), (int32_t)(o >> 4), (int32_t)((o >> 2) & 3)};  // x, y, z
+                uint64_t mask = 0;
+                for (uint32_t j = 0; j < 64; j++) {
+                    const int32_t jp[3] = {(int32_t)(j & 3), (int32_t)(j >> 4), (int32_t)((j >> 2) & 3)};
+                    int32_t p[3];
+                    bool in = true;
+                    for (int c = 0; c < 3; c++) {
+                        p[c] = op[c] + jp[c] * dir[c];
+                        in = in && p[c] >= 0 && p[c] < 4;
+                    }
+                    if (in) mask |= 1ull << (uint32_t)(p[0] | p[2] << 2 | p[1] << 4);
+                }
+                m[o + oct * 64] = mask;
+            }
+        }
+    }
+};
+const RayCellLut& ray_cell_lut() {
+    static const RayCellLut lut;
+    return lut;
+}
+
+// getStepPos (VoxelTraversal.glsl:92-131) in the reference's order: the level's mask
+// (sector at scale 8, 4^3 cell at scale 1 when the brick is allocated, sector group at
+// scale 32 when the sector is empty), with aniso (u_UseAnisotropicLods, :116-121) masked
+// by the ray's octant LUT entry, its isotropic LOD times the scale, and with coarse
+// (rayCastCoarse from iteration 31, :218) a LOD below 4 ends the ray on the mask's
+// lowest set cell (findAnyOccupiedPos, :41-53).  Returns true on a hit.
 inline bool get_step_pos_glsl(const ora_world& w, int32_t vp[3], const float dir[3], Trace& tr,
-                              bool coarse = false) {
+                              bool coarse = false, bool aniso = false) {
     const int32_t sx = vp[0] >> 5, sy = vp[1] >> 5, sz = vp[2] >> 5;
     uint32_t s = w.lin(sx, sy, sz);
     uint64_t m = w.masks[s];
     uint32_t idx = ((vp[0] >> 3) & 3) | ((vp[2] >> 3) & 3) << 2 | ((vp[1] >> 3) & 3) << 4;
     int32_t scale = 8;
+    const SectorBlock* blk = nullptr;
+    uint32_t brick = 0;
     tr.step_calls++;
     if ((m >> idx) & 1) {
-        const SectorBlock* blk = w.data[s].get();
-        uint32_t brick = idx;
+        blk = w.data[s].get();
+        brick = idx;
         uint32_t cell = ((vp[0] >> 2) & 1) | ((vp[2] >> 2) & 1) << 1 | ((vp[1] >> 2) & 1) << 2;
         m = blk->occ[brick * 8 + cell];
         idx = (vp[0] & 3) | (vp[2] & 3) << 2 | (vp[1] & 3) << 4;
@@ -239,22 +275,27 @@ inline bool get_step_pos_glsl(const ora_world& w, int32_t vp[3], const float dir
             tr.material = blk->vox[brick * 512 + vi];
             return true;
         }
-        if (coarse && m != 0) {
-            uint32_t b = 0;
-            while (!((m >> b) & 1)) b++;
-            vp[0] = (vp[0] & ~3) | (int32_t)(b & 3);
-            vp[1] = (vp[1] & ~3) | (int32_t)(b >> 4);
-            vp[2] = (vp[2] & ~3) | (int32_t)((b >> 2) & 3);
-            uint32_t vi = (vp[0] & 7) | (vp[2] & 7) << 3 | (vp[1] & 7) << 6;
-            tr.material = blk->vox[brick * 512 + vi];
-            return true;
-        }
     } else if (m == 0) {
         m = w.groups[(uint32_t)(sx >> 2) + (uint32_t)(sz >> 2) * w.gx() + (uint32_t)(sy >> 2) * w.gx() * w.gz()];
         idx = (uint32_t)((sx & 3) | (sz & 3) << 2 | (sy & 3) << 4);
         scale = 32;
     }
-    int32_t cm = iso_lod(m, idx) * scale - 1;
+    if (aniso) {
+        const uint32_t oct = (dir[0] < 0.0f ? 0u : 1u) + (dir[1] < 0.0f ? 0u : 2u) + (dir[2] < 0.0f ? 0u : 4u);
+        m &= ray_cell_lut().m[idx + oct * 64];
+    }
+    const int32_t lod = iso_lod(m, idx) * scale;
+    if (coarse && lod < 4) {
+        uint32_t b = 0;
+        while (!((m >> b) & 1)) b++;
+        vp[0] = (vp[0] & ~3) | (int32_t)(b & 3);
+        vp[1] = (vp[1] & ~3) | (int32_t)(b >> 4);
+        vp[2] = (vp[2] & ~3) | (int32_t)((b >> 2) & 3);
+        uint32_t vi = (vp[0] & 7) | (vp[2] & 7) << 3 | (vp[1] & 7) << 6;
+        tr.material = blk->vox[brick * 512 + vi];
+        return true;
+    }
+    const int32_t cm = lod - 1;
     for (int c = 0; c < 3; c++) vp[c] = dir[c] < 0.0f ? (vp[c] & ~cm) : (vp[c] | cm);
     return false;
 }
@@ -286,7 +327,7 @@ void clip_start(const ora_world& w, const float o[3], const float d[3], const fl
 // tmin + 5 ulp, the next position, bounds, getStepPos.  coarse: rayCastCoarse
 // (:206-240) instead, tmin + 0.001 and coarse steps from iteration 31.
 void trace_ray_glsl(const ora_world& w, const float o[3], const float d[3], const int32_t wo[3],
-                    uint32_t max_iters, Trace& tr, bool coarse = false) {
+                    uint32_t max_iters, Trace& tr, bool coarse = false, bool aniso = false) {
     tr.hit = false;
     tr.glsl = true;
     tr.tb = 0.0f;
@@ -320,7 +361,7 @@ void trace_ray_glsl(const ora_world& w, const float o[3], const float d[3], cons
             tr.steps = (uint16_t)i;
             return;
         }
-        if (get_step_pos_glsl(w, vp, d, tr, coarse && i >= 31)) {
+        if (get_step_pos_glsl(w, vp, d, tr, coarse && i >= 31, aniso)) {
             tr.hit = true;
             tr.tb = t;
             tr.steps = (uint16_t)i;
@@ -512,12 +553,15 @@ void bounce_dir(uint32_t pixel, uint32_t bounce, const float n[3], float out[3])
 
 // Traversal of one ray in the given mode.  secondary: a shadow or bounce ray, which the
 // GPU renderer casts with rayCastCoarse (VoxelRender.comp:56,74,81; cap 96).
-inline void trace_mode(const ora_world& w, bool glsl, const float o[3], const float d[3], const int32_t wo[3],
+// mode: 0 the CPU traversal, kModeGlsl the GLSL mode, | kModeAniso its anisotropic LODs.
+constexpr uint32_t kModeGlsl = 1, kModeAniso = 2;
+inline void trace_mode(const ora_world& w, uint32_t mode, const float o[3], const float d[3], const int32_t wo[3],
                        uint32_t max_iters, Trace& tr, bool secondary = false) {
-    if (glsl && secondary)
-        trace_ray_glsl(w, o, d, wo, std::min<uint32_t>(max_iters, VRT_GLSL_COARSE_MAX_ITERS), tr, true);
-    else if (glsl)
-        trace_ray_glsl(w, o, d, wo, max_iters, tr);
+    const bool aniso = (mode & kModeAniso) != 0;
+    if ((mode & kModeGlsl) && secondary)
+        trace_ray_glsl(w, o, d, wo, std::min<uint32_t>(max_iters, VRT_GLSL_COARSE_MAX_ITERS), tr, true, aniso);
+    else if (mode & kModeGlsl)
+        trace_ray_glsl(w, o, d, wo, max_iters, tr, false, aniso);
     else
         trace_ray(w, o, d, wo, max_iters, tr);
 }
@@ -663,17 +707,24 @@ uint64_t ora_world_allocated_bricks(const ora_world* w) {
     return n;
 }
 
+int ora_ray_cell_lut(uint64_t* out) {
+    if (!out) return -1;
+    std::memcpy(out, ray_cell_lut().m, sizeof(uint64_t) * 512);
+    return 0;
+}
+
 int ora_cast(const ora_world* w, const vrt_ray* rays, uint64_t n, const vrt_cast_params* params,
              vrt_hit* hits, int threads, ora_stats* stats) {
     if (!w || (n && (!rays || !hits)) || !params) return -1;
     const bool glsl = (params->flags & VRT_CAST_GLSL) != 0;
     const bool coarse = glsl && (params->flags & VRT_CAST_GLSL_COARSE) != 0;
+    const uint32_t mode = glsl ? (kModeGlsl | ((params->flags & VRT_CAST_GLSL_ANISO) ? kModeAniso : 0u)) : 0u;
     uint32_t iters = eff_iters_mode(params->max_iters, glsl);
     StatAcc acc(threads);
     parallel_for(n, (int)acc.per.size(), [&](int tid, uint64_t b, uint64_t e) {
         Trace tr;
         for (uint64_t i = b; i < e; i++) {
-            trace_mode(*w, glsl, rays[i].origin, rays[i].dir, params->world_origin, iters, tr, coarse);
+            trace_mode(*w, mode, rays[i].origin, rays[i].dir, params->world_origin, iters, tr, coarse);
             fill_hit(tr, rays[i].dir, rays[i].tag, hits[i]);
             acc.add(tid, tr);
         }
@@ -697,7 +748,7 @@ int ora_camera_rays(const vrt_camera* cam, vrt_ray* rays) {
 int ora_render_view(const ora_world* w, const vrt_camera* cam, uint32_t max_iters, uint32_t mode, vrt_hit* hits,
                     int threads, ora_stats* stats) {
     if (!w || !cam || !hits) return -1;
-    const bool glsl = mode != 0;
+    const bool glsl = (mode & kModeGlsl) != 0;
     uint32_t iters = eff_iters_mode(max_iters, glsl);
     uint64_t n = (uint64_t)cam->width * cam->height;
     StatAcc acc(threads);
@@ -706,7 +757,7 @@ int ora_render_view(const ora_world* w, const vrt_camera* cam, uint32_t max_iter
         float o[3], d[3];
         for (uint64_t i = b; i < e; i++) {
             camera_ray(*cam, (uint32_t)(i % cam->width), (uint32_t)(i / cam->width), o, d);
-            trace_mode(*w, glsl, o, d, cam->world_origin, iters, tr);
+            trace_mode(*w, mode, o, d, cam->world_origin, iters, tr);
             fill_hit(tr, d, (uint32_t)i, hits[i]);
             acc.add(tid, tr);
         }
@@ -719,7 +770,7 @@ int ora_render_view_shadow(const ora_world* w, const vrt_camera* cam, const floa
                            uint32_t max_iters, uint32_t mode, vrt_hit* primary, vrt_hit* shadow, int threads,
                            ora_stats* stats) {
     if (!w || !cam || !sun_dir || !primary || !shadow) return -1;
-    const bool glsl = mode != 0;
+    const bool glsl = (mode & kModeGlsl) != 0;
     uint32_t iters = eff_iters_mode(max_iters, glsl);
     uint64_t n = (uint64_t)cam->width * cam->height;
     StatAcc acc(threads);
@@ -728,7 +779,7 @@ int ora_render_view_shadow(const ora_world* w, const vrt_camera* cam, const floa
         float o[3], d[3], nrm[3], so[3];
         for (uint64_t i = b; i < e; i++) {
             camera_ray(*cam, (uint32_t)(i % cam->width), (uint32_t)(i / cam->width), o, d);
-            trace_mode(*w, glsl, o, d, cam->world_origin, iters, tr);
+            trace_mode(*w, mode, o, d, cam->world_origin, iters, tr);
             fill_hit(tr, d, (uint32_t)i, primary[i]);
             acc.add(tid, tr);
             if (!tr.hit) {
@@ -737,7 +788,7 @@ int ora_render_view_shadow(const ora_world* w, const vrt_camera* cam, const floa
             }
             hit_normal(tr, d, nrm);
             offset_origin(tr, nrm, so);
-            trace_mode(*w, glsl, so, sun_dir, cam->world_origin, iters, ts, true);
+            trace_mode(*w, mode, so, sun_dir, cam->world_origin, iters, ts, true);
             fill_hit(ts, sun_dir, (uint32_t)i, shadow[i]);
             acc.add(tid, ts);
         }
@@ -749,7 +800,7 @@ int ora_render_view_shadow(const ora_world* w, const vrt_camera* cam, const floa
 int ora_render_view_bounces(const ora_world* w, const vrt_camera* cam, uint32_t n_bounces,
                             uint32_t max_iters, uint32_t mode, vrt_hit* hits, int threads, ora_stats* stats) {
     if (!w || !cam || !hits) return -1;
-    const bool glsl = mode != 0;
+    const bool glsl = (mode & kModeGlsl) != 0;
     uint32_t iters = eff_iters_mode(max_iters, glsl);
     uint64_t n = (uint64_t)cam->width * cam->height;
     StatAcc acc(threads);
@@ -770,7 +821,7 @@ int ora_render_view_bounces(const ora_world* w, const vrt_camera* cam, uint32_t 
                     offset_origin(tr, nrm, o);
                     bounce_dir((uint32_t)i, k, nrm, d);
                 }
-                trace_mode(*w, glsl, o, d, cam->world_origin, iters, tr, k > 0);
+                trace_mode(*w, mode, o, d, cam->world_origin, iters, tr, k > 0);
                 fill_hit(tr, d, (uint32_t)i, h);
                 acc.add(tid, tr);
                 alive = tr.hit;

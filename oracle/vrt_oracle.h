@@ -54,7 +54,11 @@ int ora_cast(const ora_world* w, const vrt_ray* rays, uint64_t n, const vrt_cast
              vrt_hit* hits, int threads, ora_stats* stats);
 /* Camera rays of a view (the ray generation of vrt_camera). */
 int ora_camera_rays(const vrt_camera* cam, vrt_ray* rays);
-/* mode: 0 = the reference CPU traversal, nonzero = the GLSL mode (VRT_VIEW_GLSL). */
+/* RayCellInteractionMaskLUT (GpuRenderer.cpp:193-210): 512 masks, entry idx + octant*64. */
+int ora_ray_cell_lut(uint64_t* out);
+
+/* mode: 0 = the reference CPU traversal, 1 = the GLSL mode (VRT_VIEW_GLSL), 3 = the GLSL
+ * mode with anisotropic LODs (VRT_VIEW_GLSL_ANISO). */
 int ora_render_view(const ora_world* w, const vrt_camera* cam, uint32_t max_iters, uint32_t mode, vrt_hit* hits,
                     int threads, ora_stats* stats);
 /* Primary ray, then for every hit one shadow ray from hitPos + normal*0.01

@@ -51,6 +51,7 @@ inline float __uint_as_float(unsigned u) {
     return f;
 }
 inline int __popc(unsigned x) { return __builtin_popcount(x); }
+inline int __ffsll(long long x) { return __builtin_ffsll(x); }
 template <typename T>
 inline T __ldg(const T* p) {
     return *p;
@@ -74,11 +75,24 @@ int main(int argc, char** argv) {
     if (std::fread(bricks.data(), 4, npos, f) != npos) return 5;
     if (std::fread(codes.data(), 1, codes.size(), f) != codes.size()) return 6;
     if (std::fread(payload.data(), 1, payload.size(), f) != payload.size()) return 7;
+    const size_t nsec = (size_t)dims[0] * dims[1] * dims[2];
+    const size_t ngroups = (size_t)((dims[0] + 3) / 4) * ((dims[1] + 3) / 4) * ((dims[2] + 3) / 4);
+    std::vector<uint64_t> cells((size_t)nslots * 8), groups(ngroups);
+    std::vector<SectorRec> sectors(nsec);
+    if (std::fread(cells.data(), 8, cells.size(), f) != cells.size()) return 9;
+    if (std::fread(sectors.data(), sizeof(SectorRec), nsec, f) != nsec) return 10;
+    if (std::fread(groups.data(), 8, ngroups, f) != ngroups) return 11;
     std::fclose(f);
     DevWorld w{};
     w.bricks = bricks.data();
     w.codes = codes.data();
     w.payload = payload.data();
+    w.cells = cells.data();
+    w.sectors = sectors.data();
+    w.groups = groups.data();
+    w.sx = dims[0];
+    w.sz = dims[2];
+    w.sxz = dims[0] * dims[2];
     w.bsx = dims[0] * 4;
     w.bsxz = dims[0] * 4 * dims[2] * 4;
     w.size_x = dims[0] * 32;
@@ -93,6 +107,7 @@ int main(int argc, char** argv) {
     const uint32_t max_iters = (uint32_t)std::atoi(argv[4]);
     const bool glsl = argc > 8 && std::atoi(argv[8]) != 0;
     const bool coarse = argc > 9 && std::atoi(argv[9]) != 0;
+    const bool aniso = argc > 10 && std::atoi(argv[10]) != 0;
     const int wo[3] = {std::atoi(argv[5]), std::atoi(argv[6]), std::atoi(argv[7])};
     std::vector<uint4> out(rays.size());
     for (size_t i = 0; i < rays.size(); i++) {
@@ -101,7 +116,7 @@ int main(int argc, char** argv) {
         const vrt_ray& q = rays[i];
         if (glsl) {
             trace_ray<false, true>(w, q.origin[0], q.origin[1], q.origin[2], q.dir[0], q.dir[1], q.dir[2], wo[0],
-                                   wo[1], wo[2], max_iters, res, cnt, coarse);
+                                   wo[1], wo[2], max_iters, res, cnt, coarse, aniso);
             out[i] = pack_hit<true>(res, q.dir[0], q.dir[1], q.dir[2], q.tag);
         } else {
             trace_ray<false, false>(w, q.origin[0], q.origin[1], q.origin[2], q.dir[0], q.dir[1], q.dir[2], wo[0],

@@ -85,12 +85,14 @@ def make_rays(origins, dirs, tags=None) -> np.ndarray:
 def oracle_view(o: OracleWorld, view) -> np.ndarray:
     """All records of a vrt_view from the oracle, shaped (kinds, width*height)."""
     glsl = bool(view.flags & v.VIEW_GLSL)
+    aniso = bool(view.flags & v.capi.VIEW_GLSL_ANISO)
     if view.flags & v.VIEW_SHADOW:
-        p, s = o.render_view_shadow(view.cam, np.array(view.sun_dir[:], np.float32), view.max_iters, glsl=glsl)
+        p, s = o.render_view_shadow(view.cam, np.array(view.sun_dir[:], np.float32), view.max_iters, glsl=glsl,
+                                    aniso=aniso)
         return np.stack([p, s])
     if view.n_bounces:
-        return o.render_view_bounces(view.cam, view.n_bounces, view.max_iters, glsl=glsl)
-    return o.render_view(view.cam, view.max_iters, glsl=glsl)[None]
+        return o.render_view_bounces(view.cam, view.n_bounces, view.max_iters, glsl=glsl, aniso=aniso)
+    return o.render_view(view.cam, view.max_iters, glsl=glsl, aniso=aniso)[None]
 
 
 def cell_corner_world(shape=(32, 32, 128), material=7) -> v.SectorData:

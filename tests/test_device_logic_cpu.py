@@ -73,15 +73,35 @@ def device_layout(data: v.SectorData) -> bytes:
     up = lambda a, k: a.repeat(k, 1).repeat(k, 2).repeat(k, 3)
     code = np.where(solid, 2, np.where(~up(cell_any, 4), 3, np.where(~up(block_any, 2), 1, 0))).astype(np.uint8)
     head = np.array([sx, sy, sz, nb], np.uint32).tobytes()
+    # the raw masks the anisotropic LODs read: 8 cell masks per slot (cell cx | cz<<1 | cy<<2,
+    # bit vx + vz*4 + vy*16), the sector records, the sector-group masks
+    bits = np.uint64(1) << np.arange(64, dtype=np.uint64)
+    cv = solid.reshape(nb, 2, 4, 2, 4, 2, 4).transpose(0, 1, 3, 5, 2, 4, 6)  # (n, cy, cz, cx, vy, vz, vx)
+    cells = (cv.reshape(nb, 8, 64).astype(np.uint64) * bits).sum(axis=2, dtype=np.uint64)
+    sectors = np.zeros((sy, sz, sx, 4), np.uint32)
+    base = 0
+    masks = {}
+    for idx, m in zip(data.sector_idx.tolist(), data.alloc_mask.tolist()):
+        masks[(idx & 4095, (idx >> 12) & 4095, (idx >> 24) & 255)] = m
+    for (x, z, y), m in masks.items():
+        sectors[y, z, x] = [m & 0xFFFFFFFF, m >> 32, base, 0]
+        base += bin(m).count("1")
+    gxn, gyn, gzn = (sx + 3) // 4, (sy + 3) // 4, (sz + 3) // 4
+    groups = np.zeros((gyn, gzn, gxn), np.uint64)
+    for (x, z, y), m in masks.items():
+        if m:
+            groups[y >> 2, z >> 2, x >> 2] |= np.uint64(1) << np.uint64((x & 3) | (z & 3) << 2 | (y & 3) << 4)
     # one code byte per voxel, x | z<<3 | y<<6 within the slot (the payload's order)
-    return head + table.tobytes() + code.tobytes() + data.bricks.tobytes()
+    return (head + table.tobytes() + code.tobytes() + data.bricks.tobytes() + cells.tobytes() + sectors.tobytes() +
+            groups.tobytes())
 
 
-def run(exe, tmp_path, data, rays, max_iters=128, wo=(0, 0, 0), glsl=False, coarse=False):
+def run(exe, tmp_path, data, rays, max_iters=128, wo=(0, 0, 0), glsl=False, coarse=False, aniso=False):
     (tmp_path / "w.bin").write_bytes(device_layout(data))
     np.ascontiguousarray(rays, v.RAY_DTYPE).tofile(tmp_path / "r.bin")
     subprocess.run([str(exe), str(tmp_path / "w.bin"), str(tmp_path / "r.bin"), str(tmp_path / "o.bin"),
-                    str(max_iters), *map(str, wo), "1" if glsl else "0", "1" if coarse else "0"], check=True)
+                    str(max_iters), *map(str, wo), "1" if glsl else "0", "1" if coarse else "0",
+                    "1" if aniso else "0"], check=True)
     return np.fromfile(tmp_path / "o.bin", v.HIT_DTYPE)
 
 
@@ -151,6 +171,12 @@ def test_glsl_mode_against_oracle(exe, tmp_path, seed):
         # hits from iteration 31, cap 96
         assert_hits_equal(run(exe, tmp_path, data, rays, 96, wo, glsl=True, coarse=True),
                           o.cast(rays, world_origin=wo, max_iters=96, glsl=True, coarse=True))
+        # anisotropic LODs (raw masks restricted to the cells ahead of the ray), alone and
+        # with rayCastCoarse
+        # (the cast API caps a coarse ray at 96 iterations; this harness takes the cap as given)
+        for coarse, cap in ((False, 256), (True, 96)):
+            assert_hits_equal(run(exe, tmp_path, data, rays, cap, wo, glsl=True, coarse=coarse, aniso=True),
+                              o.cast(rays, world_origin=wo, max_iters=cap, glsl=True, coarse=coarse, aniso=True))
 
 
 def test_glsl_coarse_known_answer(exe, tmp_path):

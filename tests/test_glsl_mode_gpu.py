@@ -152,3 +152,82 @@ def test_glsl_coarse_casts_match_oracle(gpu):
         p = v.capi.CastParams((v.C.c_int32 * 3)(0, 0, 0), 0, v.capi.CAST_GLSL_COARSE)
         v.check(v.lib().vrt_cast(w.handle, None, 0, v.C.byref(p), None, None))
     w.close()
+
+
+def test_glsl_aniso_casts_match_oracle(gpu):
+    """Anisotropic LODs (VRT_CAST_GLSL_ANISO, u_UseAnisotropicLods): the raw cell,
+    sector and group masks restricted to the 4x4x4 box ahead of the ray; alone and with
+    rayCastCoarse, through both cast kernels.  Same voxels as the isotropic mode where
+    neither is capped and no direction component is zero, in no more steps."""
+    rng = np.random.default_rng(17)
+    for data in (sparse_world(17), v.synth_mix(96, seed=17), cell_corner_world()):
+        size = [s * 32 for s in data.sectors]
+        w, o = both_worlds(data)
+        for n in (30_000, (1 << 18) + 3):
+            rays, wo = camera_frame_rays(rng, size, n)
+            got = w.cast(rays, world_origin=wo, aniso=True)
+            assert_hits_equal(got, o.cast(rays, world_origin=wo, glsl=True, aniso=True))
+            iso = w.cast(rays, world_origin=wo, glsl=True)
+            # a zero direction component makes a side distance NaN (0 * inf) wherever the
+            # stepped-to voxel is not above the origin on that axis, and the shader's min then
+            # drops a side: such rays may part ways between the two modes
+            nz = (rays["dir"] != 0).all(axis=1)
+            both = (got["steps"] < 256) & (iso["steps"] < 256) & nz
+            assert np.array_equal(got["voxel"][both], iso["voxel"][both])
+            assert (got["steps"][both] <= iso["steps"][both]).all()
+            assert got["steps"].astype(np.int64).sum() < iso["steps"].astype(np.int64).sum()
+            c = w.cast(rays, world_origin=wo, coarse=True, aniso=True)
+            assert_hits_equal(c, o.cast(rays, world_origin=wo, glsl=True, coarse=True, aniso=True))
+        w.close()
+    with pytest.raises(v.VrtError):  # anisotropic LODs without the GLSL mode
+        w, _ = both_worlds(cell_corner_world())
+        p = v.capi.CastParams((v.C.c_int32 * 3)(0, 0, 0), 0, v.capi.CAST_GLSL_ANISO)
+        try:
+            v.check(v.lib().vrt_cast(w.handle, None, 0, v.C.byref(p), None, None))
+        finally:
+            w.close()
+
+
+def test_glsl_aniso_paths_and_batch_match_oracle(gpu):
+    rng = np.random.default_rng(19)
+    worlds, oracles, views = [], [], []
+    for i in range(4):
+        data = sparse_world(40 + i, shape=(96, 160, 128), blobs=20) if i % 2 else v.synth_mix(96, seed=50 + i)
+        w, o = both_worlds(data)
+        worlds.append(w)
+        oracles.append(o)
+        size = [s * 32 for s in data.sectors]
+        for k in range(3):
+            cam = v.look_at(rng.uniform(0, size), rng.uniform(0, size), 70.0, *[(64, 48), (33, 65), (80, 40)][k])
+            views.append(v.make_view(cam, world=i, aniso=True, **[{}, {"shadow_dir": SUN}, {"n_bounces": 2}][k]))
+    for vw in views[:3]:
+        got, want = v.render_path(worlds[vw.world], vw), oracle_view(oracles[vw.world], vw)
+        for k in range(want.shape[0]):
+            assert_hits_equal(got[k], want[k])
+    for cfg in (None, v.BatchConfig(32, 1, 0, 4, 0, 28, 1, 2)):
+        b = v.Batch(worlds, views, cfg)
+        hits = b.run()
+        for i, vw in enumerate(views):
+            got, want = b.view_hits(hits, i), oracle_view(oracles[vw.world], vw)
+            for k in range(want.shape[0]):
+                assert_hits_equal(got[k], want[k])
+        b.close()
+    # one traversal mode per launch: GLSL and GLSL with anisotropic LODs do not mix
+    with pytest.raises(v.VrtError):
+        v.Batch(worlds, views[:2] + [v.make_view(views[0].cam, world=0, glsl=True)])
+    bad = v.make_view(views[0].cam, world=0)
+    bad.flags |= v.capi.VIEW_GLSL_ANISO  # without the GLSL mode
+    with pytest.raises(v.VrtError):
+        v.Batch(worlds, [bad])
+    # edits re-derive the cell masks the anisotropic LODs read
+    e = np.zeros(2, v.EDIT_DTYPE)
+    e["center"] = [[40, 40, 40], [60, 30, 50]]
+    e["radius"] = [20, 9]
+    e["material"] = [0, 33]
+    worlds[0].edit(e)
+    oracles[0].edit(e)
+    rays, wo = camera_frame_rays(rng, [96, 96, 96], 40_000)
+    assert_hits_equal(worlds[0].cast(rays, world_origin=wo, aniso=True),
+                      oracles[0].cast(rays, world_origin=wo, glsl=True, aniso=True))
+    for w in worlds:
+        w.close()

@@ -13,7 +13,7 @@ import pytest
 
 import voxelrt_gb300 as v
 from oracle.oracle import OracleWorld
-from tests.helpers import assert_hits_equal
+from tests.helpers import assert_hits_equal, oracle_view
 
 pytestmark = pytest.mark.gpu
 
@@ -170,17 +170,17 @@ def test_wait_timeout_and_unknown_ticket(setup):
 
 
 def test_resident_mode_switches_and_idle_restart(setup):
-    """Requests in the GLSL traversal mode close the running launch and start one in
-    their mode; an idle launch closes itself and the next request starts a new one."""
+    """Requests in another traversal mode (GLSL, GLSL with anisotropic LODs) close the
+    running launch and start one in their mode; an idle launch closes itself and the next request starts a new one."""
     import time
     datas, worlds, oracles = setup
     rng = np.random.default_rng(6)
     srv = v.Server(worlds, resident=True, idle_us=200)
     views = []
+    modes = (0, v.VIEW_GLSL, v.VIEW_GLSL | v.capi.VIEW_GLSL_ANISO, 0)
     for i in range(24):
         vw = random_view(rng, i % 4, datas[i % 4].sectors[0] * 32)
-        if (i // 6) % 2:
-            vw.flags |= v.VIEW_GLSL
+        vw.flags |= modes[i // 6]
         views.append(vw)
     outs = [v.PinnedHits(v.view_records(vw)) for vw in views]
     ts = [srv.submit_render(vw, o.array) for vw, o in zip(views, outs)]
@@ -191,17 +191,9 @@ def test_resident_mode_switches_and_idle_restart(setup):
     lo = v.PinnedHits(v.view_records(late))
     srv.wait(srv.submit_render(late, lo.array))
     for vw, o in zip(views, outs):
-        glsl = bool(vw.flags & v.VIEW_GLSL)
-        o_ = oracles[vw.world]
-        if vw.flags & v.VIEW_SHADOW:
-            want = np.concatenate(o_.render_view_shadow(vw.cam, np.array(vw.sun_dir[:], np.float32), glsl=glsl))
-        elif vw.n_bounces:
-            want = o_.render_view_bounces(vw.cam, vw.n_bounces, glsl=glsl).reshape(-1)
-        else:
-            want = o_.render_view(vw.cam, glsl=glsl)
-        assert_hits_equal(o.array, want)
+        assert_hits_equal(o.array, oracle_view(oracles[vw.world], vw).reshape(-1))
     assert_hits_equal(lo.array, oracle_records(oracles[late.world], late))
-    assert srv.stats()["launches"] >= 4  # 4 mode changes, then a restart after the idle end
+    assert srv.stats()["launches"] >= 5  # 4 modes in turn, then a restart after the idle end
     srv.close()
 
 

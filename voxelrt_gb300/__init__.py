@@ -137,8 +137,9 @@ def random_rays(size, seed: int, n: int, first: int = 0, threads: int = 0) -> np
     return rays
 
 
-def cast_flags(glsl: bool, coarse: bool) -> int:
-    return (CAST_GLSL if glsl or coarse else 0) | (capi.CAST_GLSL_COARSE if coarse else 0)
+def cast_flags(glsl: bool, coarse: bool, aniso: bool = False) -> int:
+    return ((CAST_GLSL if glsl or coarse or aniso else 0) | (capi.CAST_GLSL_COARSE if coarse else 0) |
+            (capi.CAST_GLSL_ANISO if aniso else 0))
 
 
 def _stream_ptr(stream) -> int | None:
@@ -225,18 +226,19 @@ class World:
         return mask.value, bricks
 
     def cast(self, rays: np.ndarray, world_origin=(0, 0, 0), max_iters: int = 0, stream=None,
-             glsl: bool = False, coarse: bool = False) -> np.ndarray:
+             glsl: bool = False, coarse: bool = False, aniso: bool = False) -> np.ndarray:
         """glsl: the GPU renderer's rayCast (VRT_CAST_GLSL) instead of the CPU traversal;
-        coarse: its rayCastCoarse (VRT_CAST_GLSL_COARSE, with glsl)."""
+        coarse: its rayCastCoarse (VRT_CAST_GLSL_COARSE); aniso: its anisotropic LODs
+        (VRT_CAST_GLSL_ANISO)."""
         rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
         hits = np.zeros(len(rays), HIT_DTYPE)
-        p = CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), cast_flags(glsl, coarse))
+        p = CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), cast_flags(glsl, coarse, aniso))
         check(lib().vrt_cast(self._h, ptr(rays), len(rays), C.byref(p), ptr(hits), _stream_ptr(stream)))
         return hits
 
     def cast_device(self, rays, n: int, hits, world_origin=(0, 0, 0), max_iters: int = 0, stream=None,
-                    glsl: bool = False, coarse: bool = False) -> None:
-        p = CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), cast_flags(glsl, coarse))
+                    glsl: bool = False, coarse: bool = False, aniso: bool = False) -> None:
+        p = CastParams((C.c_int32 * 3)(*world_origin), int(max_iters), cast_flags(glsl, coarse, aniso))
         check(lib().vrt_cast_device(self._h, ptr(rays), int(n), C.byref(p), ptr(hits), _stream_ptr(stream)))
 
     def render_view(self, cam: Camera, max_iters: int = 0, stream=None) -> np.ndarray:
@@ -249,15 +251,17 @@ class World:
 
 
 def make_view(cam: Camera, world: int = 0, max_iters: int = 0, n_bounces: int = 0, shadow_dir=None,
-              glsl: bool = False) -> View:
+              glsl: bool = False, aniso: bool = False) -> View:
     """A view: primary rays plus shadow rays toward shadow_dir, or n_bounces diffuse bounces.
-    glsl: trace with the GPU renderer's rayCast (VRT_VIEW_GLSL) instead of the CPU traversal."""
+    glsl: trace with the GPU renderer's rayCast (VRT_VIEW_GLSL) instead of the CPU traversal;
+    aniso: with its anisotropic LODs (VRT_VIEW_GLSL_ANISO)."""
     vw = View()
     vw.cam = cam
     vw.world = int(world)
     vw.max_iters = int(max_iters)
     vw.n_bounces = int(n_bounces)
-    vw.flags = (VIEW_SHADOW if shadow_dir is not None else 0) | (VIEW_GLSL if glsl else 0)
+    vw.flags = ((VIEW_SHADOW if shadow_dir is not None else 0) | (VIEW_GLSL if glsl or aniso else 0) |
+                (capi.VIEW_GLSL_ANISO if aniso else 0))
     if shadow_dir is not None:
         vw.sun_dir[:] = [float(c) for c in shadow_dir]
     return vw

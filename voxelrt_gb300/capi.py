@@ -74,6 +74,8 @@ VIEW_SHADOW = 1
 VIEW_GLSL = 2        # the GPU renderer's rayCast (VoxelTraversal.glsl) instead of the CPU traversal
 CAST_GLSL = 1
 CAST_GLSL_COARSE = 2
+CAST_GLSL_ANISO = 4
+VIEW_GLSL_ANISO = 4
 GLSL_MAX_ITERS = 256
 
 

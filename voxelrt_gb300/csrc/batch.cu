@@ -34,31 +34,17 @@ __device__ __forceinline__ uint32_t compact_even_bits(uint32_t k) {
 template <bool kCount, bool kGlsl>
 __device__ __forceinline__ bool run_ray(RayState& s, bool safe, const DevWorld& w, int32_t wox, int32_t woy,
                                         int32_t woz, uint32_t max_iters, uint32_t& steps, TraceCounters& cnt,
-                                        bool coarse_ray = false) {
-    uint32_t st = kStepOut, i = 0;
-    if (kGlsl && coarse_ray) {
-        for (; i < max_iters; i++) {
-            st = safe ? ray_step<kCount, true, kGlsl, true>(s, w, wox, woy, woz, cnt, coarse_bits(true, i))
-                      : ray_step<kCount, false, kGlsl, true>(s, w, wox, woy, woz, cnt, coarse_bits(true, i));
-            if (st != kStepContinue) break;
-        }
-    } else if (safe) {
-        for (; i < max_iters; i++) {
-            st = ray_step<kCount, true, kGlsl>(s, w, wox, woy, woz, cnt);
-            if (st != kStepContinue) break;
-        }
-    } else {
-        for (; i < max_iters; i++) {
-            st = ray_step<kCount, false, kGlsl>(s, w, wox, woy, woz, cnt);
-            if (st != kStepContinue) break;
-        }
-    }
+                                        bool coarse_ray = false, bool aniso = false) {
+    uint32_t i = 0;
+    uint32_t st = dda_steps_mode<kCount, kGlsl>(s, w, wox, woy, woz, cnt, safe, coarse_ray, coarse_ray, aniso, 0, i,
+                                                max_iters);
+    if (max_iters == 0) st = kStepOut;
     steps = i;
     return st == kStepHit && i < max_iters;
 }
 
 // One thread per pixel, whole path (VoxelRender.comp:27-93 structure).
-template <bool kGlsl>
+template <bool kGlsl, bool kAniso = false>
 __global__ void __launch_bounds__(64) view_path_kernel(DevWorld w, ViewDev v, uint4* __restrict__ out) {
     const uint32_t px = blockIdx.x * 8 + threadIdx.x;
     const uint32_t py = blockIdx.y * 8 + threadIdx.y;
@@ -72,7 +58,7 @@ __global__ void __launch_bounds__(64) view_path_kernel(DevWorld w, ViewDev v, ui
     RayState s;
     bool safe = ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
     uint32_t steps;
-    bool hit = run_ray<false, kGlsl>(s, safe, w, wox, woy, woz, v.max_iters, steps, cnt);
+    bool hit = run_ray<false, kGlsl>(s, safe, w, wox, woy, woz, v.max_iters, steps, cnt, false, kAniso);
     uint4* o = out + v.out_base + pixel;
     o[0] = pack_state<kGlsl>(s, hit, steps, pixel);
     const uint32_t last = v.last_kind();
@@ -85,7 +71,7 @@ __global__ void __launch_bounds__(64) view_path_kernel(DevWorld w, ViewDev v, ui
         safe = ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
         // GLSL mode: shadow and bounce rays are rayCastCoarse's (VoxelRender.comp:56,74)
         hit = run_ray<false, kGlsl>(s, safe, w, wox, woy, woz, kGlsl ? min(v.max_iters, kCoarseMaxIters) : v.max_iters,
-                                    steps, cnt, kGlsl);
+                                    steps, cnt, kGlsl, kAniso);
         o[k * plane] = pack_state<kGlsl>(s, hit, steps, pixel);
     }
 }
@@ -217,7 +203,7 @@ __device__ __forceinline__ void resident_pixels_done(const BatchParams& p, uint3
     }
 }
 
-template <bool kCount, bool kGlsl, bool kResident = false>
+template <bool kCount, bool kGlsl, bool kResident = false, bool kAniso = false>
 __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt = (1u << lane) - 1u;
@@ -477,27 +463,10 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
         if (active) {
             const uint32_t kmax = min(p.inner, max_iters - iter);
             uint32_t k = 0, st = kStepContinue;
-            if (any_coarse) {
-                // GLSL mode, some lane traces a shadow or bounce ray: rayCastCoarse's
-                const bool coarse_ray = (path & 0xFFu) != 0;
-                for (; k < kmax; k++) {
-                    st = all_safe ? ray_step<kCount, true, kGlsl, true>(s, w, wox, woy, woz, cnt,
-                                                                        coarse_bits(coarse_ray, iter + k))
-                                  : ray_step<kCount, false, kGlsl, true>(s, w, wox, woy, woz, cnt,
-                                                                         coarse_bits(coarse_ray, iter + k));
-                    if (st != kStepContinue) break;
-                }
-            } else if (all_safe) {
-                for (; k < kmax; k++) {
-                    st = ray_step<kCount, true, kGlsl>(s, w, wox, woy, woz, cnt);
-                    if (st != kStepContinue) break;
-                }
-            } else {
-                for (; k < kmax; k++) {
-                    st = ray_step<kCount, false, kGlsl>(s, w, wox, woy, woz, cnt);
-                    if (st != kStepContinue) break;
-                }
-            }
+            // GLSL mode: the rayCastCoarse variant while some lane traces a shadow or
+            // bounce ray, the anisotropic one for views that ask for it
+            st = dda_steps_mode<kCount, kGlsl>(s, w, wox, woy, woz, cnt, all_safe, any_coarse, (path & 0xFFu) != 0,
+                                               kAniso, iter, k, kmax);
             iter += k;  // the iteration a ray left on, or max_iters when the cap ran out
             if (st != kStepContinue)
                 path |= kEnded | (st == kStepHit ? kHit : 0u);
@@ -551,6 +520,7 @@ ViewDev make_view_dev(const vrt_view& v) {
     set_view_camera(d, v.cam);
     d.world = v.world;
     d.max_iters = eff_iters(v.max_iters, view_glsl(v));
+    d.aniso = view_aniso(v) ? 1u : 0u;
     const uint32_t shadow = (v.flags & VRT_VIEW_SHADOW) ? 1u : 0u;
     d.path = (shadow ? 1u : v.n_bounces) << 8 | shadow << 16;
     for (int c = 0; c < 3; c++) d.sun[c] = v.sun_dir[c];
@@ -561,10 +531,13 @@ namespace {
 
 vrt_status launch_view_path(vrt_world* w, const ViewDev& v, bool glsl, vrt_hit* hits, cudaStream_t stream) {
     dim3 block(8, 8), grid((v.width + 7) / 8, (v.height + 7) / 8);
-    if (glsl)
-        view_path_kernel<true><<<grid, block, 0, stream>>>(w->dev(), v, reinterpret_cast<uint4*>(hits));
+    uint4* out = reinterpret_cast<uint4*>(hits);
+    if (glsl && v.aniso)
+        view_path_kernel<true, true><<<grid, block, 0, stream>>>(w->dev(), v, out);
+    else if (glsl)
+        view_path_kernel<true><<<grid, block, 0, stream>>>(w->dev(), v, out);
     else
-        view_path_kernel<false><<<grid, block, 0, stream>>>(w->dev(), v, reinterpret_cast<uint4*>(hits));
+        view_path_kernel<false><<<grid, block, 0, stream>>>(w->dev(), v, out);
     VRT_CUDA(cudaGetLastError());
     return VRT_OK;
 }
@@ -578,8 +551,8 @@ uint32_t eff_iters(uint32_t m, bool glsl) {
 
 vrt_status check_same_mode(const vrt_view* views, uint32_t n) {
     for (uint32_t i = 1; i < n; i++)
-        if (view_glsl(views[i]) != view_glsl(views[0])) {
-            set_error("the views of one launch must share one traversal mode (VRT_VIEW_GLSL)");
+        if (view_mode(views[i]) != view_mode(views[0])) {
+            set_error("the views of one launch must share one traversal mode (VRT_VIEW_GLSL, VRT_VIEW_GLSL_ANISO)");
             return VRT_ERR_INVALID_ARG;
         }
     return VRT_OK;
@@ -587,10 +560,11 @@ vrt_status check_same_mode(const vrt_view* views, uint32_t n) {
 
 vrt_status check_view(const vrt_view* v) {
     if (!v || v->cam.width == 0 || v->cam.height == 0 || v->cam.width > 16384 || v->cam.height > 16384 ||
-        v->n_bounces > VRT_MAX_BOUNCES || (v->flags & ~(VRT_VIEW_SHADOW | VRT_VIEW_GLSL)) ||
+        v->n_bounces > VRT_MAX_BOUNCES || (v->flags & ~(VRT_VIEW_SHADOW | VRT_VIEW_GLSL | VRT_VIEW_GLSL_ANISO)) ||
+        ((v->flags & VRT_VIEW_GLSL_ANISO) && !(v->flags & VRT_VIEW_GLSL)) ||
         ((v->flags & VRT_VIEW_SHADOW) && v->n_bounces) || !world_origin_ok(v->cam.world_origin)) {
         set_error("bad view: camera 1..16384 px, |world origin| <= 2^30, n_bounces <= 15, shadow and bounces "
-                  "exclusive");
+                  "exclusive, anisotropic LODs only with the GLSL mode");
         return VRT_ERR_INVALID_ARG;
     }
     return VRT_OK;
@@ -633,6 +607,7 @@ vrt_status plan_views(const vrt_view* views, uint32_t n, uint32_t n_worlds, cons
     }
     if ((st = check_same_mode(views, n)) != VRT_OK) return st;
     plan.glsl = n > 0 && view_glsl(views[0]);
+    plan.aniso = n > 0 && view_aniso(views[0]);
     plan.cfg = cfg;
     plan.tile_w_log2 = log2u(cfg.tile_w);
     plan.tile_size_log2 = log2u(cfg.tile_w * cfg.tile_h);
@@ -697,11 +672,14 @@ BatchParams make_params(const LaunchPlan& plan, const DevWorld* worlds, const Vi
     p.refill = plan.cfg.refill_threshold;
     p.inner = plan.cfg.inner_iters;
     p.glsl = plan.glsl ? 1u : 0u;
+    p.aniso = plan.aniso ? 1u : 0u;
     return p;
 }
 
 vrt_status launch_resident(const BatchParams& p, int blocks, int threads, cudaStream_t stream) {
-    if (p.glsl)
+    if (p.glsl && p.aniso)
+        persistent_kernel<false, true, true, true><<<blocks, threads, 0, stream>>>(p);
+    else if (p.glsl)
         persistent_kernel<false, true, true><<<blocks, threads, 0, stream>>>(p);
     else
         persistent_kernel<false, false, true><<<blocks, threads, 0, stream>>>(p);
@@ -712,10 +690,14 @@ vrt_status launch_resident(const BatchParams& p, int blocks, int threads, cudaSt
 vrt_status launch_persistent(const BatchParams& p, int blocks, int threads, bool count, cudaStream_t stream,
                              bool reset_counters) {
     VRT_CUDA(cudaMemsetAsync(p.queue, 0, reset_counters ? 64 : 4, stream));
-    if (count && p.glsl)
+    if (count && p.glsl && p.aniso)
+        persistent_kernel<true, true, false, true><<<blocks, threads, 0, stream>>>(p);
+    else if (count && p.glsl)
         persistent_kernel<true, true><<<blocks, threads, 0, stream>>>(p);
     else if (count)
         persistent_kernel<true, false><<<blocks, threads, 0, stream>>>(p);
+    else if (p.glsl && p.aniso)
+        persistent_kernel<false, true, false, true><<<blocks, threads, 0, stream>>>(p);
     else if (p.glsl)
         persistent_kernel<false, true><<<blocks, threads, 0, stream>>>(p);
     else

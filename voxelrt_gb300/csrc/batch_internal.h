@@ -28,7 +28,8 @@ struct alignas(16) ViewDev {
     uint32_t chunk_base;      // first queue chunk of the view
     uint64_t out_base;        // first record of the view
     float sun[3];
-    uint32_t pad[3];
+    uint32_t aniso;           // GLSL mode with anisotropic LODs (VRT_VIEW_GLSL_ANISO)
+    uint32_t pad[2];
     VRT_HD uint32_t shadow() const { return (path >> 16) & 1u; }
     VRT_HD uint32_t last_kind() const { return (path >> 8) & 0xFFu; }
 };
@@ -60,6 +61,7 @@ struct BatchParams {
     uint32_t refill;
     uint32_t inner;
     uint32_t glsl;  // traversal mode of every view (VRT_VIEW_GLSL)
+    uint32_t aniso;  // ... with anisotropic LODs (VRT_VIEW_GLSL_ANISO)
     // resident launches (request server): views are published while the kernel runs
     unsigned long long* mailbox;  // host-mapped: published chunks | published views << 32 | closed << 63
     uint32_t* next_chunk;         // device: next chunk to claim
@@ -86,12 +88,16 @@ struct LaunchPlan {
     std::vector<uint32_t> chunk_base;  // n_views + 1
     uint64_t records = 0;
     uint32_t chunks = 0;
-    bool glsl = false;  // every view traces in the GLSL mode
+    bool glsl = false;   // every view traces in the GLSL mode
+    bool aniso = false;  // ... with anisotropic LODs
 };
 
 // Iteration cap of a view or cast: 0 = the mode's default, at most 65535.
 uint32_t eff_iters(uint32_t max_iters, bool glsl = false);
 inline bool view_glsl(const vrt_view& v) { return (v.flags & VRT_VIEW_GLSL) != 0; }
+inline bool view_aniso(const vrt_view& v) { return (v.flags & VRT_VIEW_GLSL_ANISO) != 0; }
+// A view's traversal mode: the CPU traversal, GLSL, or GLSL with anisotropic LODs.
+inline uint32_t view_mode(const vrt_view& v) { return v.flags & (VRT_VIEW_GLSL | VRT_VIEW_GLSL_ANISO); }
 // All views of one launch share a traversal mode (VRT_ERR_INVALID_ARG otherwise).
 vrt_status check_same_mode(const vrt_view* views, uint32_t n);
 uint64_t view_record_count(const vrt_view& v);

@@ -47,6 +47,7 @@ constexpr int kEditWarps = 8;
 __global__ void __launch_bounds__(kEditWarps * 32)
     edit_bricks_kernel(const TouchedBrick* __restrict__ bricks, uint32_t n, const EditDev* __restrict__ edits,
                        uint32_t n_edits, uint8_t* __restrict__ payload, uint4* __restrict__ codes,
+                       uint64_t* __restrict__ cell_masks,
                        uint8_t* __restrict__ empty) {
     __shared__ __align__(16) uint8_t sb[kEditWarps][512];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -77,6 +78,7 @@ __global__ void __launch_bounds__(kEditWarps * 32)
         __syncwarp();
         const uint64_t cells = warp_cell_mask(sb[wib], lane);
         codes[(size_t)tb.slot * 32 + lane] = warp_voxel_codes(sb[wib], cells, lane);
+        if (lane < 8) cell_masks[(size_t)tb.slot * 8 + lane] = cells;
         const bool any = __any_sync(0xffffffffu, cells != 0);
         if (lane == 0) empty[k] = any ? 0 : 1;
         __syncwarp();
@@ -179,6 +181,7 @@ extern "C" vrt_status vrt_world_edit(vrt_world* w, const vrt_edit* edits, uint32
     const uint32_t blocks = std::max(1u, std::min<uint32_t>(((uint32_t)tb.size() + kEditWarps - 1) / kEditWarps, 152u * 16u));
     edit_bricks_kernel<<<blocks, kEditWarps * 32, 0, stream>>>((const TouchedBrick*)(base + boff), (uint32_t)tb.size(),
                                                                (const EditDev*)base, n, w->d_payload, w->d_codes,
+                                                               w->d_cells,
                                                                base + foff);
     VRT_CUDA(cudaGetLastError());
     std::vector<uint8_t> empty(tb.size());

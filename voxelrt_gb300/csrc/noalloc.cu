@@ -149,6 +149,7 @@ extern "C" vrt_status vrt_render_views_static(vrt_world* const* worlds, uint32_t
     p.refill = cfg.refill_threshold;
     p.inner = cfg.inner_iters;
     p.glsl = glsl ? 1u : 0u;
+    p.aniso = n_views > 0 && view_aniso(views[0]) ? 1u : 0u;
     int blocks = 0, threads = 0;
     if ((st = persistent_grid(device, cfg, false, blocks, threads)) != VRT_OK) return st;
     // launch_persistent zeroes the queue counter and the launch counters first

@@ -88,7 +88,8 @@ struct Resident {
     unsigned long long* h_hint = nullptr;  // pinned staging of the hint words, one per publish or close
     uint32_t n_hints = 0;                  // staging entries used by the current launch
     uint32_t cap = 0;
-    bool live = false, closing = false, glsl = false;
+    bool live = false, closing = false;
+    uint32_t mode = 0;  // traversal mode of the launch's views (view_mode)
     uint32_t n_views = 0, n_chunks = 0;
     uint32_t first_open = 0;       // slots below it are all finished
     std::vector<Request*> req;     // per view slot
@@ -289,7 +290,7 @@ void worker_main(vrt_server* sv) {
                 std::vector<Request*> rs;
                 while (!sv->queue.empty() && sv->queue.front()->kind == 0 && rs.size() < sv->cfg.max_batch_requests) {
                     Request* r = sv->queue.front();
-                    if (!rs.empty() && view_glsl(r->view) != view_glsl(rs[0]->view)) break;  // one mode per launch
+                    if (!rs.empty() && view_mode(r->view) != view_mode(rs[0]->view)) break;  // one mode per launch
                     const uint32_t base = sv->pages.realloc(0, 0, r->pages);
                     if (base == 0) break;  // budget full: wait for launches to retire
                     r->page_base = base;
@@ -429,11 +430,12 @@ bool resident_publish(vrt_server* sv, const std::vector<Request*>& rs, vrt_statu
     return true;
 }
 
-vrt_status resident_start(vrt_server* sv, bool glsl) {
+vrt_status resident_start(vrt_server* sv, uint32_t mode) {
+    const bool glsl = (mode & VRT_VIEW_GLSL) != 0;
     Resident& R = sv->res;
     R.n_views = R.n_chunks = R.first_open = 0;
     R.closing = false;
-    R.glsl = glsl;
+    R.mode = mode;
     R.n_hints = 0;
     VRT_CUDA(cudaStreamSynchronize(R.ctl));  // staging of the last launch is free again
     __atomic_store_n(R.mailbox, 0ull, __ATOMIC_SEQ_CST);
@@ -448,6 +450,7 @@ vrt_status resident_start(vrt_server* sv, bool glsl) {
     while ((1u << r) < cfg.tile_w * cfg.tile_h) r++;
     plan.tile_size_log2 = r;
     plan.glsl = glsl;
+    plan.aniso = (mode & VRT_VIEW_GLSL_ANISO) != 0;
     BatchParams p = make_params(plan, sv->d_worlds, (const ViewDev*)R.views.ptr, (const uint32_t*)R.chunk_base.ptr,
                                 (uint32_t*)R.queue.ptr, (vrt_hit*)sv->arena);
     p.mailbox = R.d_mailbox;
@@ -557,8 +560,8 @@ bool resident_schedule(vrt_server* sv, std::unique_lock<std::mutex>& lk) {
         sv->done_cv.notify_all();
         return true;
     }
-    const bool glsl = view_glsl(front->view);
-    if (R.live && (R.closing || glsl != R.glsl || R.n_views >= R.cap)) {
+    const uint32_t mode = view_mode(front->view);
+    if (R.live && (R.closing || mode != R.mode || R.n_views >= R.cap)) {
         if (!R.closing) resident_close(R);  // a new launch takes the next requests
         return false;
     }
@@ -566,7 +569,7 @@ bool resident_schedule(vrt_server* sv, std::unique_lock<std::mutex>& lk) {
     std::vector<Request*> rs;
     const uint32_t room = R.live ? R.cap - R.n_views : R.cap;
     for (Request* r : sv->queue) {
-        if (r->kind != 0 || view_glsl(r->view) != glsl || rs.size() >= sv->cfg.max_batch_requests ||
+        if (r->kind != 0 || view_mode(r->view) != mode || rs.size() >= sv->cfg.max_batch_requests ||
             rs.size() >= room)
             break;
         const uint32_t base = sv->pages.realloc(0, 0, r->pages);
@@ -576,7 +579,7 @@ bool resident_schedule(vrt_server* sv, std::unique_lock<std::mutex>& lk) {
     }
     if (rs.empty()) return false;
     const bool fresh = !R.live;
-    vrt_status st = fresh ? resident_start(sv, glsl) : VRT_OK;
+    vrt_status st = fresh ? resident_start(sv, mode) : VRT_OK;
     const bool ok = st == VRT_OK && resident_publish(sv, rs, st);
     if (ok && fresh) st = resident_launch(sv);
     if (ok && st == VRT_OK) {

@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(64) render_view_kernel(DevWorld w, vrt_camera 
     out[pix] = pack_hit(r, dx, dy, dz, pix);
 }
 
-template <bool kGlsl>
+template <bool kGlsl, bool kAniso = false>
 __global__ void __launch_bounds__(256) cast_kernel(DevWorld w, const float4* __restrict__ rays, uint32_t n,
                                                   int32_t wox, int32_t woy, int32_t woz, uint32_t max_iters,
                                                   uint4* __restrict__ out, bool coarse) {
@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(256) cast_kernel(DevWorld w, const float4* __r
     const float4 a = rays[2 * (size_t)i], b = rays[2 * (size_t)i + 1];
     TraceResult r;
     TraceCounters cnt;
-    trace_ray<false, kGlsl>(w, a.x, a.y, a.z, a.w, b.x, b.y, wox, woy, woz, max_iters, r, cnt, coarse);
+    trace_ray<false, kGlsl>(w, a.x, a.y, a.z, a.w, b.x, b.y, wox, woy, woz, max_iters, r, cnt, coarse, kAniso);
     out[i] = pack_hit<kGlsl>(r, a.w, b.x, b.y, __float_as_uint(b.z));
 }
 
@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(256) cast_kernel(DevWorld w, const float4* __r
 // device queue: calls on different streams stay independent.  Same records as
 // cast_kernel: a lane's steps continue from where its ray left off, and a ray's record
 // is packed from the state at its exit.
-template <bool kGlsl>
+template <bool kGlsl, bool kAniso = false>
 __global__ void __maxnreg__(48) cast_persistent_kernel(DevWorld w, const float4* __restrict__ rays, uint32_t n,
                                                              int32_t wox, int32_t woy, int32_t woz, uint32_t max_iters,
                                                              uint32_t inner, uint32_t refill, uint4* __restrict__ out,
@@ -107,26 +107,10 @@ __global__ void __maxnreg__(48) cast_persistent_kernel(DevWorld w, const float4*
         const bool all_safe = __all_sync(0xffffffffu, !active || safe);
         if (active) {
             const uint32_t kmax = min(inner, max_iters - iter);
-            uint32_t k = 0, st = kStepContinue;
-            if (kGlsl && coarse) {  // rayCastCoarse rays (uniform over the launch)
-                for (; k < kmax; k++) {
-                    st = all_safe ? ray_step<false, true, kGlsl, true>(s, w, wox, woy, woz, cnt,
-                                                                       coarse_bits(true, iter + k))
-                                  : ray_step<false, false, kGlsl, true>(s, w, wox, woy, woz, cnt,
-                                                                        coarse_bits(true, iter + k));
-                    if (st != kStepContinue) break;
-                }
-            } else if (all_safe) {
-                for (; k < kmax; k++) {
-                    st = ray_step<false, true, kGlsl>(s, w, wox, woy, woz, cnt);
-                    if (st != kStepContinue) break;
-                }
-            } else {
-                for (; k < kmax; k++) {
-                    st = ray_step<false, false, kGlsl>(s, w, wox, woy, woz, cnt);
-                    if (st != kStepContinue) break;
-                }
-            }
+            uint32_t k = 0;
+            // GLSL variants (rayCastCoarse, anisotropic LODs) are uniform over the launch
+            const uint32_t st = dda_steps_mode<false, kGlsl>(s, w, wox, woy, woz, cnt, all_safe, coarse, coarse, kAniso,
+                                                             iter, k, kmax);
             iter += k;
             if (st != kStepContinue || iter >= max_iters) {
                 ended = true;
@@ -166,17 +150,19 @@ constexpr uint32_t kCastPersistentMin = 1u << 18;
 vrt_status launch_cast(vrt_world* w, const vrt_ray* rays, uint32_t n, const vrt_cast_params* p, vrt_hit* hits,
                        cudaStream_t stream) {
     if (n == 0) return VRT_OK;
-    const bool glsl = (p->flags & VRT_CAST_GLSL) != 0, coarse = (p->flags & VRT_CAST_GLSL_COARSE) != 0;
+    const bool glsl = (p->flags & VRT_CAST_GLSL) != 0, coarse = (p->flags & VRT_CAST_GLSL_COARSE) != 0,
+               aniso = (p->flags & VRT_CAST_GLSL_ANISO) != 0;
     const float4* r4 = reinterpret_cast<const float4*>(rays);
     uint4* o4 = reinterpret_cast<uint4*>(hits);
     uint32_t iters = eff_iters(p->max_iters, glsl);
     if (coarse) iters = std::min<uint32_t>(iters, VRT_GLSL_COARSE_MAX_ITERS);
     if (n < kCastPersistentMin) {
-        auto kernel = glsl ? cast_kernel<true> : cast_kernel<false>;
+        auto kernel = glsl ? (aniso ? cast_kernel<true, true> : cast_kernel<true>) : cast_kernel<false>;
         kernel<<<(n + 255) / 256, 256, 0, stream>>>(w->dev(), r4, n, p->world_origin[0], p->world_origin[1],
                                                     p->world_origin[2], iters, o4, coarse);
     } else {
-        auto kernel = glsl ? cast_persistent_kernel<true> : cast_persistent_kernel<false>;
+        auto kernel = glsl ? (aniso ? cast_persistent_kernel<true, true> : cast_persistent_kernel<true>)
+                           : cast_persistent_kernel<false>;
         int dev = 0, sms = 0, occ = 0;
         VRT_CUDA(cudaGetDevice(&dev));
         VRT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -190,10 +176,11 @@ vrt_status launch_cast(vrt_world* w, const vrt_ray* rays, uint32_t n, const vrt_
 }
 
 vrt_status check_params(const vrt_cast_params* p) {
-    if (!p || (p->flags & ~(VRT_CAST_GLSL | VRT_CAST_GLSL_COARSE)) != 0 ||
-        (p->flags & (VRT_CAST_GLSL | VRT_CAST_GLSL_COARSE)) == VRT_CAST_GLSL_COARSE || !world_origin_ok(p->world_origin)) {
-        set_error("cast params missing, flags other than VRT_CAST_GLSL [| VRT_CAST_GLSL_COARSE], or "
-                  "|world origin| > 2^30");
+    const uint32_t glsl_opts = VRT_CAST_GLSL_COARSE | VRT_CAST_GLSL_ANISO;
+    if (!p || (p->flags & ~(VRT_CAST_GLSL | glsl_opts)) != 0 ||
+        ((p->flags & glsl_opts) && !(p->flags & VRT_CAST_GLSL)) || !world_origin_ok(p->world_origin)) {
+        set_error("cast params missing, flags other than VRT_CAST_GLSL [| VRT_CAST_GLSL_COARSE | "
+                  "VRT_CAST_GLSL_ANISO], or |world origin| > 2^30");
         return VRT_ERR_INVALID_ARG;
     }
     return VRT_OK;

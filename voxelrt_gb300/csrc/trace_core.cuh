@@ -197,6 +197,29 @@ __device__ __forceinline__ bool ray_start(RayState& s, const DevWorld& w, float 
 
 enum : uint32_t { kStepContinue = 0, kStepHit = 1, kStepOut = 2 };
 
+// The 4^3 cells ahead of cell idx (x | z<<2 | y<<4) along the ray: on each axis idx's
+// coordinate and above (dir >= 0) or and below (dir < 0); g = -1 where dir < 0.  The
+// entry idx + octant*64 of RayCellInteractionMaskLUT (GpuRenderer.cpp:193-210, octant
+// bit per axis set for dir >= 0, VoxelTraversal.glsl:119), built here from 4-bit
+// ranges: x bits, spread to z rows at bits 4z and y planes at bits 16y.
+__device__ __forceinline__ uint64_t forward_cells(uint32_t idx, int32_t gx, int32_t gy, int32_t gz) {
+    const uint32_t x = idx & 3u, z = (idx >> 2) & 3u, y = idx >> 4;
+    const uint32_t xr = gx ? (0xFu >> (3u - x)) : ((0xFu << x) & 0xFu);
+    const uint32_t zr = gz ? (0xFu >> (3u - z)) : ((0xFu << z) & 0xFu);
+    const uint32_t yr = gy ? (0xFu >> (3u - y)) : ((0xFu << y) & 0xFu);
+    const uint32_t zs = (zr & 1u) | (zr & 2u) << 3 | (zr & 4u) << 6 | (zr & 8u) << 9;
+    const uint64_t ys = (uint64_t)(yr & 1u) | (uint64_t)(yr & 2u) << 15 | (uint64_t)(yr & 4u) << 30 |
+                        (uint64_t)(yr & 8u) << 45;
+    return (uint64_t)(xr * zs) * ys;
+}
+
+// getIsotropicLod (VoxelTraversal.glsl:24-34): the cell size 4, 2 or 1 at idx of a mask.
+__device__ __forceinline__ uint32_t iso_cell_size(uint64_t m, uint32_t idx) {
+    if (m == 0) return 4u;
+    const uint32_t half = idx < 32 ? (uint32_t)m : (uint32_t)(m >> 32);
+    return ((half >> (idx & 0xAu)) & 0x00330033u) == 0 ? 2u : 1u;
+}
+
 // GLSL mode: rayCastCoarse (VoxelTraversal.glsl:206-240), the GPU renderer's shadow and
 // bounce rays (VoxelRender.comp:56,74,81): kCoarseRay for every step of such a ray,
 // kCoarseNow from its iteration 31 on (`coarse = i > 30`, :218).
@@ -218,7 +241,10 @@ __device__ __forceinline__ uint32_t coarse_bits(bool coarse_ray, uint32_t i) {
 // (:213) instead, and from iteration 31 an empty voxel whose 4^3 cell holds a solid
 // voxel stops the ray at the cell's first solid voxel in mask order (getStepPos with
 // coarse, :125-128, and findAnyOccupiedPos, :41-53).  Without kCoarse `coarse` is 0.
-template <bool kCount, bool kSafe = false, bool kGlsl = false, bool kCoarse = false>
+// kAniso (with kGlsl): anisotropic LODs (u_UseAnisotropicLods, :116-121): the mask of
+// the current level (cell, sector or sector group, read raw instead of through the
+// precomputed codes) is restricted to the cells ahead of the ray before its LOD is taken.
+template <bool kCount, bool kSafe = false, bool kGlsl = false, bool kCoarse = false, bool kAniso = false>
 __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int32_t wox, int32_t woy, int32_t woz,
                                              TraceCounters& cnt, uint32_t coarse = 0) {
     if (kGlsl) {
@@ -265,7 +291,46 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
     const uint32_t bx = (uint32_t)vx >> 3, by = (uint32_t)vy >> 3, bz = (uint32_t)vz >> 3;
     const uint32_t e = __ldg(w.bricks + bx + bz * w.bsx + by * w.bsxz);
     int32_t m;
-    if (e < kBrickEmpty) {
+    if (kGlsl && kAniso) {
+        if (e < kBrickEmpty) {
+            if (kCount) cnt.occ_fetches++;
+            const uint32_t lx = (uint32_t)vx & 7u, ly = (uint32_t)vy & 7u, lz = (uint32_t)vz & 7u;
+            const uint64_t cm = __ldg(w.cells + (size_t)e * 8 + ((lx >> 2) | (lz >> 2) << 1 | (ly >> 2) << 2));
+            const uint32_t idx = (lx & 3u) | (lz & 3u) << 2 | (ly & 3u) << 4;
+            if ((cm >> idx) & 1u) {
+                s.material = __ldg(w.payload + (size_t)e * 512 + (lx | lz << 3 | ly << 6));
+                s.vx = vx;
+                s.vy = vy;
+                s.vz = vz;
+                return kStepHit;
+            }
+            const uint64_t am = cm & forward_cells(idx, s.gx, s.gy, s.gz);
+            if (kCoarse && (coarse & kCoarseNow) && am != 0) {
+                // findAnyOccupiedPos on the masked cell mask: its lowest set bit
+                const uint32_t j = (uint32_t)__ffsll((long long)am) - 1u;
+                s.vx = (vx & ~3) | (int32_t)(j & 3u);
+                s.vy = (vy & ~3) | (int32_t)(j >> 4);
+                s.vz = (vz & ~3) | (int32_t)((j >> 2) & 3u);
+                s.material = __ldg(w.payload + (size_t)e * 512 +
+                                   (((uint32_t)s.vx & 7u) | ((uint32_t)s.vz & 7u) << 3 | ((uint32_t)s.vy & 7u) << 6));
+                return kStepHit;
+            }
+            m = (int32_t)iso_cell_size(am, idx) - 1;
+        } else if ((e & 31u) != 31u) {
+            // the brick's sector holds bricks: its mask at the brick scale (8)
+            const SectorRec r = w.sectors[(uint32_t)vx / 32u + ((uint32_t)vz / 32u) * w.sx + ((uint32_t)vy / 32u) * w.sxz];
+            const uint32_t idx = (bx & 3u) | (bz & 3u) << 2 | (by & 3u) << 4;
+            const uint64_t sm = ((uint64_t)r.mask_hi << 32 | r.mask_lo) & forward_cells(idx, s.gx, s.gy, s.gz);
+            m = (int32_t)(iso_cell_size(sm, idx) * 8u) - 1;
+        } else {
+            // an empty sector: the mask of its group of 4^3 sectors at the sector scale (32)
+            const uint32_t sx = (uint32_t)vx / 32u, sy = (uint32_t)vy / 32u, sz = (uint32_t)vz / 32u;
+            const uint32_t gxn = (w.sx + 3u) >> 2, gzn = (w.sz + 3u) >> 2;
+            const uint64_t gm = __ldg(w.groups + (sx >> 2) + (sz >> 2) * gxn + (sy >> 2) * gxn * gzn);
+            const uint32_t idx = (sx & 3u) | (sz & 3u) << 2 | (sy & 3u) << 4;
+            m = (int32_t)(iso_cell_size(gm & forward_cells(idx, s.gx, s.gy, s.gz), idx) * 32u) - 1;
+        }
+    } else if (e < kBrickEmpty) {
         if (kCount) cnt.occ_fetches++;
         // voxel in brick v = x | z<<3 | y<<6 from v - 8*(v >> 3) per axis; its code byte
         const uint32_t lx = imad(bx, 0xFFFFFFF8u, (uint32_t)vx), ly = imad(by, 0xFFFFFFF8u, (uint32_t)vy),
@@ -321,31 +386,60 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
     return kStepContinue;
 }
 
-// Whole RayCast (or rayCast, kGlsl) for one ray.
-template <bool kCount, bool kGlsl = false>
-__device__ __forceinline__ void trace_ray(const DevWorld& w, float ox, float oy, float oz, float dx, float dy,
-                                          float dz, int32_t wox, int32_t woy, int32_t woz, uint32_t max_iters,
-                                          TraceResult& r, TraceCounters& cnt, bool coarse_ray = false) {
-    RayState s;
-    const bool safe = ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
-    uint32_t st = kStepOut, i = 0;
-    if (kGlsl && coarse_ray) {
-        for (; i < max_iters; i++) {
-            st = safe ? ray_step<kCount, true, kGlsl, true>(s, w, wox, woy, woz, cnt, coarse_bits(true, i))
-                      : ray_step<kCount, false, kGlsl, true>(s, w, wox, woy, woz, cnt, coarse_bits(true, i));
-            if (st != kStepContinue) break;
-        }
-    } else if (safe) {
-        for (; i < max_iters; i++) {
-            st = ray_step<kCount, true, kGlsl>(s, w, wox, woy, woz, cnt);
+// Steps k = k .. kmax-1 of a ray whose first step here is its iteration i0 + k, until
+// one ends it (the returned status) or kmax is reached (kStepContinue).  safe: the
+// fast step (ray_init's bounds hold); coarse_ray: a rayCastCoarse ray (kCoarse only).
+template <bool kCount, bool kGlsl, bool kCoarse, bool kAniso>
+__device__ __forceinline__ uint32_t dda_steps(RayState& s, const DevWorld& w, int32_t wox, int32_t woy, int32_t woz,
+                                              TraceCounters& cnt, bool safe, bool coarse_ray, uint32_t i0,
+                                              uint32_t& k, uint32_t kmax) {
+    uint32_t st = kStepContinue;
+    if (safe) {
+        for (; k < kmax; k++) {
+            st = ray_step<kCount, true, kGlsl, kCoarse, kAniso>(s, w, wox, woy, woz, cnt,
+                                                                kCoarse ? coarse_bits(coarse_ray, i0 + k) : 0u);
             if (st != kStepContinue) break;
         }
     } else {
-        for (; i < max_iters; i++) {
-            st = ray_step<kCount, false, kGlsl>(s, w, wox, woy, woz, cnt);
+        for (; k < kmax; k++) {
+            st = ray_step<kCount, false, kGlsl, kCoarse, kAniso>(s, w, wox, woy, woz, cnt,
+                                                                 kCoarse ? coarse_bits(coarse_ray, i0 + k) : 0u);
             if (st != kStepContinue) break;
         }
     }
+    return st;
+}
+
+// dda_steps with the GLSL variants picked at run time: coarse (some ray of the caller's
+// group may be a rayCastCoarse ray; coarse_ray says whether this one is) and aniso.
+template <bool kCount, bool kGlsl>
+__device__ __forceinline__ uint32_t dda_steps_mode(RayState& s, const DevWorld& w, int32_t wox, int32_t woy,
+                                                   int32_t woz, TraceCounters& cnt, bool safe, bool coarse,
+                                                   bool coarse_ray, bool aniso, uint32_t i0, uint32_t& k,
+                                                   uint32_t kmax) {
+    if constexpr (!kGlsl) {
+        return dda_steps<kCount, false, false, false>(s, w, wox, woy, woz, cnt, safe, false, i0, k, kmax);
+    } else {
+        if (aniso)
+            return coarse ? dda_steps<kCount, true, true, true>(s, w, wox, woy, woz, cnt, safe, coarse_ray, i0, k, kmax)
+                          : dda_steps<kCount, true, false, true>(s, w, wox, woy, woz, cnt, safe, false, i0, k, kmax);
+        return coarse ? dda_steps<kCount, true, true, false>(s, w, wox, woy, woz, cnt, safe, coarse_ray, i0, k, kmax)
+                      : dda_steps<kCount, true, false, false>(s, w, wox, woy, woz, cnt, safe, false, i0, k, kmax);
+    }
+}
+
+// Whole RayCast (or rayCast / rayCastCoarse, kGlsl) for one ray.
+template <bool kCount, bool kGlsl = false>
+__device__ __forceinline__ void trace_ray(const DevWorld& w, float ox, float oy, float oz, float dx, float dy,
+                                          float dz, int32_t wox, int32_t woy, int32_t woz, uint32_t max_iters,
+                                          TraceResult& r, TraceCounters& cnt, bool coarse_ray = false,
+                                          bool aniso = false) {
+    RayState s;
+    const bool safe = ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
+    uint32_t i = 0;
+    uint32_t st = dda_steps_mode<kCount, kGlsl>(s, w, wox, woy, woz, cnt, safe, coarse_ray, coarse_ray, aniso, 0, i,
+                                                max_iters);
+    if (max_iters == 0) st = kStepOut;
     r.cx = s.cx;
     r.cy = s.cy;
     r.cz = s.cz;

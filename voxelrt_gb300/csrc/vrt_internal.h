@@ -20,7 +20,11 @@
 //            level = skip_levels of its 4^3 cell's occupancy mask (cell
 //            cx | cz<<1 | cy<<2, bit vx + vz*4 + vy*16: UpdateOccupancy,
 //            CpuRenderer.cpp:63-83, and GetStepPos :146-167);
-//   payload  512 B of u8 voxel ids per brick slot, voxel x | z<<3 | y<<6.
+//   payload  512 B of u8 voxel ids per brick slot, voxel x | z<<3 | y<<6;
+//   cells    the 8 cell masks of each brick slot (UpdateOccupancy, cell cx | cz<<1 |
+//            cy<<2, bit vx + vz*4 + vy*16), read only by the GLSL mode's anisotropic
+//            LODs, which mask them per ray octant;
+//   groups   per group of 4^3 sectors, bit x | z<<2 | y<<4 set per non-empty sector.
 // A brick's slot is base + popcount(mask & ((1<<b)-1)) (VoxelMap.glsl:45-64,
 // BrickSlotAllocator.h:37-41).  The traversal reads bricks, codes and payload
 // only: one 4-byte load per step, one byte more on an allocated brick.
@@ -68,8 +72,10 @@ struct alignas(16) DevWorld {
     uint32_t bsx, bsxz;               // brick-table strides: 4*SX, 4*SX * 4*SZ
     uint32_t size_x, size_y, size_z;  // voxels
     uint32_t sx, sz, sxz;             // sector-table strides
+    const uint64_t* cells;            // 8 cell masks per brick slot (GLSL anisotropic LODs)
+    const uint64_t* groups;           // sector-group masks (GLSL anisotropic LODs)
 };
-static_assert(sizeof(DevWorld) == 64, "world table entries are 64 bytes");
+static_assert(sizeof(DevWorld) == 80, "world table entries are 80 bytes");
 
 // World origins stay within +-2^30 so that saturated float->int conversions of
 // far-away positions always land outside the grid (the traversal relies on it).

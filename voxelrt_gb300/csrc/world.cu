@@ -60,7 +60,8 @@ constexpr int kOpsWarps = 8;
 
 __global__ void gather_bricks_kernel(const uint32_t* __restrict__ src_slots, uint32_t n,
                                      const uint8_t* __restrict__ payload, const uint4* __restrict__ codes,
-                                     uint8_t* __restrict__ scratch_payload, uint4* __restrict__ scratch_codes) {
+                                     const uint64_t* __restrict__ cells, uint8_t* __restrict__ scratch_payload,
+                                     uint4* __restrict__ scratch_codes, uint64_t* __restrict__ scratch_cells) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -69,13 +70,15 @@ __global__ void gather_bricks_kernel(const uint32_t* __restrict__ src_slots, uin
         const uint4 v = reinterpret_cast<const uint4*>(payload + s * 512)[lane];
         reinterpret_cast<uint4*>(scratch_payload + (size_t)k * 512)[lane] = v;
         scratch_codes[(size_t)k * 32 + lane] = codes[s * 32 + lane];
+        if (lane < 8) scratch_cells[(size_t)k * 8 + lane] = cells[s * 8 + lane];
     }
 }
 
 __global__ void __launch_bounds__(kOpsWarps * 32)
     brick_ops_kernel(const BrickOp* __restrict__ ops, uint32_t n, const uint8_t* __restrict__ stage,
                      const uint8_t* __restrict__ scratch_payload, const uint4* __restrict__ scratch_codes,
-                     uint8_t* __restrict__ payload, uint4* __restrict__ codes) {
+                     const uint64_t* __restrict__ scratch_cells, uint8_t* __restrict__ payload,
+                     uint4* __restrict__ codes, uint64_t* __restrict__ cells) {
     __shared__ __align__(16) uint8_t sbrick[kOpsWarps][512];
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t wib = threadIdx.x >> 5;
@@ -89,9 +92,11 @@ __global__ void __launch_bounds__(kOpsWarps * 32)
             const uint4 v = reinterpret_cast<const uint4*>(scratch_payload + (size_t)si * 512)[lane];
             reinterpret_cast<uint4*>(payload + d * 512)[lane] = v;
             codes[d * 32 + lane] = scratch_codes[(size_t)si * 32 + lane];
+            if (lane < 8) cells[d * 8 + lane] = scratch_cells[(size_t)si * 8 + lane];
         } else if (kind == kOpZero) {
             reinterpret_cast<uint4*>(payload + d * 512)[lane] = make_uint4(0, 0, 0, 0);
             codes[d * 32 + lane] = empty_brick_codes();
+            if (lane < 8) cells[d * 8 + lane] = 0;
         } else {
             const uint4 v = reinterpret_cast<const uint4*>(stage + (size_t)si * 512)[lane];
             reinterpret_cast<uint4*>(payload + d * 512)[lane] = v;
@@ -99,6 +104,7 @@ __global__ void __launch_bounds__(kOpsWarps * 32)
             __syncwarp();
             const uint64_t m = warp_cell_mask(sbrick[wib], lane);
             codes[d * 32 + lane] = warp_voxel_codes(sbrick[wib], m, lane);
+            if (lane < 8) cells[d * 8 + lane] = m;
             __syncwarp();
         }
     }
@@ -176,22 +182,28 @@ vrt_status grow_pool(vrt_world* w, uint32_t min_capacity, cudaStream_t stream) {
     uint32_t cap = (uint32_t)want;
     uint4* codes = nullptr;
     uint8_t* payload = nullptr;
+    uint64_t* cells = nullptr;
     cudaError_t e = cudaMalloc(&codes, (size_t)cap * 512);
     if (e == cudaSuccess) e = cudaMalloc(&payload, (size_t)cap * 512);
+    if (e == cudaSuccess) e = cudaMalloc(&cells, (size_t)cap * 64);
     if (e != cudaSuccess) {
         if (codes) cudaFree(codes);
+        if (payload) cudaFree(payload);
         cudaGetLastError();
         return cuda_fail(e, "grow brick pool");
     }
     if (w->capacity) {
         VRT_CUDA(cudaMemcpyAsync(codes, w->d_codes, (size_t)w->capacity * 512, cudaMemcpyDeviceToDevice, stream));
         VRT_CUDA(cudaMemcpyAsync(payload, w->d_payload, (size_t)w->capacity * 512, cudaMemcpyDeviceToDevice, stream));
+        VRT_CUDA(cudaMemcpyAsync(cells, w->d_cells, (size_t)w->capacity * 64, cudaMemcpyDeviceToDevice, stream));
         VRT_CUDA(cudaStreamSynchronize(stream));
     }
     if (w->d_codes) cudaFree(w->d_codes);
     if (w->d_payload) cudaFree(w->d_payload);
+    if (w->d_cells) cudaFree(w->d_cells);
     w->d_codes = codes;
     w->d_payload = payload;
+    w->d_cells = cells;
     w->capacity = cap;
     w->arena.grow(cap);
     return VRT_OK;
@@ -272,19 +284,21 @@ vrt_status run_batch(vrt_world* w, SyncBatch& b, cudaStream_t stream) {
     }
     const size_t ng = b.gathers.size();
     if (ng) {
-        VRT_CUDA(w->d_scratch.reserve(ng * 1024));
+        VRT_CUDA(w->d_scratch.reserve(ng * 1088));
         uint8_t* sp = (uint8_t*)w->d_scratch.ptr;
         uint4* sc = (uint4*)(sp + ng * 512);
+        uint64_t* sm = (uint64_t*)(sp + ng * 1024);
         gather_bricks_kernel<<<ops_grid((uint32_t)ng), kOpsWarps * 32, 0, stream>>>(
-            (const uint32_t*)w->d_ops.ptr, (uint32_t)ng, w->d_payload, w->d_codes, sp, sc);
+            (const uint32_t*)w->d_ops.ptr, (uint32_t)ng, w->d_payload, w->d_codes, w->d_cells, sp, sc, sm);
         VRT_CUDA(cudaGetLastError());
     }
     if (!b.ops.empty()) {
         uint8_t* sp = (uint8_t*)w->d_scratch.ptr;
         uint4* sc = sp ? (uint4*)(sp + ng * 512) : nullptr;
+        uint64_t* sm = sp ? (uint64_t*)(sp + ng * 1024) : nullptr;
         brick_ops_kernel<<<ops_grid((uint32_t)b.ops.size()), kOpsWarps * 32, 0, stream>>>(
             (const BrickOp*)((uint8_t*)w->d_ops.ptr + ooff), (uint32_t)b.ops.size(), (const uint8_t*)w->d_stage.ptr,
-            sp, sc, w->d_payload, w->d_codes);
+            sp, sc, sm, w->d_payload, w->d_codes, w->d_cells);
         VRT_CUDA(cudaGetLastError());
     }
     // sector headers: copy the span of touched records
@@ -385,6 +399,7 @@ vrt_status vrt_world_destroy(vrt_world* w) {
     if (w->d_groups) cudaFree(w->d_groups);
     if (w->d_codes) cudaFree(w->d_codes);
     if (w->d_payload) cudaFree(w->d_payload);
+    if (w->d_cells) cudaFree(w->d_cells);
     w->d_stage.release();
     w->d_ops.release();
     w->d_scratch.release();

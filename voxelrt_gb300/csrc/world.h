@@ -62,6 +62,7 @@ struct vrt_world {
     uint32_t* d_bricks = nullptr;  // brick table, derived from the sector table on the device
     uint64_t* d_groups = nullptr;  // sector-group masks of the GLSL mode's 4th level
     uint4* d_codes = nullptr;      // byte voxel codes, 512 B (32 x 16 B) per slot
+    uint64_t* d_cells = nullptr;   // 8 cell masks per slot
     uint8_t* d_payload = nullptr;
     uint32_t capacity = 0;  // brick slots in the device pools
 
@@ -92,6 +93,8 @@ struct vrt_world {
         w.sx = sx;
         w.sz = sz;
         w.sxz = sx * sz;
+        w.cells = d_cells;
+        w.groups = d_groups;
         w.size_x = sx * 32;
         w.size_y = sy * 32;
         w.size_z = sz * 32;
