@@ -63,6 +63,7 @@ using std::signbit;
 using namespace vrt;
 
 int main(int argc, char** argv) {
+    fill_forward_lut_entries(0, 1);
     if (argc < 8) return 2;
     FILE* f = std::fopen(argv[1], "rb");
     if (!f) return 3;

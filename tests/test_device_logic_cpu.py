@@ -28,6 +28,54 @@ def exe():
     return EXE
 
 
+def forward_boxes() -> np.ndarray:
+    """(64 cells, 8 octants) u64: the cells of a 4^3 block on or ahead of the cell along
+    the octant's directions (octant bit per axis set for dir >= 0), bit x + z*4 + y*16."""
+    c = np.arange(64)
+    x, z, y = c & 3, (c >> 2) & 3, c >> 4
+    out = np.zeros((64, 8), np.uint64)
+    for o in range(8):
+        ok = lambda a, b, pos: (b >= a) if pos else (b <= a)
+        keep = (ok(x[:, None], x[None, :], o & 1) & ok(y[:, None], y[None, :], o & 2) &
+                ok(z[:, None], z[None, :], o & 4))
+        out[:, o] = (keep.astype(np.uint64) << c[None, :].astype(np.uint64)).sum(axis=1, dtype=np.uint64)
+    return out
+
+
+def skip_level(masked: np.ndarray, idx: np.ndarray) -> np.ndarray:
+    """2 when the 4^3 mask is empty, 1 when the aligned 2^3 block around idx is, else 0."""
+    c = np.arange(64)
+    x, z, y = c & 3, (c >> 2) & 3, c >> 4
+    blk = np.zeros(64, np.uint64)
+    for i in range(64):
+        inb = ((x >> 1) == (x[i] >> 1)) & ((z >> 1) == (z[i] >> 1)) & ((y >> 1) == (y[i] >> 1))
+        blk[i] = (inb.astype(np.uint64) << c.astype(np.uint64)).sum(dtype=np.uint64)
+    return np.where(masked == 0, 2, np.where((masked & blk[idx]) == 0, 1, 0)).astype(np.uint32)
+
+
+def aniso_bits(alloc: np.ndarray, sector_any: np.ndarray) -> np.ndarray:
+    """Bits 5 and 15-30 of every brick position's table entry (only empty ones use them)."""
+    nby, nbz, nbx = alloc.shape
+    sy, sz, sx = nby // 4, nbz // 4, nbx // 4
+    bits = np.uint64(1) << np.arange(64, dtype=np.uint64)
+    # sector masks (bit bx&3 | (bz&3)<<2 | (by&3)<<4) and group masks over padded sectors
+    sm = (alloc.reshape(sy, 4, sz, 4, sx, 4).transpose(0, 2, 4, 1, 3, 5).reshape(sy, sz, sx, 64).astype(np.uint64)
+          * bits).sum(axis=3, dtype=np.uint64)
+    gy, gz, gx = sector_any.shape[0] // 4, sector_any.shape[1] // 4, sector_any.shape[2] // 4
+    gm = (sector_any.reshape(gy, 4, gz, 4, gx, 4).transpose(0, 2, 4, 1, 3, 5).reshape(gy, gz, gx, 64)
+          .astype(np.uint64) * bits).sum(axis=3, dtype=np.uint64)
+    by, bz, bx = np.meshgrid(np.arange(nby), np.arange(nbz), np.arange(nbx), indexing="ij")
+    ys, zs, xs = by >> 2, bz >> 2, bx >> 2
+    empty_sector = sm[ys, zs, xs] == 0
+    lm = np.where(empty_sector, gm[ys >> 2, zs >> 2, xs >> 2], sm[ys, zs, xs])
+    li = np.where(empty_sector, (xs & 3) | (zs & 3) << 2 | (ys & 3) << 4, (bx & 3) | (bz & 3) << 2 | (by & 3) << 4)
+    fwd = forward_boxes()
+    out = np.where(empty_sector, 1 << 5, 0).astype(np.uint32)
+    for o in range(8):
+        out |= skip_level(lm & fwd[li, o], li) << (15 + 2 * o)
+    return out
+
+
 def device_layout(data: v.SectorData) -> bytes:
     """Brick table + slot pools as the device holds them (slots in stream order).
 
@@ -65,7 +113,11 @@ def device_layout(data: v.SectorData) -> bytes:
     g4, g2 = g4[:sy, :sz, :sx], g2[:sy, :sz, :sx]
     sector_level = np.where(~g4, 127, np.where(~g2, 63, 31)).astype(np.uint32)
     glsl = np.where(~up4(sector_any), up4(sector_level), level).astype(np.uint32)
-    table = np.where(alloc, slot_of, np.uint32(0x80000000) | level | glsl << 8).astype(np.uint32)
+    # anisotropic LODs (bit 5, bits 15-30): per ray octant, the skip level of the brick's
+    # sector mask (or, in an empty sector, its sector-group mask) kept only on the 4^3 cells
+    # from the brick (sector) towards the ray; bit 5 marks the group scale
+    table = np.where(alloc, slot_of, np.uint32(0x80000000) | level | glsl << 8 | aniso_bits(alloc, sa)).astype(
+        np.uint32)
     nb = data.n_bricks
     solid = data.bricks.reshape(nb, 8, 8, 8) != 0             # (n, y, z, x)
     cell_any = solid.reshape(nb, 2, 4, 2, 4, 2, 4).any(axis=(2, 4, 6))

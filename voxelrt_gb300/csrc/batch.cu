@@ -46,6 +46,7 @@ __device__ __forceinline__ bool run_ray(RayState& s, bool safe, const DevWorld& 
 // One thread per pixel, whole path (VoxelRender.comp:27-93 structure).
 template <bool kGlsl, bool kAniso = false>
 __global__ void __launch_bounds__(64) view_path_kernel(DevWorld w, ViewDev v, uint4* __restrict__ out) {
+    if constexpr (kAniso) fill_forward_lut();
     const uint32_t px = blockIdx.x * 8 + threadIdx.x;
     const uint32_t py = blockIdx.y * 8 + threadIdx.y;
     if (px >= v.width || py >= v.height) return;
@@ -205,6 +206,7 @@ __device__ __forceinline__ void resident_pixels_done(const BatchParams& p, uint3
 
 template <bool kCount, bool kGlsl, bool kResident = false, bool kAniso = false>
 __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
+    if constexpr (kAniso) fill_forward_lut();
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt = (1u << lane) - 1u;
     // warp-uniform queue state: rays [q_next, q_end) of view q_view

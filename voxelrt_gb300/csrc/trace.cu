@@ -40,6 +40,7 @@ template <bool kGlsl, bool kAniso = false>
 __global__ void __launch_bounds__(256) cast_kernel(DevWorld w, const float4* __restrict__ rays, uint32_t n,
                                                   int32_t wox, int32_t woy, int32_t woz, uint32_t max_iters,
                                                   uint4* __restrict__ out, bool coarse) {
+    if constexpr (kAniso) fill_forward_lut();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 a = rays[2 * (size_t)i], b = rays[2 * (size_t)i + 1];
@@ -63,6 +64,7 @@ __global__ void __maxnreg__(48) cast_persistent_kernel(DevWorld w, const float4*
                                                              int32_t wox, int32_t woy, int32_t woz, uint32_t max_iters,
                                                              uint32_t inner, uint32_t refill, uint4* __restrict__ out,
                                                              bool coarse) {
+    if constexpr (kAniso) fill_forward_lut();
     const uint32_t lane = threadIdx.x & 31, lt = (1u << lane) - 1u;
     const uint32_t stride = (gridDim.x * blockDim.x) & ~31u;  // rays between a warp's chunks
     uint32_t next = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;  // first ray of the warp's next chunk

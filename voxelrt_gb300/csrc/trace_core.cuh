@@ -197,28 +197,33 @@ __device__ __forceinline__ bool ray_start(RayState& s, const DevWorld& w, float 
 
 enum : uint32_t { kStepContinue = 0, kStepHit = 1, kStepOut = 2 };
 
-// The 4^3 cells ahead of cell idx (x | z<<2 | y<<4) along the ray: on each axis idx's
-// coordinate and above (dir >= 0) or and below (dir < 0); g = -1 where dir < 0.  The
-// entry idx + octant*64 of RayCellInteractionMaskLUT (GpuRenderer.cpp:193-210, octant
-// bit per axis set for dir >= 0, VoxelTraversal.glsl:119), built here from 4-bit
-// ranges: x bits, spread to z rows at bits 4z and y planes at bits 16y.
-__device__ __forceinline__ uint64_t forward_cells(uint32_t idx, int32_t gx, int32_t gy, int32_t gz) {
-    const uint32_t x = idx & 3u, z = (idx >> 2) & 3u, y = idx >> 4;
-    const uint32_t xr = gx ? (0xFu >> (3u - x)) : ((0xFu << x) & 0xFu);
-    const uint32_t zr = gz ? (0xFu >> (3u - z)) : ((0xFu << z) & 0xFu);
-    const uint32_t yr = gy ? (0xFu >> (3u - y)) : ((0xFu << y) & 0xFu);
-    const uint32_t zs = (zr & 1u) | (zr & 2u) << 3 | (zr & 4u) << 6 | (zr & 8u) << 9;
-    const uint64_t ys = (uint64_t)(yr & 1u) | (uint64_t)(yr & 2u) << 15 | (uint64_t)(yr & 4u) << 30 |
-                        (uint64_t)(yr & 8u) << 45;
-    return (uint64_t)(xr * zs) * ys;
+// Anisotropic LODs: RayCellInteractionMaskLUT (GpuRenderer.cpp:193-210) in shared
+// memory, entry idx + 64 * octant (octant = (dx >= 0) | (dy >= 0) << 1 | (dz >= 0) << 2),
+// [0] the forward box of cell idx and [1] its part inside idx's aligned 2^3 block, so
+// that getIsotropicLod of the masked mask (VoxelTraversal.glsl:24-34) is two tests.
+// Every kernel that traces with anisotropic LODs fills it first (fill_forward_lut).
+#if defined(__CUDACC__)
+static __shared__ uint64_t s_forward_lut[2][512];
+#else
+inline uint64_t s_forward_lut[2][512];
+#endif
+
+__device__ __forceinline__ void fill_forward_lut_entries(uint32_t first, uint32_t step) {
+    for (uint32_t i = first; i < 512; i += step) {
+        const uint32_t idx = i & 63u, o = i >> 6;
+        const uint64_t f = forward_cells(idx, (o & 1u) ? 0 : -1, (o & 2u) ? 0 : -1, (o & 4u) ? 0 : -1);
+        s_forward_lut[0][i] = f;
+        s_forward_lut[1][i] = f & (0x330033ull << (idx & 0x2Au));
+    }
 }
 
-// getIsotropicLod (VoxelTraversal.glsl:24-34): the cell size 4, 2 or 1 at idx of a mask.
-__device__ __forceinline__ uint32_t iso_cell_size(uint64_t m, uint32_t idx) {
-    if (m == 0) return 4u;
-    const uint32_t half = idx < 32 ? (uint32_t)m : (uint32_t)(m >> 32);
-    return ((half >> (idx & 0xAu)) & 0x00330033u) == 0 ? 2u : 1u;
+#if defined(__CUDACC__)
+// all threads of the block, before any of them returns
+__device__ __forceinline__ void fill_forward_lut() {
+    fill_forward_lut_entries(threadIdx.x + threadIdx.y * blockDim.x, blockDim.x * blockDim.y);
+    __syncthreads();
 }
+#endif
 
 // GLSL mode: rayCastCoarse (VoxelTraversal.glsl:206-240), the GPU renderer's shadow and
 // bounce rays (VoxelRender.comp:56,74,81): kCoarseRay for every step of such a ray,
@@ -304,7 +309,8 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
                 s.vz = vz;
                 return kStepHit;
             }
-            const uint64_t am = cm & forward_cells(idx, s.gx, s.gy, s.gz);
+            const uint32_t li = idx + 64u * ((uint32_t)(s.gx + 1) | (uint32_t)(s.gy + 1) << 1 | (uint32_t)(s.gz + 1) << 2);
+            const uint64_t am = cm & s_forward_lut[0][li];
             if (kCoarse && (coarse & kCoarseNow) && am != 0) {
                 // findAnyOccupiedPos on the masked cell mask: its lowest set bit
                 const uint32_t j = (uint32_t)__ffsll((long long)am) - 1u;
@@ -315,20 +321,14 @@ __device__ __forceinline__ uint32_t ray_step(RayState& s, const DevWorld& w, int
                                    (((uint32_t)s.vx & 7u) | ((uint32_t)s.vz & 7u) << 3 | ((uint32_t)s.vy & 7u) << 6));
                 return kStepHit;
             }
-            m = (int32_t)iso_cell_size(am, idx) - 1;
-        } else if ((e & 31u) != 31u) {
-            // the brick's sector holds bricks: its mask at the brick scale (8)
-            const SectorRec r = w.sectors[(uint32_t)vx / 32u + ((uint32_t)vz / 32u) * w.sx + ((uint32_t)vy / 32u) * w.sxz];
-            const uint32_t idx = (bx & 3u) | (bz & 3u) << 2 | (by & 3u) << 4;
-            const uint64_t sm = ((uint64_t)r.mask_hi << 32 | r.mask_lo) & forward_cells(idx, s.gx, s.gy, s.gz);
-            m = (int32_t)(iso_cell_size(sm, idx) * 8u) - 1;
+            m = am == 0 ? 3 : ((cm & s_forward_lut[1][li]) == 0 ? 1 : 0);
         } else {
-            // an empty sector: the mask of its group of 4^3 sectors at the sector scale (32)
-            const uint32_t sx = (uint32_t)vx / 32u, sy = (uint32_t)vy / 32u, sz = (uint32_t)vz / 32u;
-            const uint32_t gxn = (w.sx + 3u) >> 2, gzn = (w.sz + 3u) >> 2;
-            const uint64_t gm = __ldg(w.groups + (sx >> 2) + (sz >> 2) * gxn + (sy >> 2) * gxn * gzn);
-            const uint32_t idx = (sx & 3u) | (sz & 3u) << 2 | (sy & 3u) << 4;
-            m = (int32_t)(iso_cell_size(gm & forward_cells(idx, s.gx, s.gy, s.gz), idx) * 32u) - 1;
+            // an empty brick: the sector mask (scale 8) or, in an empty sector, the
+            // sector-group mask (scale 32) restricted to the ray's octant, whose skip level
+            // the table entry carries per octant
+            const uint32_t oct2 = ((uint32_t)(s.gx + 1) | (uint32_t)(s.gy + 1) << 1 | (uint32_t)(s.gz + 1) << 2) * 2u;
+            const uint32_t skip = ((e >> (kAnisoShift + oct2)) & 3u) + ((e >> 4) & 2u);
+            m = (int32_t)((8u << skip) - 1u);
         }
     } else if (e < kBrickEmpty) {
         if (kCount) cnt.occ_fetches++;

@@ -13,7 +13,8 @@
 //            in bits 0-7, and in bits 8-15 the mask of the GLSL mode's getStepPos
 //            (VoxelTraversal.glsl:100-131): the same where the sector holds a brick,
 //            else (32 << skip_levels of the sector-group mask) - 1, cells of 32, 64
-//            or 128 voxels;
+//            or 128 voxels; bit 5 and bits 15-30 hold the anisotropic LODs' skip
+//            levels per ray octant (kAnisoGroupBit, kAnisoShift);
 //   codes    voxel codes, one byte per voxel (512 B per brick slot), voxel
 //            v = x | z<<3 | y<<6 at byte v (as the payload): kCodeSolid, or
 //            for an empty voxel the alignment mask (1 << level) - 1 (0, 1 or 3) of
@@ -62,6 +63,30 @@ VRT_HD inline uint32_t skip_levels(uint32_t lo, uint32_t hi, uint32_t idx) {
     const uint32_t half = idx < 32 ? lo : hi;
     return (lo | hi) == 0 ? 2u : (((half >> (idx & 0xA)) & 0x00330033u) == 0 ? 1u : 0u);
 }
+
+// The 4^3 cells ahead of cell idx (x | z<<2 | y<<4) along the ray: on each axis idx's
+// coordinate and above (dir >= 0) or and below (dir < 0); g = -1 where dir < 0.  The
+// entry idx + octant*64 of RayCellInteractionMaskLUT (GpuRenderer.cpp:193-210, octant
+// bit per axis set for dir >= 0, VoxelTraversal.glsl:119), built here from 4-bit
+// ranges: x bits, spread to z rows at bits 4z and y planes at bits 16y.
+VRT_HD inline uint64_t forward_cells(uint32_t idx, int32_t gx, int32_t gy, int32_t gz) {
+    const uint32_t x = idx & 3u, z = (idx >> 2) & 3u, y = idx >> 4;
+    const uint32_t xr = gx ? (0xFu >> (3u - x)) : ((0xFu << x) & 0xFu);
+    const uint32_t zr = gz ? (0xFu >> (3u - z)) : ((0xFu << z) & 0xFu);
+    const uint32_t yr = gy ? (0xFu >> (3u - y)) : ((0xFu << y) & 0xFu);
+    const uint32_t zs = (zr & 1u) | (zr & 2u) << 3 | (zr & 4u) << 6 | (zr & 8u) << 9;
+    const uint64_t ys = (uint64_t)(yr & 1u) | (uint64_t)(yr & 2u) << 15 | (uint64_t)(yr & 4u) << 30 |
+                        (uint64_t)(yr & 8u) << 45;
+    return (uint64_t)(xr * zs) * ys;
+}
+
+// An empty brick's table entry also carries what the anisotropic LODs need there:
+// kAnisoGroupBit when its sector is empty (the step then works at the sector-group
+// scale 32, else at the brick scale 8), and at bit kAnisoShift + 2*octant
+// (octant = (dx >= 0) | (dy >= 0) << 1 | (dz >= 0) << 2) the skip level (0-2) of that
+// level's mask restricted to forward_cells of the brick's (or sector's) index.
+constexpr uint32_t kAnisoGroupBit = 1u << 5;
+constexpr uint32_t kAnisoShift = 15;
 
 // Kernel-side view of one world (passed by value or stored in a world table).
 struct alignas(16) DevWorld {

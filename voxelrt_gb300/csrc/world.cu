@@ -159,6 +159,20 @@ __global__ void brick_table_kernel(const SectorRec* __restrict__ sectors, const 
             glsl_m = (32u << skip_levels((uint32_t)g, (uint32_t)(g >> 32), si)) - 1u;
         }
         e = kBrickEmpty | cpu_m | glsl_m << 8;
+        // anisotropic LODs: the level's mask and index (sector, or group where the
+        // sector is empty), its skip level per ray octant
+        uint64_t lm = (uint64_t)hi << 32 | lo;
+        uint32_t li = b;
+        if ((lo | hi) == 0) {
+            const uint32_t gx = (sx + 3) / 4, gz = (sz + 3) / 4;
+            lm = groups[(x >> 2) + (z >> 2) * gx + (y >> 2) * gx * gz];
+            li = (x & 3) | (z & 3) << 2 | (y & 3) << 4;
+            e |= kAnisoGroupBit;
+        }
+        for (uint32_t o = 0; o < 8; o++) {
+            const uint64_t f = lm & forward_cells(li, (o & 1u) ? 0 : -1, (o & 2u) ? 0 : -1, (o & 4u) ? 0 : -1);
+            e |= skip_levels((uint32_t)f, (uint32_t)(f >> 32), li) << (kAnisoShift + 2 * o);
+        }
     }
     bricks[bx + bz * (sx * 4) + by * (sx * 4) * (sz * 4)] = e;
 }
