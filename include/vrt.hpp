@@ -203,14 +203,20 @@ class GpuRenderer {
         map_->MarkAllDirty();
     }
     // One frame: sync dirty bricks, then primary rays (+ secondary rays per
-    // `view`'s flags) into host records laid out as vrt_view_records().
+    // `view`'s flags) into host records laid out as vrt_view_records().  With
+    // UseAnisotropicLods the frame traces in the GLSL mode with anisotropic LODs.
     std::vector<vrt_hit> RenderFrame(const vrt_view& view, void* stream = nullptr) {
         storage_.SyncBuffers(*map_, stream);
-        std::vector<vrt_hit> hits(vrt_view_records(&view));
-        check(vrt_render_path(storage_.handle(), &view, hits.data(), stream));
+        vrt_view v = view;
+        if (UseAnisotropicLods) v.flags |= VRT_VIEW_GLSL | VRT_VIEW_GLSL_ANISO;
+        std::vector<vrt_hit> hits(vrt_view_records(&v));
+        check(vrt_render_path(storage_.handle(), &v, hits.data(), stream));
         return hits;
     }
     GpuVoxelStorage& storage() { return storage_; }
+
+    // the renderer setting of the same name (Renderer.h:45, VoxelTraversal.glsl:116-121)
+    bool UseAnisotropicLods = false;
 
   private:
     std::shared_ptr<VoxelMap> map_;

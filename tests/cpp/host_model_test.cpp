@@ -71,10 +71,13 @@ int main(int argc, char** argv) {
         // an edit between frames, then the next frame sees it
         sphere(*map, 32, 12, 32, 10, 0, 2);
         std::vector<vrt_hit> b = renderer.RenderFrame(view);
+        renderer.UseAnisotropicLods = true;
+        std::vector<vrt_hit> c = renderer.RenderFrame(view);
         uint64_t n = a.size();
         fwrite(&n, 8, 1, f);
         fwrite(a.data(), sizeof(vrt_hit), a.size(), f);
         fwrite(b.data(), sizeof(vrt_hit), b.size(), f);
+        fwrite(c.data(), sizeof(vrt_hit), c.size(), f);
         fwrite(&view.cam, sizeof(vrt_camera), 1, f);
     }
     std::fclose(f);

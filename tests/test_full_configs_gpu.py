@@ -21,9 +21,9 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 
-def eff_iters(m: int) -> int:
-    """The iteration cap a view runs with (0 = 128, at most 65535)."""
-    return 128 if m == 0 else min(m, 65535)
+def eff_iters(m: int, glsl: bool = False) -> int:
+    """The iteration cap a view runs with (0 = 128, or 256 in the GLSL mode; at most 65535)."""
+    return (256 if glsl else 128) if m == 0 else min(m, 65535)
 
 
 def load(wl):
@@ -72,7 +72,8 @@ def check_invariants(b, rec, wl):
         h = vv != -1
         assert bool(((vv & 0x7FF) < size[0] * 32)[h].all() and (((vv >> 11) & 0x3FF) < size[1] * 32)[h].all()
                     and (((vv >> 21) & 0x7FF) < size[2] * 32)[h].all()), f"view {i}: hit outside its world"
-        assert bool((((rv[..., 1] >> 16) & 0xFFFF) <= eff_iters(vw.max_iters)).all()), f"view {i}: steps"
+        cap = eff_iters(vw.max_iters, bool(vw.flags & v.VIEW_GLSL))
+        assert bool((((rv[..., 1] >> 16) & 0xFFFF) <= cap).all()), f"view {i}: steps"
         assert bool((rv[0, :, 3] == torch.arange(npx, device=rv.device, dtype=torch.int32)).all())
         for k in range(1, kinds):
             ended = (rv[k - 1, :, 0] == -1) | (rv[k - 1, :, 3] == -1)
@@ -110,6 +111,16 @@ def run_config(wl, n_sample, seed):
 def test_uneven_batch_full_size(gpu):
     """128 worlds, 1,119 views, 352.9 M records; 24 views checked against the oracle."""
     run_config(W.uneven_batch(), n_sample=24, seed=5)
+
+
+@pytest.mark.parametrize("aniso", [False, True])
+def test_uneven_batch_full_size_glsl_modes(gpu, aniso):
+    """The same batch in the GLSL traversal mode, with and without anisotropic LODs:
+    batched equals per-view, the invariants hold, 8 views checked against the oracle."""
+    wl = W.uneven_batch()
+    for vw in wl.views:
+        vw.flags |= v.VIEW_GLSL | (v.capi.VIEW_GLSL_ANISO if aniso else 0)
+    run_config(wl, n_sample=8, seed=15 + aniso)
 
 
 def test_large_world_full_size(gpu):

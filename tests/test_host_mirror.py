@@ -87,7 +87,8 @@ def test_gpu_renderer_frames_match_oracle(exe, tmp_path, gpu):
     off += 8
     a = np.frombuffer(buf, v.HIT_DTYPE, n, off)
     b = np.frombuffer(buf, v.HIT_DTYPE, n, off + 16 * n)
-    cam = v.Camera.from_buffer_copy(buf[off + 32 * n: off + 32 * n + 68])
+    c = np.frombuffer(buf, v.HIT_DTYPE, n, off + 32 * n)
+    cam = v.Camera.from_buffer_copy(buf[off + 48 * n: off + 48 * n + 68])
     o = oracle_model()
     assert_hits_equal(a, o.render_view(cam))
     e = np.zeros(1, v.EDIT_DTYPE)
@@ -95,3 +96,5 @@ def test_gpu_renderer_frames_match_oracle(exe, tmp_path, gpu):
     o.edit(e)
     assert_hits_equal(b, o.render_view(cam))
     assert not np.array_equal(a["voxel"], b["voxel"])
+    # GpuRenderer::UseAnisotropicLods: the next frame in the GLSL mode with anisotropic LODs
+    assert_hits_equal(c, o.render_view(cam, glsl=True, aniso=True))

@@ -134,13 +134,10 @@ __global__ void group_masks_kernel(const SectorRec* __restrict__ sectors, uint32
     if (lane == 0) groups[g] = (unsigned long long)half[0] | (unsigned long long)half[1] << 32;
 }
 
-// Brick-table entries of sectors [s_lo, s_hi), one thread per brick position.
-__global__ void brick_table_kernel(const SectorRec* __restrict__ sectors, const unsigned long long* __restrict__ groups,
-                                   uint32_t s_lo, uint32_t s_hi, uint32_t sx, uint32_t sz,
-                                   uint32_t* __restrict__ bricks) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (s_hi - s_lo) * 64u) return;
-    const uint32_t s = s_lo + (i >> 6), b = i & 63;
+// The brick-table entry of brick b of sector s, written at its brick position.
+__device__ __forceinline__ void write_table_entry(const SectorRec* __restrict__ sectors,
+                                                  const unsigned long long* __restrict__ groups, uint32_t s,
+                                                  uint32_t b, uint32_t sx, uint32_t sz, uint32_t* __restrict__ bricks) {
     const SectorRec rec = sectors[s];
     const uint32_t x = s % sx, z = (s / sx) % sz, y = s / (sx * sz);
     const uint32_t bx = x * 4 + (b & 3), bz = z * 4 + ((b >> 2) & 3), by = y * 4 + (b >> 4);
@@ -151,30 +148,52 @@ __global__ void brick_table_kernel(const SectorRec* __restrict__ sectors, const 
         e = rec.base + (b < 32 ? __popc(lo & below) : __popc(lo) + __popc(hi & below));
     } else {
         const uint32_t cpu_m = (8u << skip_levels(lo, hi, b)) - 1u;
-        uint32_t glsl_m = cpu_m;
-        if ((lo | hi) == 0) {
-            const uint32_t gx = (sx + 3) / 4, gz = (sz + 3) / 4;
-            const unsigned long long g = groups[(x >> 2) + (z >> 2) * gx + (y >> 2) * gx * gz];
-            const uint32_t si = (x & 3) | (z & 3) << 2 | (y & 3) << 4;
-            glsl_m = (32u << skip_levels((uint32_t)g, (uint32_t)(g >> 32), si)) - 1u;
-        }
-        e = kBrickEmpty | cpu_m | glsl_m << 8;
-        // anisotropic LODs: the level's mask and index (sector, or group where the
-        // sector is empty), its skip level per ray octant
+        e = kBrickEmpty | cpu_m;
+        // the level the GLSL mode and its anisotropic LODs read: the sector's mask, or
+        // where the sector is empty its group's mask, at the sector's index in the group
         uint64_t lm = (uint64_t)hi << 32 | lo;
         uint32_t li = b;
         if ((lo | hi) == 0) {
             const uint32_t gx = (sx + 3) / 4, gz = (sz + 3) / 4;
             lm = groups[(x >> 2) + (z >> 2) * gx + (y >> 2) * gx * gz];
             li = (x & 3) | (z & 3) << 2 | (y & 3) << 4;
-            e |= kAnisoGroupBit;
+            e |= kAnisoGroupBit | ((32u << skip_levels((uint32_t)lm, (uint32_t)(lm >> 32), li)) - 1u) << 8;
+        } else {
+            e |= cpu_m << 8;
         }
+        // anisotropic LODs: that mask's skip level per ray octant
         for (uint32_t o = 0; o < 8; o++) {
             const uint64_t f = lm & forward_cells(li, (o & 1u) ? 0 : -1, (o & 2u) ? 0 : -1, (o & 4u) ? 0 : -1);
             e |= skip_levels((uint32_t)f, (uint32_t)(f >> 32), li) << (kAnisoShift + 2 * o);
         }
     }
     bricks[bx + bz * (sx * 4) + by * (sx * 4) * (sz * 4)] = e;
+}
+
+// Brick-table entries of sectors [s_lo, s_hi), one thread per brick position.
+__global__ void brick_table_kernel(const SectorRec* __restrict__ sectors, const unsigned long long* __restrict__ groups,
+                                   uint32_t s_lo, uint32_t s_hi, uint32_t sx, uint32_t sz,
+                                   uint32_t* __restrict__ bricks) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (s_hi - s_lo) * 64u) return;
+    write_table_entry(sectors, groups, s_lo + (i >> 6), i & 63u, sx, sz, bricks);
+}
+
+// Brick-table entries of the sectors of listed sector groups (4^3 sectors, index
+// x + z*GX + y*GX*GZ), 4096 threads per group: after an edit, only the groups of the
+// sectors it changed are re-derived (a sector's emptiness changes its group's mask,
+// which the GLSL entries of the group's empty sectors read).
+__global__ void brick_table_groups_kernel(const SectorRec* __restrict__ sectors,
+                                          const unsigned long long* __restrict__ groups,
+                                          const uint32_t* __restrict__ list, uint32_t n, uint32_t sx, uint32_t sy,
+                                          uint32_t sz, uint32_t* __restrict__ bricks) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * 4096u) return;
+    const uint32_t g = list[i >> 12], si = (i >> 6) & 63u, gx = (sx + 3) / 4, gz = (sz + 3) / 4;
+    const uint32_t x = (g % gx) * 4 + (si & 3u), z = ((g / gx) % gz) * 4 + ((si >> 2) & 3u),
+                   y = (g / (gx * gz)) * 4 + (si >> 4);
+    if (x >= sx || y >= sy || z >= sz) return;
+    write_table_entry(sectors, groups, x + z * sx + y * sx * sz, i & 63u, sx, sz, bricks);
 }
 
 uint32_t ops_grid(uint32_t n) {
@@ -280,6 +299,35 @@ cudaError_t rebuild_brick_table(vrt_world* w, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
+// The same for the groups of the given sectors only (device list in `list`, at most
+// num_groups entries); the whole table when they are most of the world.
+vrt_status rebuild_brick_table_for(vrt_world* w, const std::vector<uint32_t>& sectors, cudaStream_t stream) {
+    const uint32_t gx = (w->sx + 3) / 4, gz = (w->sz + 3) / 4;
+    std::vector<uint32_t> gl;
+    gl.reserve(sectors.size());
+    for (uint32_t s : sectors) {
+        const uint32_t x = s % w->sx, z = (s / w->sx) % w->sz, y = s / (w->sx * w->sz);
+        gl.push_back((x >> 2) + (z >> 2) * gx + (y >> 2) * gx * gz);
+    }
+    std::sort(gl.begin(), gl.end());
+    gl.erase(std::unique(gl.begin(), gl.end()), gl.end());
+    if ((uint64_t)gl.size() * 4 >= w->num_groups()) {
+        VRT_CUDA(rebuild_brick_table(w, stream));
+        return VRT_OK;
+    }
+    VRT_CUDA(w->d_glist.reserve(gl.size() * sizeof(uint32_t)));
+    VRT_CUDA(cudaMemcpyAsync(w->d_glist.ptr, gl.data(), gl.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
+    const uint32_t ng = w->num_groups();
+    group_masks_kernel<<<(ng + 3) / 4, 128, 0, stream>>>(w->d_sectors, w->sx, w->sy, w->sz,
+                                                       (unsigned long long*)w->d_groups);
+    const uint32_t n = (uint32_t)gl.size() * 4096u;
+    brick_table_groups_kernel<<<(n + 255) / 256, 256, 0, stream>>>(
+        w->d_sectors, (const unsigned long long*)w->d_groups, (const uint32_t*)w->d_glist.ptr, (uint32_t)gl.size(),
+        w->sx, w->sy, w->sz, w->d_bricks);
+    VRT_CUDA(cudaGetLastError());
+    return VRT_OK;
+}
+
 vrt_status run_batch(vrt_world* w, SyncBatch& b, cudaStream_t stream) {
     if (b.ops.empty() && b.touched.empty()) return VRT_OK;
     const size_t stage_bytes = (size_t)b.n_stage * 512;
@@ -321,7 +369,8 @@ vrt_status run_batch(vrt_world* w, SyncBatch& b, cudaStream_t stream) {
         const uint32_t lo = *mm.first, hi = *mm.second + 1;
         VRT_CUDA(cudaMemcpyAsync(w->d_sectors + lo, w->h_table.data() + lo, (size_t)(hi - lo) * sizeof(SectorRec),
                                  cudaMemcpyHostToDevice, stream));
-        VRT_CUDA(rebuild_brick_table(w, stream));
+        vrt_status st = rebuild_brick_table_for(w, b.touched, stream);
+        if (st != VRT_OK) return st;
     }
     VRT_CUDA(cudaStreamSynchronize(stream));
     b = SyncBatch();
@@ -391,6 +440,9 @@ vrt_status vrt_world_create(const vrt_world_desc* desc, vrt_world** out) {
         if (e == cudaSuccess) e = cudaMemset(w->d_sectors, 0, (size_t)w->num_sectors() * sizeof(SectorRec));
         if (e == cudaSuccess) e = cudaMalloc(&w->d_bricks, w->num_brick_positions() * sizeof(uint32_t));
         if (e == cudaSuccess) e = cudaMalloc(&w->d_groups, (size_t)w->num_groups() * sizeof(uint64_t));
+        // the group list of incremental table rebuilds, at its largest size: it never
+        // grows (a growing buffer's cudaFree would wait for the whole device)
+        if (e == cudaSuccess) e = w->d_glist.reserve((size_t)w->num_groups() * sizeof(uint32_t));
         if (e == cudaSuccess) e = rebuild_brick_table(w, 0);
         if (e == cudaSuccess) e = cudaStreamSynchronize(0);
         if (e != cudaSuccess) st = cuda_fail(e, "allocate sector table");
@@ -418,6 +470,7 @@ vrt_status vrt_world_destroy(vrt_world* w) {
     w->d_ops.release();
     w->d_scratch.release();
     w->d_io.release();
+    w->d_glist.release();
     delete w;
     return VRT_OK;
 }
@@ -433,8 +486,11 @@ vrt_status vrt_world_get_stats(const vrt_world* w, vrt_world_stats* out) {
     out->allocated_bricks = w->arena.allocated();
     out->brick_capacity = w->capacity;
     out->free_ranges = (uint32_t)w->arena.num_ranges();
-    out->device_bytes = (uint64_t)w->num_sectors() * sizeof(SectorRec) + (uint64_t)w->capacity * 576 +
-                        w->d_stage.bytes + w->d_ops.bytes + w->d_scratch.bytes + w->d_io.bytes;
+    // sector records, brick table, group masks, per slot 512 B payload + 512 B codes +
+    // 64 B cell masks, and the scratch buffers
+    out->device_bytes = (uint64_t)w->num_sectors() * sizeof(SectorRec) + (uint64_t)w->num_brick_positions() * 4 +
+                        (uint64_t)w->num_groups() * 8 + (uint64_t)w->capacity * 1088 + w->d_stage.bytes +
+                        w->d_ops.bytes + w->d_scratch.bytes + w->d_io.bytes + w->d_glist.bytes;
     return VRT_OK;
 }
 

@@ -70,6 +70,7 @@ struct vrt_world {
     vrt::DevBuf d_stage;    // uploaded brick bytes
     vrt::DevBuf d_ops;      // brick operation lists
     vrt::DevBuf d_scratch;  // bricks in flight during a repack
+    vrt::DevBuf d_glist;    // sector groups whose brick-table entries an edit re-derives
     vrt::DevBuf d_io;       // ray/hit staging for host-buffer calls
     std::vector<vrt::SectorRec> h_table;  // host copy of the sector table
 
