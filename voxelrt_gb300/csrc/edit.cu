@@ -174,7 +174,7 @@ extern "C" vrt_status vrt_world_edit(vrt_world* w, const vrt_edit* edits, uint32
     }
     const size_t eb = ed.size() * sizeof(EditDev), bb = tb.size() * sizeof(TouchedBrick);
     const size_t boff = (eb + 15) & ~size_t(15), foff = (boff + bb + 15) & ~size_t(15);
-    VRT_CUDA(w->d_ops.reserve(foff + tb.size()));
+    VRT_CUDA(w->d_ops.reserve(foff + tb.size(), true));
     uint8_t* base = (uint8_t*)w->d_ops.ptr;
     VRT_CUDA(cudaMemcpyAsync(base, ed.data(), eb, cudaMemcpyHostToDevice, stream));
     VRT_CUDA(cudaMemcpyAsync(base + boff, tb.data(), bb, cudaMemcpyHostToDevice, stream));

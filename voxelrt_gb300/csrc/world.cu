@@ -339,14 +339,14 @@ vrt_status run_batch(vrt_world* w, SyncBatch& b, cudaStream_t stream) {
     const size_t obytes = b.ops.size() * sizeof(BrickOp);
     const size_t ooff = (gbytes + 15) & ~size_t(15);
     if (gbytes + obytes) {
-        VRT_CUDA(w->d_ops.reserve(ooff + obytes));
+        VRT_CUDA(w->d_ops.reserve(ooff + obytes, true));
         if (gbytes) VRT_CUDA(cudaMemcpyAsync(w->d_ops.ptr, b.gathers.data(), gbytes, cudaMemcpyHostToDevice, stream));
         if (obytes)
             VRT_CUDA(cudaMemcpyAsync((uint8_t*)w->d_ops.ptr + ooff, b.ops.data(), obytes, cudaMemcpyHostToDevice, stream));
     }
     const size_t ng = b.gathers.size();
     if (ng) {
-        VRT_CUDA(w->d_scratch.reserve(ng * 1088));
+        VRT_CUDA(w->d_scratch.reserve(ng * 1088, true));
         uint8_t* sp = (uint8_t*)w->d_scratch.ptr;
         uint4* sc = (uint4*)(sp + ng * 512);
         uint64_t* sm = (uint64_t*)(sp + ng * 1024);

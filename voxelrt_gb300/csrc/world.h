@@ -28,8 +28,11 @@ vrt_status cuda_fail(cudaError_t e, const char* what);
 struct DevBuf {
     void* ptr = nullptr;
     size_t bytes = 0;
-    cudaError_t reserve(size_t n) {
+    // geometric: at least double, for buffers that grow call by call (each growth frees
+    // the old buffer, and cudaFree waits for the whole device)
+    cudaError_t reserve(size_t n, bool geometric = false) {
         if (n <= bytes) return cudaSuccess;
+        if (geometric && bytes * 2 > n) n = bytes * 2;
         void* p = nullptr;
         cudaError_t e = cudaMalloc(&p, n);
         if (e != cudaSuccess) return e;
