@@ -191,10 +191,14 @@ def peak_hbm():
     return 6800.0, "fallback"
 
 
-def traffic_from_profile(workload: str):
-    """DRAM bytes per launch of the persistent kernel from a committed ncu summary."""
+def traffic_from_profile(workload: str, args=None):
+    """DRAM bytes per launch of the persistent kernel from a committed ncu summary, for
+    the configuration that summary covers (the workload at its default sizes, default
+    traversal); None for any other."""
     p = ROOT / "profiles" / "traffic.json"
     if not p.exists():
+        return None
+    if args is not None and (args.glsl or args.aniso or args.worlds != 128 or args.max_views != 16):
         return None
     try:
         return json.loads(p.read_text()).get(workload)
@@ -386,7 +390,7 @@ def run_ours(args):
     peak, peak_src = peak_hbm()
     achieved = alg_bytes / (ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic_from_profile(wl.name), "peak_source": peak_src,
+                "traffic": traffic_from_profile(wl.name, args), "peak_source": peak_src,
                 "algorithmic_bytes_per_launch": alg_bytes,
                 "bytes_formula": "8*step_calls + 12*occ_fetches + 1*hits + 16*records"}
 
