@@ -231,3 +231,28 @@ def test_glsl_aniso_paths_and_batch_match_oracle(gpu):
                       oracles[0].cast(rays, world_origin=wo, glsl=True, aniso=True))
     for w in worlds:
         w.close()
+
+
+def test_edits_rederive_only_their_sector_groups(gpu):
+    """A world of 3 x 1 x 3 sector groups: each edit changes one or two groups, whose
+    brick-table entries alone are re-derived (the rest keep theirs).  Filling empty
+    sectors and carving whole blobs away flips sector emptiness, so the group masks the
+    GLSL and anisotropic entries read change; casts in all three modes match the oracle."""
+    data = sparse_world(5)
+    assert data.sectors == (9, 4, 10)
+    w, o = both_worlds(data)
+    rng = np.random.default_rng(5)
+    size = [s * 32 for s in data.sectors]
+    edits = [((40, 60, 40), 20, 9), ((250, 100, 280), 30, 0), ((150, 20, 150), 12, 33), ((260, 64, 40), 24, 0),
+             ((30, 110, 300), 16, 77)]
+    for center, radius, material in edits:
+        e = np.zeros(1, v.EDIT_DTYPE)
+        e["center"], e["radius"], e["material"] = center, radius, material
+        w.edit(e)
+        o.edit(e)
+        rays, wo = camera_frame_rays(rng, size, 20_000, zero_frac=0.0)
+        assert_hits_equal(w.cast(rays, world_origin=wo), o.cast(rays, world_origin=wo))
+        assert_hits_equal(w.cast(rays, world_origin=wo, glsl=True), o.cast(rays, world_origin=wo, glsl=True))
+        assert_hits_equal(w.cast(rays, world_origin=wo, aniso=True),
+                          o.cast(rays, world_origin=wo, glsl=True, aniso=True))
+    w.close()
