@@ -76,24 +76,14 @@ int main(int argc, char** argv) {
     if (std::fread(bricks.data(), 4, npos, f) != npos) return 5;
     if (std::fread(codes.data(), 1, codes.size(), f) != codes.size()) return 6;
     if (std::fread(payload.data(), 1, payload.size(), f) != payload.size()) return 7;
-    const size_t nsec = (size_t)dims[0] * dims[1] * dims[2];
-    const size_t ngroups = (size_t)((dims[0] + 3) / 4) * ((dims[1] + 3) / 4) * ((dims[2] + 3) / 4);
-    std::vector<uint64_t> cells((size_t)nslots * 8), groups(ngroups);
-    std::vector<SectorRec> sectors(nsec);
+    std::vector<uint64_t> cells((size_t)nslots * 8);
     if (std::fread(cells.data(), 8, cells.size(), f) != cells.size()) return 9;
-    if (std::fread(sectors.data(), sizeof(SectorRec), nsec, f) != nsec) return 10;
-    if (std::fread(groups.data(), 8, ngroups, f) != ngroups) return 11;
     std::fclose(f);
     DevWorld w{};
     w.bricks = bricks.data();
     w.codes = codes.data();
     w.payload = payload.data();
     w.cells = cells.data();
-    w.sectors = sectors.data();
-    w.groups = groups.data();
-    w.sx = dims[0];
-    w.sz = dims[2];
-    w.sxz = dims[0] * dims[2];
     w.bsx = dims[0] * 4;
     w.bsxz = dims[0] * 4 * dims[2] * 4;
     w.size_x = dims[0] * 32;

@@ -125,27 +125,13 @@ def device_layout(data: v.SectorData) -> bytes:
     up = lambda a, k: a.repeat(k, 1).repeat(k, 2).repeat(k, 3)
     code = np.where(solid, 2, np.where(~up(cell_any, 4), 3, np.where(~up(block_any, 2), 1, 0))).astype(np.uint8)
     head = np.array([sx, sy, sz, nb], np.uint32).tobytes()
-    # the raw masks the anisotropic LODs read: 8 cell masks per slot (cell cx | cz<<1 | cy<<2,
-    # bit vx + vz*4 + vy*16), the sector records, the sector-group masks
+    # the raw masks the anisotropic LODs read on allocated bricks: 8 cell masks per slot
+    # (cell cx | cz<<1 | cy<<2, bit vx + vz*4 + vy*16)
     bits = np.uint64(1) << np.arange(64, dtype=np.uint64)
     cv = solid.reshape(nb, 2, 4, 2, 4, 2, 4).transpose(0, 1, 3, 5, 2, 4, 6)  # (n, cy, cz, cx, vy, vz, vx)
     cells = (cv.reshape(nb, 8, 64).astype(np.uint64) * bits).sum(axis=2, dtype=np.uint64)
-    sectors = np.zeros((sy, sz, sx, 4), np.uint32)
-    base = 0
-    masks = {}
-    for idx, m in zip(data.sector_idx.tolist(), data.alloc_mask.tolist()):
-        masks[(idx & 4095, (idx >> 12) & 4095, (idx >> 24) & 255)] = m
-    for (x, z, y), m in masks.items():
-        sectors[y, z, x] = [m & 0xFFFFFFFF, m >> 32, base, 0]
-        base += bin(m).count("1")
-    gxn, gyn, gzn = (sx + 3) // 4, (sy + 3) // 4, (sz + 3) // 4
-    groups = np.zeros((gyn, gzn, gxn), np.uint64)
-    for (x, z, y), m in masks.items():
-        if m:
-            groups[y >> 2, z >> 2, x >> 2] |= np.uint64(1) << np.uint64((x & 3) | (z & 3) << 2 | (y & 3) << 4)
     # one code byte per voxel, x | z<<3 | y<<6 within the slot (the payload's order)
-    return (head + table.tobytes() + code.tobytes() + data.bricks.tobytes() + cells.tobytes() + sectors.tobytes() +
-            groups.tobytes())
+    return head + table.tobytes() + code.tobytes() + data.bricks.tobytes() + cells.tobytes()
 
 
 def run(exe, tmp_path, data, rays, max_iters=128, wo=(0, 0, 0), glsl=False, coarse=False, aniso=False):

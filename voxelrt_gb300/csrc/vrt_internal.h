@@ -28,7 +28,8 @@
 //   groups   per group of 4^3 sectors, bit x | z<<2 | y<<4 set per non-empty sector.
 // A brick's slot is base + popcount(mask & ((1<<b)-1)) (VoxelMap.glsl:45-64,
 // BrickSlotAllocator.h:37-41).  The traversal reads bricks, codes and payload
-// only: one 4-byte load per step, one byte more on an allocated brick.
+// only: one 4-byte load per step, one byte more on an allocated brick (the
+// anisotropic LODs read the brick's 8-byte cell mask instead of its code byte).
 #pragma once
 
 #include <cstdint>
@@ -98,7 +99,6 @@ struct alignas(16) DevWorld {
     uint32_t size_x, size_y, size_z;  // voxels
     uint32_t sx, sz, sxz;             // sector-table strides
     const uint64_t* cells;            // 8 cell masks per brick slot (GLSL anisotropic LODs)
-    const uint64_t* groups;           // sector-group masks (GLSL anisotropic LODs)
 };
 static_assert(sizeof(DevWorld) == 80, "world table entries are 80 bytes");
 

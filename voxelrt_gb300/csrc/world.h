@@ -98,7 +98,6 @@ struct vrt_world {
         w.sz = sz;
         w.sxz = sx * sz;
         w.cells = d_cells;
-        w.groups = d_groups;
         w.size_x = sx * 32;
         w.size_y = sy * 32;
         w.size_z = sz * 32;
