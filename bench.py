@@ -36,7 +36,7 @@ METRIC = "Grays/s batched vs per-view launch (bit-exact hits); p50/p99 request l
 HIT_BYTES = 16
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -63,7 +63,7 @@ def parse():
     ap.add_argument("--max-views", type=int, default=16, help="uneven_batch: views per world, at most")
     ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
                     help="N>1: every rank traces its own batch (weak) or a share, by world, of one batch (strong)")
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def dist_setup(args):
