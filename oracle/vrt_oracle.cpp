@@ -340,6 +340,15 @@ void trace_ray_glsl(const ora_world& w, const float o[3], const float d[3], cons
     const int32_t size[3] = {(int32_t)w.sx * 32, (int32_t)w.sy * 32, (int32_t)w.sz * 32};
     float* cur = tr.cur;
     clip_start(w, o, d, inv, wo, cur);
+    // rayCastCoarse replaces the origin by the clipped start (VoxelTraversal.glsl:207-210):
+    // tStart and positions count from it; rayCast keeps the origin (:162-167)
+    float oc[3];
+    const float* org = o;
+    if (coarse) {
+        for (int c = 0; c < 3; c++) oc[c] = cur[c];
+        for (int c = 0; c < 3; c++) ts[c] = ((d[c] < 0.0f ? 0.0f : 1.0f) - oc[c]) * inv[c];
+        org = oc;
+    }
     int32_t* vp = tr.vp;
     for (int c = 0; c < 3; c++) vp[c] = wadd(wo[c], floor2i(cur[c]));
     float* side = tr.side;
@@ -354,7 +363,7 @@ void trace_ray_glsl(const ora_world& w, const float o[3], const float d[3], cons
             bits += 5u;
             std::memcpy(&t, &bits, 4);
         }
-        for (int c = 0; c < 3; c++) cur[c] = o[c] + t * d[c];
+        for (int c = 0; c < 3; c++) cur[c] = org[c] + t * d[c];
         for (int c = 0; c < 3; c++) vp[c] = wadd(wo[c], floor2i(cur[c]));
         if (!((uint32_t)vp[0] < (uint32_t)size[0] && (uint32_t)vp[1] < (uint32_t)size[1] &&
               (uint32_t)vp[2] < (uint32_t)size[2])) {

@@ -1,7 +1,7 @@
 """The GLSL traversal mode on the device against the oracle's restatement of the GPU
 renderer's rayCast (VoxelTraversal.glsl:100-204): casts, single-view paths, batches,
-edits that change the 4th-level group masks.  Parity unpinned: the shader itself
-cannot run here, so the oracle's restatement is the reference."""
+edits that change the 4th-level group masks.  The oracle's restatement is itself
+pinned to the reference's shader source compiled as C++ (tests/test_glsl_pin.py)."""
 import numpy as np
 import pytest
 

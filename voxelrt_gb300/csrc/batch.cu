@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(64) view_path_kernel(DevWorld w, ViewDev v, ui
             continue;
         }
         next_path_ray<kGlsl>(s, v.shadow() != 0, v.sun, pixel, k, ox, oy, oz, dx, dy, dz);
-        safe = ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
+        safe = ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz, false, kGlsl);
         // GLSL mode: shadow and bounce rays are rayCastCoarse's (VoxelRender.comp:56,74)
         hit = run_ray<false, kGlsl>(s, safe, w, wox, woy, woz, kGlsl ? min(v.max_iters, kCoarseMaxIters) : v.max_iters,
                                     steps, cnt, kGlsl, kAniso);
@@ -260,7 +260,7 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                                       vget<kResident>(&v->sun[2], vs)};
                 next_path_ray<kGlsl>(s, ((path >> 16) & 1u) != 0, sun, pixel, kind, ox, oy, oz, dx, dy, dz);
                 path &= ~kSafe;
-                if (ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz)) path |= kSafe;
+                if (ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz, false, kGlsl)) path |= kSafe;
                 iter = 0;
                 if (kGlsl) max_iters = min(max_iters, kCoarseMaxIters);  // rayCastCoarse's cap
             } else {

@@ -97,7 +97,7 @@ __global__ void __maxnreg__(48) cast_persistent_kernel(DevWorld w, const float4*
                     ri = q_next + rank;
                     const float4 a = __ldg(rays + 2 * (size_t)ri), b = __ldg(rays + 2 * (size_t)ri + 1);
                     tag = __float_as_uint(b.z);
-                    safe = ray_start<kGlsl>(s, w, a.x, a.y, a.z, a.w, b.x, b.y, wox, woy, woz);
+                    safe = ray_start<kGlsl>(s, w, a.x, a.y, a.z, a.w, b.x, b.y, wox, woy, woz, false, coarse);
                     iter = 0;
                     active = true;
                 }

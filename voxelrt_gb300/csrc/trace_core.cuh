@@ -182,10 +182,22 @@ __device__ __forceinline__ bool ray_init(RayState& s, const DevWorld& w, float o
 // GLSL mode (VoxelTraversal.glsl rayCast): the start voxel worldOrigin + floor(start),
 // from which iteration 0 takes its side distances (:164-167).
 template <bool kGlsl>
+// coarse_origin (GLSL mode, a rayCastCoarse ray): the clipped start replaces the origin,
+// so tStart, positions and the hit distance count from it (VoxelTraversal.glsl:207-210);
+// rayCast keeps the origin and starts from the clipped voxel only (:162-167).  Without
+// a clip the start is the origin and nothing changes.
 __device__ __forceinline__ bool ray_start(RayState& s, const DevWorld& w, float ox, float oy, float oz, float dx,
                                           float dy, float dz, int32_t wox, int32_t woy, int32_t woz,
-                                          bool inside_safe = false) {
+                                          bool inside_safe = false, bool coarse_origin = false) {
     const bool safe = ray_init(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz, inside_safe);
+    if (kGlsl && coarse_origin) {
+        s.ox = s.cx;
+        s.oy = s.cy;
+        s.oz = s.cz;
+        s.tsx = __fmul_rn(__fsub_rn(dx < 0.0f ? 0.0f : 1.0f, s.ox), s.ix);
+        s.tsy = __fmul_rn(__fsub_rn(dy < 0.0f ? 0.0f : 1.0f, s.oy), s.iy);
+        s.tsz = __fmul_rn(__fsub_rn(dz < 0.0f ? 0.0f : 1.0f, s.oz), s.iz);
+    }
     if (kGlsl) {
         s.vx = wadd(wox, floor2i(s.cx));
         s.vy = wadd(woy, floor2i(s.cy));
@@ -435,7 +447,7 @@ __device__ __forceinline__ void trace_ray(const DevWorld& w, float ox, float oy,
                                           TraceResult& r, TraceCounters& cnt, bool coarse_ray = false,
                                           bool aniso = false) {
     RayState s;
-    const bool safe = ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz);
+    const bool safe = ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz, false, coarse_ray);
     uint32_t i = 0;
     uint32_t st = dda_steps_mode<kCount, kGlsl>(s, w, wox, woy, woz, cnt, safe, coarse_ray, coarse_ray, aniso, 0, i,
                                                 max_iters);
