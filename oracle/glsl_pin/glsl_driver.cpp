@@ -71,4 +71,36 @@ void glsl_ref_cast(const float* rays, uint32_t n, const int32_t* wo, int coarse,
         mat[i] = h.mat.Data.x;
     }
 }
+
+// A primary rayCast per ray and, for the rays that hit, the shadow ray the GPU renderer
+// casts toward the sun (VoxelRender.comp:56: rayCastCoarse(hit.pos + hit.normal*0.01,
+// sunDir, sunHit)).  Primary outputs as glsl_ref_cast; shadow: hit flag (2 where no
+// shadow ray was cast), dist, iters (0xFFFFFFFF where unset), material id.
+void glsl_ref_shadow(const float* rays, uint32_t n, const int32_t* wo, const float* sun, int aniso, uint8_t* hit,
+                     float* dist, float* pos, float* normal, uint32_t* iters, uint32_t* mat, uint8_t* s_hit,
+                     float* s_dist, uint32_t* s_iters, uint32_t* s_mat) {
+    u_WorldOrigin = ivec3(wo[0], wo[1], wo[2]);
+    u_UseAnisotropicLods = aniso != 0;
+    const vec3 sunDir(sun[0], sun[1], sun[2]);
+    for (uint32_t i = 0; i < n; i++) {
+        const float* r = rays + 6 * (size_t)i;
+        HitInfo h, sh;
+        std::memset(&h, 0, sizeof(h));
+        std::memset(&sh, 0, sizeof(sh));
+        h.iters = sh.iters = 0xFFFFFFFFu;
+        h.dist = sh.dist = NAN;
+        const bool ok = rayCast(vec3(r[0], r[1], r[2]), vec3(r[3], r[4], r[5]), h);
+        hit[i] = ok ? 1 : 0;
+        dist[i] = h.dist;
+        pos[3 * i] = h.pos.x, pos[3 * i + 1] = h.pos.y, pos[3 * i + 2] = h.pos.z;
+        normal[3 * i] = h.normal.x, normal[3 * i + 1] = h.normal.y, normal[3 * i + 2] = h.normal.z;
+        iters[i] = h.iters;
+        mat[i] = h.mat.Data.x;
+        s_hit[i] = 2;
+        if (ok) s_hit[i] = rayCastCoarse(h.pos + h.normal * 0.01f, sunDir, sh) ? 1 : 0;
+        s_dist[i] = sh.dist;
+        s_iters[i] = sh.iters;
+        s_mat[i] = sh.mat.Data.x;
+    }
+}
 }

@@ -31,6 +31,7 @@ sys.path.insert(0, str(ROOT))
 
 SXZ, SY = 8, 4  # sectors the shader build is sized for: 256 x 128 x 256 voxels
 MODES = ((False, False), (True, False), (False, True), (True, True))  # (coarse, aniso)
+SUN = (np.array([0.3, 0.8, 0.5]) / np.linalg.norm([0.3, 0.8, 0.5])).astype(np.float32)
 
 
 def glsl_world(kind: str, seed: int) -> np.ndarray:
@@ -122,6 +123,31 @@ def main(ref: str) -> None:
                 out[f"{m}/mat"] = mat.astype(np.uint8)
                 out[f"{m}/pos"] = pos
                 out[f"{m}/normal"] = np.sign(nrm).astype(np.int8)
+        # a view with shadow rays: the oracle's camera rays (the library's camera model), a
+        # primary rayCast each and the renderer's shadow ray where it hits
+        import voxelrt_gb300 as v
+        from oracle.oracle import camera_rays
+        rng = np.random.default_rng(200 + wi)
+        size = np.array([SXZ * 32, SY * 32, SXZ * 32], np.float64)
+        cam = v.look_at(rng.uniform(size * 0.2, size * 0.8), rng.uniform(size * 0.2, size * 0.8), 70.0, 64, 48)
+        out[f"{wi}/cam"] = np.frombuffer(bytes(cam), np.uint8)
+        cr = camera_rays(cam)
+        rays = np.ascontiguousarray(np.concatenate([cr["origin"], cr["dir"]], axis=1), np.float32)
+        wo = np.array(cam.world_origin[:], np.int32)
+        n = len(rays)
+        for aniso in (False, True):
+            a = {k: np.zeros(n, t) for k, t in (("hit", np.uint8), ("dist", np.float32), ("iters", np.uint32),
+                                                 ("mat", np.uint32), ("s_hit", np.uint8), ("s_dist", np.float32),
+                                                 ("s_iters", np.uint32), ("s_mat", np.uint32))}
+            pos, nrm = np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32)
+            lib.glsl_ref_shadow(p(rays), C.c_uint32(n), p(wo), p(SUN), int(aniso), p(a["hit"]), p(a["dist"]), p(pos),
+                                p(nrm), p(a["iters"]), p(a["mat"]), p(a["s_hit"]), p(a["s_dist"]), p(a["s_iters"]),
+                                p(a["s_mat"]))
+            m = f"{wi}/view/{int(aniso)}"
+            for k, arr in a.items():
+                out[f"{m}/{k}"] = arr.astype(np.uint8) if k in ("mat", "s_mat") else arr
+            out[f"{m}/pos"], out[f"{m}/normal"] = pos, np.sign(nrm).astype(np.int8)
+    out["sun"] = SUN
     np.savez_compressed(ROOT / "tests" / "golden" / "refglsl.npz", **out)
     print("wrote tests/golden/refglsl.npz")
 
