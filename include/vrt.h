@@ -120,6 +120,8 @@ typedef struct vrt_cast_params {
  * The GPU renderer casts shadow and bounce rays with rayCastCoarse instead
  * (VoxelTraversal.glsl:206-240, VoxelRender.comp:56,74,81), and so do the secondary
  * rays of VRT_VIEW_GLSL views and casts with VRT_CAST_GLSL_COARSE:
+ *   - the entry-clipped start replaces the ray origin: tStart, positions and the
+ *     reported t count from it (rayCast keeps the origin and clips the start voxel);
  *   - tmin = min(sides) + 0.001 instead of + 5 ulp;
  *   - from iteration 31 on, an empty voxel whose 4^3 cell holds a solid voxel ends
  *     the ray as a hit on the cell's first solid voxel in mask order (x, then z, then
