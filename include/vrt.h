@@ -388,7 +388,10 @@ vrt_status vrt_batch_measure(vrt_batch* batch, vrt_hit* hits_device, void* strea
  * worlds and 1024 views (VRT_ERR_INVALID_ARG beyond).  The first call on a device
  * looks up that array's address; make it before any stream capture.  All calls
  * share the array: calls whose launches overlap on the GPU race, so order them on
- * one stream.  Records are laid out as for vrt_batch (views back to back). */
+ * one stream.  The world and view tables are staged in library-owned host tables,
+ * so a call first waits on the host until the table copies of the previous call on
+ * the same device have run.  The caller's current device is the same when the call
+ * returns.  Records are laid out as for vrt_batch (views back to back). */
 vrt_status vrt_render_views_static(vrt_world* const* worlds, uint32_t n_worlds, const vrt_view* views,
                                    uint32_t n_views, const vrt_batch_config* cfg, vrt_hit* hits_device,
                                    void* stream);

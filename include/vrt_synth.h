@@ -1,5 +1,8 @@
 /*
- * vrt_synth.h - seeded synthetic worlds and ray sets (part of libvrt.so).
+ * vrt_synth.h - seeded synthetic worlds and ray sets (libvrt_synth.so, a host-only
+ * library: it needs no GPU and links no CUDA; it also exports vrt_camera_look_at and
+ * vrt_sector_stream_free of vrt.h, so that test and benchmark inputs can be built
+ * without loading libvrt.so).
  *
  * The reference builds worlds with FastNoise2 terrain (src/VoxelRT/TerrainGenerator.cpp:5-34)
  * or by voxelizing meshes; neither is reproducible here, so benchmark and test
@@ -32,6 +35,9 @@ typedef struct vrt_synth_terrain {
     double cave_scale, cave_threshold;
     uint64_t cave_seed;
 } vrt_synth_terrain;
+
+/* Message of the last failed call of this library on the calling thread. */
+const char* vrt_synth_last_error(void);
 
 /* threads = 0 uses every hardware thread. The stream is freed with vrt_sector_stream_free. */
 vrt_status vrt_synth_terrain_world(const vrt_synth_terrain* desc, int threads, vrt_sector_stream** out);

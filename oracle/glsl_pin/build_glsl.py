@@ -18,6 +18,7 @@ reference sets them from its view size, GpuRenderer.cpp:9-14) are given per buil
 
 Usage: python oracle/glsl_pin/build_glsl.py [reference checkout] [sectors_xz] [sectors_y]
 """
+import os
 import re
 import subprocess
 import sys
@@ -41,7 +42,10 @@ def rewrite(text: str, shader_dir: Path) -> str:
 
 
 def main() -> None:
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref_arg = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("VRT_REFERENCE_DIR")
+    if not ref_arg:
+        sys.exit("usage: build_glsl.py <reference checkout> [sectors_xz sectors_y] (or $VRT_REFERENCE_DIR)")
+    ref = Path(ref_arg)
     sxz = int(sys.argv[2]) if len(sys.argv) > 2 else 8
     sy = int(sys.argv[3]) if len(sys.argv) > 3 else 4
     shaders = ref / "src" / "VoxelRT" / "Shaders"

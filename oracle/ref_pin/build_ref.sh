@@ -4,7 +4,11 @@
 # SIMD layer supports nothing else); run where the reference checkout exists.
 # Float semantics: no -ffast-math and no FMA contraction (the reading the oracle pins).
 set -e
-REF=${1:-/root/reference}
+REF=${1:-$VRT_REFERENCE_DIR}
+if [ -z "$REF" ]; then
+    echo "usage: build_ref.sh <reference checkout> (or set VRT_REFERENCE_DIR)" >&2
+    exit 2
+fi
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/../_ref"
 mkdir -p "$OUT"

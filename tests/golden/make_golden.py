@@ -13,12 +13,13 @@ The reference's FlatVoxelStorage spans a fixed 2048x512x2048 view (64x16x64
 sectors, CpuRenderer.cpp:13-16) and has no entry clip, so rays start inside it and
 the oracle is run on a world of that extent.
 
-Usage: python tests/golden/make_golden.py [reference checkout, default /root/reference]
+Usage: python tests/golden/make_golden.py <reference checkout> (or $VRT_REFERENCE_DIR)
 """
 from __future__ import annotations
 
 import ctypes as C
 import subprocess
+import os
 import sys
 from pathlib import Path
 
@@ -151,4 +152,7 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("VRT_REFERENCE_DIR")
+    if not ref:
+        sys.exit("usage: give the reference checkout as the argument or in $VRT_REFERENCE_DIR")
+    main(ref)

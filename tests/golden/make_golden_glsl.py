@@ -17,10 +17,11 @@ UpdateOccupancy.comp fill them (GpuRenderer.cpp:45-167):
     tests/test_oracle_cpu.py checks against the forward box for all 512 entries;
   * Palette[i] encodes id i, so a hit's material is the voxel id.
 
-Usage: python tests/golden/make_golden_glsl.py [reference checkout, default /root/reference]
+Usage: python tests/golden/make_golden_glsl.py <reference checkout> (or $VRT_REFERENCE_DIR)
 """
 import ctypes as C
 import subprocess
+import os
 import sys
 from pathlib import Path
 
@@ -153,4 +154,7 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("VRT_REFERENCE_DIR")
+    if not ref:
+        sys.exit("usage: give the reference checkout as the argument or in $VRT_REFERENCE_DIR")
+    main(ref)

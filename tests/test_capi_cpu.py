@@ -11,12 +11,9 @@ ROOT = Path(__file__).resolve().parent.parent
 DECL = re.compile(r"^[A-Za-z_][\w\s\*]*?\b(vrt_\w+)\s*\(", re.M)
 
 
-def declared_symbols():
-    names = set()
-    for h in (ROOT / "include").glob("*.h"):
-        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
-        names.update(m.group(1) for m in DECL.finditer(text))
-    return names
+def declared_symbols(header="vrt.h"):
+    text = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / header).read_text(), flags=re.S)
+    return {m.group(1) for m in DECL.finditer(text)}
 
 
 def test_every_declared_symbol_is_exported():
@@ -27,6 +24,21 @@ def test_every_declared_symbol_is_exported():
     assert not missing, missing
     # and the Python binding declares a prototype for each of them
     assert names <= set(v.capi.PROTOTYPES), sorted(names - set(v.capi.PROTOTYPES))
+    # the synthetic-input generators are not part of the product library
+    assert not any(hasattr(lib, n) for n in declared_symbols("vrt_synth.h"))
+
+
+def test_synth_library_is_host_only():
+    """libvrt_synth.so exports what include/vrt_synth.h declares (plus the camera builder and
+    the stream release of vrt.h) and links no CUDA library."""
+    path = ROOT / "voxelrt_gb300" / "_lib" / "libvrt_synth.so"
+    lib = C.CDLL(str(path))
+    names = declared_symbols("vrt_synth.h") | {"vrt_camera_look_at", "vrt_sector_stream_free"}
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+    assert names <= set(v.capi.SYNTH_PROTOTYPES)
+    needed = [ln for ln in path.read_bytes().split(b"\0") if ln.startswith(b"libcuda")]
+    assert not needed, needed
 
 
 def test_struct_layouts_match_header():
@@ -39,7 +51,14 @@ def test_host_logic_without_gpu():
     # WorldSectorIndexer packing (VoxelMap.h:95-100): x | z<<12 | y<<24, 12/8/12 signed bits
     assert v.sector_index(1, 2, 3) == 1 | 3 << 12 | 2 << 24
     assert v.sector_index(-1, 0, 0) == 0xFFF
+    for xyz in [(1, 2, 3), (-1, 0, 0), (5, -2, 7), (-3, -128, 2047), (100, 127, -100)]:
+        assert v.sector_index(*xyz) == v.lib().vrt_sector_index(*xyz)
     cam = v.look_at((128, 200, -40), (128, 80, 128), 90.0, 640, 360)
+    # the product library's camera builder is the same code
+    cam2 = v.Camera()
+    p3, t3 = (C.c_double * 3)(128, 200, -40), (C.c_double * 3)(128, 80, 128)
+    v.check(v.lib().vrt_camera_look_at(p3, t3, 90.0, 640, 360, C.byref(cam2)))
+    assert bytes(cam) == bytes(cam2)
     assert list(cam.world_origin) == [128, 200, -40] and cam.width == 640
     # the centre pixel looks at the target
     d = np.array(cam.d0[:]) + 320 * np.array(cam.du[:]) + 180 * np.array(cam.dv[:])

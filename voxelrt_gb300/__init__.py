@@ -19,7 +19,7 @@ import numpy as np
 from . import capi
 from .capi import (CAST_GLSL, EDIT_DTYPE, HIT_DTYPE, MISS_FACE, MISS_VOXEL, NO_RAY, RAY_DTYPE, VIEW_GLSL, VIEW_SHADOW,
                    BatchConfig, Camera,
-                   CastParams, View, VrtError, check, lib, ptr)
+                   CastParams, View, VrtError, check, check_synth, lib, ptr, synth_lib)
 
 __all__ = ["Server", "PinnedHits", "view_records", "render_path", "cvox_read", "cvox_write", "World", "Camera", "View",
            "make_view", "Batch", "BatchConfig", "VIEW_SHADOW", "VIEW_GLSL", "CAST_GLSL", "look_at", "synth_terrain", "synth_mix", "random_rays", "SectorData", "VrtError",
@@ -28,8 +28,10 @@ __all__ = ["Server", "PinnedHits", "view_records", "render_path", "cvox_read", "
 
 
 def sector_index(x: int, y: int, z: int) -> int:
-    """WorldSectorIndexer packing (VoxelMap.h:100)."""
-    return lib().vrt_sector_index(x, y, z)
+    """WorldSectorIndexer packing (VoxelMap.h:100): x | z<<12 | y<<24 in 12/12/8-bit
+    fields, as a signed 32-bit value (vrt_sector_index computes the same)."""
+    u = (x & 4095) | (z & 4095) << 12 | (y & 255) << 24
+    return u - (1 << 32) if u >= (1 << 31) else u
 
 
 def unpack_voxel(v: np.ndarray) -> np.ndarray:
@@ -39,10 +41,11 @@ def unpack_voxel(v: np.ndarray) -> np.ndarray:
 
 
 def look_at(pos, target, vfov_deg: float, width: int, height: int) -> Camera:
+    """vrt_camera_look_at, from the host-only input library (the same code as libvrt.so's)."""
     cam = Camera()
     p = (C.c_double * 3)(*map(float, pos))
     t = (C.c_double * 3)(*map(float, target))
-    check(lib().vrt_camera_look_at(p, t, float(vfov_deg), int(width), int(height), C.byref(cam)))
+    check_synth(synth_lib().vrt_camera_look_at(p, t, float(vfov_deg), int(width), int(height), C.byref(cam)))
     return cam
 
 
@@ -61,14 +64,15 @@ class SectorData:
         return self.bricks.shape[0]
 
     @classmethod
-    def _from_native(cls, sp) -> "SectorData":
+    def _from_native(cls, sp, owner=None) -> "SectorData":
+        """Copy a native sector stream; `owner` is the library that made it (it frees it)."""
         s = sp.contents
         n, nb = s.n_sectors, s.n_bricks
         idx = np.ctypeslib.as_array(s.sector_idx, shape=(max(n, 1),))[:n].copy()
         mask = np.ctypeslib.as_array(s.alloc_mask, shape=(max(n, 1),))[:n].copy()
         bricks = np.ctypeslib.as_array(s.bricks, shape=(max(nb, 1) * 512,))[: nb * 512].copy()
         sectors = (s.sectors_x, s.sectors_y, s.sectors_z)
-        lib().vrt_sector_stream_free(sp)
+        (owner or lib()).vrt_sector_stream_free(sp)
         return cls(sectors, idx, mask, bricks)
 
     def dense(self) -> np.ndarray:
@@ -92,13 +96,13 @@ def synth_terrain(size, base, amplitude, seed, scale=128.0, octaves=4, cave_octa
                   cave_threshold=0.35, cave_seed=0, threads=0) -> SectorData:
     d = _terrain_desc(size, base, amplitude, seed, scale, octaves, cave_octaves, cave_scale, cave_threshold, cave_seed)
     out = C.POINTER(capi.SectorStream)()
-    check(lib().vrt_synth_terrain_world(C.byref(d), int(threads), C.byref(out)))
-    return SectorData._from_native(out)
+    check_synth(synth_lib().vrt_synth_terrain_world(C.byref(d), int(threads), C.byref(out)))
+    return SectorData._from_native(out, synth_lib())
 
 
 def terrain_height(x, z, size, base, amplitude, seed, scale=128.0, octaves=4) -> float:
     d = _terrain_desc(size, base, amplitude, seed, scale, octaves, 0, 64.0, 0.35, 0)
-    return lib().vrt_synth_terrain_height(C.byref(d), float(x), float(z))
+    return synth_lib().vrt_synth_terrain_height(C.byref(d), float(x), float(z))
 
 
 def _terrain_desc(size, base, amplitude, seed, scale, octaves, cave_octaves, cave_scale, cave_threshold, cave_seed):
@@ -126,14 +130,14 @@ def cvox_read(path) -> SectorData:
 
 def synth_mix(edge: int, seed: int, threads: int = 0) -> SectorData:
     out = C.POINTER(capi.SectorStream)()
-    check(lib().vrt_synth_mix_world(int(edge), int(seed), int(threads), C.byref(out)))
-    return SectorData._from_native(out)
+    check_synth(synth_lib().vrt_synth_mix_world(int(edge), int(seed), int(threads), C.byref(out)))
+    return SectorData._from_native(out, synth_lib())
 
 
 def random_rays(size, seed: int, n: int, first: int = 0, threads: int = 0) -> np.ndarray:
     rays = np.zeros(n, RAY_DTYPE)
     s = (C.c_uint32 * 3)(*[int(v) for v in size])
-    check(lib().vrt_synth_random_rays(s, int(seed), int(first), int(n), int(threads), rays.ctypes.data))
+    check_synth(synth_lib().vrt_synth_random_rays(s, int(seed), int(first), int(n), int(threads), rays.ctypes.data))
     return rays
 
 

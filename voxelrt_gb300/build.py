@@ -3,8 +3,9 @@
 Run as ``python -m voxelrt_gb300.build`` or through ``__graft_entry__.build()``.
 Translation units compile in parallel; outputs stay in-tree:
 
-* ``voxelrt_gb300/_lib/libvrt.so`` - the product library (C ABI of include/vrt.h,
-  include/vrt_synth.h);
+* ``voxelrt_gb300/_lib/libvrt.so`` - the product library (C ABI of include/vrt.h);
+* ``voxelrt_gb300/_lib/libvrt_synth.so`` - host-only generators of seeded worlds, cameras
+  and rays (include/vrt_synth.h), for tests and the benchmark; no CUDA;
 * ``oracle/_build/libvrt_oracle.so`` - the CPU oracle, a test/benchmark checker.
 """
 from __future__ import annotations
@@ -22,6 +23,10 @@ CSRC = PKG / "csrc"
 LIB_DIR = PKG / "_lib"
 OBJ_DIR = PKG / "_build"
 LIBVRT = LIB_DIR / "libvrt.so"
+LIBSYNTH = LIB_DIR / "libvrt_synth.so"
+# host sources of the synthetic-input library (and nothing of it goes into libvrt.so)
+SYNTH_SRC = ["synth.cpp"]
+SHARED_HOST_SRC = ["host_common.cpp"]
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_LIB = ORACLE_DIR / "_build" / "libvrt_oracle.so"
 
@@ -56,7 +61,7 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
     nvcc = _nvcc()
     headers = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted((ROOT / "include").glob("*.h"))
     cu = sorted(CSRC.glob("*.cu"))
-    cpp = sorted(CSRC.glob("*.cpp"))
+    cpp = sorted(p for p in CSRC.glob("*.cpp") if p.name not in SYNTH_SRC)
     OBJ_DIR.mkdir(parents=True, exist_ok=True)
     LIB_DIR.mkdir(parents=True, exist_ok=True)
     jobs = []
@@ -82,6 +87,17 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
     return LIBVRT
 
 
+def build_synth(force: bool = False) -> Path:
+    srcs = [CSRC / n for n in SYNTH_SRC + SHARED_HOST_SRC]
+    deps = srcs + sorted(CSRC.glob("*.h")) + sorted((ROOT / "include").glob("*.h"))
+    LIB_DIR.mkdir(parents=True, exist_ok=True)
+    if force or _stale(LIBSYNTH, deps):
+        tmp = LIBSYNTH.with_suffix(".so.tmp")
+        _run(["g++", *CXX_FLAGS, "-shared", "-I", str(ROOT / "include"), "-o", str(tmp), *map(str, srcs)])
+        os.replace(tmp, LIBSYNTH)
+    return LIBSYNTH
+
+
 def build_oracle(force: bool = False) -> Path:
     src = ORACLE_DIR / "vrt_oracle.cpp"
     deps = [src, ORACLE_DIR / "vrt_oracle.h", ROOT / "include" / "vrt.h"]
@@ -94,14 +110,14 @@ def build_oracle(force: bool = False) -> Path:
 
 
 def build_all(force: bool = False, verbose: bool = False) -> None:
-    with cf.ThreadPoolExecutor(max_workers=2) as ex:
-        f1 = ex.submit(build_library, force, verbose)
-        f2 = ex.submit(build_oracle, force)
-        f1.result()
-        f2.result()
+    with cf.ThreadPoolExecutor(max_workers=3) as ex:
+        futs = [ex.submit(build_library, force, verbose), ex.submit(build_oracle, force), ex.submit(build_synth, force)]
+        for f in futs:
+            f.result()
 
 
 if __name__ == "__main__":
     build_all(force="--force" in sys.argv, verbose="-v" in sys.argv)
     print(LIBVRT)
+    print(LIBSYNTH)
     print(ORACLE_LIB)

@@ -11,6 +11,7 @@ from pathlib import Path
 import numpy as np
 
 _LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libvrt.so"
+_SYNTH_PATH = Path(__file__).resolve().parent / "_lib" / "libvrt_synth.so"
 
 VRT_OK = 0
 VRT_ERR_INVALID_ARG = 1
@@ -190,11 +191,19 @@ PROTOTYPES = {
     "vrt_server_wait": (_st, [_vp, _u64, _u32, C.POINTER(RequestInfo)]),
     "vrt_server_drain": (_st, [_vp, _u32]),
     "vrt_server_get_stats": (_st, [_vp, C.c_int, C.POINTER(ServerStats)]),
+    "vrt_sector_stream_free": (None, [C.POINTER(SectorStream)]),
+}
+
+# libvrt_synth.so (include/vrt_synth.h): host-only generators of seeded inputs, plus its
+# own copies of vrt_camera_look_at and vrt_sector_stream_free
+SYNTH_PROTOTYPES = {
+    "vrt_synth_last_error": (C.c_char_p, []),
     "vrt_synth_terrain_world": (_st, [C.POINTER(SynthTerrain), C.c_int, C.POINTER(C.POINTER(SectorStream))]),
     "vrt_synth_terrain_height": (C.c_double, [C.POINTER(SynthTerrain), C.c_double, C.c_double]),
     "vrt_synth_mix_world": (_st, [_u32, _u64, C.c_int, C.POINTER(C.POINTER(SectorStream))]),
-    "vrt_sector_stream_free": (None, [C.POINTER(SectorStream)]),
     "vrt_synth_random_rays": (_st, [C.POINTER(_u32), _u64, _u64, _u64, C.c_int, _vp]),
+    "vrt_camera_look_at": PROTOTYPES["vrt_camera_look_at"],
+    "vrt_sector_stream_free": PROTOTYPES["vrt_sector_stream_free"],
 }
 
 
@@ -205,20 +214,38 @@ class VrtError(RuntimeError):
 
 
 _lib = None
+_synth = None
+
+
+def _load(path: Path, prototypes: dict) -> C.CDLL:
+    if not path.exists():
+        raise ImportError(f"{path} is missing: run `python -m voxelrt_gb300.build` first")
+    L = C.CDLL(str(path))
+    for name, (res, args) in prototypes.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    return L
+
+
+def synth_lib() -> C.CDLL:
+    """Load libvrt_synth.so, the host-only input generators (raises if it has not been built)."""
+    global _synth
+    if _synth is None:
+        _synth = _load(_SYNTH_PATH, SYNTH_PROTOTYPES)
+    return _synth
+
+
+def check_synth(status: int) -> None:
+    if status != VRT_OK:
+        raise VrtError(status, synth_lib().vrt_synth_last_error().decode(errors="replace"))
 
 
 def lib() -> C.CDLL:
     """Load libvrt.so (raises if it has not been built)."""
     global _lib
     if _lib is None:
-        if not _LIB_PATH.exists():
-            raise ImportError(f"{_LIB_PATH} is missing: run `python -m voxelrt_gb300.build` first")
-        L = C.CDLL(str(_LIB_PATH))
-        for name, (res, args) in PROTOTYPES.items():
-            fn = getattr(L, name)
-            fn.restype = res
-            fn.argtypes = args
-        _lib = L
+        _lib = _load(_LIB_PATH, PROTOTYPES)
     return _lib
 
 

@@ -641,14 +641,43 @@ vrt_status plan_views(const vrt_view* views, uint32_t n, uint32_t n_worlds, cons
     return VRT_OK;
 }
 
-vrt_status persistent_grid(int device, const vrt_batch_config& cfg, bool count, int& blocks, int& threads) {
+namespace {
+
+// Resident blocks per SM of the instantiation that a launch of this kind runs: the GLSL
+// and anisotropic variants differ from the default one in registers and shared memory
+// (the anisotropic LUT is 8 KB per block).
+cudaError_t persistent_occupancy(int& occ, int threads, bool count, bool glsl, bool aniso, bool resident) {
+    if (resident) {
+        if (glsl && aniso)
+            return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<false, true, true, true>,
+                                                                 threads, 0);
+        if (glsl)
+            return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<false, true, true>, threads, 0);
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<false, false, true>, threads, 0);
+    }
+    if (count) {
+        if (glsl && aniso)
+            return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<true, true, false, true>,
+                                                                 threads, 0);
+        if (glsl)
+            return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<true, true>, threads, 0);
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<true, false>, threads, 0);
+    }
+    if (glsl && aniso)
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<false, true, false, true>, threads,
+                                                             0);
+    if (glsl) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<false, true>, threads, 0);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<false, false>, threads, 0);
+}
+
+}  // namespace
+
+vrt_status persistent_grid(int device, const vrt_batch_config& cfg, bool count, bool glsl, bool aniso, bool resident,
+                           int& blocks, int& threads) {
     int sms = 0, occ = 0;
     threads = (int)cfg.warps_per_block * 32;
     VRT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    if (count)
-        VRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<true, false>, threads, 0));
-    else
-        VRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<false, false>, threads, 0));
+    VRT_CUDA(persistent_occupancy(occ, threads, count, glsl, aniso, resident));
     occ = std::max(occ, 1);
     const int per_sm = (!count && cfg.blocks_per_sm) ? std::min<int>((int)cfg.blocks_per_sm, occ) : occ;
     blocks = sms * per_sm;
@@ -831,8 +860,11 @@ vrt_status vrt_batch_create(vrt_world* const* worlds, uint32_t n_worlds, const v
     if (e != cudaSuccess) return fail(cuda_fail(e, "batch allocation"));
     b->d_counters = reinterpret_cast<unsigned long long*>(reinterpret_cast<uint8_t*>(b->d_queue) + 16);
     if ((st = refresh_worlds(b, 0)) != VRT_OK) return fail(st);
-    if ((st = persistent_grid(b->device, cfg, false, b->blocks, b->threads)) != VRT_OK) return fail(st);
-    if ((st = persistent_grid(b->device, cfg, true, b->blocks_count, b->threads_count)) != VRT_OK) return fail(st);
+    const bool glsl = b->plan.glsl, aniso = b->plan.aniso;
+    if ((st = persistent_grid(b->device, cfg, false, glsl, aniso, false, b->blocks, b->threads)) != VRT_OK)
+        return fail(st);
+    if ((st = persistent_grid(b->device, cfg, true, glsl, aniso, false, b->blocks_count, b->threads_count)) != VRT_OK)
+        return fail(st);
     *out = b;
     return VRT_OK;
 }

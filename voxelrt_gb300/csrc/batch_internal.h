@@ -107,8 +107,10 @@ vrt_status normalize_batch_config(const vrt_batch_config* in, vrt_batch_config& 
 // Validate views against n_worlds and lay them out (tiles, queue chunks, record offsets).
 vrt_status plan_views(const vrt_view* views, uint32_t n, uint32_t n_worlds, const vrt_batch_config& cfg,
                       LaunchPlan& plan);
-// Grid of the persistent kernel: every SM, as many blocks as fit (or cfg.blocks_per_sm).
-vrt_status persistent_grid(int device, const vrt_batch_config& cfg, bool count, int& blocks, int& threads);
+// Grid of the persistent kernel: every SM, as many blocks of the launched instantiation
+// (counting, traversal mode, resident) as fit, or cfg.blocks_per_sm of them.
+vrt_status persistent_grid(int device, const vrt_batch_config& cfg, bool count, bool glsl, bool aniso, bool resident,
+                           int& blocks, int& threads);
 BatchParams make_params(const LaunchPlan& plan, const DevWorld* worlds, const ViewDev* views,
                         const uint32_t* chunk_base, uint32_t* queue, vrt_hit* out);
 // Queue reset (the tile counter, and with reset_counters the launch counters: 64

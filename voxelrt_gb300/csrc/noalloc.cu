@@ -36,16 +36,39 @@ constexpr size_t kScratchBytes = align256(kChunkOff + (kStaticMaxViews + 1) * si
 // device address comes from cudaGetSymbolAddress below.
 static __device__ __align__(256) uint8_t g_static_scratch[kScratchBytes];
 
-// Host side of one call.  Pageable host copies are staged before
-// cudaMemcpyAsync returns, so these buffers are free again when the call returns.
+// Host side of the calls.  The tables below are the sources of the call's
+// host-to-device copies.  Those copies are from pageable memory, which a device with a
+// coherent host link (GB300 over NVLink-C2C) may read while the copy runs, after
+// cudaMemcpyAsync has returned.  So each device's `copied` event is recorded behind the
+// three copies, and the next call waits for it before it rewrites the tables.  The
+// events are created with the scratch address at a device's first call; creating an
+// event allocates no device memory.
 struct StaticState {
     std::mutex mu;
     uint8_t* scratch[kStaticMaxDevices] = {};  // device address per device ordinal
+    cudaEvent_t copied[kStaticMaxDevices] = {};
     DevWorld worlds[kStaticMaxWorlds];
     ViewDev views[kStaticMaxViews];
     uint32_t chunk_base[kStaticMaxViews + 1];
 };
 StaticState g_state;
+
+// Makes `device` current for the call and gives the caller's current device back when
+// the call returns.
+struct DeviceScope {
+    int prev = -1;
+    cudaError_t enter(int device) {
+        cudaError_t e = cudaGetDevice(&prev);
+        if (e != cudaSuccess) {
+            prev = -1;
+            return e;
+        }
+        return prev == device ? cudaSuccess : cudaSetDevice(device);
+    }
+    ~DeviceScope() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
 
 uint32_t log2u_static(uint32_t v) {
     uint32_t r = 0;
@@ -92,14 +115,21 @@ extern "C" vrt_status vrt_render_views_static(vrt_world* const* worlds, uint32_t
     if ((st = check_same_mode(views, n_views)) != VRT_OK) return st;
     const bool glsl = n_views > 0 && view_glsl(views[0]);
     std::lock_guard<std::mutex> lock(g_state.mu);
-    VRT_CUDA(cudaSetDevice(device));
-    // first call on this device: look up the device address of the scratch array
+    DeviceScope scope;
+    VRT_CUDA(scope.enter(device));
+    // first call on this device: look up the device address of the scratch array, and
+    // create the event that guards the host tables
     if (!g_state.scratch[device]) {
         void* p = nullptr;
         VRT_CUDA(cudaGetSymbolAddress(&p, g_static_scratch));
+        cudaEvent_t ev = nullptr;
+        VRT_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        g_state.copied[device] = ev;
         g_state.scratch[device] = static_cast<uint8_t*>(p);
     }
     uint8_t* scratch = g_state.scratch[device];
+    // the copies of the last call on this device have read the host tables
+    VRT_CUDA(cudaEventSynchronize(g_state.copied[device]));
     // lay the views out behind one tile queue (same layout as vrt_batch)
     const uint32_t tw_log2 = log2u_static(cfg.tile_w), ts_log2 = log2u_static(cfg.tile_w * cfg.tile_h);
     uint64_t chunks = 0, records = 0;
@@ -133,6 +163,7 @@ extern "C" vrt_status vrt_render_views_static(vrt_world* const* worlds, uint32_t
                              stream));
     VRT_CUDA(cudaMemcpyAsync(scratch + kChunkOff, g_state.chunk_base, (n_views + 1) * sizeof(uint32_t),
                              cudaMemcpyHostToDevice, stream));
+    VRT_CUDA(cudaEventRecord(g_state.copied[device], stream));
     BatchParams p{};
     p.worlds = reinterpret_cast<const DevWorld*>(scratch + kWorldsOff);
     p.views = reinterpret_cast<const ViewDev*>(scratch + kViewsOff);
@@ -151,7 +182,8 @@ extern "C" vrt_status vrt_render_views_static(vrt_world* const* worlds, uint32_t
     p.glsl = glsl ? 1u : 0u;
     p.aniso = n_views > 0 && view_aniso(views[0]) ? 1u : 0u;
     int blocks = 0, threads = 0;
-    if ((st = persistent_grid(device, cfg, false, blocks, threads)) != VRT_OK) return st;
+    if ((st = persistent_grid(device, cfg, false, p.glsl != 0, p.aniso != 0, false, blocks, threads)) != VRT_OK)
+        return st;
     // launch_persistent zeroes the queue counter and the launch counters first
     return launch_persistent(p, blocks, threads, false, stream);
 }

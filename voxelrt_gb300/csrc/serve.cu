@@ -121,7 +121,12 @@ struct vrt_server {
     std::vector<vrt_world*> worlds;
     vrt_server_config cfg{};
     vrt_batch_config bcfg{};
-    int blocks = 0, threads = 0;
+    // persistent grid per traversal mode (view_mode: 0, GLSL, GLSL + anisotropic) of the
+    // instantiation the server launches in its scheduling mode: blocks, threads
+    int grid[3][2] = {};
+    const int* grid_of(uint32_t mode) const {
+        return grid[(mode & VRT_VIEW_GLSL_ANISO) ? 2 : (mode & VRT_VIEW_GLSL) ? 1 : 0];
+    }
     DevWorld* d_worlds = nullptr;
     uint8_t* arena = nullptr;  // output records of admitted requests
     FreeList pages;
@@ -224,7 +229,8 @@ vrt_status launch_slot(vrt_server* sv, Slot& s, std::vector<Request*>& rs) {
                              s.stream));
     BatchParams p = make_params(plan, sv->d_worlds, (const ViewDev*)s.views.ptr, (const uint32_t*)s.chunk_base.ptr,
                                 (uint32_t*)s.queue.ptr, (vrt_hit*)sv->arena);
-    if ((st = launch_persistent(p, sv->blocks, sv->threads, false, s.stream)) != VRT_OK) return st;
+    const int* g = sv->grid_of(view_mode(views[0]));
+    if ((st = launch_persistent(p, g[0], g[1], false, s.stream)) != VRT_OK) return st;
     for (size_t i = 0; i < rs.size(); i++) {
         const Request* r = rs[i];
         VRT_CUDA(cudaMemcpyAsync(r->host_out, sv->arena + plan.views[i].out_base * sizeof(vrt_hit),
@@ -467,7 +473,8 @@ vrt_status resident_start(vrt_server* sv, uint32_t mode) {
 
 vrt_status resident_launch(vrt_server* sv) {
     Resident& R = sv->res;
-    vrt_status st = launch_resident(R.params, sv->blocks, sv->threads, R.stream);
+    const int* g = sv->grid_of(R.mode);
+    vrt_status st = launch_resident(R.params, g[0], g[1], R.stream);
     if (st != VRT_OK) return st;
     VRT_CUDA(cudaEventRecord(R.ended, R.stream));
     R.live = true;
@@ -764,7 +771,6 @@ vrt_status vrt_server_create(vrt_world* const* worlds, uint32_t n_worlds, const 
     if ((st = refresh_world_table(sv)) != VRT_OK) return fail(st);
     if ((e = cudaStreamCreateWithFlags(&sv->edit_stream, cudaStreamNonBlocking)) != cudaSuccess)
         return fail(cuda_fail(e, "edit stream"));
-    if ((st = persistent_grid(sv->device, sv->bcfg, false, sv->blocks, sv->threads)) != VRT_OK) return fail(st);
     for (uint32_t i = 0; i < sv->cfg.max_inflight; i++) {
         auto s = std::make_unique<Slot>();
         s->server = sv;
@@ -793,6 +799,10 @@ vrt_status vrt_server_create(vrt_world* const* worlds, uint32_t n_worlds, const 
         resident = native != 0;
     }
     sv->resident = resident;
+    for (int m = 0; m < 3; m++)
+        if ((st = persistent_grid(sv->device, sv->bcfg, false, m >= 1, m == 2, resident, sv->grid[m][0],
+                                  sv->grid[m][1])) != VRT_OK)
+            return fail(st);
     if (resident && (st = resident_init(sv)) != VRT_OK) return fail(st);
     sv->worker = resident ? std::thread(worker_resident, sv) : std::thread(worker_main, sv);
     *out = sv;

@@ -18,6 +18,7 @@
 
 namespace vrt {
 void set_error(const std::string& msg);
+const char* last_error_cstr();
 }
 
 namespace {
@@ -216,6 +217,8 @@ struct Sphere {
 
 extern "C" {
 
+const char* vrt_synth_last_error(void) { return vrt::last_error_cstr(); }
+
 double vrt_synth_terrain_height(const vrt_synth_terrain* d, double x, double z) {
     return d->base + d->amplitude * fbm2(x / d->scale, z / d->scale, d->octaves, d->seed);
 }
@@ -331,14 +334,6 @@ vrt_status vrt_synth_mix_world(uint32_t edge, uint64_t seed, int threads, vrt_se
         return any;
     };
     return build_stream(ns, ns, ns, threads, fill, out);
-}
-
-void vrt_sector_stream_free(vrt_sector_stream* s) {
-    if (!s) return;
-    std::free(s->sector_idx);
-    std::free(s->alloc_mask);
-    std::free(s->bricks);
-    std::free(s);
 }
 
 vrt_status vrt_synth_random_rays(const uint32_t size[3], uint64_t seed, uint64_t first, uint64_t n, int threads,

@@ -21,13 +21,6 @@
 
 namespace vrt {
 
-namespace {
-thread_local std::string g_last_error;
-}
-
-void set_error(const std::string& msg) { g_last_error = msg; }
-const char* last_error_cstr() { return g_last_error.c_str(); }
-
 vrt_status cuda_fail(cudaError_t e, const char* what) {
     set_error(std::string(what) + ": " + cudaGetErrorString(e));
     if (e == cudaErrorMemoryAllocation) return VRT_ERR_OUT_OF_MEMORY;
