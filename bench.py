@@ -6,20 +6,24 @@ Default workload: the uneven batch - 128 seeded worlds (edge 64..512 voxels) wit
 launch fed by the device tile queue and replayed from a CUDA graph.  The same line
 reports the plain one-launch-per-view kernel on the same views (the comparison the
 metric names), the end-to-end host-buffer call, the HBM roofline of the persistent
-kernel and the CPU oracle timed on a bounded sample.
+kernel, the CPU oracle timed on a bounded sample, the large-world (primary + shadow)
+and incoherent (4 bounces + 2^26 random rays) workloads as sub-results, and the
+request server under Poisson arrivals with edits, replayed against the oracle.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--workload uneven_batch|large_world|incoherent|single_view]
 
-Multi-GPU (torchrun, one rank per GPU): every rank traverses its own batch of the
-same shape (weak scaling, no collective on the data path); the time is the max
-over ranks.
+Multi-GPU: with --gpus N > 1 and no torchrun environment, bench.py starts itself
+under torch.distributed.run with N ranks, one per GPU.  Every rank traverses its own
+batch of the same shape (weak scaling, no collective on the data path); the time is
+the max over ranks and the rays are the sum over ranks.
 """
 from __future__ import annotations
 
 import argparse
 import json
 import os
+import socket
 import subprocess
 import sys
 import time
@@ -34,6 +38,7 @@ sys.path.insert(0, str(ROOT))
 SLOT_BYTES = 512 + 512 + 64
 METRIC = "Grays/s batched vs per-view launch (bit-exact hits); p50/p99 request latency"
 HIT_BYTES = 16
+BYTES_FORMULA = "8*step_calls + 12*occ_fetches + 1*hits + 16*records"
 
 
 def parse(argv=None):
@@ -48,8 +53,11 @@ def parse(argv=None):
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-per-view", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the request-server run")
-    ap.add_argument("--no-stress", action="store_true", help="incoherent: skip the 2^26 stress rays")
-    ap.add_argument("--stress-rays", type=int, default=1 << 26, help="incoherent: number of stress rays")
+    ap.add_argument("--no-sub", action="store_true",
+                    help="uneven_batch: skip the large-world and incoherent sub-results")
+    ap.add_argument("--sub-steps", type=int, default=5, help="timed launches of each sub-result")
+    ap.add_argument("--no-stress", action="store_true", help="skip the 2^26 stress rays")
+    ap.add_argument("--stress-rays", type=int, default=1 << 26, help="number of stress rays")
     ap.add_argument("--glsl", action="store_true",
                     help="trace every view in the GLSL mode (the GPU renderer's rayCast) instead of the CPU traversal")
     ap.add_argument("--aniso", action="store_true", help="the GLSL mode with anisotropic LODs (implies --glsl)")
@@ -59,6 +67,10 @@ def parse(argv=None):
                     help="renders per arrival rate, at least (longer runs at low rates)")
     ap.add_argument("--serve-worlds", type=int, default=32)
     ap.add_argument("--serve-max-edge", type=int, default=1024)
+    ap.add_argument("--serve-check-worlds", type=int, default=8,
+                    help="worlds (the largest and smallest among them) whose renders are replayed on the oracle")
+    ap.add_argument("--serve-check-cap", type=int, default=160,
+                    help="replayed renders per arrival rate and mode, at most")
     ap.add_argument("--worlds", type=int, default=128, help="uneven_batch: number of worlds")
     ap.add_argument("--max-views", type=int, default=16, help="uneven_batch: views per world, at most")
     ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
@@ -66,16 +78,40 @@ def parse(argv=None):
     return ap.parse_args(argv)
 
 
-def dist_setup(args):
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+# ---------------------------------------------------------------------------------------
+# ranks
+
+def free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def relaunch_cmd(gpus: int, argv: list[str], port: int) -> list[str]:
+    """The torchrun command that runs this script as `gpus` ranks on this node."""
+    return [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={gpus}",
+            "--master-addr", "127.0.0.1", "--master-port", str(port), str(Path(__file__).resolve()), *argv]
+
+
+def rank_env():
+    """(world size, rank, local rank) of this process (1, 0, 0 without torchrun)."""
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def dist_setup(backend: str = "nccl"):
+    """Process group of a torchrun job (None for one process).  nccl binds the rank's GPU;
+    gloo (CPU) is what the multi-rank tests use."""
+    ws, rank, local = rank_env()
     pg = None
     if ws > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        else:
+            dist.init_process_group(backend)
         pg = dist
     return ws, rank, local, pg
 
@@ -85,15 +121,18 @@ def barrier(pg):
     shard.barrier(pg)
 
 
-def max_over_ranks(pg, x: float) -> float:
+def max_over_ranks(pg, x: float, device="cuda") -> float:
     from voxelrt_gb300 import shard
-    return shard.max_over_ranks(pg, x, "cuda")
+    return shard.max_over_ranks(pg, x, device)
 
 
-def sum_over_ranks(pg, x: float) -> float:
+def sum_over_ranks(pg, x: float, device="cuda") -> float:
     from voxelrt_gb300 import shard
-    return shard.sum_over_ranks(pg, x, "cuda")
+    return shard.sum_over_ranks(pg, x, device)
 
+
+# ---------------------------------------------------------------------------------------
+# workloads
 
 def build_workload(name: str, rank: int, args=None, world_size: int = 1):
     """The rank's workload: its own seeded batch (weak scaling) or its share, by world, of
@@ -228,6 +267,20 @@ def view_is_aniso(vw) -> bool:
     return bool(vw.flags & capi.VIEW_GLSL_ANISO)
 
 
+def oracle_view(o, vw):
+    """Every record of a view from the oracle, shaped (kinds, width*height)."""
+    glsl, aniso = view_is_glsl(vw), view_is_aniso(vw)
+    if vw.flags & 1 and vw.n_bounces:
+        return o.render_view_path(vw.cam, np.array(vw.sun_dir[:], np.float32), vw.n_bounces, vw.max_iters,
+                                  glsl=glsl, aniso=aniso)
+    if vw.flags & 1:
+        return np.stack(o.render_view_shadow(vw.cam, np.array(vw.sun_dir[:], np.float32), vw.max_iters,
+                                             glsl=glsl, aniso=aniso))
+    if vw.n_bounces:
+        return o.render_view_bounces(vw.cam, vw.n_bounces, vw.max_iters, glsl=glsl, aniso=aniso)
+    return o.render_view(vw.cam, vw.max_iters, glsl=glsl, aniso=aniso)[None]
+
+
 def cpu_oracle_sample(wl, seconds: float, threads: int = 0):
     """Time the CPU oracle on whole views of the workload until `seconds` of work."""
     from oracle.oracle import OracleWorld
@@ -244,7 +297,10 @@ def cpu_oracle_sample(wl, seconds: float, threads: int = 0):
         o = cache[vw.world]
         glsl, aniso = view_is_glsl(vw), view_is_aniso(vw)
         t0 = time.perf_counter()
-        if vw.flags & 1:
+        if vw.flags & 1 and vw.n_bounces:
+            o.render_view_path(vw.cam, np.array(vw.sun_dir[:], np.float32), vw.n_bounces, vw.max_iters, threads,
+                               glsl=glsl, aniso=aniso)
+        elif vw.flags & 1:
             o.render_view_shadow(vw.cam, np.array(vw.sun_dir[:], np.float32), vw.max_iters, threads, glsl=glsl,
                                  aniso=aniso)
         elif vw.n_bounces:
@@ -260,12 +316,14 @@ def cpu_oracle_sample(wl, seconds: float, threads: int = 0):
 
 
 def run_reference(args):
-    """Reference arm: the CPU restatement of the reference traversal on all host cores."""
-    ws, rank, _, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0, None
+    """Reference arm: the CPU restatement of the reference traversal on all host cores.
+    Loads the oracle and the host-only input generators, never the product library."""
+    ws, rank, _ = rank_env()
     if rank != 0:
         return
     from voxelrt_gb300 import build
-    build.build_all()
+    build.build_oracle()
+    build.build_synth()
     wl = build_workload(args.workload, 0, args)
     cores = host_cores()
     per_step = max(2.0, min(20.0, args.cpu_seconds))
@@ -294,152 +352,275 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def run_ours(args):
+# ---------------------------------------------------------------------------------------
+# our arm: an engine measures one rank; run_ours reduces over ranks and prints the line
+
+class GpuEngine:
+    """One rank's measurement on its GPU: the persistent batch (CUDA graph), the per-view
+    launches, the end-to-end host-buffer call, and on rank 0 the parity sample, the CPU
+    baseline, the sub-results and the serving run."""
+
+    def __init__(self, args, rank: int, world_size: int, local: int):
+        import torch
+
+        import voxelrt_gb300 as v
+        from voxelrt_gb300 import autotune
+        self.args, self.rank, self.dev = args, rank, local
+        self.torch, self.v = torch, v
+        torch.cuda.set_device(local)
+        self.wl = build_workload(args.workload, rank, args, world_size)
+        self.worlds = []
+        for d in self.wl.worlds:
+            w = v.World(d.sectors, brick_capacity=d.n_bricks + 64, device=local)
+            w.upload(d)
+            self.worlds.append(w)
+        self.cfg, self.cfg_src = autotune.lookup(self.wl.name)
+        self.batch = v.Batch(self.worlds, self.wl.views, self.cfg)
+        self.n_rec = self.batch.total_records
+        self.stream = torch.cuda.Stream()
+        self.hits = torch.empty(self.n_rec * HIT_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+        self.parity = parity_sample(self.wl, self.batch, self.hits, self.stream) if rank == 0 else None
+        # counting launch (untimed): algorithmic bytes of one launch
+        self.meas = self.batch.measure(self.hits, self.stream)
+        self.rays_per_step = self.meas["rays_cast"]
+        m = self.meas
+        self.alg_bytes = 8 * m["step_calls"] + 12 * m["occ_fetches"] + 1 * m["hits"] + HIT_BYTES * self.n_rec
+        self.h2d_bytes = 128 * len(self.wl.views)
+        self.d2h_bytes = self.n_rec * HIT_BYTES
+        self.ms = None
+
+    def time_batched(self, sync):
+        """ms per persistent launch (graph replay) over `steps`, and the clocks meanwhile."""
+        torch, s = self.torch, self.stream
+        with torch.cuda.stream(s):
+            for _ in range(max(3, self.args.warmup)):
+                self.batch.launch(self.hits, s, graph=True)
+        s.synchronize()
+        sync()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(self.dev) as clk:
+            torch.cuda.synchronize()
+            sync()
+            ev0.record(s)
+            for _ in range(self.args.steps):
+                self.batch.launch(self.hits, s, graph=True)
+            ev1.record(s)
+            ev1.synchronize()
+            torch.cuda.synchronize()
+        sync()
+        self.ms = ev0.elapsed_time(ev1) / self.args.steps
+        return self.ms, clk.summary()
+
+    def time_per_view(self):
+        """ms per pass of one plain launch per view over the same views."""
+        torch, s = self.torch, self.stream
+        with torch.cuda.stream(s):
+            for _ in range(2):
+                self.batch.launch_per_view(self.hits, s)
+        s.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        k = max(1, min(self.args.steps, 5))
+        e0.record(s)
+        for _ in range(k):
+            self.batch.launch_per_view(self.hits, s)
+        e1.record(s)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / k, k
+
+    def time_e2e(self, sync):
+        """Seconds per end-to-end call through the host-buffer API: new cameras in (H2D), all
+        records out to pinned host memory from vrt_host_alloc (the copies of finished parts
+        overlap the traversal of later ones)."""
+        v = self.v
+        host = v.PinnedHits(self.n_rec)
+        cams = [vw.cam for vw in self.wl.views]
+        self.batch.update_cameras(cams, self.stream)
+        self.batch.run(host.array, self.stream)
+        ke = max(1, min(self.args.steps, 5))
+        sync()
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            self.batch.update_cameras(cams, self.stream)
+            self.batch.run(host.array, self.stream)
+        sec = (time.perf_counter() - t0) / ke
+        host.close()
+        return sec
+
+    def d2h_link_gbs(self):
+        return d2h_link_gbs(self.torch, self.stream)
+
+    def config(self):
+        from voxelrt_gb300 import autotune
+        wl = self.wl
+        return {"workload": wl.name, "description": wl.description, "worlds": len(wl.worlds),
+                "views": len(wl.views), "rays_per_step": self.rays_per_step, "records_per_step": self.n_rec,
+                "world_bytes": int(sum(d.n_bricks for d in wl.worlds) * SLOT_BYTES),
+                "l2": "inputs larger than L2 (brick pools of all worlds)",
+                "batch_config": autotune.describe(self.cfg), "batch_config_source": self.cfg_src,
+                "launch": "persistent kernel + queue reset, CUDA graph replay",
+                "traversal": traversal_name(self.args)}
+
+    def extras(self):
+        """Rank 0's further results (parity, roofline inputs, CPU baseline, sub-results,
+        serving); frees the batch's device memory first where a later part needs it."""
+        args, v = self.args, self.v
+        out = {"parity_sample": self.parity,
+               "traversal": {"step_calls": self.meas["step_calls"], "occ_fetches": self.meas["occ_fetches"],
+                             "hits": self.meas["hits"],
+                             "mean_steps_per_ray": self.meas["step_calls"] / max(self.rays_per_step, 1)}}
+        peak, peak_src = peak_hbm()
+        achieved = self.alg_bytes / (self.ms * 1e-3) / 1e9
+        out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                           "traffic": traffic_from_profile(self.wl.name, args), "peak_source": peak_src,
+                           "algorithmic_bytes_per_launch": self.alg_bytes, "bytes_formula": BYTES_FORMULA}
+        cpu = None
+        if not args.no_cpu:
+            cores = host_cores()
+            r, t, nv = cpu_oracle_sample(self.wl, args.cpu_seconds, cores)
+            cpu = {"value": r / t / 1e9, "unit": "Grays/s", "cores": cores, "kind": "port",
+                   "sample": f"{nv} smallest views of the workload, {r} rays, CPU oracle (scalar restatement of "
+                             f"CpuRenderer.cpp RayCast) on all host threads"}
+        out["cpu_baseline"] = cpu
+        if args.workload == "incoherent" and not args.no_stress:
+            out["stress"] = run_stress(v, self.worlds[0], self.wl.worlds[0], args, self.stream, n=args.stress_rays)
+        self.close()
+        if args.workload == "uneven_batch" and not args.no_sub:
+            out["sub_results"] = run_sub_results(args, self.dev)
+        if args.workload == "uneven_batch" and not args.no_serving:
+            out["serving"] = run_serving(args, self.dev)
+        return out
+
+    def close(self):
+        if self.batch is not None:
+            self.batch.close()
+            self.batch = None
+            self.hits = None
+            for w in self.worlds:
+                w.close()
+            self.worlds = []
+            self.torch.cuda.synchronize()
+            self.torch.cuda.empty_cache()
+
+
+def run_ours(args, engine_cls=None, backend: str = "nccl", device: str = "cuda"):
+    """Measure on every rank with `engine_cls` (GpuEngine by default), reduce over ranks
+    (time: max, rays and bytes: sum) and print rank 0's JSON line."""
+    ws, rank, local, pg = dist_setup(backend)
+    eng = (engine_cls or GpuEngine)(args, rank, ws, local)
+    sync = lambda: barrier(pg)  # noqa: E731
+    ms_rank, clocks = eng.time_batched(sync)
+    ms = max_over_ranks(pg, ms_rank, device)
+    job_rays = sum_over_ranks(pg, eng.rays_per_step, device)
+    value = job_rays / (ms * 1e-3) / 1e9
+
+    per_view = None
+    if not args.no_per_view:
+        pms_rank, k = eng.time_per_view()
+        pms = max_over_ranks(pg, pms_rank, device)
+        per_view = {"value": job_rays / (pms * 1e-3) / 1e9, "unit": "Grays/s", "ms_per_step": pms,
+                    "launches_per_step": int(sum_over_ranks(pg, len(eng.wl.views), device)), "steps": k,
+                    "kernel": "view_path_kernel, 8x8 blocks, thread per pixel"}
+
+    e2e_s = max_over_ranks(pg, eng.time_e2e(sync), device)
+    d2h = sum_over_ranks(pg, eng.d2h_bytes, device)
+    e2e = {"value": job_rays / e2e_s / 1e9, "unit": "Grays/s", "ms_per_step": e2e_s * 1e3,
+           "h2d_bytes_per_step": int(sum_over_ranks(pg, eng.h2d_bytes, device)), "d2h_bytes_per_step": int(d2h),
+           "api": "vrt_batch_update_cameras + vrt_batch_run (pinned host records)"}
+    link = eng.d2h_link_gbs()
+    e2e["d2h_link_gbs"] = link
+    e2e["d2h_link_frac"] = eng.d2h_bytes / (e2e_s * 1e9) / link
+    barrier(pg)
+
+    if rank == 0:
+        extra = eng.extras()
+        line = {
+            "metric": METRIC, "value": value, "unit": "Grays/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": args.scaling,
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": eng.config(),
+            "roofline": extra.pop("roofline"), "cpu_baseline": extra.pop("cpu_baseline"), "e2e": e2e,
+            "gpu_launches": args.steps, "clocks": clocks, "per_view": per_view,
+            "batched_over_per_view": (value / per_view["value"]) if per_view else None,
+            "job_rays_per_step": job_rays,
+        }
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    else:
+        eng.close()
+    barrier(pg)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------------------
+# sub-results: the large world (config 1) and the incoherent workload (config 3)
+
+def measure_workload(v, wl, dev, steps, stream, check_views=2, stress=None):
+    """Persistent-launch throughput of one workload (CUDA graph replay, inputs resident),
+    its roofline and an oracle check of `check_views` whole views."""
     import torch
 
-    import voxelrt_gb300 as v
     from voxelrt_gb300 import autotune
-
-    ws, rank, local, pg = dist_setup(args)
-    torch.cuda.set_device(local)
-    dev = local
-    wl = build_workload(args.workload, rank, args, ws)
     worlds = []
     for d in wl.worlds:
         w = v.World(d.sectors, brick_capacity=d.n_bricks + 64, device=dev)
         w.upload(d)
         worlds.append(w)
-    cfg, cfg_src = autotune.lookup(wl.name)
+    cfg, src = autotune.lookup(wl.name)
     batch = v.Batch(worlds, wl.views, cfg)
     n_rec = batch.total_records
-    stream = torch.cuda.Stream()
     hits = torch.empty(n_rec * HIT_BYTES, dtype=torch.uint8, device=f"cuda:{dev}")
-
-    # parity sample: a few views of the batch vs the CPU oracle (bit-exact integer fields)
-    parity = None
-    if rank == 0:
-        parity = parity_sample(wl, batch, hits, stream)
-
-    # counting launch (untimed): algorithmic bytes of one launch
+    parity = parity_sample(wl, batch, hits, stream, max_views=check_views, pick="largest")
     meas = batch.measure(hits, stream)
-    rays_per_step = meas["rays_cast"]
-    alg_bytes = 8 * meas["step_calls"] + 12 * meas["occ_fetches"] + 1 * meas["hits"] + HIT_BYTES * n_rec
-
+    alg = 8 * meas["step_calls"] + 12 * meas["occ_fetches"] + meas["hits"] + HIT_BYTES * n_rec
     with torch.cuda.stream(stream):
-        for _ in range(max(3, args.warmup)):
+        for _ in range(3):
             batch.launch(hits, stream, graph=True)
-    stream.synchronize()
-    barrier(pg)
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(dev) as clk:
-        torch.cuda.synchronize()
-        barrier(pg)
-        ev0.record(stream)
-        for _ in range(args.steps):
-            batch.launch(hits, stream, graph=True)
-        ev1.record(stream)
-        ev1.synchronize()
-        torch.cuda.synchronize()
-    barrier(pg)
-    ms = ev0.elapsed_time(ev1) / args.steps
-    ms = max_over_ranks(pg, ms)
-    job_rays = sum_over_ranks(pg, rays_per_step)  # all ranks' rays per step
-    value = job_rays / (ms * 1e-3) / 1e9
-
-    # per-view baseline: one plain launch per view, same views and records
-    per_view = None
-    if not args.no_per_view:
-        with torch.cuda.stream(stream):
-            for _ in range(2):
-                batch.launch_per_view(hits, stream)
-        stream.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        k = max(1, min(args.steps, 5))
-        e0.record(stream)
-        for _ in range(k):
-            batch.launch_per_view(hits, stream)
-        e1.record(stream)
-        e1.synchronize()
-        pms = max_over_ranks(pg, e0.elapsed_time(e1) / k)
-        per_view = {"value": job_rays / (pms * 1e-3) / 1e9, "unit": "Grays/s", "ms_per_step": pms,
-                    "launches_per_step": len(wl.views), "steps": k,
-                    "kernel": "view_path_kernel, 8x8 blocks, thread per pixel"}
-
-    # end to end through the host-buffer API: new cameras in (H2D), all records out to
-    # pinned host memory from vrt_host_alloc (the copies of finished parts overlap the
-    # traversal of later ones)
-    host = v.PinnedHits(n_rec)
-    host_np = host.array
-    cams = [vw.cam for vw in wl.views]
-    batch.update_cameras(cams, stream)
-    batch.run(host_np, stream)
-    ke = max(1, min(args.steps, 5))
-    barrier(pg)
-    t0 = time.perf_counter()
-    for _ in range(ke):
-        batch.update_cameras(cams, stream)
-        batch.run(host_np, stream)
-    e2e_s = max_over_ranks(pg, (time.perf_counter() - t0) / ke)
-    e2e = {"value": job_rays / e2e_s / 1e9, "unit": "Grays/s", "ms_per_step": e2e_s * 1e3,
-           "h2d_bytes_per_step": 128 * len(wl.views), "d2h_bytes_per_step": n_rec * HIT_BYTES,
-           "api": "vrt_batch_update_cameras + vrt_batch_run (pinned host records)"}
-    link = d2h_link_gbs(torch, stream)
-    e2e["d2h_link_gbs"] = link
-    e2e["d2h_link_frac"] = n_rec * HIT_BYTES / e2e_s / 1e9 / link
-
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        batch.launch(hits, stream, graph=True)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
     peak, peak_src = peak_hbm()
-    achieved = alg_bytes / (ms * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic_from_profile(wl.name, args), "peak_source": peak_src,
-                "algorithmic_bytes_per_launch": alg_bytes,
-                "bytes_formula": "8*step_calls + 12*occ_fetches + 1*hits + 16*records"}
+    out = {"workload": wl.name, "description": wl.description, "value": meas["rays_cast"] / (ms * 1e-3) / 1e9,
+           "unit": "Grays/s", "ms_per_step": ms, "steps": steps, "rays_per_step": meas["rays_cast"],
+           "records_per_step": n_rec, "mean_steps_per_ray": meas["step_calls"] / max(meas["rays_cast"], 1),
+           "roofline": {"achieved": alg / (ms * 1e-3) / 1e9, "peak": peak, "frac": alg / (ms * 1e-3) / 1e9 / peak,
+                        "peak_source": peak_src, "algorithmic_bytes_per_launch": alg},
+           "batch_config": autotune.describe(cfg), "batch_config_source": src,
+           "world_bytes": int(sum(d.n_bricks for d in wl.worlds) * SLOT_BYTES), "parity_sample": parity}
+    del hits
+    batch.close()
+    if stress is not None:
+        out["stress"] = run_stress(v, worlds[0], wl.worlds[0], stress, stream, n=stress.stress_rays)
+    for w in worlds:
+        w.close()
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return out
 
-    cpu = None
-    if rank == 0 and not args.no_cpu:
-        cores = host_cores()
-        r, t, nv = cpu_oracle_sample(wl, args.cpu_seconds, cores)
-        cpu = {"value": r / t / 1e9, "unit": "Grays/s", "cores": cores, "kind": "port",
-               "sample": f"{nv} smallest views of the workload, {r} rays, CPU oracle (scalar restatement of "
-                         f"CpuRenderer.cpp RayCast) on all host threads"}
 
-    stress = None
-    if rank == 0 and args.workload == "incoherent" and not args.no_stress:
-        stress = run_stress(v, worlds[0], wl.worlds[0], args, stream, n=args.stress_rays)
+def run_sub_results(args, dev):
+    """Configs 1 and 3 at their full sizes, each with its own persistent launch."""
+    import torch
 
-    serving = None
-    if rank == 0 and not args.no_serving and args.workload == "uneven_batch":
-        del hits, host_np, host, batch
-        for w in worlds:
-            w.close()
-        worlds = []
-        torch.cuda.empty_cache()
-        serving = run_serving(args, dev)
+    import voxelrt_gb300 as v
+    from voxelrt_gb300 import workloads as W
+    stream = torch.cuda.Stream()
+    out = {}
+    for name, make in (("large_world", W.large_world), ("incoherent", W.incoherent)):
+        wl = make()
+        if args.glsl or args.aniso:
+            for vw in wl.views:
+                vw.flags |= v.VIEW_GLSL | (v.capi.VIEW_GLSL_ANISO if args.aniso else 0)
+        stress = args if (name == "incoherent" and not args.no_stress) else None
+        out[name] = measure_workload(v, wl, dev, args.sub_steps, stream, stress=stress)
+    return out
 
-    if rank == 0:
-        line = {
-            "metric": METRIC, "value": value, "unit": "Grays/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": args.scaling,
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": wl.name, "description": wl.description, "worlds": len(wl.worlds),
-                       "views": len(wl.views), "rays_per_step": rays_per_step, "records_per_step": n_rec,
-                       "world_bytes": int(sum(d.n_bricks for d in wl.worlds) * SLOT_BYTES),
-                       "l2": "inputs larger than L2 (brick pools of all worlds)",
-                       "batch_config": autotune.describe(cfg), "batch_config_source": cfg_src,
-                       "launch": "persistent kernel + queue reset, CUDA graph replay",
-                       "traversal": traversal_name(args)},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
-            "clocks": clk.summary(), "per_view": per_view,
-            "batched_over_per_view": (value / per_view["value"]) if per_view else None,
-            "parity_sample": parity,
-            "serving": serving,
-            "stress": stress,
-            "traversal": {"step_calls": meas["step_calls"], "occ_fetches": meas["occ_fetches"],
-                          "hits": meas["hits"], "mean_steps_per_ray": meas["step_calls"] / max(rays_per_step, 1)},
-        }
-        print(json.dumps(line), flush=True)
-    if pg is not None:
-        pg.destroy_process_group()
 
+# ---------------------------------------------------------------------------------------
+# serving
 
 def surface_points(w, edge, n, seed):
     """Random surface voxels: rays cast straight down from the top of random columns."""
@@ -465,6 +646,21 @@ def load_serving_worlds(v, datas, dev):
     return worlds, edges, surf
 
 
+def check_worlds(edges, n) -> list[int]:
+    """Worlds whose renders the oracle replays: the largest, the smallest, and the rest
+    drawn evenly from the others by edge."""
+    order = sorted(range(len(edges)), key=lambda i: (edges[i], i))
+    n = min(n, len(order))
+    if n >= len(order):
+        return order
+    picks = {order[-1], order[0]}
+    k = 1
+    while len(picks) < n:
+        picks.add(order[(k * (len(order) - 1)) // (n - 1)])
+        k += 1
+    return sorted(picks)
+
+
 def run_serving(args, dev):
     """Poisson render arrivals (+100 edits/s) against the request server, per arrival rate,
     in both scheduling modes, each on freshly uploaded worlds: the default, one resident
@@ -474,12 +670,14 @@ def run_serving(args, dev):
     from voxelrt_gb300 import workloads as W
     datas = W.serving_worlds(n_worlds=args.serve_worlds, max_edge=args.serve_max_edge)
     modes = {}
+    reserve = SampleReserve(v, args.serve_check_cap)
     for name, resident in (("launches", False), ("resident", True)):
         worlds, edges, surf = load_serving_worlds(v, datas, dev)
-        modes[name] = serve_sweep(args, v, datas, worlds, edges, surf, resident)
+        modes[name] = serve_sweep(args, v, datas, worlds, edges, surf, resident, reserve)
         if name != "resident":
             for w in worlds:
                 w.close()
+    reserve.close()
     edit_lat = edit_latency(v, worlds, edges, surf)
     for w in worlds:
         w.close()
@@ -509,7 +707,29 @@ def d2h_link_gbs(torch, stream, nbytes=1 << 30, reps=3):
     return reps * nbytes / (a.elapsed_time(b) * 1e-3) / 1e9
 
 
-def serve_sweep(args, v, datas, worlds, edges, surf, resident):
+class SampleReserve:
+    """Pinned record buffers (1080p each) that stand in for the rotation buffers of renders
+    kept for the oracle replay, so keeping a render's records costs the request loop no copy."""
+
+    def __init__(self, v, n, max_rec=1920 * 1080):
+        self.free = [v.PinnedHits(max_rec) for _ in range(n)]
+        self.all = list(self.free)
+
+    def take(self):
+        return self.free.pop() if self.free else None
+
+    def give(self, buf):
+        self.free.append(buf)
+
+    def close(self):
+        for b in self.all:
+            b.close()
+
+
+def serve_sweep(args, v, datas, worlds, edges, surf, resident, reserve):
+    """One scheduling mode over every arrival rate.  Every render of the checked worlds is
+    kept (up to --serve-check-cap per rate) and, after each rate, replayed on oracle copies
+    of those worlds that apply every edit of the log in submission order."""
     import collections
 
     from oracle.oracle import OracleWorld
@@ -518,25 +738,34 @@ def serve_sweep(args, v, datas, worlds, edges, surf, resident):
     max_rec = 1920 * 1080
     bufs = [v.PinnedHits(max_rec) for _ in range(24)]
     out = []
-    check_world = int(np.argmin(edges))
-    replay = {"renders": 0, "bit_exact": True}
+    checked = check_worlds(edges, args.serve_check_worlds)
+    oracles = {}
+    for wi in checked:
+        o = OracleWorld(datas[wi].sectors)
+        o.upload(datas[wi])
+        oracles[wi] = o
+    replay = {"renders": 0, "bit_exact": True, "worlds": checked, "world_edges": [edges[i] for i in checked],
+              "by_rate": [], "renders_1080p": 0, "records": 0}
     for ri, lam in enumerate(float(x) for x in args.serve_rates.split(",")):
         seconds = max(args.serve_seconds, args.serve_min_requests / lam)
         sched = W.serving_schedule(lam, seconds, len(worlds), edges, seed=100 + ri)
         srv.stats(reset=True)
         free = list(range(len(bufs)))
         inflight = collections.deque()
-        infos, log, samples = [], [], []
-        rng = np.random.default_rng(ri)
+        infos, log = [], []
+        kept = 0
+        # keep every `stride`-th render of the checked worlds, so the kept ones span the run
+        expect = sum(1 for e in sched if e[1] == "render" and e[2] in oracles)
+        stride = max(1, -(-expect // max(1, args.serve_check_cap)))
+        seen = 0
 
         def retire():
             t, b, res, sample = inflight.popleft()
             info = srv.wait(t, timeout_ms=60000)
             info["res"] = res
             infos.append(info)
-            if sample is not None:
-                sample["got"] = bufs[b].array[:sample["n"]].copy()
-            free.append(b)
+            if sample is None:
+                free.append(b)
 
         t0 = time.perf_counter()
         for (t, kind, wi, payload) in sched:
@@ -546,17 +775,26 @@ def serve_sweep(args, v, datas, worlds, edges, surf, resident):
                     break
                 time.sleep(min(t - now, 2e-4))
             if kind == "render":
-                while not free:
-                    retire()
-                b = free.pop()
                 n = v.view_records(payload)
                 sample = None
-                if ri == 0 and wi == check_world and len(samples) < 6:
-                    sample = {"view": payload, "n": n, "order": len(log)}
-                    samples.append(sample)
-                tk = srv.submit_render(payload, bufs[b].array[:n])
+                keep = wi in oracles and seen % stride == 0 and kept < args.serve_check_cap
+                seen += int(wi in oracles)
+                if keep:
+                    rb = reserve.take()
+                    if rb is not None:
+                        sample = {"view": payload, "n": n, "buf": rb}
+                        kept += 1
+                if sample is not None:
+                    target = sample["buf"].array[:n]
+                    b = None
+                else:
+                    while not free:
+                        retire()
+                    b = free.pop()
+                    target = bufs[b].array[:n]
+                tk = srv.submit_render(payload, target)
                 inflight.append((tk, b, (payload.cam.width, payload.cam.height), sample))
-                log.append(("render", wi, None))
+                log.append(("render", wi, sample))
             else:
                 radius, material, pick = payload
                 c = surf[wi][pick % len(surf[wi])]
@@ -578,26 +816,30 @@ def serve_sweep(args, v, datas, worlds, edges, surf, resident):
                     "p99_1080p_ms": float(np.percentile(hd, 99)) if len(hd) else None,
                     "mean_batch": float(np.mean([i["batch_size"] for i in infos])), "busy_s": st["busy_seconds"],
                     "wall_s": wall})
-        if ri == 0 and samples:
-            # replay the log of the checked world on the oracle: edits in submission order
-            o = OracleWorld(datas[check_world].sectors)
-            o.upload(datas[check_world])
-            si = 0
-            for k, (kind, wi, e) in enumerate(log):
-                while si < len(samples) and samples[si]["order"] == k:
-                    vw = samples[si]["view"]
-                    want = o.render_view(vw.cam, vw.max_iters)
-                    got = samples[si]["got"]
-                    ok = all(np.array_equal(got[f], want[f]) for f in ("voxel", "face", "material", "steps", "tag"))
-                    fin = np.isfinite(want["t"])
-                    ok &= bool(np.allclose(got["t"][fin], want["t"][fin], rtol=1e-6, atol=0))
-                    replay["bit_exact"] &= ok
-                    replay["renders"] += 1
-                    si += 1
-                if kind == "edit" and wi == check_world:
-                    o.edit(e)
-            o.close()
+        # replay the log of the checked worlds on the oracle: edits in submission order
+        n_ok, n_1080 = 0, 0
+        for kind, wi, item in log:
+            if wi not in oracles:
+                continue
+            o = oracles[wi]
+            if kind == "edit":
+                o.edit(item)
+            elif item is not None:
+                vw = item["view"]
+                want = o.render_view(vw.cam, vw.max_iters)
+                got = item["buf"].array[:item["n"]]
+                ok = hits_match(got, want)
+                replay["bit_exact"] &= ok
+                n_ok += int(ok)
+                n_1080 += int((vw.cam.width, vw.cam.height) == (1920, 1080))
+                replay["records"] += item["n"]
+                reserve.give(item["buf"])
+        replay["by_rate"].append({"rate_req_s": lam, "renders": kept, "bit_exact": n_ok == kept, "renders_1080p": n_1080})
+        replay["renders"] += kept
+        replay["renders_1080p"] += n_1080
     srv.close()
+    for o in oracles.values():
+        o.close()
     for b in bufs:
         b.close()
     return {"rates": out, "oracle_replay": replay, "launches": sum(r["launches"] for r in out)}
@@ -665,41 +907,60 @@ def run_stress(v, world, data, args, stream, n=1 << 26, steps=3):
             "bit_exact": ok}
 
 
-def parity_sample(wl, batch, hits, stream, max_views=3):
-    """Compare a few views of one batch launch with the CPU oracle."""
+def parity_sample(wl, batch, hits, stream, max_views=48, pick="spread"):
+    """Compare whole views of one batch launch with the CPU oracle: `max_views` views spread
+    evenly over the batch in its order (every world size, resolution and path kind of the
+    workload is drawn), or its largest views (pick="largest")."""
     import voxelrt_gb300 as v
     from oracle.oracle import OracleWorld
     batch.launch(hits, stream)
     stream.synchronize()
-    order = np.argsort([vw.cam.width * vw.cam.height for vw in wl.views], kind="stable")[:max_views]
-    rays, ok = 0, True
-    for i in order.tolist():
+    n = len(wl.views)
+    if pick == "largest":
+        sizes = [vw.cam.width * vw.cam.height for vw in wl.views]
+        order = sorted(np.argsort(sizes, kind="stable")[::-1][:max_views].tolist())
+    else:
+        order = sorted({(k * n) // max_views for k in range(min(max_views, n))})
+    rays, ok, bad = 0, True, []
+    cache = {}
+    for i in order:
         vw = wl.views[i]
-        o = OracleWorld(wl.worlds[vw.world].sectors)
-        o.upload(wl.worlds[vw.world])
-        glsl, aniso = view_is_glsl(vw), view_is_aniso(vw)
-        if vw.flags & 1:
-            want = np.stack(o.render_view_shadow(vw.cam, np.array(vw.sun_dir[:], np.float32), vw.max_iters,
-                                                 glsl=glsl, aniso=aniso))
-        elif vw.n_bounces:
-            want = o.render_view_bounces(vw.cam, vw.n_bounces, vw.max_iters, glsl=glsl, aniso=aniso)
-        else:
-            want = o.render_view(vw.cam, vw.max_iters, glsl=glsl, aniso=aniso)[None]
+        if vw.world not in cache:
+            for o in cache.values():
+                o.close()
+            cache = {vw.world: OracleWorld(wl.worlds[vw.world].sectors)}
+            cache[vw.world].upload(wl.worlds[vw.world])
+        want = oracle_view(cache[vw.world], vw)
         a, b = int(batch.offsets[i]), int(batch.offsets[i + 1])
         got = hits[a * HIT_BYTES:b * HIT_BYTES].cpu().numpy().view(v.HIT_DTYPE).reshape(want.shape)
-        ok &= hits_match(got, want)
+        match = hits_match(got, want)
+        ok &= match
+        if not match:
+            bad.append(i)
         rays += want.size
+    for o in cache.values():
         o.close()
-    return {"views": len(order), "records": rays, "bit_exact": ok}
+    return {"views": len(order), "of_views": n, "pick": pick, "records": rays, "bit_exact": ok,
+            "mismatched_views": bad[:8]}
 
 
-def main():
-    args = parse()
+def main(argv=None):
+    argv = sys.argv[1:] if argv is None else argv
+    args = parse(argv)
+    ws_env = os.environ.get("WORLD_SIZE")
+    if ws_env is None and args.gpus > 1:
+        # one process per GPU: run this script again under torchrun
+        return subprocess.call(relaunch_cmd(args.gpus, argv, free_port()))
+    ws = int(ws_env or 1)
+    if ws != args.gpus:
+        print(f"bench.py: WORLD_SIZE={ws} disagrees with --gpus {args.gpus}", file=sys.stderr)
+        return 2
     if args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
+    return 0
 
 
 if __name__ == "__main__":
-    main()
+    sys.exit(main())

@@ -195,9 +195,9 @@ typedef struct vrt_world_desc {
 
 typedef struct vrt_world_stats {
     uint32_t sectors_x, sectors_y, sectors_z;
-    uint32_t allocated_bricks;  /* FreeList::NumAllocated */
+    uint32_t allocated_bricks;  /* FreeList::NumAllocated: live bricks */
     uint32_t brick_capacity;    /* slots in the device pool */
-    uint32_t free_ranges;       /* FreeList::FreeRanges.size() */
+    uint32_t free_ranges;       /* FreeList::FreeRanges.size(): the gaps between live ranges and the tail */
     uint64_t device_bytes;      /* device memory held by the world */
 } vrt_world_stats;
 
@@ -227,9 +227,29 @@ vrt_status vrt_world_sync_sectors(vrt_world* world, uint32_t n, const int32_t* s
 /* Apply sphere edits in order (VoxelMap::RegionDispatchSIMD + brick GC,
  * VoxelMap.h:222-263): bricks are allocated for fills, voxels written on the device,
  * cell masks re-derived, and bricks that became empty are freed, so the allocation
- * mask stays the set of non-empty bricks.  Ordered on `stream` after earlier work
- * (edits land between frames); returns when done. */
+ * mask stays the set of non-empty bricks.
+ * The whole edit runs on the device, allocation included (BrickSlotAllocator.cpp:5-94
+ * allocates on the host): a sector that gains bricks takes a new slot range from a
+ * device bump allocator, one that loses bricks shrinks in place.  The call enqueues the
+ * work on `stream` after earlier work there and after the world's previous edit, and
+ * returns without waiting for the device; traversals on other streams must be ordered
+ * after it by the caller (edits land between frames), and vrt_world_wait waits for it
+ * on the host.  The host reads the device's allocator state only when its own bound of
+ * the bump pointer reaches the end of the pool; the call then compacts the pool first
+ * (as vrt_world_defrag, growing it when the live bricks fill 3/4 of it) and returns
+ * when that is done.  Host-side readers of the world (read_sector, save, stats) and
+ * vrt_world_sync_sectors wait for earlier edits themselves. */
 vrt_status vrt_world_edit(vrt_world* world, const vrt_edit* edits, uint32_t n, void* stream);
+
+/* Wait on the host until the world's last edit has run on the device. */
+vrt_status vrt_world_wait(vrt_world* world);
+
+/* Defragment the brick pool: every live brick is packed from slot 0 in sector order
+ * into a pool of `capacity` slots (0 = the current size; never fewer than the live
+ * bricks), reclaiming the slots edits left behind; the reference leaves this as a TODO
+ * (BrickSlotAllocator.cpp:14).  Content, masks and every traversal result are unchanged.
+ * Returns when done (the pool is copied once; the old one is freed). */
+vrt_status vrt_world_defrag(vrt_world* world, uint32_t capacity, void* stream);
 
 /* Read one sector back: its allocation mask and popcount(mask) x 512 bytes. */
 vrt_status vrt_world_read_sector(vrt_world* world, int32_t sector_idx, uint64_t* alloc_mask,
@@ -309,15 +329,22 @@ vrt_status vrt_pick(vrt_world* world, const vrt_pick_ray* rays, uint32_t n, uint
  *   - up to n_bounces diffuse bounces (CpuRenderer.cpp:342-393): origin
  *     hitPos + normal*0.01, direction normalize(normal + s), s uniform on the unit
  *     sphere by rejection from [-1,1]^3 with PCG32(initstate = pixel ^ bounce,
- *     initseq = 0x9E3779B97F4A7C15); a path ends at its first miss.
- * Records are laid out per view as [primary w*h][shadow w*h] or
- * [primary w*h][bounce 1 w*h]...[bounce n w*h]; rays never cast (shadow of a miss,
- * bounces after a miss) get a miss record with steps 0 and tag VRT_NO_RAY. */
+ *     initseq = 0x9E3779B97F4A7C15); a path ends at its first miss, or
+ *   - with both VRT_VIEW_SHADOW and n_bounces > 0, the GPU renderer's whole path
+ *     (VoxelRender.comp:51-86, u_MaxBounces = n_bounces): a sun ray toward sun_dir from
+ *     the primary hit, then the bounces as above (bounce k from the hit of bounce k-1,
+ *     not from a sun ray), the first two bounce hits each followed by a sun ray from
+ *     them; a sun ray's hit or miss does not end the path.
+ * Records are laid out per view as [primary w*h][shadow w*h], or
+ * [primary w*h][bounce 1 w*h]...[bounce n w*h], or for the whole path
+ * [primary][sun 0][bounce 1][sun 1][bounce 2][sun 2][bounce 3]...[bounce n]
+ * (2 + n + min(n, 2) planes of w*h); rays never cast (shadow of a miss, bounces after
+ * a miss) get a miss record with steps 0 and tag VRT_NO_RAY. */
 typedef struct vrt_view {
     vrt_camera cam;
     uint32_t world;     /* index into the batch's world list */
     uint32_t max_iters; /* 0 = VRT_DEFAULT_MAX_ITERS */
-    uint32_t n_bounces; /* 0..15, exclusive with VRT_VIEW_SHADOW */
+    uint32_t n_bounces; /* 0..15 */
     uint32_t flags;     /* VRT_VIEW_SHADOW, VRT_VIEW_GLSL, VRT_VIEW_GLSL_ANISO */
     float sun_dir[3];
 } vrt_view;
@@ -333,6 +360,28 @@ typedef struct vrt_view {
 uint64_t vrt_view_records(const vrt_view* view);
 vrt_status vrt_render_path(vrt_world* world, const vrt_view* view, vrt_hit* hits, void* stream);
 vrt_status vrt_render_path_device(vrt_world* world, const vrt_view* view, vrt_hit* hits, void* stream);
+
+/* ---- G-buffer of a view's primary hits (the consumer of the hits) ---- */
+/* The headless G-buffer the reference's renderers write from each pixel's primary hit
+ * (VoxelRender.comp:39-46,91-93, GBuffer.glsl:18-21; CpuRenderer.cpp:364-376), traced in
+ * the view's traversal mode (its shadow and bounce fields are ignored):
+ *   albedo_normal[p]  RGBA8: r, g, b = round-half-even(255 * c^2) of the hit material's
+ *                     RGB565 color palette[material] & 0xFFFF (c = field/31, /63, /31 as
+ *                     getMaterialColor computes them, each op rounded on its own), and
+ *                     a = (n.x+1) | (n.y+1)<<2 | (n.z+1)<<4 with n the hit normal
+ *                     (packGNormal; in the GLSL mode n may have several axes); on a miss
+ *                     0x00FFFFFF (white; the shader leaves the normal unset there);
+ *   depth[p]          projPos.z / projPos.w, projPos = proj * (hitPos / 16, 1) with proj
+ *                     column-major 4x4 and hitPos the hit position in the ray frame (relative
+ *                     to cam.world_origin), every op rounded on its own in the order
+ *                     ((m[r]*x + m[4+r]*y) + m[8+r]*z) + m[12+r]; -1 on a miss.
+ * palette: 256 Material words (the reference's Palette encodings); proj: 16 floats. */
+vrt_status vrt_render_gbuffer(vrt_world* world, const vrt_view* view, const uint32_t* palette, const float* proj,
+                              uint32_t* albedo_normal, float* depth, void* stream);
+/* Device buffers, asynchronous; hits (may be NULL) also receives the primary records. */
+vrt_status vrt_render_gbuffer_device(vrt_world* world, const vrt_view* view, const uint32_t* palette,
+                                     const float* proj, uint32_t* albedo_normal, float* depth, vrt_hit* hits,
+                                     void* stream);
 
 /* ---- batched persistent traversal over many worlds and views ---- */
 typedef struct vrt_batch_config {

@@ -62,6 +62,9 @@ def lib() -> C.CDLL:
                                              C.POINTER(Stats)]
         L.ora_render_view_bounces.argtypes = [_vp, _vp, C.c_uint32, C.c_uint32, C.c_uint32, _vp, C.c_int,
                                               C.POINTER(Stats)]
+        L.ora_render_view_path.argtypes = [_vp, _vp, _vp, C.c_uint32, C.c_uint32, C.c_uint32, _vp, C.c_int,
+                                           C.POINTER(Stats)]
+        L.ora_render_gbuffer.argtypes = [_vp, _vp, C.c_uint32, C.c_uint32, _vp, _vp, _vp, _vp, _vp, C.c_int]
         L.ora_world_edit.argtypes = [_vp, _vp, C.c_uint32]
         L.ora_pick.argtypes = [_vp, _vp, C.c_uint64, C.c_uint32, _vp]
         _lib = L
@@ -181,6 +184,29 @@ class OracleWorld:
                                            hits.ctypes.data, int(threads), C.byref(s)))
         self.last_stats = _stats(s)
         return hits.reshape(n_bounces + 1, n)
+
+    def render_view_path(self, cam, sun_dir, n_bounces, max_iters=0, threads=0, glsl=False, aniso=False) -> np.ndarray:
+        """The GPU renderer's per-pixel path (primary, sun, bounces with a sun ray after the
+        first two): (2 + n + min(n, 2), width*height) records."""
+        n = cam.width * cam.height
+        kinds = 2 + n_bounces + min(n_bounces, 2)
+        hits = np.zeros(kinds * n, HIT_DTYPE)
+        sd = np.ascontiguousarray(sun_dir, dtype=np.float32)
+        s = Stats()
+        _chk(lib().ora_render_view_path(self._h, C.addressof(cam), sd.ctypes.data, int(n_bounces), int(max_iters),
+                                        _mode(glsl, aniso), hits.ctypes.data, int(threads), C.byref(s)))
+        self.last_stats = _stats(s)
+        return hits.reshape(kinds, n)
+
+    def render_gbuffer(self, cam, palette, proj, max_iters=0, threads=0, glsl=False, aniso=False):
+        """(albedo_normal u32, depth f32, primary records) of a view's primary hits."""
+        n = cam.width * cam.height
+        pal = np.ascontiguousarray(palette, dtype=np.uint32)
+        pm = np.ascontiguousarray(proj, dtype=np.float32).reshape(16)
+        tex, dep, hits = np.zeros(n, np.uint32), np.zeros(n, np.float32), np.zeros(n, HIT_DTYPE)
+        _chk(lib().ora_render_gbuffer(self._h, C.addressof(cam), int(max_iters), _mode(glsl, aniso), pal.ctypes.data,
+                                      pm.ctypes.data, tex.ctypes.data, dep.ctypes.data, hits.ctypes.data, int(threads)))
+        return tex, dep, hits
 
     def pick(self, rays: np.ndarray, max_iters: int = 0) -> np.ndarray:
         """rays: (n, 6) float64 (origin, dir) -> PICK_DTYPE records."""

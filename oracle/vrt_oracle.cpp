@@ -841,6 +841,106 @@ int ora_render_view_bounces(const ora_world* w, const vrt_camera* cam, uint32_t 
     return 0;
 }
 
+// The GPU renderer's whole per-pixel path (VoxelRender.comp:51-86) with u_MaxBounces =
+// n_bounces > 0: the primary ray; a sun ray from its hit (:54-61); then bounce i = 1..n
+// from the last hit (:63-74), stopping at the first miss (:76-79), each of the first two
+// bounce hits followed by a sun ray from it (:81).  Every sun and bounce ray starts at
+// hitPos + normal*0.01; the bounce direction is bounce_dir (the contract of
+// vrt_view).  Records: [primary][sun 0][bounce 1][sun 1][bounce 2][sun 2][bounce 3]...
+// [bounce n], planes of width*height; rays never cast are VRT_NO_RAY records.
+int ora_render_view_path(const ora_world* w, const vrt_camera* cam, const float sun_dir[3], uint32_t n_bounces,
+                         uint32_t max_iters, uint32_t mode, vrt_hit* hits, int threads, ora_stats* stats) {
+    if (!w || !cam || !sun_dir || !hits || n_bounces == 0 || n_bounces > VRT_MAX_BOUNCES) return -1;
+    const bool glsl = (mode & kModeGlsl) != 0;
+    const uint32_t iters = eff_iters_mode(max_iters, glsl);
+    const uint64_t n = (uint64_t)cam->width * cam->height;
+    const uint32_t kinds = 2 + n_bounces + std::min<uint32_t>(n_bounces, 2);
+    StatAcc acc(threads);
+    parallel_for(n, (int)acc.per.size(), [&](int tid, uint64_t b, uint64_t e) {
+        Trace tr, ts;
+        float o[3], d[3], nrm[3], so[3];
+        for (uint64_t i = b; i < e; i++) {
+            uint32_t k = 0;  // next record plane
+            auto put = [&](const Trace& t, const float* dir) {
+                fill_hit(t, dir, (uint32_t)i, hits[(uint64_t)k++ * n + i]);
+                acc.add(tid, t);
+            };
+            camera_ray(*cam, (uint32_t)(i % cam->width), (uint32_t)(i / cam->width), o, d);
+            trace_mode(*w, mode, o, d, cam->world_origin, iters, tr);
+            put(tr, d);
+            for (uint32_t bnc = 0; tr.hit && bnc <= n_bounces; bnc++) {
+                // from the last hit: its sun ray (after the primary and the first two
+                // bounces), then the next bounce
+                hit_normal(tr, d, nrm);
+                offset_origin(tr, nrm, so);
+                if (bnc <= 2) {
+                    trace_mode(*w, mode, so, sun_dir, cam->world_origin, iters, ts, true);
+                    put(ts, sun_dir);
+                }
+                if (bnc == n_bounces) break;
+                for (int c = 0; c < 3; c++) o[c] = so[c];
+                bounce_dir((uint32_t)i, bnc + 1, nrm, d);
+                trace_mode(*w, mode, o, d, cam->world_origin, iters, tr, true);
+                put(tr, d);
+            }
+            for (; k < kinds; k++) fill_no_ray(hits[(uint64_t)k * n + i]);
+        }
+    });
+    acc.store(stats);
+    return 0;
+}
+
+// G-buffer of the primary hits (VoxelRender.comp:39-46,91-93; CpuRenderer.cpp:364-376):
+//   albedo_normal  RGBA8: rgb = round-half-even(255 * c*c) per channel of the material's
+//                  RGB565 color (c = field / 31, / 63, / 31; getMaterialColor, its square
+//                  the "srgb gamma hack"), a = the packed normal (n.x+1) | (n.y+1)<<2 |
+//                  (n.z+1)<<4 (packGNormal; CpuRenderer's bits 24-29); on a miss
+//                  0x00FFFFFF (white, normal bits 0);
+//   depth          projPos.z / projPos.w with projPos = proj * (hitPos / 16, 1), proj
+//                  column-major, every op rounded on its own in the order
+//                  ((m[r]*x + m[4+r]*y) + m[8+r]*z) + m[12+r]; -1 on a miss.
+static void gbuffer_texel(const Trace& tr, const float d[3], const uint32_t* palette, const float* proj, uint32_t& texel,
+                   float& depth) {
+    if (!tr.hit) {
+        texel = 0x00FFFFFFu;
+        depth = -1.0f;
+        return;
+    }
+    const uint32_t m = palette[tr.material];
+    const float c[3] = {(float)((m >> 11) & 31u) * (1.0f / 31), (float)((m >> 5) & 63u) * (1.0f / 63),
+                        (float)(m & 31u) * (1.0f / 31)};
+    texel = 0;
+    for (int k = 0; k < 3; k++) texel |= (uint32_t)std::nearbyint(c[k] * c[k] * 255.0f) << (8 * k);
+    float nrm[3];
+    hit_normal(tr, d, nrm);
+    const uint32_t a = (uint32_t)(nrm[0] + 1.0f) | (uint32_t)(nrm[1] + 1.0f) << 2 | (uint32_t)(nrm[2] + 1.0f) << 4;
+    texel |= a << 24;
+    const float p[3] = {tr.cur[0] * 0.0625f, tr.cur[1] * 0.0625f, tr.cur[2] * 0.0625f};
+    const float z = ((proj[2] * p[0] + proj[6] * p[1]) + proj[10] * p[2]) + proj[14];
+    const float wv = ((proj[3] * p[0] + proj[7] * p[1]) + proj[11] * p[2]) + proj[15];
+    depth = z / wv;
+}
+
+int ora_render_gbuffer(const ora_world* w, const vrt_camera* cam, uint32_t max_iters, uint32_t mode,
+                       const uint32_t* palette, const float* proj, uint32_t* albedo_normal, float* depth, vrt_hit* hits,
+                       int threads) {
+    if (!w || !cam || !palette || !proj || !albedo_normal || !depth) return -1;
+    const uint32_t iters = eff_iters_mode(max_iters, (mode & kModeGlsl) != 0);
+    const uint64_t n = (uint64_t)cam->width * cam->height;
+    StatAcc acc(threads);
+    parallel_for(n, (int)acc.per.size(), [&](int, uint64_t b, uint64_t e) {
+        Trace tr;
+        float o[3], d[3];
+        for (uint64_t i = b; i < e; i++) {
+            camera_ray(*cam, (uint32_t)(i % cam->width), (uint32_t)(i / cam->width), o, d);
+            trace_mode(*w, mode, o, d, cam->world_origin, iters, tr);
+            gbuffer_texel(tr, d, palette, proj, albedo_normal[i], depth[i]);
+            if (hits) fill_hit(tr, d, (uint32_t)i, hits[i]);
+        }
+    });
+    return 0;
+}
+
 // VoxelMap::RayCast (VoxelMap.cpp:140-170) with GetStepLevel (:125-139) over the
 // oracle's sectors; glm::min(x, y) = y < x ? y : x, glm::step(0, d) = d < 0 ? 0 : 1,
 // double -> int as x86 cvttsd2si (INT32_MIN out of range).

@@ -76,6 +76,18 @@ int ora_render_view_shadow(const ora_world* w, const vrt_camera* cam, const floa
 int ora_render_view_bounces(const ora_world* w, const vrt_camera* cam, uint32_t n_bounces,
                             uint32_t max_iters, uint32_t mode, vrt_hit* hits, int threads, ora_stats* stats);
 
+/* The GPU renderer's per-pixel path with u_MaxBounces = n_bounces (1..15), VoxelRender.comp:51-86:
+ * primary; sun ray from its hit; bounces 1..n (stop at the first miss), the first two each
+ * followed by a sun ray.  Planes [primary][sun 0][bounce 1][sun 1][bounce 2][sun 2][bounce 3]..
+ * [bounce n] (2 + n + min(n, 2) of them), VRT_NO_RAY where no ray was cast. */
+int ora_render_view_path(const ora_world* w, const vrt_camera* cam, const float sun_dir[3], uint32_t n_bounces,
+                         uint32_t max_iters, uint32_t mode, vrt_hit* hits, int threads, ora_stats* stats);
+/* G-buffer of the primary hits (VoxelRender.comp:39-46,91-93): RGBA8 albedo + packed normal
+ * and projected depth per pixel (vrt_render_gbuffer_device's contract); hits may be NULL. */
+int ora_render_gbuffer(const ora_world* w, const vrt_camera* cam, uint32_t max_iters, uint32_t mode,
+                       const uint32_t* palette, const float* proj, uint32_t* albedo_normal, float* depth, vrt_hit* hits,
+                       int threads);
+
 /* Picking ray cast (VoxelMap::RayCast, VoxelMap.cpp:125-170), double precision.
  * rays: 6 doubles each (origin, dir).  max_iters 0 = 1024. */
 int ora_pick(const ora_world* w, const double* rays, uint64_t n, uint32_t max_iters, vrt_pick_hit* hits);

@@ -86,6 +86,9 @@ def oracle_view(o: OracleWorld, view) -> np.ndarray:
     """All records of a vrt_view from the oracle, shaped (kinds, width*height)."""
     glsl = bool(view.flags & v.VIEW_GLSL)
     aniso = bool(view.flags & v.capi.VIEW_GLSL_ANISO)
+    if view.flags & v.VIEW_SHADOW and view.n_bounces:
+        return o.render_view_path(view.cam, np.array(view.sun_dir[:], np.float32), view.n_bounces, view.max_iters,
+                                  glsl=glsl, aniso=aniso)
     if view.flags & v.VIEW_SHADOW:
         p, s = o.render_view_shadow(view.cam, np.array(view.sun_dir[:], np.float32), view.max_iters, glsl=glsl,
                                     aniso=aniso)

@@ -140,9 +140,9 @@ def test_batch_rejects_bad_input(mix):
         v.Batch(worlds, [bad])
     with pytest.raises(v.VrtError):
         v.Batch(worlds, views, v.BatchConfig(tile_w=4, tile_h=4))
-    both = v.make_view(cfg0_camera(8, 8), n_bounces=1, shadow_dir=SUN)
+    too_many = v.make_view(cfg0_camera(8, 8), n_bounces=16, shadow_dir=SUN)
     with pytest.raises(v.VrtError):
-        v.Batch(worlds, [both])
+        v.Batch(worlds, [too_many])
     # camera updates keep each view's resolution and a world origin within +-2^30
     b = v.Batch(worlds, views)
     cams = [v.Camera.from_buffer_copy(vw.cam) for vw in views]

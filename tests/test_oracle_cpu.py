@@ -343,3 +343,61 @@ def test_anisotropic_lods_find_the_same_voxels_in_fewer_steps():
     assert np.array_equal(iso["voxel"], ani["voxel"]) and np.array_equal(iso["material"], ani["material"])
     assert (ani["steps"] <= iso["steps"]).all()
     assert ani["steps"].astype(np.int64).sum() < 0.9 * iso["steps"].astype(np.int64).sum()
+
+
+@pytest.mark.parametrize("glsl", [False, True])
+def test_renderer_path_decomposes_into_shadow_and_bounce_paths(glsl):
+    """The GPU renderer's whole path (VoxelRender.comp:51-86) interleaves sun rays with the
+    bounce chain without changing it: its primary and bounce planes equal the bounce-only
+    path, its first sun plane the shadow path, and a sun ray is cast exactly after the
+    primary and the first two bounce hits."""
+    data = cfg0_world()
+    o = OracleWorld(data.sectors)
+    o.upload(data)
+    cam = cfg0_camera(96, 54)
+    sun = np.array([0.3, 0.9, -0.28], np.float32) / np.float32(np.linalg.norm([0.3, 0.9, -0.28]))
+    n = 4
+    full = o.render_view_path(cam, sun, n, glsl=glsl)
+    assert full.shape == (2 + n + 2, 96 * 54)
+    bounces = o.render_view_bounces(cam, n, glsl=glsl)
+    prim, shad = o.render_view_shadow(cam, sun, glsl=glsl)
+    planes_of_bounce = [0, 2, 4, 6, 7]  # primary, bounce 1..4
+    for k, p in enumerate(planes_of_bounce):
+        assert np.array_equal(full[p], bounces[k])
+    assert np.array_equal(full[0], prim) and np.array_equal(full[1], shad)
+    for sun_plane, after in ((1, 0), (3, 2), (5, 4)):
+        cast = full[sun_plane]["tag"] != 0xFFFFFFFF
+        assert np.array_equal(cast, full[after]["voxel"] != 0xFFFFFFFF)
+    o.close()
+
+
+def test_gbuffer_texels_follow_the_material_and_normal():
+    """G-buffer of the oracle on a world of one material: every hit texel carries the squared
+    RGB565 color rounded to 8 bits and a single-axis normal opposite the ray's direction."""
+    vol = np.zeros((64, 64, 64), np.uint8)
+    vol[:20] = 5
+    data = dense_to_stream(vol)
+    o = OracleWorld(data.sectors)
+    o.upload(data)
+    cam = v.look_at((32.0, 50.0, 32.0), (32.0, 0.0, 33.0), 60.0, 32, 32)
+    pal = np.zeros(256, np.uint32)
+    pal[5] = (20 << 11) | (40 << 5) | 10
+    proj = np.eye(4, dtype=np.float32).reshape(16)
+    tex, depth, hits = o.render_gbuffer(cam, pal, proj)
+    hit = hits["voxel"] != 0xFFFFFFFF
+    assert hit.all()
+    rgb = [round((20 / 31) ** 2 * 255), round((40 / 63) ** 2 * 255), round((10 / 31) ** 2 * 255)]
+    assert np.all(tex & 0xFFFFFF == rgb[0] | rgb[1] << 8 | rgb[2] << 16)
+    # the CPU traversal's normal has the one axis of the record's face, opposite the ray:
+    # field 2 where dir < 0 (face odd), 0 where dir >= 0, the other fields 1
+    axis, neg = hits["face"] >> 1, hits["face"] & 1
+    want_a = np.zeros(len(hits), np.uint32)
+    for c in range(3):
+        want_a |= np.where(axis == c, np.where(neg == 1, 2, 0), 1).astype(np.uint32) << (2 * c)
+    assert np.array_equal(tex >> 24, want_a)
+    assert np.any(axis == 1)
+    # identity projection: depth = z of hitPos / 16, hitPos in the ray frame (relative to the
+    # camera's world origin), within the hit voxel's z extent
+    zrel = (hits["voxel"] >> 21).astype(np.float64) - cam.world_origin[2]
+    assert np.all((depth >= (zrel - 1e-3) / 16) & (depth <= (zrel + 1 + 1e-3) / 16))
+    o.close()

@@ -32,20 +32,18 @@ def make_worlds(n=4, seed=0):
 def random_view(rng, world, edge, res=None):
     w, h = res or [(64, 64), (96, 54), (160, 90), (33, 17)][int(rng.integers(0, 4))]
     cam = v.look_at(rng.uniform(0, edge, 3), rng.uniform(0, edge, 3) + 0.5, float(rng.uniform(50, 90)), w, h)
-    kind = int(rng.integers(0, 3))
+    kind = int(rng.integers(0, 4))
     if kind == 1:
         return v.make_view(cam, world=world, shadow_dir=(0.3, 0.8, 0.5))
     if kind == 2:
         return v.make_view(cam, world=world, n_bounces=2)
+    if kind == 3:  # the GPU renderer's whole path: sun rays among the bounces
+        return v.make_view(cam, world=world, n_bounces=3, shadow_dir=(0.3, 0.8, 0.5))
     return v.make_view(cam, world=world)
 
 
 def oracle_records(o: OracleWorld, view) -> np.ndarray:
-    if view.flags & v.VIEW_SHADOW:
-        return np.concatenate(o.render_view_shadow(view.cam, np.array(view.sun_dir[:], np.float32)))
-    if view.n_bounces:
-        return o.render_view_bounces(view.cam, view.n_bounces).reshape(-1)
-    return o.render_view(view.cam)
+    return oracle_view(o, view).reshape(-1)
 
 
 @pytest.fixture(scope="module")
@@ -217,3 +215,52 @@ def test_default_mode_and_mode_flags(setup):
     wh = (C.c_void_p * len(worlds))(*[w.handle.value for w in worlds])
     h = C.c_void_p()
     assert capi.lib().vrt_server_create(wh, len(worlds), C.byref(cfg), C.byref(h)) == capi.VRT_ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("resident", MODES)
+def test_concurrent_1080p_renders_with_edits(gpu, resident):
+    """Four 1080p renders in flight at once with sphere edits submitted between them: every
+    render equals the oracle replaying the submission log (edits in order)."""
+    rng = np.random.default_rng(21)
+    datas = [v.synth_mix(edge, seed=800 + i) for i, edge in enumerate((128, 192))]
+    worlds, oracles = [], []
+    for d in datas:
+        w = v.World(d.sectors, brick_capacity=d.n_bricks + 4096)
+        w.upload(d)
+        worlds.append(w)
+        o = OracleWorld(d.sectors)
+        o.upload(d)
+        oracles.append(o)
+    srv = v.Server(worlds, max_inflight=3, resident=resident)
+    log, outs, tickets = [], [], []
+    for k in range(10):
+        wi = k % 2
+        edge = datas[wi].sectors[0] * 32
+        if k in (2, 5, 7):
+            e = np.zeros(2, v.EDIT_DTYPE)
+            e["center"] = rng.integers(edge // 4, 3 * edge // 4, (2, 3))
+            e["radius"] = rng.integers(4, 20, 2)
+            e["material"] = [0, int(rng.integers(1, 256))]
+            tickets.append(srv.submit_edit(wi, e))
+            log.append(("edit", wi, e))
+            continue
+        cam = v.look_at(rng.uniform(0, edge, 3), rng.uniform(0, edge, 3) + 0.5, 80.0, 1920, 1080)
+        vw = v.make_view(cam, world=wi) if k % 3 else v.make_view(cam, world=wi, shadow_dir=(0.3, 0.8, 0.5))
+        out = v.PinnedHits(v.view_records(vw))
+        outs.append(out)
+        tickets.append(srv.submit_render(vw, out.array))
+        log.append(("render", wi, (vw, out)))
+    infos = [srv.wait(t, timeout_ms=120000) for t in tickets]
+    assert all(i["state"] == v.capi.REQ_DONE for i in infos)
+    renders = 0
+    for kind, wi, item in log:
+        if kind == "edit":
+            oracles[wi].edit(item)
+        else:
+            vw, out = item
+            assert_hits_equal(out.array, oracle_records(oracles[wi], vw))
+            renders += 1
+    assert renders == 7
+    srv.close()
+    for w in worlds:
+        w.close()

@@ -89,3 +89,89 @@ def test_two_gloo_ranks(tmp_path):
         assert r["total"] == r["all_rays"]            # the job's rays: each view on exactly one rank
         assert sorted(r["own"][0] + r["own"][1]) == list(range(6))
         assert not set(r["own"][0]) & set(r["own"][1])
+
+
+class StubEngine:
+    """CPU stand-in for bench.GpuEngine: the rank's own seeded workload (bench's weak-scaling
+    layout), its primary rays as the rays of a step, and fixed per-rank times (the slower
+    rank 1 sets the job's time)."""
+
+    def __init__(self, args, rank, world_size, local):
+        import bench
+        self.args, self.rank = args, rank
+        self.wl = bench.build_workload("uneven_batch", rank, args, world_size)
+        self.rays_per_step = self.wl.primary_rays
+        self.h2d_bytes = 128 * len(self.wl.views)
+        self.d2h_bytes = 16 * self.rays_per_step
+
+    def time_batched(self, sync):
+        sync()
+        return 2.0 + self.rank, {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+
+    def time_per_view(self):
+        return 5.0 + self.rank, 1
+
+    def time_e2e(self, sync):
+        sync()
+        return 0.010 * (1 + self.rank)
+
+    def d2h_link_gbs(self):
+        return 100.0
+
+    def config(self):
+        return {"workload": self.wl.name, "rays_per_step": self.rays_per_step}
+
+    def extras(self):
+        return {"roofline": None, "cpu_baseline": None, "rank_rays": self.rays_per_step}
+
+    def close(self):
+        pass
+
+
+def _bench_rank(rank, world_size, port, out_dir):
+    import contextlib
+    import io
+    import os
+    os.environ.update(WORLD_SIZE=str(world_size), RANK=str(rank), LOCAL_RANK=str(rank),
+                      MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    import bench
+    args = bench.parse(["--gpus", str(world_size), "--worlds", "3", "--max-views", "2"])
+    buf = io.StringIO()
+    with contextlib.redirect_stdout(buf):
+        bench.run_ours(args, engine_cls=StubEngine, backend="gloo", device="cpu")
+    rays = StubEngine(args, rank, world_size, rank).rays_per_step
+    with open(f"{out_dir}/bench{rank}.json", "w") as f:
+        json.dump({"stdout": buf.getvalue(), "rays": rays}, f)
+
+
+def test_bench_two_gloo_ranks(tmp_path):
+    """bench.run_ours over two gloo ranks: one JSON line from rank 0 with n_gpus 2, the job's
+    rays the sum of both ranks' rays and its time the slower rank's."""
+    mp = pytest.importorskip("torch.multiprocessing")
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    mp.start_processes(_bench_rank, args=(2, port, str(tmp_path)), nprocs=2, join=True, start_method="spawn")
+    res = [json.loads((tmp_path / f"bench{r}.json").read_text()) for r in range(2)]
+    assert res[1]["stdout"] == ""
+    lines = [ln for ln in res[0]["stdout"].splitlines() if ln.strip()]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    job = res[0]["rays"] + res[1]["rays"]
+    assert res[0]["rays"] != res[1]["rays"]  # each rank traced its own seeded batch
+    assert line["n_gpus"] == 2 and line["scaling"] == "weak"
+    assert line["job_rays_per_step"] == job
+    assert line["ms_per_step"] == 3.0
+    assert abs(line["value"] - job / 3.0e-3 / 1e9) < 1e-12
+    assert abs(line["per_view"]["value"] - job / 6.0e-3 / 1e9) < 1e-12
+    assert abs(line["e2e"]["value"] - job / 0.020 / 1e9) < 1e-12
+    assert line["e2e"]["d2h_bytes_per_step"] == 16 * job
+
+
+def test_bench_rank_count_checks(monkeypatch):
+    import bench
+    cmd = bench.relaunch_cmd(4, ["--gpus", "4", "--steps", "5"], 29512)
+    assert cmd[1:3] == ["-m", "torch.distributed.run"] and "--nproc-per-node=4" in cmd
+    assert cmd[cmd.index("--master-addr") + 1] == "127.0.0.1" and cmd[-4:] == ["--gpus", "4", "--steps", "5"]
+    monkeypatch.setenv("WORLD_SIZE", "2")
+    assert bench.main(["--gpus", "4"]) == 2  # a torchrun job whose size disagrees is refused

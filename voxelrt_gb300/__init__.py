@@ -21,7 +21,7 @@ from .capi import (CAST_GLSL, EDIT_DTYPE, HIT_DTYPE, MISS_FACE, MISS_VOXEL, NO_R
                    BatchConfig, Camera,
                    CastParams, View, VrtError, check, check_synth, lib, ptr, synth_lib)
 
-__all__ = ["Server", "PinnedHits", "view_records", "render_path", "cvox_read", "cvox_write", "World", "Camera", "View",
+__all__ = ["Server", "PinnedHits", "view_records", "render_path", "render_gbuffer", "cvox_read", "cvox_write", "World", "Camera", "View",
            "make_view", "Batch", "BatchConfig", "VIEW_SHADOW", "VIEW_GLSL", "CAST_GLSL", "look_at", "synth_terrain", "synth_mix", "random_rays", "SectorData", "VrtError",
            "RAY_DTYPE", "HIT_DTYPE", "EDIT_DTYPE", "MISS_VOXEL", "MISS_FACE", "NO_RAY", "unpack_voxel", "sector_index",
            "lib"]
@@ -210,10 +210,17 @@ class World:
         check(lib().vrt_pick(self._h, ptr(r), len(r), int(max_iters), ptr(out), _stream_ptr(stream)))
         return out
 
-    def edit(self, edits, stream=None) -> None:
-        """Apply vrt_edit records (EDIT_DTYPE array) in order."""
+    def edit(self, edits, stream=None, wait: bool = True) -> None:
+        """Apply vrt_edit records (EDIT_DTYPE array) in order, on the device; with `wait`
+        (the default) return once the device has applied them (vrt_world_wait)."""
         e = np.ascontiguousarray(edits, dtype=EDIT_DTYPE)
         check(lib().vrt_world_edit(self._h, ptr(e), len(e), _stream_ptr(stream)))
+        if wait:
+            check(lib().vrt_world_wait(self._h))
+
+    def defrag(self, capacity: int = 0, stream=None) -> None:
+        """Pack the live bricks from slot 0 (vrt_world_defrag); capacity 0 keeps the pool size."""
+        check(lib().vrt_world_defrag(self._h, int(capacity), _stream_ptr(stream)))
 
     def save_cvox(self, path) -> None:
         check(lib().vrt_world_save_cvox(self._h, str(path).encode()))
@@ -256,7 +263,9 @@ class World:
 
 def make_view(cam: Camera, world: int = 0, max_iters: int = 0, n_bounces: int = 0, shadow_dir=None,
               glsl: bool = False, aniso: bool = False) -> View:
-    """A view: primary rays plus shadow rays toward shadow_dir, or n_bounces diffuse bounces.
+    """A view: primary rays plus shadow rays toward shadow_dir, or n_bounces diffuse bounces,
+    or with both the GPU renderer's whole path (sun rays after the primary and the first two
+    bounce hits).
     glsl: trace with the GPU renderer's rayCast (VRT_VIEW_GLSL) instead of the CPU traversal;
     aniso: with its anisotropic LODs (VRT_VIEW_GLSL_ANISO)."""
     vw = View()
@@ -281,6 +290,20 @@ def render_path(world: "World", view: View, stream=None) -> np.ndarray:
     hits = np.zeros(n, HIT_DTYPE)
     check(lib().vrt_render_path(world.handle, C.byref(view), ptr(hits), _stream_ptr(stream)))
     return hits.reshape(-1, view.cam.width * view.cam.height)
+
+
+def render_gbuffer(world: "World", view: View, palette, proj, stream=None):
+    """G-buffer of a view's primary hits (vrt_render_gbuffer): (albedo_normal u32, depth f32),
+    each width*height.  palette: 256 material words; proj: 4x4 column-major (16 floats)."""
+    n = view.cam.width * view.cam.height
+    pal = np.ascontiguousarray(palette, dtype=np.uint32)
+    pm = np.ascontiguousarray(proj, dtype=np.float32).reshape(16)
+    if pal.size != 256:
+        raise ValueError("palette needs 256 entries")
+    tex, depth = np.zeros(n, np.uint32), np.zeros(n, np.float32)
+    check(lib().vrt_render_gbuffer(world.handle, C.byref(view), ptr(pal), ptr(pm), ptr(tex), ptr(depth),
+                                   _stream_ptr(stream)))
+    return tex, depth
 
 
 class Batch:

@@ -155,6 +155,8 @@ PROTOTYPES = {
     "vrt_world_get_stats": (_st, [_vp, C.POINTER(WorldStats)]),
     "vrt_world_sync_sectors": (_st, [_vp, _u32, _vp, _vp, _vp, _vp, _vp]),
     "vrt_world_edit": (_st, [_vp, _vp, _u32, _vp]),
+    "vrt_world_wait": (_st, [_vp]),
+    "vrt_world_defrag": (_st, [_vp, _u32, _vp]),
     "vrt_world_read_sector": (_st, [_vp, _i32, C.POINTER(_u64), _vp, C.c_size_t, _vp]),
     "vrt_cvox_write": (_st, [C.c_char_p, _u32, _vp, _vp, _vp]),
     "vrt_cvox_read": (_st, [C.c_char_p, C.POINTER(C.POINTER(SectorStream))]),
@@ -170,6 +172,8 @@ PROTOTYPES = {
     "vrt_view_records": (_u64, [C.POINTER(View)]),
     "vrt_render_path": (_st, [_vp, C.POINTER(View), _vp, _vp]),
     "vrt_render_path_device": (_st, [_vp, C.POINTER(View), _vp, _vp]),
+    "vrt_render_gbuffer": (_st, [_vp, C.POINTER(View), _vp, _vp, _vp, _vp, _vp]),
+    "vrt_render_gbuffer_device": (_st, [_vp, C.POINTER(View), _vp, _vp, _vp, _vp, _vp, _vp]),
     "vrt_batch_create": (_st, [C.POINTER(_vp), _u32, C.POINTER(View), _u32, C.POINTER(BatchConfig), C.POINTER(_vp)]),
     "vrt_batch_destroy": (_st, [_vp]),
     "vrt_batch_output_layout": (_st, [_vp, C.POINTER(_u64)]),

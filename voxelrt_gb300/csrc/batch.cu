@@ -63,17 +63,36 @@ __global__ void __launch_bounds__(64) view_path_kernel(DevWorld w, ViewDev v, ui
     uint4* o = out + v.out_base + pixel;
     o[0] = pack_state<kGlsl>(s, hit, steps, pixel);
     const uint32_t last = v.last_kind();
+    const bool full = (v.path & kPathFull) != 0;
+    float pox = 0.0f, poy = 0.0f, poz = 0.0f, pnx = 0.0f, pny = 0.0f, pnz = 0.0f;  // full path: last hit frame
     for (uint32_t k = 1; k <= last; k++) {
         if (!hit) {
             o[k * plane] = no_ray_hit();
             continue;
         }
-        next_path_ray<kGlsl>(s, v.shadow() != 0, v.sun, pixel, k, ox, oy, oz, dx, dy, dz);
+        if (full) {
+            // a sun ray starts from the hit just traced; a bounce from the hit before its
+            // sun ray (saved), or from the bounce just traced when no sun ray follows it
+            if (full_is_sun(k) || !full_is_sun(k - 1)) hit_frame<kGlsl>(s, pox, poy, poz, pnx, pny, pnz);
+            ox = pox;
+            oy = poy;
+            oz = poz;
+            if (full_is_sun(k)) {
+                dx = v.sun[0];
+                dy = v.sun[1];
+                dz = v.sun[2];
+            } else {
+                bounce_dir(pixel, full_bounce(k), pnx, pny, pnz, dx, dy, dz);
+            }
+        } else {
+            next_path_ray<kGlsl>(s, v.shadow() != 0, v.sun, pixel, k, ox, oy, oz, dx, dy, dz);
+        }
         safe = ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz, false, kGlsl);
         // GLSL mode: shadow and bounce rays are rayCastCoarse's (VoxelRender.comp:56,74)
         hit = run_ray<false, kGlsl>(s, safe, w, wox, woy, woz, kGlsl ? min(v.max_iters, kCoarseMaxIters) : v.max_iters,
                                     steps, cnt, kGlsl, kAniso);
         o[k * plane] = pack_state<kGlsl>(s, hit, steps, pixel);
+        if (full && full_is_sun(k)) hit = true;  // the path goes on after a sun ray, hit or miss
     }
 }
 
@@ -234,6 +253,9 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
     // that ray setup reads shared memory instead of making L2 round trips
     __shared__ ViewDev s_views[16];
     ViewDev& sview = s_views[threadIdx.x >> 5];
+    // the GPU renderer's whole path: the hit frame (origin xyz, normal xyz) kept across a
+    // sun ray, 6 floats per thread (dynamic shared memory, sized only for such batches)
+    extern __shared__ float s_pend[];
 
     for (;;) {
         bool finished = false;  // a pixel's path ended this round (resident completion)
@@ -252,13 +274,47 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
             rec[(size_t)kind * plane] = pack_state<kGlsl>(s, hit, iter, pixel);
             rays++;
             if (kCount && hit) hits++;
-            if (hit && kind < last_kind) {
+            // the GPU renderer's whole path goes on after a sun ray, hit or miss
+            const bool full = (path & kPathFull) != 0, after_sun = full && full_is_sun(kind);
+            if ((hit || after_sun) && kind < last_kind) {
                 path++;
                 kind++;
                 float ox, oy, oz, dx, dy, dz;
                 const float sun[3] = {vget<kResident>(&v->sun[0], vs), vget<kResident>(&v->sun[1], vs),
                                       vget<kResident>(&v->sun[2], vs)};
-                next_path_ray<kGlsl>(s, ((path >> 16) & 1u) != 0, sun, pixel, kind, ox, oy, oz, dx, dy, dz);
+                if (full) {
+                    // a sun ray starts from the hit just traced, whose frame is kept (shared
+                    // memory, one slot per thread) for the bounce after it; a bounce after a
+                    // sun ray starts from that kept frame, one after a bounce from its hit
+                    float nx, ny, nz;
+                    float* pend = s_pend + threadIdx.x;
+                    const uint32_t bs = blockDim.x;
+                    if (after_sun) {
+                        ox = pend[0];
+                        oy = pend[bs];
+                        oz = pend[2 * bs];
+                        nx = pend[3 * bs];
+                        ny = pend[4 * bs];
+                        nz = pend[5 * bs];
+                    } else {
+                        hit_frame<kGlsl>(s, ox, oy, oz, nx, ny, nz);
+                    }
+                    if (full_is_sun(kind)) {
+                        pend[0] = ox;
+                        pend[bs] = oy;
+                        pend[2 * bs] = oz;
+                        pend[3 * bs] = nx;
+                        pend[4 * bs] = ny;
+                        pend[5 * bs] = nz;
+                        dx = sun[0];
+                        dy = sun[1];
+                        dz = sun[2];
+                    } else {
+                        bounce_dir(pixel, full_bounce(kind), nx, ny, nz, dx, dy, dz);
+                    }
+                } else {
+                    next_path_ray<kGlsl>(s, ((path >> 16) & 1u) != 0, sun, pixel, kind, ox, oy, oz, dx, dy, dz);
+                }
                 path &= ~kSafe;
                 if (ray_start<kGlsl>(s, w, ox, oy, oz, dx, dy, dz, wox, woy, woz, false, kGlsl)) path |= kSafe;
                 iter = 0;
@@ -524,7 +580,10 @@ ViewDev make_view_dev(const vrt_view& v) {
     d.max_iters = eff_iters(v.max_iters, view_glsl(v));
     d.aniso = view_aniso(v) ? 1u : 0u;
     const uint32_t shadow = (v.flags & VRT_VIEW_SHADOW) ? 1u : 0u;
-    d.path = (shadow ? 1u : v.n_bounces) << 8 | shadow << 16;
+    if (shadow && v.n_bounces)  // the GPU renderer's whole path: sun rays among the bounces
+        d.path = (uint32_t)(view_record_count(v) / ((uint64_t)v.cam.width * v.cam.height) - 1) << 8 | kPathFull;
+    else
+        d.path = (shadow ? 1u : v.n_bounces) << 8 | shadow << 16;
     for (int c = 0; c < 3; c++) d.sun[c] = v.sun_dir[c];
     return d;
 }
@@ -563,17 +622,18 @@ vrt_status check_same_mode(const vrt_view* views, uint32_t n) {
 vrt_status check_view(const vrt_view* v) {
     if (!v || v->cam.width == 0 || v->cam.height == 0 || v->cam.width > 16384 || v->cam.height > 16384 ||
         v->n_bounces > VRT_MAX_BOUNCES || (v->flags & ~(VRT_VIEW_SHADOW | VRT_VIEW_GLSL | VRT_VIEW_GLSL_ANISO)) ||
-        ((v->flags & VRT_VIEW_GLSL_ANISO) && !(v->flags & VRT_VIEW_GLSL)) ||
-        ((v->flags & VRT_VIEW_SHADOW) && v->n_bounces) || !world_origin_ok(v->cam.world_origin)) {
-        set_error("bad view: camera 1..16384 px, |world origin| <= 2^30, n_bounces <= 15, shadow and bounces "
-                  "exclusive, anisotropic LODs only with the GLSL mode");
+        ((v->flags & VRT_VIEW_GLSL_ANISO) && !(v->flags & VRT_VIEW_GLSL)) || !world_origin_ok(v->cam.world_origin)) {
+        set_error("bad view: camera 1..16384 px, |world origin| <= 2^30, n_bounces <= 15, anisotropic LODs only "
+                  "with the GLSL mode");
         return VRT_ERR_INVALID_ARG;
     }
     return VRT_OK;
 }
 
 uint64_t view_record_count(const vrt_view& v) {
-    const uint64_t kinds = 1 + ((v.flags & VRT_VIEW_SHADOW) ? 1 : v.n_bounces);
+    const uint64_t n = v.n_bounces;
+    // primary; shadow; bounces; or the renderer's path: sun, bounces, sun after the first two
+    const uint64_t kinds = 1 + ((v.flags & VRT_VIEW_SHADOW) ? (n ? 1 + n + std::min<uint64_t>(n, 2) : 1) : n);
     return kinds * v.cam.width * v.cam.height;
 }
 
@@ -610,6 +670,8 @@ vrt_status plan_views(const vrt_view* views, uint32_t n, uint32_t n_worlds, cons
     if ((st = check_same_mode(views, n)) != VRT_OK) return st;
     plan.glsl = n > 0 && view_glsl(views[0]);
     plan.aniso = n > 0 && view_aniso(views[0]);
+    plan.full = false;
+    for (uint32_t i = 0; i < n; i++) plan.full |= view_full_path(views[i]);
     plan.cfg = cfg;
     plan.tile_w_log2 = log2u(cfg.tile_w);
     plan.tile_size_log2 = log2u(cfg.tile_w * cfg.tile_h);
@@ -704,16 +766,18 @@ BatchParams make_params(const LaunchPlan& plan, const DevWorld* worlds, const Vi
     p.inner = plan.cfg.inner_iters;
     p.glsl = plan.glsl ? 1u : 0u;
     p.aniso = plan.aniso ? 1u : 0u;
+    p.full = plan.full ? 1u : 0u;
     return p;
 }
 
 vrt_status launch_resident(const BatchParams& p, int blocks, int threads, cudaStream_t stream) {
+    const size_t smem = pend_bytes(p, threads);
     if (p.glsl && p.aniso)
-        persistent_kernel<false, true, true, true><<<blocks, threads, 0, stream>>>(p);
+        persistent_kernel<false, true, true, true><<<blocks, threads, smem, stream>>>(p);
     else if (p.glsl)
-        persistent_kernel<false, true, true><<<blocks, threads, 0, stream>>>(p);
+        persistent_kernel<false, true, true><<<blocks, threads, smem, stream>>>(p);
     else
-        persistent_kernel<false, false, true><<<blocks, threads, 0, stream>>>(p);
+        persistent_kernel<false, false, true><<<blocks, threads, smem, stream>>>(p);
     VRT_CUDA(cudaGetLastError());
     return VRT_OK;
 }
@@ -721,18 +785,19 @@ vrt_status launch_resident(const BatchParams& p, int blocks, int threads, cudaSt
 vrt_status launch_persistent(const BatchParams& p, int blocks, int threads, bool count, cudaStream_t stream,
                              bool reset_counters) {
     VRT_CUDA(cudaMemsetAsync(p.queue, 0, reset_counters ? 64 : 4, stream));
+    const size_t smem = pend_bytes(p, threads);
     if (count && p.glsl && p.aniso)
-        persistent_kernel<true, true, false, true><<<blocks, threads, 0, stream>>>(p);
+        persistent_kernel<true, true, false, true><<<blocks, threads, smem, stream>>>(p);
     else if (count && p.glsl)
-        persistent_kernel<true, true><<<blocks, threads, 0, stream>>>(p);
+        persistent_kernel<true, true><<<blocks, threads, smem, stream>>>(p);
     else if (count)
-        persistent_kernel<true, false><<<blocks, threads, 0, stream>>>(p);
+        persistent_kernel<true, false><<<blocks, threads, smem, stream>>>(p);
     else if (p.glsl && p.aniso)
-        persistent_kernel<false, true, false, true><<<blocks, threads, 0, stream>>>(p);
+        persistent_kernel<false, true, false, true><<<blocks, threads, smem, stream>>>(p);
     else if (p.glsl)
-        persistent_kernel<false, true><<<blocks, threads, 0, stream>>>(p);
+        persistent_kernel<false, true><<<blocks, threads, smem, stream>>>(p);
     else
-        persistent_kernel<false, false><<<blocks, threads, 0, stream>>>(p);
+        persistent_kernel<false, false><<<blocks, threads, smem, stream>>>(p);
     VRT_CUDA(cudaGetLastError());
     return VRT_OK;
 }

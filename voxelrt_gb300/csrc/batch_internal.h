@@ -62,6 +62,7 @@ struct BatchParams {
     uint32_t inner;
     uint32_t glsl;  // traversal mode of every view (VRT_VIEW_GLSL)
     uint32_t aniso;  // ... with anisotropic LODs (VRT_VIEW_GLSL_ANISO)
+    uint32_t full;   // some view traces the GPU renderer's whole path (sun rays among bounces)
     // resident launches (request server): views are published while the kernel runs
     unsigned long long* mailbox;  // host-mapped: published chunks | published views << 32 | closed << 63
     uint32_t* next_chunk;         // device: next chunk to claim
@@ -90,7 +91,12 @@ struct LaunchPlan {
     uint32_t chunks = 0;
     bool glsl = false;   // every view traces in the GLSL mode
     bool aniso = false;  // ... with anisotropic LODs
+    bool full = false;   // some view traces the GPU renderer's whole path
 };
+
+// Dynamic shared memory of a persistent launch: the hit frame a lane keeps across a sun
+// ray of the GPU renderer's whole path (6 floats per thread), only where a view needs it.
+inline size_t pend_bytes(const BatchParams& p, int threads) { return p.full ? (size_t)threads * 6 * sizeof(float) : 0; }
 
 // Iteration cap of a view or cast: 0 = the mode's default, at most 65535.
 uint32_t eff_iters(uint32_t max_iters, bool glsl = false);
@@ -98,6 +104,8 @@ inline bool view_glsl(const vrt_view& v) { return (v.flags & VRT_VIEW_GLSL) != 0
 inline bool view_aniso(const vrt_view& v) { return (v.flags & VRT_VIEW_GLSL_ANISO) != 0; }
 // A view's traversal mode: the CPU traversal, GLSL, or GLSL with anisotropic LODs.
 inline uint32_t view_mode(const vrt_view& v) { return v.flags & (VRT_VIEW_GLSL | VRT_VIEW_GLSL_ANISO); }
+// A sun direction and bounces: the GPU renderer's whole path (VoxelRender.comp:51-86).
+inline bool view_full_path(const vrt_view& v) { return (v.flags & VRT_VIEW_SHADOW) && v.n_bounces; }
 // All views of one launch share a traversal mode (VRT_ERR_INVALID_ARG otherwise).
 vrt_status check_same_mode(const vrt_view* views, uint32_t n);
 uint64_t view_record_count(const vrt_view& v);

@@ -87,6 +87,20 @@ uint32_t FreeList::high_water() const {
     return capacity_ + 1;
 }
 
+void FreeList::assign_used(uint32_t capacity, const std::vector<std::pair<uint32_t, uint32_t>>& used) {
+    ranges_.clear();
+    capacity_ = capacity;
+    allocated_ = 0;
+    uint32_t next = 1;  // first slot not yet accounted for
+    for (const auto& u : used) {
+        if (u.second == 0) continue;
+        if (u.first > next) ranges_[next] = u.first - next;
+        allocated_ += u.second;
+        next = u.first + u.second;
+    }
+    if (next <= capacity) ranges_[next] = capacity + 1 - next;
+}
+
 bool sector_free(FreeList& fl, SectorSlots& s, uint64_t remove) {
     uint64_t nm = s.mask & ~remove;
     if (nm == s.mask) return true;

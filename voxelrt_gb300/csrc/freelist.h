@@ -17,6 +17,8 @@
 
 #include <cstdint>
 #include <map>
+#include <utility>
+#include <vector>
 
 namespace vrt {
 
@@ -42,6 +44,9 @@ class FreeList {
     const std::map<uint32_t, uint32_t>& ranges() const { return ranges_; }
     // Largest slot index in use + 1 (1 when nothing is allocated).
     uint32_t high_water() const;
+    // Reset to `capacity` slots of which exactly the given ranges (1-based start, length;
+    // sorted by start, disjoint) are allocated: the free ranges are the gaps between them.
+    void assign_used(uint32_t capacity, const std::vector<std::pair<uint32_t, uint32_t>>& used);
 
   private:
     void take_front(std::map<uint32_t, uint32_t>::iterator it, uint32_t count);

@@ -181,6 +181,8 @@ extern "C" vrt_status vrt_render_views_static(vrt_world* const* worlds, uint32_t
     p.inner = cfg.inner_iters;
     p.glsl = glsl ? 1u : 0u;
     p.aniso = n_views > 0 && view_aniso(views[0]) ? 1u : 0u;
+    p.full = 0u;
+    for (uint32_t i = 0; i < n_views; i++) p.full |= view_full_path(views[i]) ? 1u : 0u;
     int blocks = 0, threads = 0;
     if ((st = persistent_grid(device, cfg, false, p.glsl != 0, p.aniso != 0, false, blocks, threads)) != VRT_OK)
         return st;

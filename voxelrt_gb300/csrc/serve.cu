@@ -279,6 +279,7 @@ void worker_main(vrt_server* sv) {
                 lk.unlock();
                 vrt_status st = vrt_world_edit(sv->worlds[r->world], r->edits.data(), (uint32_t)r->edits.size(),
                                                sv->edit_stream);
+                if (st == VRT_OK) st = vrt_world_wait(sv->worlds[r->world]);  // applied before later launches
                 if (st == VRT_OK) st = refresh_world_table(sv);
                 lk.lock();
                 finish(sv, r, st, now_us(sv->t0));
@@ -457,6 +458,7 @@ vrt_status resident_start(vrt_server* sv, uint32_t mode) {
     plan.tile_size_log2 = r;
     plan.glsl = glsl;
     plan.aniso = (mode & VRT_VIEW_GLSL_ANISO) != 0;
+    plan.full = true;  // requests with the GPU renderer's whole path may arrive while it runs
     BatchParams p = make_params(plan, sv->d_worlds, (const ViewDev*)R.views.ptr, (const uint32_t*)R.chunk_base.ptr,
                                 (uint32_t*)R.queue.ptr, (vrt_hit*)sv->arena);
     p.mailbox = R.d_mailbox;
@@ -561,6 +563,7 @@ bool resident_schedule(vrt_server* sv, std::unique_lock<std::mutex>& lk) {
         lk.unlock();
         vrt_status st = vrt_world_edit(sv->worlds[front->world], front->edits.data(),
                                        (uint32_t)front->edits.size(), sv->edit_stream);
+        if (st == VRT_OK) st = vrt_world_wait(sv->worlds[front->world]);  // applied before later launches
         if (st == VRT_OK) st = refresh_world_table(sv);
         lk.lock();
         finish(sv, front, st, now_us(sv->t0));

@@ -593,6 +593,29 @@ __device__ __forceinline__ uint4 pack_state(const RayState& s, bool hit, uint32_
     return pack_hit<kGlsl>(r, s.dx, s.dy, s.dz, tag);
 }
 
+// Where the secondary rays of a hit start and the hit's normal (secondary_origin).
+template <bool kGlsl = false>
+__device__ __forceinline__ void hit_frame(const RayState& s, float& ox, float& oy, float& oz, float& nx, float& ny,
+                                          float& nz) {
+    TraceResult r;
+    r.cx = s.cx;
+    r.cy = s.cy;
+    r.cz = s.cz;
+    r.sx = s.sx;
+    r.sy = s.sy;
+    r.sz = s.sz;
+    r.tb = s.tb;
+    secondary_origin<kGlsl>(r, s.dx, s.dy, s.dz, ox, oy, oz, nx, ny, nz);
+}
+
+// The GPU renderer's whole path (VoxelRender.comp:51-86), a view with a sun direction
+// and bounces: record plane k >= 1 holds a sun ray for k = 1, 3, 5 (after the primary
+// hit and the first two bounce hits) and otherwise bounce k/2 (k <= 4) or k - 3
+// (k >= 6).  Flag in ViewDev::path.
+constexpr uint32_t kPathFull = 1u << 20;
+__host__ __device__ __forceinline__ bool full_is_sun(uint32_t k) { return k <= 5u && (k & 1u); }
+__host__ __device__ __forceinline__ uint32_t full_bounce(uint32_t k) { return k <= 4u ? k >> 1 : k - 3u; }
+
 // Origin and direction of the next ray of a path after a hit: the shadow ray
 // (kind 1 with shadows) or bounce `bounce` (1-based).
 template <bool kGlsl = false>

@@ -321,6 +321,26 @@ vrt_status rebuild_brick_table_for(vrt_world* w, const std::vector<uint32_t>& se
     return VRT_OK;
 }
 
+}  // namespace
+
+vrt_status rebuild_table_groups(vrt_world* w, const uint32_t* d_groups, uint32_t n, cudaStream_t stream) {
+    if (!d_groups || (uint64_t)n * 4 >= w->num_groups()) {
+        VRT_CUDA(rebuild_brick_table(w, stream));
+        return VRT_OK;
+    }
+    if (n == 0) return VRT_OK;
+    const uint32_t ng = w->num_groups();
+    group_masks_kernel<<<(ng + 3) / 4, 128, 0, stream>>>(w->d_sectors, w->sx, w->sy, w->sz,
+                                                       (unsigned long long*)w->d_groups);
+    const uint32_t k = n * 4096u;
+    brick_table_groups_kernel<<<(k + 255) / 256, 256, 0, stream>>>(w->d_sectors, (const unsigned long long*)w->d_groups,
+                                                                 d_groups, n, w->sx, w->sy, w->sz, w->d_bricks);
+    VRT_CUDA(cudaGetLastError());
+    return VRT_OK;
+}
+
+namespace {
+
 vrt_status run_batch(vrt_world* w, SyncBatch& b, cudaStream_t stream) {
     if (b.ops.empty() && b.touched.empty()) return VRT_OK;
     const size_t stage_bytes = (size_t)b.n_stage * 512;
@@ -365,23 +385,14 @@ vrt_status run_batch(vrt_world* w, SyncBatch& b, cudaStream_t stream) {
         vrt_status st = rebuild_brick_table_for(w, b.touched, stream);
         if (st != VRT_OK) return st;
     }
+    vrt_status st = alloc_publish(w, stream);
+    if (st != VRT_OK) return st;
     VRT_CUDA(cudaStreamSynchronize(stream));
     b = SyncBatch();
     return VRT_OK;
 }
 
 }  // namespace
-
-// Re-lay out sectors to new allocation masks, keeping the content of bricks that
-// stay and zero-filling bricks that appear (used by the edit path).
-vrt_status world_repack(vrt_world* w, const std::map<uint32_t, uint64_t>& new_masks, cudaStream_t stream) {
-    SyncBatch batch;
-    for (const auto& kv : new_masks) {
-        vrt_status st = plan_sector(w, batch, kv.first, kv.second, 0, 0, stream);
-        if (st != VRT_OK) return st;
-    }
-    return run_batch(w, batch, stream);
-}
 
 }  // namespace vrt
 
@@ -436,11 +447,22 @@ vrt_status vrt_world_create(const vrt_world_desc* desc, vrt_world** out) {
         // the group list of incremental table rebuilds, at its largest size: it never
         // grows (a growing buffer's cudaFree would wait for the whole device)
         if (e == cudaSuccess) e = w->d_glist.reserve((size_t)w->num_groups() * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc(&w->d_alloc, sizeof(DevAlloc));
+        if (e == cudaSuccess) e = cudaMemset(w->d_alloc, 0, sizeof(DevAlloc));
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w->edited, cudaEventDisableTiming);
+        // edit scratch for batches of up to a few thousand touched sectors: a buffer that
+        // grows later frees its old block, and cudaFree waits for the whole device
+        if (e == cudaSuccess) e = w->d_edit.reserve(256 << 10);
+        if (e == cudaSuccess) e = w->d_gc.reserve(64 << 10);
+        for (auto& stage : w->edit_stage)
+            if (e == cudaSuccess) e = stage.acquire(64 << 10);
         if (e == cudaSuccess) e = rebuild_brick_table(w, 0);
         if (e == cudaSuccess) e = cudaStreamSynchronize(0);
         if (e != cudaSuccess) st = cuda_fail(e, "allocate sector table");
     }
     if (st == VRT_OK) st = grow_pool(w, desc->brick_capacity ? desc->brick_capacity : 4096, 0);
+    if (st == VRT_OK) st = alloc_publish(w, 0);
+    if (st == VRT_OK && cudaStreamSynchronize(0) != cudaSuccess) st = cuda_fail(cudaGetLastError(), "create world");
     if (st != VRT_OK) {
         vrt_world_destroy(w);
         return st;
@@ -464,15 +486,27 @@ vrt_status vrt_world_destroy(vrt_world* w) {
     w->d_scratch.release();
     w->d_io.release();
     w->d_glist.release();
+    w->d_edit.release();
+    w->d_gc.release();
+    for (auto& stage : w->edit_stage) stage.destroy();
+    if (w->d_alloc) cudaFree(w->d_alloc);
+    if (w->edited) cudaEventDestroy(w->edited);
     delete w;
     return VRT_OK;
 }
 
-vrt_status vrt_world_get_stats(const vrt_world* w, vrt_world_stats* out) {
-    if (!w || !out) {
+vrt_status vrt_world_get_stats(const vrt_world* cw, vrt_world_stats* out) {
+    if (!cw || !out) {
         set_error("null argument");
         return VRT_ERR_INVALID_ARG;
     }
+    // the host mirror is rebuilt from the device after device edits (a cache of the
+    // device's state, not a change to the world)
+    vrt_world* w = const_cast<vrt_world*>(cw);
+    vrt_status st = world_enter(w);
+    if (st != VRT_OK) return st;
+    std::lock_guard<std::mutex> lock(w->mu);
+    if ((st = refresh_host_mirror(w)) != VRT_OK) return st;
     out->sectors_x = w->sx;
     out->sectors_y = w->sy;
     out->sectors_z = w->sz;
@@ -483,7 +517,8 @@ vrt_status vrt_world_get_stats(const vrt_world* w, vrt_world_stats* out) {
     // 64 B cell masks, and the scratch buffers
     out->device_bytes = (uint64_t)w->num_sectors() * sizeof(SectorRec) + (uint64_t)w->num_brick_positions() * 4 +
                         (uint64_t)w->num_groups() * 8 + (uint64_t)w->capacity * 1088 + w->d_stage.bytes +
-                        w->d_ops.bytes + w->d_scratch.bytes + w->d_io.bytes + w->d_glist.bytes;
+                        w->d_ops.bytes + w->d_scratch.bytes + w->d_io.bytes + w->d_glist.bytes + w->d_edit.bytes +
+                        w->d_gc.bytes;
     return VRT_OK;
 }
 
@@ -496,6 +531,7 @@ vrt_status vrt_world_sync_sectors(vrt_world* w, uint32_t n, const int32_t* secto
         return VRT_ERR_INVALID_ARG;
     }
     std::lock_guard<std::mutex> lock(w->mu);
+    if ((st = refresh_host_mirror(w)) != VRT_OK) return st;
     cudaStream_t stream = (cudaStream_t)stream_;
     const uint64_t kBatchBricks = 1ull << 19;  // 256 MiB of staged bricks per batch
     SyncBatch batch;
@@ -540,6 +576,7 @@ vrt_status vrt_world_save_cvox(vrt_world* w, const char* path) {
     std::vector<uint8_t> bricks;
     {
         std::lock_guard<std::mutex> lock(w->mu);
+        if ((st = refresh_host_mirror(w)) != VRT_OK) return st;
         for (uint32_t y = 0; y < w->sy; y++)
             for (uint32_t z = 0; z < w->sz; z++)
                 for (uint32_t x = 0; x < w->sx; x++) {
@@ -577,6 +614,7 @@ vrt_status vrt_world_read_sector(vrt_world* w, int32_t sector_idx, uint64_t* all
         return VRT_ERR_INVALID_ARG;
     }
     std::lock_guard<std::mutex> lock(w->mu);
+    if ((st = refresh_host_mirror(w)) != VRT_OK) return st;
     const SectorSlots& s = w->slots[w->lin(x, y, z)];
     if (alloc_mask) *alloc_mask = s.mask;
     const size_t need = (size_t)__builtin_popcountll(s.mask) * 512;

@@ -48,6 +48,46 @@ struct DevBuf {
     }
 };
 
+// Pinned host buffer for asynchronous uploads.  A pageable source may still be read
+// after cudaMemcpyAsync returns (a device with a coherent host link reads it during the
+// copy), so uploads go through this buffer, and a call that rewrites it first waits for
+// the copy that last read it (the `read` event).
+struct HostStage {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    cudaEvent_t read = nullptr;
+    cudaError_t acquire(size_t n) {
+        if (!read) {
+            cudaError_t e = cudaEventCreateWithFlags(&read, cudaEventDisableTiming);
+            if (e != cudaSuccess) return e;
+        }
+        cudaError_t e = cudaEventSynchronize(read);
+        if (e != cudaSuccess || n <= bytes) return e;
+        if (bytes * 2 > n) n = bytes * 2;
+        void* p = nullptr;
+        if ((e = cudaHostAlloc(&p, n, cudaHostAllocDefault)) != cudaSuccess) return e;
+        if (ptr) cudaFreeHost(ptr);
+        ptr = p;
+        bytes = n;
+        return cudaSuccess;
+    }
+    cudaError_t release(cudaStream_t stream) { return cudaEventRecord(read, stream); }
+    void destroy() {
+        if (read) cudaEventSynchronize(read), cudaEventDestroy(read);
+        if (ptr) cudaFreeHost(ptr);
+        ptr = nullptr;
+        read = nullptr;
+        bytes = 0;
+    }
+};
+
+// Device side of the brick-slot allocator: slots [0, top) have been handed out (live
+// bricks and the garbage left behind by relocated sectors), `live` are in use, `cap`
+// is the pool size; `overflow` is set when an allocation did not fit (it is skipped).
+struct DevAlloc {
+    uint32_t top, live, cap, overflow;
+};
+
 }  // namespace vrt
 
 struct vrt_world {
@@ -76,6 +116,17 @@ struct vrt_world {
     vrt::DevBuf d_glist;    // sector groups whose brick-table entries an edit re-derives
     vrt::DevBuf d_io;       // ray/hit staging for host-buffer calls
     std::vector<vrt::SectorRec> h_table;  // host copy of the sector table
+
+    // device-side edits (alloc.cu): the bump allocator in device memory, the edit batch
+    // upload, and what the host knows of the device's layout
+    vrt::DevAlloc* d_alloc = nullptr;
+    vrt::HostStage edit_stage[4];  // pinned uploads of the last edit batches, used in turn
+    uint32_t edit_stage_next = 0;
+    vrt::DevBuf d_edit;         // the edit batch on the device
+    vrt::DevBuf d_gc;           // per touched sector: bricks an edit emptied
+    cudaEvent_t edited = nullptr;  // recorded behind the last device edit
+    bool host_stale = false;    // slots / arena / h_table predate device edits
+    uint64_t top_bound = 0;     // upper bound of d_alloc->top without reading it
 
     uint32_t num_sectors() const { return sx * sy * sz; }
     size_t num_brick_positions() const { return (size_t)num_sectors() * 64; }
@@ -108,4 +159,18 @@ struct vrt_world {
 namespace vrt {
 // Make `world` current on the calling thread.
 vrt_status world_enter(vrt_world* world);
+
+// alloc.cu (callers hold world->mu)
+// Rebuild the host mirror (slots, arena, h_table) from the device after device edits.
+vrt_status refresh_host_mirror(vrt_world* w);
+// After host planning: publish the host allocator's state to the device allocator.
+vrt_status alloc_publish(vrt_world* w, cudaStream_t stream);
+// Make room for `need` more bump-allocated slots: compacts (and grows) the pool when
+// the bound of the bump pointer says it may not fit.
+vrt_status ensure_headroom(vrt_world* w, uint64_t need, cudaStream_t stream);
+// Pack the live bricks from slot 0 in sector order into a pool of `capacity` slots.
+vrt_status world_compact(vrt_world* w, uint32_t capacity, cudaStream_t stream);
+// Brick-table entries of the listed sector groups (device list of n groups), or of the
+// whole world when they are a quarter of it or more.
+vrt_status rebuild_table_groups(vrt_world* w, const uint32_t* d_groups, uint32_t n, cudaStream_t stream);
 }  // namespace vrt
