@@ -5,16 +5,23 @@
 // that runs the reference's static RayCast (CpuRenderer.cpp:172-224) over
 // FlatVoxelStorage (CpuRenderer.cpp:20-84) filled through VoxelMap and SyncBuffers.
 // The AVX-512 code only runs on x86-64; its outputs are committed as golden
-// vectors (tests/golden/) that pin the portable oracle.
+// vectors (tests/golden/) that pin the portable oracle.  World files go through the
+// reference's own VoxelMap::Serialize / Deserialize (VoxelMap.cpp:211-273) and
+// BinaryIO.cpp framing, compiled in place with the system's libzstd.
 #include "CpuRenderer.cpp"
 #include "VoxelMap.cpp"
 
+#include <algorithm>
 #include <stdexcept>
+#include <vector>
 
+#if !VRT_REF_BINARY_IO
+// no libzstd: the world-file entry points below report failure
 namespace glim::io {
 void WriteCompressed(std::ostream&, const void*, size_t) { throw std::runtime_error("zstd is not available"); }
 void ReadCompressed(std::istream&, void*, size_t) { throw std::runtime_error("zstd is not available"); }
 }  // namespace glim::io
+#endif
 
 namespace {
 struct RefWorld {
@@ -100,6 +107,55 @@ int ref_raycast(void* p, uint64_t n, const float* origins, const float* dirs, co
         }
     }
     return 0;
+}
+
+// VoxelMap::Serialize (VoxelMap.cpp:246-273) of the loaded map to `path`; 0 or -1.
+int ref_serialize(void* p, const char* path) {
+    try {
+        static_cast<RefWorld*>(p)->map->Serialize(path);
+        return 0;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}
+
+// A world read by VoxelMap::Deserialize (VoxelMap.cpp:211-244), or NULL when it throws.
+void* ref_world_from_file(const char* path) {
+    auto* w = new RefWorld;
+    try {
+        w->map->Deserialize(path);
+    } catch (const std::exception&) {
+        delete w;
+        return nullptr;
+    }
+    return w;
+}
+
+// Sectors of the map in ascending index order: count, then (index, allocation mask,
+// bricks in bit order) into the given arrays (bricks: total popcount x 512 bytes).
+uint32_t ref_world_sector_count(void* p, uint64_t* n_bricks) {
+    auto* w = static_cast<RefWorld*>(p);
+    uint64_t nb = 0;
+    for (auto& [idx, sector] : w->map->Sectors) nb += (uint64_t)std::popcount(sector.GetAllocationMask());
+    *n_bricks = nb;
+    return (uint32_t)w->map->Sectors.size();
+}
+
+void ref_world_export(void* p, int32_t* idx_out, uint64_t* mask_out, uint8_t* bricks_out) {
+    auto* w = static_cast<RefWorld*>(p);
+    std::vector<uint32_t> keys;
+    for (auto& kv : w->map->Sectors) keys.push_back(kv.first);
+    std::sort(keys.begin(), keys.end());
+    for (uint32_t idx : keys) {
+        Sector& sector = w->map->Sectors[idx];
+        const uint64_t mask = sector.GetAllocationMask();
+        *idx_out++ = (int32_t)idx;
+        *mask_out++ = mask;
+        for (uint64_t m = mask; m; m &= m - 1) {
+            std::memcpy(bricks_out, sector.GetBrick((uint32_t)std::countr_zero(m))->Data, 512);
+            bricks_out += 512;
+        }
+    }
 }
 
 // VoxelMap::RayCast (VoxelMap.cpp:140-170) on the loaded map; rays: 6 doubles each.

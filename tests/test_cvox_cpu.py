@@ -115,3 +115,47 @@ def test_rejects_bad_files(tmp_path):
     with pytest.raises(v.VrtError) as e:
         v.cvox_read(tmp_path / "missing.cvox")
     assert e.value.status == v.capi.VRT_ERR_IO
+
+
+def _sorted_stream(idx, masks, bricks):
+    """Sector records in ascending index order (files keep the writer's order)."""
+    order = np.argsort(np.asarray(idx, np.int64), kind="stable")
+    counts = np.array([bin(int(m)).count("1") for m in masks], np.int64)
+    starts = np.concatenate([[0], np.cumsum(counts)])
+    out = [bricks[starts[i]:starts[i + 1]] for i in order]
+    return (np.asarray(idx)[order], np.asarray(masks)[order],
+            np.concatenate(out) if out else np.zeros((0, 512), np.uint8))
+
+
+def test_reads_the_reference_writer():
+    """tests/golden/refworld.cvox was written by the reference's own VoxelMap::Serialize with
+    its zstd framing (compressed packs, checksums), compiled in place by
+    tests/golden/make_golden_cvox.py; reading it gives back the seeded world byte for byte."""
+    from tests.golden.make_golden_cvox import OUT_FILE, build_world
+    data = build_world()
+    try:
+        got = v.cvox_read(OUT_FILE)
+    except v.VrtError as e:
+        if "libzstd" in str(e):
+            pytest.skip("compressed packs need the system libzstd.so.1")
+        raise
+    want = _sorted_stream(data.sector_idx, data.alloc_mask, data.bricks)
+    have = _sorted_stream(got.sector_idx, got.alloc_mask, got.bricks)
+    assert np.array_equal(have[0], want[0]) and np.array_equal(have[1], want[1])
+    assert np.array_equal(have[2], want[2])
+
+
+def test_reference_reads_this_writer(tmp_path):
+    """The reference's own VoxelMap::Deserialize read a file written by vrt_cvox_write
+    (tests/golden/refcvox.npz holds what it read and the file's SHA-256): it read the seeded
+    world byte for byte, and vrt_cvox_write still writes that same file."""
+    import hashlib
+    from tests.golden.make_golden_cvox import OUT_NPZ, build_world
+    z = np.load(OUT_NPZ)
+    data = build_world()
+    p = tmp_path / "ours.cvox"
+    v.cvox_write(p, data)
+    assert hashlib.sha256(p.read_bytes()).hexdigest() == str(z["ours_sha256"])
+    want = _sorted_stream(data.sector_idx, data.alloc_mask, data.bricks)
+    assert np.array_equal(z["sector_idx"], want[0]) and np.array_equal(z["alloc_mask"], want[1])
+    assert np.array_equal(z["bricks"], want[2])

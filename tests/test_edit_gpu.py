@@ -156,3 +156,24 @@ def test_world_cvox_save_load(gpu, tmp_path):
     assert_worlds_equal(w2, o)
     w.close()
     w2.close()
+
+
+def test_world_loads_the_reference_file(gpu):
+    """A device world loads the file the reference's own Serialize wrote
+    (tests/golden/refworld.cvox) into the seeded world's content, and traces like the oracle."""
+    from tests.golden.make_golden_cvox import OUT_FILE, build_world
+    data = build_world()
+    w = v.World(data.sectors)
+    try:
+        w.load_cvox(OUT_FILE)
+    except v.VrtError as e:
+        w.close()
+        if "libzstd" in str(e):
+            pytest.skip("compressed packs need the system libzstd.so.1")
+        raise
+    o = OracleWorld(data.sectors)
+    o.upload(data)
+    assert_worlds_equal(w, o)
+    rays = v.random_rays(w.size, seed=8, n=20_000)
+    assert_hits_equal(w.cast(rays), o.cast(rays))
+    w.close()
