@@ -847,21 +847,37 @@ def serve_sweep(args, v, datas, worlds, edges, surf, resident, reserve):
 
 def edit_latency(v, worlds, edges, surf):
     """Sphere edits (radius 4..32, carve or fill at surface points) applied one at a time to
-    the largest resident world through vrt_world_edit."""
+    the largest resident world: the host call of vrt_world_edit (the work is queued on the
+    device, allocation included) and the time to completion (vrt_world_wait after it); then
+    one vrt_world_defrag of the pool the edits fragmented."""
     big = int(np.argmax(edges))
+    w = worlds[big]
     rng = np.random.default_rng(77)
-    edit_ms = []
+    call_ms, done_ms = [], []
     for k in range(200):
         e = np.zeros(1, v.EDIT_DTYPE)
         e["center"] = surf[big][int(rng.integers(0, len(surf[big])))]
         e["radius"] = int(rng.integers(4, 33))
         e["material"] = 0 if k % 2 else int(rng.integers(1, 256))
         t0 = time.perf_counter()
-        worlds[big].edit(e)
-        edit_ms.append((time.perf_counter() - t0) * 1e3)
-    edit_lat = {"edits": len(edit_ms), "world_edge": edges[big], "p50_ms": float(np.percentile(edit_ms, 50)),
-                "p99_ms": float(np.percentile(edit_ms, 99)), "api": "vrt_world_edit, host call to completion"}
-    return edit_lat
+        w.edit(e, wait=False)
+        t1 = time.perf_counter()
+        v.check(v.lib().vrt_world_wait(w.handle))
+        t2 = time.perf_counter()
+        call_ms.append((t1 - t0) * 1e3)
+        done_ms.append((t2 - t0) * 1e3)
+    before = w.stats()
+    t0 = time.perf_counter()
+    w.defrag()
+    defrag_ms = (time.perf_counter() - t0) * 1e3
+    after = w.stats()
+    return {"edits": len(call_ms), "world_edge": edges[big],
+            "p50_ms": float(np.percentile(done_ms, 50)), "p99_ms": float(np.percentile(done_ms, 99)),
+            "call_p50_ms": float(np.percentile(call_ms, 50)), "call_p99_ms": float(np.percentile(call_ms, 99)),
+            "api": "vrt_world_edit (device allocation, no host sync) + vrt_world_wait; p50/p99 to completion",
+            "defrag": {"ms": defrag_ms, "live_bricks": after["allocated_bricks"],
+                       "free_ranges_before": before["free_ranges"], "free_ranges_after": after["free_ranges"],
+                       "capacity": after["brick_capacity"]}}
 
 
 def hits_match(got, want) -> bool:
