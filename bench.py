@@ -69,7 +69,7 @@ def parse(argv=None):
     ap.add_argument("--serve-max-edge", type=int, default=1024)
     ap.add_argument("--serve-check-worlds", type=int, default=8,
                     help="worlds (the largest and smallest among them) whose renders are replayed on the oracle")
-    ap.add_argument("--serve-check-cap", type=int, default=160,
+    ap.add_argument("--serve-check-cap", type=int, default=200,
                     help="replayed renders per arrival rate and mode, at most")
     ap.add_argument("--worlds", type=int, default=128, help="uneven_batch: number of worlds")
     ap.add_argument("--max-views", type=int, default=16, help="uneven_batch: views per world, at most")
@@ -756,7 +756,7 @@ def serve_sweep(args, v, datas, worlds, edges, surf, resident, reserve):
         kept = 0
         # keep every `stride`-th render of the checked worlds, so the kept ones span the run
         expect = sum(1 for e in sched if e[1] == "render" and e[2] in oracles)
-        stride = max(1, -(-expect // max(1, args.serve_check_cap)))
+        stride = max(1, expect // max(1, args.serve_check_cap))
         seen = 0
 
         def retire():

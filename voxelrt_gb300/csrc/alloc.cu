@@ -184,9 +184,14 @@ vrt_status world_compact(vrt_world* w, uint32_t capacity, cudaStream_t stream) {
 
 vrt_status ensure_headroom(vrt_world* w, uint64_t need, cudaStream_t stream) {
     if (w->top_bound + need <= w->capacity) return VRT_OK;
-    vrt_status st = refresh_host_mirror(w);  // reads the device's bump pointer
-    if (st != VRT_OK) return st;
+    // the device's bump pointer (16 bytes read once the world's last edit has run)
+    VRT_CUDA(cudaEventSynchronize(w->edited));
+    DevAlloc a;
+    VRT_CUDA(cudaMemcpy(&a, w->d_alloc, sizeof(a), cudaMemcpyDeviceToHost));
+    w->top_bound = a.top;
     if (w->top_bound + need <= w->capacity) return VRT_OK;
+    vrt_status st = refresh_host_mirror(w);  // the live bricks, for the pool size below
+    if (st != VRT_OK) return st;
     const uint64_t live = w->arena.allocated();
     uint64_t cap = w->capacity;
     // keep the pool size while the live bricks and this edit fill at most 3/4 of it
