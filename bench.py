@@ -582,8 +582,21 @@ def measure_workload(v, wl, dev, steps, stream, check_views=2, stress=None):
     e1.record(stream)
     e1.synchronize()
     ms = e0.elapsed_time(e1) / steps
+    # the plain one-launch-per-view kernel on the same views
+    for _ in range(2):
+        batch.launch_per_view(hits, stream)
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    for _ in range(steps):
+        batch.launch_per_view(hits, stream)
+    p1.record(stream)
+    p1.synchronize()
+    pms = p0.elapsed_time(p1) / steps
     peak, peak_src = peak_hbm()
     out = {"workload": wl.name, "description": wl.description, "value": meas["rays_cast"] / (ms * 1e-3) / 1e9,
+           "per_view": {"value": meas["rays_cast"] / (pms * 1e-3) / 1e9, "ms_per_step": pms,
+                        "launches_per_step": len(wl.views)},
+           "batched_over_per_view": pms / ms,
            "unit": "Grays/s", "ms_per_step": ms, "steps": steps, "rays_per_step": meas["rays_cast"],
            "records_per_step": n_rec, "mean_steps_per_ray": meas["step_calls"] / max(meas["rays_cast"], 1),
            "roofline": {"achieved": alg / (ms * 1e-3) / 1e9, "peak": peak, "frac": alg / (ms * 1e-3) / 1e9 / peak,
