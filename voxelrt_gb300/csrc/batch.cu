@@ -223,7 +223,9 @@ __device__ __forceinline__ void resident_pixels_done(const BatchParams& p, uint3
     }
 }
 
-template <bool kCount, bool kGlsl, bool kResident = false, bool kAniso = false>
+// kFull: the launch may hold views with the GPU renderer's whole path (a separate
+// instantiation, so the others keep their code and registers).
+template <bool kCount, bool kGlsl, bool kResident = false, bool kAniso = false, bool kFull = false>
 __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
     if constexpr (kAniso) fill_forward_lut();
     const uint32_t lane = threadIdx.x & 31;
@@ -275,7 +277,7 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
             rays++;
             if (kCount && hit) hits++;
             // the GPU renderer's whole path goes on after a sun ray, hit or miss
-            const bool full = (path & kPathFull) != 0, after_sun = full && full_is_sun(kind);
+            const bool full = kFull && (path & kPathFull) != 0, after_sun = full && full_is_sun(kind);
             if ((hit || after_sun) && kind < last_kind) {
                 path++;
                 kind++;
@@ -708,38 +710,36 @@ namespace {
 // Resident blocks per SM of the instantiation that a launch of this kind runs: the GLSL
 // and anisotropic variants differ from the default one in registers and shared memory
 // (the anisotropic LUT is 8 KB per block).
-cudaError_t persistent_occupancy(int& occ, int threads, bool count, bool glsl, bool aniso, bool resident) {
-    if (resident) {
-        if (glsl && aniso)
-            return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<false, true, true, true>,
-                                                                 threads, 0);
-        if (glsl)
-            return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<false, true, true>, threads, 0);
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<false, false, true>, threads, 0);
-    }
-    if (count) {
-        if (glsl && aniso)
-            return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<true, true, false, true>,
-                                                                 threads, 0);
-        if (glsl)
-            return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<true, true>, threads, 0);
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<true, false>, threads, 0);
-    }
-    if (glsl && aniso)
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<false, true, false, true>, threads,
-                                                             0);
-    if (glsl) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<false, true>, threads, 0);
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_kernel<false, false>, threads, 0);
+// The instantiation a launch runs: counting, traversal mode, resident, whole-path views.
+using PersistentFn = void (*)(BatchParams);
+template <bool kCount, bool kResident, bool kFull>
+PersistentFn persistent_fn_mode(bool glsl, bool aniso) {
+    if (glsl && aniso) return persistent_kernel<kCount, true, kResident, true, kFull>;
+    if (glsl) return persistent_kernel<kCount, true, kResident, false, kFull>;
+    return persistent_kernel<kCount, false, kResident, false, kFull>;
+}
+PersistentFn persistent_fn(bool count, bool glsl, bool aniso, bool resident, bool full) {
+    if (resident) return full ? persistent_fn_mode<false, true, true>(glsl, aniso)
+                              : persistent_fn_mode<false, true, false>(glsl, aniso);
+    if (count) return full ? persistent_fn_mode<true, false, true>(glsl, aniso)
+                           : persistent_fn_mode<true, false, false>(glsl, aniso);
+    return full ? persistent_fn_mode<false, false, true>(glsl, aniso) : persistent_fn_mode<false, false, false>(glsl, aniso);
+}
+
+cudaError_t persistent_occupancy(int& occ, int threads, bool count, bool glsl, bool aniso, bool resident, bool full) {
+    const size_t smem = full ? (size_t)threads * 6 * sizeof(float) : 0;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persistent_fn(count, glsl, aniso, resident, full),
+                                                         threads, smem);
 }
 
 }  // namespace
 
 vrt_status persistent_grid(int device, const vrt_batch_config& cfg, bool count, bool glsl, bool aniso, bool resident,
-                           int& blocks, int& threads) {
+                           bool full, int& blocks, int& threads) {
     int sms = 0, occ = 0;
     threads = (int)cfg.warps_per_block * 32;
     VRT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    VRT_CUDA(persistent_occupancy(occ, threads, count, glsl, aniso, resident));
+    VRT_CUDA(persistent_occupancy(occ, threads, count, glsl, aniso, resident, full));
     occ = std::max(occ, 1);
     const int per_sm = (!count && cfg.blocks_per_sm) ? std::min<int>((int)cfg.blocks_per_sm, occ) : occ;
     blocks = sms * per_sm;
@@ -771,13 +771,8 @@ BatchParams make_params(const LaunchPlan& plan, const DevWorld* worlds, const Vi
 }
 
 vrt_status launch_resident(const BatchParams& p, int blocks, int threads, cudaStream_t stream) {
-    const size_t smem = pend_bytes(p, threads);
-    if (p.glsl && p.aniso)
-        persistent_kernel<false, true, true, true><<<blocks, threads, smem, stream>>>(p);
-    else if (p.glsl)
-        persistent_kernel<false, true, true><<<blocks, threads, smem, stream>>>(p);
-    else
-        persistent_kernel<false, false, true><<<blocks, threads, smem, stream>>>(p);
+    const PersistentFn fn = persistent_fn(false, p.glsl != 0, p.aniso != 0, true, p.full != 0);
+    fn<<<blocks, threads, pend_bytes(p, threads), stream>>>(p);
     VRT_CUDA(cudaGetLastError());
     return VRT_OK;
 }
@@ -785,19 +780,8 @@ vrt_status launch_resident(const BatchParams& p, int blocks, int threads, cudaSt
 vrt_status launch_persistent(const BatchParams& p, int blocks, int threads, bool count, cudaStream_t stream,
                              bool reset_counters) {
     VRT_CUDA(cudaMemsetAsync(p.queue, 0, reset_counters ? 64 : 4, stream));
-    const size_t smem = pend_bytes(p, threads);
-    if (count && p.glsl && p.aniso)
-        persistent_kernel<true, true, false, true><<<blocks, threads, smem, stream>>>(p);
-    else if (count && p.glsl)
-        persistent_kernel<true, true><<<blocks, threads, smem, stream>>>(p);
-    else if (count)
-        persistent_kernel<true, false><<<blocks, threads, smem, stream>>>(p);
-    else if (p.glsl && p.aniso)
-        persistent_kernel<false, true, false, true><<<blocks, threads, smem, stream>>>(p);
-    else if (p.glsl)
-        persistent_kernel<false, true><<<blocks, threads, smem, stream>>>(p);
-    else
-        persistent_kernel<false, false><<<blocks, threads, smem, stream>>>(p);
+    const PersistentFn fn = persistent_fn(count, p.glsl != 0, p.aniso != 0, false, p.full != 0);
+    fn<<<blocks, threads, pend_bytes(p, threads), stream>>>(p);
     VRT_CUDA(cudaGetLastError());
     return VRT_OK;
 }
@@ -925,10 +909,11 @@ vrt_status vrt_batch_create(vrt_world* const* worlds, uint32_t n_worlds, const v
     if (e != cudaSuccess) return fail(cuda_fail(e, "batch allocation"));
     b->d_counters = reinterpret_cast<unsigned long long*>(reinterpret_cast<uint8_t*>(b->d_queue) + 16);
     if ((st = refresh_worlds(b, 0)) != VRT_OK) return fail(st);
-    const bool glsl = b->plan.glsl, aniso = b->plan.aniso;
-    if ((st = persistent_grid(b->device, cfg, false, glsl, aniso, false, b->blocks, b->threads)) != VRT_OK)
+    const bool glsl = b->plan.glsl, aniso = b->plan.aniso, full = b->plan.full;
+    if ((st = persistent_grid(b->device, cfg, false, glsl, aniso, false, full, b->blocks, b->threads)) != VRT_OK)
         return fail(st);
-    if ((st = persistent_grid(b->device, cfg, true, glsl, aniso, false, b->blocks_count, b->threads_count)) != VRT_OK)
+    if ((st = persistent_grid(b->device, cfg, true, glsl, aniso, false, full, b->blocks_count, b->threads_count)) !=
+        VRT_OK)
         return fail(st);
     *out = b;
     return VRT_OK;

@@ -118,7 +118,7 @@ vrt_status plan_views(const vrt_view* views, uint32_t n, uint32_t n_worlds, cons
 // Grid of the persistent kernel: every SM, as many blocks of the launched instantiation
 // (counting, traversal mode, resident) as fit, or cfg.blocks_per_sm of them.
 vrt_status persistent_grid(int device, const vrt_batch_config& cfg, bool count, bool glsl, bool aniso, bool resident,
-                           int& blocks, int& threads);
+                           bool full, int& blocks, int& threads);
 BatchParams make_params(const LaunchPlan& plan, const DevWorld* worlds, const ViewDev* views,
                         const uint32_t* chunk_base, uint32_t* queue, vrt_hit* out);
 // Queue reset (the tile counter, and with reset_counters the launch counters: 64

@@ -184,7 +184,8 @@ extern "C" vrt_status vrt_render_views_static(vrt_world* const* worlds, uint32_t
     p.full = 0u;
     for (uint32_t i = 0; i < n_views; i++) p.full |= view_full_path(views[i]) ? 1u : 0u;
     int blocks = 0, threads = 0;
-    if ((st = persistent_grid(device, cfg, false, p.glsl != 0, p.aniso != 0, false, blocks, threads)) != VRT_OK)
+    if ((st = persistent_grid(device, cfg, false, p.glsl != 0, p.aniso != 0, false, p.full != 0, blocks, threads)) !=
+        VRT_OK)
         return st;
     // launch_persistent zeroes the queue counter and the launch counters first
     return launch_persistent(p, blocks, threads, false, stream);

@@ -90,6 +90,7 @@ struct Resident {
     uint32_t cap = 0;
     bool live = false, closing = false;
     uint32_t mode = 0;  // traversal mode of the launch's views (view_mode)
+    bool full = false;  // the launch takes views with the GPU renderer's whole path
     uint32_t n_views = 0, n_chunks = 0;
     uint32_t first_open = 0;       // slots below it are all finished
     std::vector<Request*> req;     // per view slot
@@ -437,12 +438,13 @@ bool resident_publish(vrt_server* sv, const std::vector<Request*>& rs, vrt_statu
     return true;
 }
 
-vrt_status resident_start(vrt_server* sv, uint32_t mode) {
+vrt_status resident_start(vrt_server* sv, uint32_t mode, bool full) {
     const bool glsl = (mode & VRT_VIEW_GLSL) != 0;
     Resident& R = sv->res;
     R.n_views = R.n_chunks = R.first_open = 0;
     R.closing = false;
     R.mode = mode;
+    R.full = full;
     R.n_hints = 0;
     VRT_CUDA(cudaStreamSynchronize(R.ctl));  // staging of the last launch is free again
     __atomic_store_n(R.mailbox, 0ull, __ATOMIC_SEQ_CST);
@@ -458,7 +460,7 @@ vrt_status resident_start(vrt_server* sv, uint32_t mode) {
     plan.tile_size_log2 = r;
     plan.glsl = glsl;
     plan.aniso = (mode & VRT_VIEW_GLSL_ANISO) != 0;
-    plan.full = true;  // requests with the GPU renderer's whole path may arrive while it runs
+    plan.full = full;  // this launch takes views with the GPU renderer's whole path
     BatchParams p = make_params(plan, sv->d_worlds, (const ViewDev*)R.views.ptr, (const uint32_t*)R.chunk_base.ptr,
                                 (uint32_t*)R.queue.ptr, (vrt_hit*)sv->arena);
     p.mailbox = R.d_mailbox;
@@ -571,17 +573,21 @@ bool resident_schedule(vrt_server* sv, std::unique_lock<std::mutex>& lk) {
         return true;
     }
     const uint32_t mode = view_mode(front->view);
-    if (R.live && (R.closing || mode != R.mode || R.n_views >= R.cap)) {
+    // a launch that takes whole-path views is its own instantiation: a running one that
+    // does not closes for the first such request, and the next launch takes every kind
+    if (R.live && (R.closing || mode != R.mode || (view_full_path(front->view) && !R.full) || R.n_views >= R.cap)) {
         if (!R.closing) resident_close(R);  // a new launch takes the next requests
         return false;
     }
     if (!R.live && !resident_idle(R)) return false;  // the last launch's records are still copying
     std::vector<Request*> rs;
     const uint32_t room = R.live ? R.cap - R.n_views : R.cap;
+    bool full = R.live && R.full;
     for (Request* r : sv->queue) {
         if (r->kind != 0 || view_mode(r->view) != mode || rs.size() >= sv->cfg.max_batch_requests ||
-            rs.size() >= room)
+            rs.size() >= room || (R.live && view_full_path(r->view) && !R.full))
             break;
+        full |= view_full_path(r->view);
         const uint32_t base = sv->pages.realloc(0, 0, r->pages);
         if (base == 0) break;  // budget full: wait for requests to finish
         r->page_base = base;
@@ -589,7 +595,7 @@ bool resident_schedule(vrt_server* sv, std::unique_lock<std::mutex>& lk) {
     }
     if (rs.empty()) return false;
     const bool fresh = !R.live;
-    vrt_status st = fresh ? resident_start(sv, mode) : VRT_OK;
+    vrt_status st = fresh ? resident_start(sv, mode, full) : VRT_OK;
     const bool ok = st == VRT_OK && resident_publish(sv, rs, st);
     if (ok && fresh) st = resident_launch(sv);
     if (ok && st == VRT_OK) {
@@ -803,7 +809,7 @@ vrt_status vrt_server_create(vrt_world* const* worlds, uint32_t n_worlds, const 
     }
     sv->resident = resident;
     for (int m = 0; m < 3; m++)
-        if ((st = persistent_grid(sv->device, sv->bcfg, false, m >= 1, m == 2, resident, sv->grid[m][0],
+        if ((st = persistent_grid(sv->device, sv->bcfg, false, m >= 1, m == 2, resident, false, sv->grid[m][0],
                                   sv->grid[m][1])) != VRT_OK)
             return fail(st);
     if (resident && (st = resident_init(sv)) != VRT_OK) return fail(st);
