@@ -1,12 +1,11 @@
-"""Parity at the full sizes of the benchmark workloads (GPU).
+"""Parity at the full sizes of the benchmark workloads (GPU): every record of every view
+(and every one of the 2^26 stress rays) against the CPU oracle.
 
-The oracle checks a seeded sample of whole views (and of the stress rays); every
-record is covered by checks that do not depend on size: the batched persistent
-launch and the one-launch-per-view kernel give identical bytes, a second launch
-repeats them exactly, and the record invariants hold (a secondary record is NO_RAY
-exactly where the path ended before it, hits lie inside their world with a non-zero
-material and a finite t, misses carry the sentinel, step counts respect the cap,
-primary tags are pixel indices).
+On top of that, size-independent checks: the batched persistent launch and the
+one-launch-per-view kernel give identical bytes, a second launch repeats them exactly,
+and the record invariants hold (a secondary record is NO_RAY exactly where the path
+ended before it, hits lie inside their world with a non-zero material and a finite t,
+misses carry the sentinel, step counts respect the cap, primary tags are pixel indices).
 """
 import numpy as np
 import pytest
@@ -80,60 +79,66 @@ def check_invariants(b, rec, wl):
             assert bool(torch.equal(rv[k, :, 3] == -1, ended)), f"view {i}: record {k} NO_RAY mismatch"
 
 
-def check_oracle_sample(b, rec, wl, picks):
+def check_oracle_all(b, rec, wl):
+    """Every view against the oracle (on all host cores), views taken in batch order so each
+    world is uploaded to the oracle once."""
+    host = rec.cpu().numpy().view(v.HIT_DTYPE)
     oracles = {}
-    for i in picks:
-        vw = wl.views[i]
+    records = 0
+    for i, vw in enumerate(wl.views):
         if vw.world not in oracles:
+            for o in oracles.values():
+                o.close()
             o = OracleWorld(wl.worlds[vw.world].sectors)
             o.upload(wl.worlds[vw.world])
             oracles = {vw.world: o}
         want = oracle_view(oracles[vw.world], vw)
         a, e = int(b.offsets[i]), int(b.offsets[i + 1])
-        got = rec[a * 16:e * 16].cpu().numpy().view(v.HIT_DTYPE).reshape(want.shape)
+        got = host[a:e].reshape(want.shape)
         for k in range(want.shape[0]):
             assert_hits_equal(got[k], want[k])
+        records += want.size
+    for o in oracles.values():
+        o.close()
+    assert records == b.total_records
 
 
-def run_config(wl, n_sample, seed):
+def run_config(wl):
     worlds = load(wl)
     b, rec = launch_both(wl, worlds)
     check_invariants(b, rec, wl)
-    rng = np.random.default_rng(seed)
-    picks = sorted(rng.choice(len(wl.views), size=min(n_sample, len(wl.views)), replace=False).tolist(),
-                   key=lambda i: wl.views[i].world)
-    check_oracle_sample(b, rec, wl, picks)
+    check_oracle_all(b, rec, wl)
     b.close()
     for w in worlds:
         w.close()
 
 
 def test_uneven_batch_full_size(gpu):
-    """128 worlds, 1,119 views, 352.9 M records; 24 views checked against the oracle."""
-    run_config(W.uneven_batch(), n_sample=24, seed=5)
+    """128 worlds, 1,119 views, 352.9 M records, every one against the oracle."""
+    run_config(W.uneven_batch())
 
 
 @pytest.mark.parametrize("aniso", [False, True])
 def test_uneven_batch_full_size_glsl_modes(gpu, aniso):
     """The same batch in the GLSL traversal mode, with and without anisotropic LODs:
-    batched equals per-view, the invariants hold, 8 views checked against the oracle."""
+    batched equals per-view, the invariants hold, every record equals the oracle's."""
     wl = W.uneven_batch()
     for vw in wl.views:
         vw.flags |= v.VIEW_GLSL | (v.capi.VIEW_GLSL_ANISO if aniso else 0)
-    run_config(wl, n_sample=8, seed=15 + aniso)
+    run_config(wl)
 
 
 def test_large_world_full_size(gpu):
-    """2048x256x2048 world, 64 views at 1920x1080 with shadow rays (265 M records); 3 views
-    checked against the oracle."""
-    run_config(W.large_world(), n_sample=3, seed=6)
+    """2048x256x2048 world, 64 views at 1920x1080 with shadow rays (265 M records), every one
+    against the oracle."""
+    run_config(W.large_world())
 
 
 def test_incoherent_full_size_and_stress_rays(gpu):
-    """1024^3 world: 1280x720 with 4 diffuse bounces against the oracle, and 2^26 random
-    rays cast on the device, 1 M of them (four blocks) against the oracle."""
+    """1024^3 world: 1280x720 with 4 diffuse bounces against the oracle, and all 2^26 random
+    rays cast on the device against the oracle."""
     wl = W.incoherent()
-    run_config(wl, n_sample=1, seed=7)
+    run_config(wl)
     d = wl.worlds[0]
     w = v.World(d.sectors, brick_capacity=d.n_bricks + 64)
     w.upload(d)
@@ -147,10 +152,12 @@ def test_incoherent_full_size_and_stress_rays(gpu):
     w.cast_device(dr, n, again)
     torch.cuda.synchronize()
     assert torch.equal(hits, again)
+    del again
+    host = hits.cpu().numpy().view(v.HIT_DTYPE)
     o = OracleWorld(d.sectors)
     o.upload(d)
-    for first in (0, 1 << 20, 37 << 20, n - (1 << 18)):
-        sub = rays[first:first + (1 << 18)]
-        got = hits[first * 16:(first + len(sub)) * 16].cpu().numpy().view(v.HIT_DTYPE)
-        assert_hits_equal(got, o.cast(sub))
+    block = 1 << 23
+    for first in range(0, n, block):
+        assert_hits_equal(host[first:first + block], o.cast(rays[first:first + block]))
+    o.close()
     w.close()
