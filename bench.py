@@ -649,9 +649,11 @@ def surface_points(w, edge, n, seed):
 
 
 def load_serving_worlds(v, datas, dev):
+    """Resident worlds with a quarter of their bricks (and at least 4096 slots) of pool room for
+    the edits, which relocate the sectors they grow."""
     worlds, edges, surf = [], [], []
     for i, d in enumerate(datas):
-        w = v.World(d.sectors, brick_capacity=d.n_bricks + 4096, device=dev)
+        w = v.World(d.sectors, brick_capacity=d.n_bricks + max(4096, d.n_bricks // 4), device=dev)
         w.upload(d)
         worlds.append(w)
         edges.append(d.sectors[0] * 32)
@@ -701,6 +703,7 @@ def run_serving(args, dev):
                                 f"{args.serve_min_requests} renders per rate for the p99",
             "mode": "resident", "rates": modes["resident"]["rates"],
             "oracle_replay": modes["resident"]["oracle_replay"], "launches": modes["launches"],
+            "pool_compactions": modes["resident"]["pool_compactions"],
             "latency": "submit to records in pinned host memory, server clock"}
 
 
@@ -855,7 +858,8 @@ def serve_sweep(args, v, datas, worlds, edges, surf, resident, reserve):
         o.close()
     for b in bufs:
         b.close()
-    return {"rates": out, "oracle_replay": replay, "launches": sum(r["launches"] for r in out)}
+    return {"rates": out, "oracle_replay": replay, "launches": sum(r["launches"] for r in out),
+            "pool_compactions": int(sum(w.stats()["compactions"] for w in worlds))}
 
 
 def edit_latency(v, worlds, edges, surf):

@@ -199,6 +199,8 @@ typedef struct vrt_world_stats {
     uint32_t brick_capacity;    /* slots in the device pool */
     uint32_t free_ranges;       /* FreeList::FreeRanges.size(): the gaps between live ranges and the tail */
     uint64_t device_bytes;      /* device memory held by the world */
+    uint32_t compactions;       /* pool compactions so far: vrt_world_defrag, and edits that ran out of room */
+    uint32_t reserved;
 } vrt_world_stats;
 
 /* ---- library ---- */

@@ -112,7 +112,7 @@ class WorldDesc(C.Structure):
 class WorldStats(C.Structure):
     _fields_ = [("sectors_x", C.c_uint32), ("sectors_y", C.c_uint32), ("sectors_z", C.c_uint32),
                 ("allocated_bricks", C.c_uint32), ("brick_capacity", C.c_uint32), ("free_ranges", C.c_uint32),
-                ("device_bytes", C.c_uint64)]
+                ("device_bytes", C.c_uint64), ("compactions", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class SectorStream(C.Structure):

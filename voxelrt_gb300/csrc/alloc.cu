@@ -76,25 +76,33 @@ __global__ void __launch_bounds__(kScanThreads)
     }
 }
 
-// Compaction, pass 2: one warp per sector copies its bricks from the old pool to their
-// packed slots in the new pool and rewrites its base.
-__global__ void compact_copy_kernel(SectorRec* __restrict__ sectors, uint32_t n, const uint32_t* __restrict__ new_base,
-                                    const uint8_t* __restrict__ old_payload, const uint4* __restrict__ old_codes,
-                                    const uint64_t* __restrict__ old_cells, uint8_t* __restrict__ payload,
-                                    uint4* __restrict__ codes, uint64_t* __restrict__ cells) {
-    const uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (s >= n) return;  // whole warps
+// Compaction, pass 2: one block per sector copies its bricks (68 16-byte words each:
+// payload, voxel codes, cell masks) from the old pool to their packed slots in the new
+// pool, every thread a strided share of the words, and rewrites the sector's base.
+constexpr uint32_t kCopyThreads = 256;
+__global__ void __launch_bounds__(kCopyThreads)
+    compact_copy_kernel(SectorRec* __restrict__ sectors, uint32_t n, const uint32_t* __restrict__ new_base,
+                        const uint8_t* __restrict__ old_payload, const uint4* __restrict__ old_codes,
+                        const uint64_t* __restrict__ old_cells, uint8_t* __restrict__ payload,
+                        uint4* __restrict__ codes, uint64_t* __restrict__ cells) {
+    const uint32_t s = blockIdx.x, t = threadIdx.x;
+    if (s >= n) return;
     const SectorRec rec = sectors[s];
     const uint32_t cnt = (uint32_t)(__popc(rec.mask_lo) + __popc(rec.mask_hi));
+    if (cnt == 0) return;  // base 0 already (an empty sector's base is 0)
     const uint32_t nb = new_base[s];
-    for (uint32_t k = 0; k < cnt; k++) {
+    for (uint32_t c = t; c < cnt * 68u; c += kCopyThreads) {
+        const uint32_t k = c / 68u, w = c - k * 68u;
         const size_t src = (size_t)rec.base + k, dst = (size_t)nb + k;
-        reinterpret_cast<uint4*>(payload + dst * 512)[lane] = reinterpret_cast<const uint4*>(old_payload + src * 512)[lane];
-        codes[dst * 32 + lane] = old_codes[src * 32 + lane];
-        if (lane < 4)
-            reinterpret_cast<uint4*>(cells + dst * 8)[lane] = reinterpret_cast<const uint4*>(old_cells + src * 8)[lane];
+        if (w < 32)
+            reinterpret_cast<uint4*>(payload + dst * 512)[w] = reinterpret_cast<const uint4*>(old_payload + src * 512)[w];
+        else if (w < 64)
+            codes[dst * 32 + (w - 32)] = old_codes[src * 32 + (w - 32)];
+        else
+            reinterpret_cast<uint4*>(cells + dst * 8)[w - 64] = reinterpret_cast<const uint4*>(old_cells + src * 8)[w - 64];
     }
-    if (lane == 0) sectors[s].base = cnt ? nb : 0u;
+    __syncthreads();  // every thread has read the old base
+    if (t == 0) sectors[s].base = nb;
 }
 
 }  // namespace
@@ -159,8 +167,8 @@ vrt_status world_compact(vrt_world* w, uint32_t capacity, cudaStream_t stream) {
     }
     const uint32_t n = w->num_sectors();
     compact_scan_kernel<<<1, kScanThreads, 0, stream>>>(w->d_sectors, n, new_base, w->d_alloc, capacity);
-    compact_copy_kernel<<<(n + 7) / 8, 256, 0, stream>>>(w->d_sectors, n, new_base, w->d_payload, w->d_codes,
-                                                         w->d_cells, payload, codes, cells);
+    compact_copy_kernel<<<n, kCopyThreads, 0, stream>>>(w->d_sectors, n, new_base, w->d_payload, w->d_codes,
+                                                        w->d_cells, payload, codes, cells);
     e = cudaGetLastError();
     if (e == cudaSuccess) {
         std::swap(w->d_codes, codes);
@@ -178,6 +186,7 @@ vrt_status world_compact(vrt_world* w, uint32_t capacity, cudaStream_t stream) {
     if (e != cudaSuccess) return cuda_fail(e, "compact brick pool");
     if (st != VRT_OK) return st;
     w->host_stale = true;
+    w->compactions++;
     VRT_CUDA(cudaEventRecord(w->edited, stream));
     return refresh_host_mirror(w);
 }

@@ -513,6 +513,8 @@ vrt_status vrt_world_get_stats(const vrt_world* cw, vrt_world_stats* out) {
     out->allocated_bricks = w->arena.allocated();
     out->brick_capacity = w->capacity;
     out->free_ranges = (uint32_t)w->arena.num_ranges();
+    out->compactions = w->compactions;
+    out->reserved = 0;
     // sector records, brick table, group masks, per slot 512 B payload + 512 B codes +
     // 64 B cell masks, and the scratch buffers
     out->device_bytes = (uint64_t)w->num_sectors() * sizeof(SectorRec) + (uint64_t)w->num_brick_positions() * 4 +

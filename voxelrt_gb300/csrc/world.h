@@ -127,6 +127,7 @@ struct vrt_world {
     cudaEvent_t edited = nullptr;  // recorded behind the last device edit
     bool host_stale = false;    // slots / arena / h_table predate device edits
     uint64_t top_bound = 0;     // upper bound of d_alloc->top without reading it
+    uint32_t compactions = 0;   // pool compactions so far (vrt_world_defrag and edits)
 
     uint32_t num_sectors() const { return sx * sy * sz; }
     size_t num_brick_positions() const { return (size_t)num_sectors() * 64; }
