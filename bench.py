@@ -61,7 +61,8 @@ def parse(argv=None):
     ap.add_argument("--glsl", action="store_true",
                     help="trace every view in the GLSL mode (the GPU renderer's rayCast) instead of the CPU traversal")
     ap.add_argument("--aniso", action="store_true", help="the GLSL mode with anisotropic LODs (implies --glsl)")
-    ap.add_argument("--serve-rates", default="50,200,1000,2000", help="render requests per second to sweep")
+    ap.add_argument("--serve-rates", default="50,200,1000,2000,8000,16000",
+                    help="render requests per second to sweep (16000 puts the host link near its limit)")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="duration of each arrival-rate run, at least")
     ap.add_argument("--serve-min-requests", type=int, default=400,
                     help="renders per arrival rate, at least (longer runs at low rates)")

@@ -122,3 +122,73 @@ def test_edit_returns_before_the_device_runs_it(gpu):
     trace_check(w, o, seed=6)
     w.close()
     o.close()
+
+
+def test_host_planned_sync_after_device_edits(gpu):
+    """Device edits, then a host-planned dirty-brick sync, then more device edits: the host
+    mirror is rebuilt from the device before the sync plans, the device's bump pointer
+    restarts behind the sync, and the world stays the oracle's throughout."""
+    rng = np.random.default_rng(17)
+    data = v.synth_mix(96, seed=31)
+    w = v.World(data.sectors, brick_capacity=data.n_bricks + 2048)
+    w.upload(data)
+    o = OracleWorld(data.sectors)
+    o.upload(data)
+    for _ in range(3):
+        for _ in range(4):
+            e = surface_edits(rng, w, 2)
+            w.edit(e, wait=False)
+            o.edit(e)
+        # rewrite a few sectors from the host: new masks, some bricks dirty
+        k = 5
+        pick = rng.choice(len(data.sector_idx), k, replace=False)
+        idx = data.sector_idx[pick]
+        masks = np.array([int(o.sector_mask(int(i))) for i in idx], np.uint64)
+        new_masks = masks.copy()
+        dirty = np.zeros(k, np.uint64)
+        bricks = []
+        for j in range(k):
+            m = int(masks[j])
+            add = int(rng.integers(0, 1 << 63)) & ~m & int(rng.integers(0, 1 << 63))
+            nm = (m & ~(m & int(rng.integers(0, 1 << 63)))) | add
+            d = nm & int(rng.integers(0, 1 << 63)) | add
+            new_masks[j], dirty[j] = nm, d
+            for _ in range(bin(d).count("1")):
+                bricks.append((rng.integers(1, 256, 512) * (rng.random(512) < 0.2)).astype(np.uint8))
+        b = np.stack(bricks) if bricks else None
+        w.sync_sectors(idx, new_masks, b, dirty)
+        o.sync_sectors(idx, new_masks, b, dirty)
+        assert_worlds_equal(w, o)
+    trace_check(w, o, seed=8)
+    w.close()
+    o.close()
+
+
+def test_save_after_edits_and_defrag(gpu, tmp_path):
+    """A world edited on the device and compacted saves to cvox and loads back equal."""
+    rng = np.random.default_rng(23)
+    data = v.synth_mix(96, seed=41)
+    w = v.World(data.sectors, brick_capacity=data.n_bricks + 1024)
+    w.upload(data)
+    o = OracleWorld(data.sectors)
+    o.upload(data)
+    for _ in range(12):
+        e = surface_edits(rng, w, 2)
+        w.edit(e, wait=False)
+        o.edit(e)
+    w.defrag(capacity=data.n_bricks * 2)
+    st = w.stats()
+    assert st["brick_capacity"] >= data.n_bricks * 2 and st["compactions"] >= 1 and st["free_ranges"] == 1
+    p = tmp_path / "edited.cvox"
+    w.save_cvox(p)
+    w2 = v.World(data.sectors)
+    w2.load_cvox(p)
+    assert_worlds_equal(w2, o)
+    trace_check(w2, o, seed=9)
+    # an empty world compacts to nothing
+    e = v.World((2, 2, 2))
+    e.defrag()
+    assert e.stats()["allocated_bricks"] == 0
+    for x in (w, w2, e):
+        x.close()
+    o.close()
