@@ -20,3 +20,21 @@ def test_mode_flags_reach_every_view():
         wl = bench.build_workload("uneven_batch", 0, args)
         assert wl.views and all((vw.flags & (v.VIEW_GLSL | v.capi.VIEW_GLSL_ANISO)) == want for vw in wl.views)
         assert bench.traversal_name(args) == {0: "cpu", v.VIEW_GLSL: "glsl"}.get(want, "glsl_aniso")
+
+
+def test_reference_arm_loads_no_product_library(tmp_path):
+    """The reference arm times the CPU restatement on inputs from the host-only generators:
+    its process maps the oracle and libvrt_synth.so, never the product library libvrt.so."""
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(bench.__file__).resolve().parent
+    code = ("import sys, json; sys.argv = ['bench.py', '--impl', 'reference', '--worlds', '2', '--max-views', '1', "
+            "'--steps', '1', '--warmup', '0', '--cpu-seconds', '0.1']; import bench; bench.main(); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('MAPS', 'libvrt.so' in maps, 'libvrt_synth.so' in maps, 'libvrt_oracle.so' in maps)")
+    r = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = [ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1]
+    assert '"impl": "reference"' in line
+    assert "MAPS False True True" in r.stdout
