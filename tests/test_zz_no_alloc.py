@@ -39,6 +39,8 @@ def seeded_views(worlds, rng, n, glsl=False, aniso=False):
             views.append(v.make_view(cam, shadow_dir=(0.3, 0.8, 0.5), **kw))
         elif i % 4 == 2:
             views.append(v.make_view(cam, n_bounces=2, **kw))
+        elif i % 8 == 7:  # the GPU renderer's whole path: sun rays among the bounces
+            views.append(v.make_view(cam, n_bounces=3, shadow_dir=(0.3, 0.8, 0.5), **kw))
         else:
             views.append(v.make_view(cam, **kw))
     return views
