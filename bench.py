@@ -72,6 +72,9 @@ def parse(argv=None):
                     help="worlds (the largest and smallest among them) whose renders are replayed on the oracle")
     ap.add_argument("--serve-check-cap", type=int, default=200,
                     help="replayed renders per arrival rate and mode, at most")
+    ap.add_argument("--l2-persist", action="store_true",
+                    help="create the workload's worlds with VRT_WORLD_L2_PERSIST (an L2 access-policy window "
+                         "over the brick table of a batch's single such world)")
     ap.add_argument("--worlds", type=int, default=128, help="uneven_batch: number of worlds")
     ap.add_argument("--max-views", type=int, default=16, help="uneven_batch: views per world, at most")
     ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
@@ -371,8 +374,9 @@ class GpuEngine:
         torch.cuda.set_device(local)
         self.wl = build_workload(args.workload, rank, args, world_size)
         self.worlds = []
+        flags = 1 if getattr(args, "l2_persist", False) else 0  # VRT_WORLD_L2_PERSIST
         for d in self.wl.worlds:
-            w = v.World(d.sectors, brick_capacity=d.n_bricks + 64, device=local)
+            w = v.World(d.sectors, brick_capacity=d.n_bricks + 64, device=local, flags=flags)
             w.upload(d)
             self.worlds.append(w)
         self.cfg, self.cfg_src = autotune.lookup(self.wl.name)
@@ -459,7 +463,8 @@ class GpuEngine:
                 "l2": "inputs larger than L2 (brick pools of all worlds)",
                 "batch_config": autotune.describe(self.cfg), "batch_config_source": self.cfg_src,
                 "launch": "persistent kernel + queue reset, CUDA graph replay",
-                "traversal": traversal_name(self.args)}
+                "traversal": traversal_name(self.args),
+                "l2_persist": bool(getattr(self.args, "l2_persist", False))}
 
     def extras(self):
         """Rank 0's further results (parity, roofline inputs, CPU baseline, sub-results,

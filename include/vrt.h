@@ -189,8 +189,13 @@ typedef struct vrt_world_desc {
     uint32_t flags;                           /* VRT_WORLD_* */
 } vrt_world_desc;
 
-/* Pin the sector table and brick-mask array in L2 with a persisting
- * access-policy window on streams passed to cast/render calls. */
+/* Keep the world's brick table (the mask level every DDA step reads, 4 bytes per brick
+ * position) persisting in L2: casts, view renders and batch launches whose batch holds
+ * exactly one such world carry an L2 access-policy window over it on the caller's stream
+ * (not on the legacy default stream, whose attributes cannot be set); the stream's own
+ * window is restored after the launch.  Creating such a world raises this process's
+ * persisting-L2 set-aside (cudaLimitPersistingL2CacheSize) to cover the table, up to the
+ * device's maximum. */
 #define VRT_WORLD_L2_PERSIST 1u
 
 typedef struct vrt_world_stats {
@@ -437,9 +442,8 @@ vrt_status vrt_batch_measure(vrt_batch* batch, vrt_hit* hits_device, void* strea
  * table, tile-queue counter) lives in one fixed 152.5 KiB device array that every GPU
  * loading the library holds until the process exits, so a call takes at most 256
  * worlds and 1024 views (VRT_ERR_INVALID_ARG beyond).  The first call on a device
- * looks up that array's address; make it before any stream capture.  All calls
- * share the array: calls whose launches overlap on the GPU race, so order them on
- * one stream.  The world and view tables are staged in library-owned host tables,
+ * looks up that array's address.  All calls share the array: calls whose launches
+ * overlap on the GPU race, so order them on one stream.  The world and view tables are staged in library-owned host tables,
  * so a call first waits on the host until the table copies of the previous call on
  * the same device have run.  The caller's current device is the same when the call
  * returns.  Records are laid out as for vrt_batch (views back to back). */

@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 import voxelrt_gb300 as v
+from oracle.oracle import OracleWorld
 from tests.helpers import (assert_hits_equal, both_worlds, cfg0_camera, cfg0_world, dense_to_stream, make_rays,
                            single_voxel_world)
 
@@ -243,3 +244,38 @@ def test_concurrent_large_casts_on_two_streams(cfg0):
             assert torch.equal(a, b)
     sub = rays[1][:1 << 16]
     assert_hits_equal(mixed[1][:sub.size * 16].cpu().numpy().view(v.HIT_DTYPE), o.cast(sub))
+
+
+def test_l2_persisting_world_matches_oracle(gpu):
+    """A VRT_WORLD_L2_PERSIST world: casts, views, paths and a single-world batch on a
+    non-default stream carry the L2 window over its brick table and give the oracle's
+    records; the stream's own (empty) window is restored after each launch."""
+    torch = pytest.importorskip("torch")
+    data = cfg0_world()
+    w = v.World(data.sectors, flags=v.capi.WORLD_L2_PERSIST)
+    w.upload(data)
+    o = OracleWorld(data.sectors)
+    o.upload(data)
+    stream = torch.cuda.Stream()
+    cam = cfg0_camera(160, 90)
+    assert_hits_equal(w.render_view(cam, stream=stream), o.render_view(cam))
+    rays = v.random_rays((256, 256, 256), seed=12, n=300_000)  # above the persistent-cast size
+    assert_hits_equal(w.cast(rays, stream=stream), o.cast(rays))
+    view = v.make_view(cam, shadow_dir=(0.3, 0.8, 0.5))
+    got = v.render_path(w, view, stream=stream)
+    want = np.stack(o.render_view_shadow(cam, np.array([0.3, 0.8, 0.5], np.float32)))
+    for k in range(2):
+        assert_hits_equal(got[k], want[k])
+    b = v.Batch([w], [view, v.make_view(cam, n_bounces=2)])
+    rec = b.run(stream=stream)
+    assert_hits_equal(b.view_hits(rec, 0), want)
+    assert_hits_equal(b.view_hits(rec, 1), o.render_view_bounces(cam, 2))
+    hits = torch.empty(b.total_records * 16, dtype=torch.uint8, device="cuda")
+    b.launch(hits, stream, graph=True)
+    stream.synchronize()
+    assert np.array_equal(hits.cpu().numpy().view(v.HIT_DTYPE), rec)
+    b.close()
+    with pytest.raises(v.VrtError):
+        v.World((1, 1, 1), flags=2)  # unknown flag
+    w.close()
+    o.close()

@@ -71,6 +71,7 @@ class BatchStats(C.Structure):
                 ("hits", C.c_uint64)]
 
 
+WORLD_L2_PERSIST = 1  # VRT_WORLD_L2_PERSIST: the brick table persisting in L2 on the caller's streams
 VIEW_SHADOW = 1
 VIEW_GLSL = 2        # the GPU renderer's rayCast (VoxelTraversal.glsl) instead of the CPU traversal
 CAST_GLSL = 1

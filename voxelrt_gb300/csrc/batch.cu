@@ -594,6 +594,9 @@ namespace {
 
 vrt_status launch_view_path(vrt_world* w, const ViewDev& v, bool glsl, vrt_hit* hits, cudaStream_t stream) {
     dim3 block(8, 8), grid((v.width + 7) / 8, (v.height + 7) / 8);
+    L2Window l2;
+    vrt_status st = l2.enter(w, stream);
+    if (st != VRT_OK) return st;
     uint4* out = reinterpret_cast<uint4*>(hits);
     if (glsl && v.aniso)
         view_path_kernel<true, true><<<grid, block, 0, stream>>>(w->dev(), v, out);
@@ -812,6 +815,9 @@ struct vrt_batch {
     // graph
     cudaGraphExec_t graph_exec = nullptr;
     vrt_hit* graph_hits = nullptr;
+    // the world whose brick table the batch's launches keep in L2: the batch's only
+    // VRT_WORLD_L2_PERSIST world (a stream carries one access-policy window), or none
+    vrt_world* l2_world = nullptr;
 };
 
 namespace {
@@ -828,6 +834,9 @@ vrt_status refresh_worlds(vrt_batch* b, cudaStream_t stream) {
 }
 
 vrt_status enqueue_batch(vrt_batch* b, vrt_hit* hits, cudaStream_t stream, bool count) {
+    L2Window l2;
+    vrt_status st = l2.enter(b->l2_world, stream);
+    if (st != VRT_OK) return st;
     BatchParams p = make_params(b->plan, b->d_worlds, b->d_views, b->d_chunk_base, b->d_queue, hits);
     return count ? launch_persistent(p, b->blocks_count, b->threads_count, true, stream)
                  : launch_persistent(p, b->blocks, b->threads, false, stream);
@@ -891,6 +900,13 @@ vrt_status vrt_batch_create(vrt_world* const* worlds, uint32_t n_worlds, const v
     }
     b->device = worlds[0]->device;
     b->worlds.assign(worlds, worlds + n_worlds);
+    uint32_t n_l2 = 0;
+    for (uint32_t i = 0; i < n_worlds; i++)
+        if (worlds[i]->flags & VRT_WORLD_L2_PERSIST) {
+            n_l2++;
+            b->l2_world = worlds[i];
+        }
+    if (n_l2 != 1) b->l2_world = nullptr;
     b->views.assign(views, views + n_views);
     auto fail = [&](vrt_status s) {
         vrt_batch_destroy(b);
@@ -1068,6 +1084,8 @@ vrt_status vrt_batch_run(vrt_batch* b, vrt_hit* hits_host, void* stream_) {
         b->part_done.push_back(e);
     }
     auto first_record = [&](size_t v) { return v < nv ? plan.views[v].out_base : plan.records; };
+    L2Window l2;
+    if ((st = l2.enter(b->l2_world, stream)) != VRT_OK) return st;
     for (size_t k = 0; k < parts; k++) {
         const size_t a = cut[k], e = cut[k + 1];
         BatchParams p = make_params(plan, b->d_worlds, b->d_views, b->d_chunk_base, b->d_queue,

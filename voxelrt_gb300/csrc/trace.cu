@@ -135,6 +135,9 @@ vrt_status launch_render(vrt_world* w, const vrt_camera* cam, uint32_t max_iters
                          cudaStream_t stream) {
     dim3 block(8, 8);
     dim3 grid((cam->width + 7) / 8, (cam->height + 7) / 8);
+    L2Window l2;
+    vrt_status st = l2.enter(w, stream);
+    if (st != VRT_OK) return st;
     render_view_kernel<<<grid, block, 0, stream>>>(w->dev(), *cam, eff_iters(max_iters),
                                                    reinterpret_cast<uint4*>(hits));
     VRT_CUDA(cudaGetLastError());
@@ -158,6 +161,9 @@ vrt_status launch_cast(vrt_world* w, const vrt_ray* rays, uint32_t n, const vrt_
     uint4* o4 = reinterpret_cast<uint4*>(hits);
     uint32_t iters = eff_iters(p->max_iters, glsl);
     if (coarse) iters = std::min<uint32_t>(iters, VRT_GLSL_COARSE_MAX_ITERS);
+    L2Window l2;
+    vrt_status st = l2.enter(w, stream);
+    if (st != VRT_OK) return st;
     if (n < kCastPersistentMin) {
         auto kernel = glsl ? (aniso ? cast_kernel<true, true> : cast_kernel<true>) : cast_kernel<false>;
         kernel<<<(n + 255) / 256, 256, 0, stream>>>(w->dev(), r4, n, p->world_origin[0], p->world_origin[1],

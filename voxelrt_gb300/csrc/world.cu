@@ -37,7 +37,45 @@ vrt_status world_enter(vrt_world* world) {
     return VRT_OK;
 }
 
+vrt_status L2Window::enter(const vrt_world* w, cudaStream_t s) {
+    if (!w || !(w->flags & VRT_WORLD_L2_PERSIST) || !s || w->l2_window_bytes == 0) return VRT_OK;
+    VRT_CUDA(cudaStreamGetAttribute(s, cudaStreamAttributeAccessPolicyWindow, &prev));
+    cudaStreamAttrValue a{};
+    a.accessPolicyWindow.base_ptr = w->d_bricks;
+    a.accessPolicyWindow.num_bytes = w->l2_window_bytes;
+    a.accessPolicyWindow.hitRatio = w->l2_hit_ratio;
+    a.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    a.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    VRT_CUDA(cudaStreamSetAttribute(s, cudaStreamAttributeAccessPolicyWindow, &a));
+    stream = s;
+    set = true;
+    return VRT_OK;
+}
+
+L2Window::~L2Window() {
+    if (set) cudaStreamSetAttribute(stream, cudaStreamAttributeAccessPolicyWindow, &prev);
+}
+
 namespace {
+
+// The window of a VRT_WORLD_L2_PERSIST world: its brick table, up to the device's largest
+// window, with the context's persisting L2 set-aside raised to cover it (up to the
+// device's maximum; the set-aside lasts as long as this process's context).
+vrt_status setup_l2_window(vrt_world* w) {
+    int max_window = 0, max_persist = 0;
+    VRT_CUDA(cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, w->device));
+    VRT_CUDA(cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, w->device));
+    if (max_window <= 0 || max_persist <= 0) return VRT_OK;  // no persisting L2: the flag does nothing
+    const size_t table = w->num_brick_positions() * sizeof(uint32_t);
+    w->l2_window_bytes = std::min(table, (size_t)max_window);
+    size_t limit = 0;
+    VRT_CUDA(cudaDeviceGetLimit(&limit, cudaLimitPersistingL2CacheSize));
+    const size_t want = std::min(w->l2_window_bytes, (size_t)max_persist);
+    if (want > limit) VRT_CUDA(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want));
+    VRT_CUDA(cudaDeviceGetLimit(&limit, cudaLimitPersistingL2CacheSize));
+    w->l2_hit_ratio = (float)std::min(1.0, (double)limit / (double)w->l2_window_bytes);
+    return VRT_OK;
+}
 
 // ---------------------------------------------------------------------------
 // Brick operations, one warp per brick.
@@ -418,6 +456,10 @@ vrt_status vrt_world_create(const vrt_world_desc* desc, vrt_world** out) {
         set_error("world extent must be 1..64 x 1..32 x 1..64 sectors");
         return VRT_ERR_INVALID_ARG;
     }
+    if (desc->flags & ~VRT_WORLD_L2_PERSIST) {
+        set_error("unknown world flags");
+        return VRT_ERR_INVALID_ARG;
+    }
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev == 0) {
@@ -462,6 +504,7 @@ vrt_status vrt_world_create(const vrt_world_desc* desc, vrt_world** out) {
     }
     if (st == VRT_OK) st = grow_pool(w, desc->brick_capacity ? desc->brick_capacity : 4096, 0);
     if (st == VRT_OK) st = alloc_publish(w, 0);
+    if (st == VRT_OK && (w->flags & VRT_WORLD_L2_PERSIST)) st = setup_l2_window(w);
     if (st == VRT_OK && cudaStreamSynchronize(0) != cudaSuccess) st = cuda_fail(cudaGetLastError(), "create world");
     if (st != VRT_OK) {
         vrt_world_destroy(w);

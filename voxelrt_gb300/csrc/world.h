@@ -95,6 +95,9 @@ struct vrt_world {
     uint32_t sx = 0, sy = 0, sz = 0;
     uint32_t flags = 0;
     std::mutex mu;
+    // VRT_WORLD_L2_PERSIST: the access-policy window over the brick table
+    size_t l2_window_bytes = 0;
+    float l2_hit_ratio = 0.0f;
 
     // host mirror of the allocation state (BrickSlotAllocator, GpuRenderer.cpp:23)
     std::vector<vrt::SectorSlots> slots;
@@ -160,6 +163,18 @@ struct vrt_world {
 namespace vrt {
 // Make `world` current on the calling thread.
 vrt_status world_enter(vrt_world* world);
+
+// While alive, kernels launched on `stream` carry an L2 access-policy window that keeps the
+// brick table of a VRT_WORLD_L2_PERSIST world persisting in L2 (the table is the mask
+// level every DDA step reads); the stream's previous window comes back when it ends.  A
+// no-op for other worlds and for the legacy default stream, whose attributes cannot be set.
+struct L2Window {
+    cudaStream_t stream = nullptr;
+    bool set = false;
+    cudaStreamAttrValue prev{};
+    vrt_status enter(const vrt_world* w, cudaStream_t s);
+    ~L2Window();
+};
 
 // alloc.cu (callers hold world->mu)
 // Rebuild the host mirror (slots, arena, h_table) from the device after device edits.
