@@ -64,6 +64,12 @@ def test_host_logic_without_gpu():
     d = np.array(cam.d0[:]) + 320 * np.array(cam.du[:]) + 180 * np.array(cam.dv[:])
     tgt = np.array([0.0, -120.0, 168.0])
     assert np.allclose(d / np.linalg.norm(d), tgt / np.linalg.norm(tgt), atol=1e-6)
+    # unknown world flags are refused before any device is touched
+    try:
+        v.World((1, 1, 1), flags=v.capi.WORLD_L2_PERSIST << 1)
+        raise AssertionError("unknown flag accepted")
+    except v.VrtError as e:
+        assert e.status == v.capi.VRT_ERR_INVALID_ARG and "flags" in str(e)
     # no device: creating a world fails with a status, not a crash
     import torch
     if not torch.cuda.is_available():
