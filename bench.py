@@ -443,11 +443,15 @@ class GpuEngine:
         self.batch.run(host.array, self.stream)
         ke = max(1, min(self.args.steps, 5))
         sync()
+        calls = []  # each call returns once its records are in host memory
         t0 = time.perf_counter()
         for _ in range(ke):
+            t1 = time.perf_counter()
             self.batch.update_cameras(cams, self.stream)
             self.batch.run(host.array, self.stream)
+            calls.append((time.perf_counter() - t1) * 1e3)
         sec = (time.perf_counter() - t0) / ke
+        self.e2e_calls_ms = calls
         host.close()
         return sec
 
@@ -527,6 +531,7 @@ def run_ours(args, engine_cls=None, backend: str = "nccl", device: str = "cuda")
                     "launches_per_step": int(sum_over_ranks(pg, len(eng.wl.views), device)), "steps": k,
                     "kernel": "view_path_kernel, 8x8 blocks, thread per pixel"}
 
+    link_before = eng.d2h_link_gbs()
     e2e_s = max_over_ranks(pg, eng.time_e2e(sync), device)
     d2h = sum_over_ranks(pg, eng.d2h_bytes, device)
     e2e = {"value": job_rays / e2e_s / 1e9, "unit": "Grays/s", "ms_per_step": e2e_s * 1e3,
@@ -534,7 +539,12 @@ def run_ours(args, engine_cls=None, backend: str = "nccl", device: str = "cuda")
            "api": "vrt_batch_update_cameras + vrt_batch_run (pinned host records)"}
     link = eng.d2h_link_gbs()
     e2e["d2h_link_gbs"] = link
+    e2e["d2h_link_gbs_before"] = link_before
     e2e["d2h_link_frac"] = eng.d2h_bytes / (e2e_s * 1e9) / link
+    calls = getattr(eng, "e2e_calls_ms", None)
+    if calls:  # this rank's calls: a slow mean from a few stalled calls shows here
+        e2e["calls_ms"] = {"n": len(calls), "min": min(calls), "median": sorted(calls)[len(calls) // 2],
+                           "max": max(calls)}
     barrier(pg)
 
     if rank == 0:
