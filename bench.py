@@ -38,6 +38,7 @@ sys.path.insert(0, str(ROOT))
 SLOT_BYTES = 512 + 512 + 64
 METRIC = "Grays/s batched vs per-view launch (bit-exact hits); p50/p99 request latency"
 HIT_BYTES = 16
+PACKED_BYTES = 12
 BYTES_FORMULA = "8*step_calls + 12*occ_fetches + 1*hits + 16*records"
 
 
@@ -391,7 +392,9 @@ class GpuEngine:
         m = self.meas
         self.alg_bytes = 8 * m["step_calls"] + 12 * m["occ_fetches"] + 1 * m["hits"] + HIT_BYTES * self.n_rec
         self.h2d_bytes = 128 * len(self.wl.views)
-        self.d2h_bytes = self.n_rec * HIT_BYTES
+        # end to end the records arrive as vrt_hit_packed (12 bytes: the per-ray output
+        # without the 16-byte record's tag, which a record's position already gives)
+        self.d2h_bytes = self.n_rec * PACKED_BYTES
         self.ms = None
 
     def time_batched(self, sync):
@@ -432,15 +435,11 @@ class GpuEngine:
         e1.synchronize()
         return e0.elapsed_time(e1) / k, k
 
-    def time_e2e(self, sync):
-        """Seconds per end-to-end call through the host-buffer API: new cameras in (H2D), all
-        records out to pinned host memory from vrt_host_alloc (the copies of finished parts
-        overlap the traversal of later ones)."""
-        v = self.v
-        host = v.PinnedHits(self.n_rec)
+    def _time_run(self, sync, run, host):
+        """Seconds per call of update_cameras + `run` into `host`, and each call's ms."""
         cams = [vw.cam for vw in self.wl.views]
         self.batch.update_cameras(cams, self.stream)
-        self.batch.run(host.array, self.stream)
+        run(host.array, self.stream)
         ke = max(1, min(self.args.steps, 5))
         sync()
         calls = []  # each call returns once its records are in host memory
@@ -448,11 +447,30 @@ class GpuEngine:
         for _ in range(ke):
             t1 = time.perf_counter()
             self.batch.update_cameras(cams, self.stream)
-            self.batch.run(host.array, self.stream)
+            run(host.array, self.stream)
             calls.append((time.perf_counter() - t1) * 1e3)
-        sec = (time.perf_counter() - t0) / ke
-        self.e2e_calls_ms = calls
-        host.close()
+        return (time.perf_counter() - t0) / ke, calls
+
+    def time_e2e(self, sync):
+        """Seconds per end-to-end call through the host-buffer API: new cameras in (H2D), all
+        records out to pinned host memory from vrt_host_alloc (the copies of finished parts
+        overlap the traversal of later ones), as 12-byte records (vrt_batch_run_packed).  The
+        16-byte records (vrt_batch_run) are timed beside them, and every packed record is
+        checked against its 16-byte record."""
+        v = self.v
+        full = v.PinnedHits(self.n_rec)
+        self.e2e_full = self._time_run(sync, self.batch.run, full)
+        packed = v.PinnedHits(self.n_rec, dtype=v.PACKED_DTYPE)
+        sec, self.e2e_calls_ms = self._time_run(sync, self.batch.run_packed, packed)
+        f = full.array.view(np.uint32).reshape(-1, 4)
+        g = packed.array.view(np.uint32).reshape(-1, 3)
+        no_ray = f[:, 3] == v.NO_RAY
+        word1 = np.where(no_ray, (f[:, 1] & 0xFFFF00FF) | (v.PACKED_NO_RAY << 8), f[:, 1])
+        self.e2e_packed_exact = bool(np.array_equal(f[:, 0], g[:, 0]) and np.array_equal(word1, g[:, 1])
+                                     and np.array_equal(f[:, 2], g[:, 2]))
+        del f, g, no_ray, word1
+        full.close()
+        packed.close()
         return sec
 
     def d2h_link_gbs(self):
@@ -536,11 +554,18 @@ def run_ours(args, engine_cls=None, backend: str = "nccl", device: str = "cuda")
     d2h = sum_over_ranks(pg, eng.d2h_bytes, device)
     e2e = {"value": job_rays / e2e_s / 1e9, "unit": "Grays/s", "ms_per_step": e2e_s * 1e3,
            "h2d_bytes_per_step": int(sum_over_ranks(pg, eng.h2d_bytes, device)), "d2h_bytes_per_step": int(d2h),
-           "api": "vrt_batch_update_cameras + vrt_batch_run (pinned host records)"}
+           "api": "vrt_batch_update_cameras + vrt_batch_run_packed (12-byte records into pinned host memory)"}
+    full = getattr(eng, "e2e_full", None)
+    if full:  # the same calls delivering 16-byte records (with tags), this rank's time
+        e2e["full_records"] = {"value": eng.rays_per_step / full[0] / 1e9, "unit": "Grays/s",
+                               "ms_per_step": full[0] * 1e3, "d2h_bytes_per_step": eng.n_rec * HIT_BYTES,
+                               "api": "vrt_batch_update_cameras + vrt_batch_run (16-byte records)"}
+    if hasattr(eng, "e2e_packed_exact"):
+        e2e["packed_equal_full"] = eng.e2e_packed_exact
     link = eng.d2h_link_gbs()
     e2e["d2h_link_gbs"] = link
     e2e["d2h_link_gbs_before"] = link_before
-    e2e["d2h_link_frac"] = eng.d2h_bytes / (e2e_s * 1e9) / link
+    e2e["d2h_link_frac"] = eng.d2h_bytes / (e2e_s * 1e9) / max(link, link_before)
     calls = getattr(eng, "e2e_calls_ms", None)
     if calls:  # this rank's calls: a slow mean from a few stalled calls shows here
         e2e["calls_ms"] = {"n": len(calls), "min": min(calls), "median": sorted(calls)[len(calls) // 2],

@@ -96,6 +96,21 @@ typedef struct vrt_hit {
     uint32_t tag;
 } vrt_hit;
 
+/* Hit record without its tag, 12 bytes: the per-ray output (voxel, face, material, steps,
+ * t) in the fields and encoding of vrt_hit.  vrt_batch_run_packed delivers these: a
+ * view's records are in pixel order, so a record's position gives the pixel its tag
+ * would name.  A record whose ray was never cast (VRT_NO_RAY in vrt_hit.tag: the shadow
+ * or bounce records after a path ended) keeps the miss fields with material
+ * VRT_PACKED_NO_RAY; a miss that was cast always has material 0. */
+typedef struct vrt_hit_packed {
+    uint32_t voxel;
+    uint8_t face;
+    uint8_t material;
+    uint16_t steps;
+    float t;
+} vrt_hit_packed;
+#define VRT_PACKED_NO_RAY 0xFFu
+
 typedef struct vrt_cast_params {
     int32_t world_origin[3]; /* FrameConstants::WorldOrigin (CpuRenderer.cpp:447) */
     uint32_t max_iters;      /* 0 = VRT_DEFAULT_MAX_ITERS (VRT_GLSL_MAX_ITERS in GLSL mode); at most 65535 */
@@ -430,6 +445,11 @@ vrt_status vrt_batch_update_cameras(vrt_batch* batch, const vrt_camera* cams, vo
  * that part is done, so the host transfer overlaps the tracing of later parts
  * (pinned memory from vrt_host_alloc keeps the copies asynchronous). */
 vrt_status vrt_batch_run(vrt_batch* batch, vrt_hit* hits_host, void* stream);
+/* vrt_batch_run delivering 12-byte records (vrt_hit_packed, same order and count): 3/4 of
+ * the bytes over the host link.  Each part's records are packed on the device once the
+ * part is traced, and the packed part is copied to records_host as vrt_batch_run copies
+ * the full one. */
+vrt_status vrt_batch_run_packed(vrt_batch* batch, vrt_hit_packed* records_host, void* stream);
 /* Counters of the last launch (synchronises the stream of that launch). */
 vrt_status vrt_batch_get_stats(vrt_batch* batch, vrt_batch_stats* out);
 /* One launch of the counting variant: fills step_calls/occ_fetches/hits. */

@@ -178,3 +178,35 @@ def test_run_into_pinned_buffers_matches_pageable(mix):
     b.close()
     whole.close()
     bigger.close()
+
+
+def test_run_packed_is_run_without_tags(mix):
+    """vrt_batch_run_packed delivers every record of vrt_batch_run without its tag (12 bytes),
+    with the records of rays never cast marked PACKED_NO_RAY; into pageable memory, and into
+    vrt_host_alloc memory at an offset that is not 16-byte aligned."""
+    worlds, views, want = mix
+    b = v.Batch(worlds, views)
+    n = b.total_records
+    full = b.run()
+    assert (full["tag"] == v.NO_RAY).any() and (full["tag"] != v.NO_RAY).any()
+    expect = v.pack_hits(full)
+    pageable = b.run_packed()
+    pinned = v.PinnedHits(n + 5, dtype=v.PACKED_DTYPE)
+    pinned.array[:] = np.frombuffer(b"\xcd" * ((n + 5) * 12), v.PACKED_DTYPE)
+    got_pinned = b.run_packed(pinned.array[3:3 + n]).copy()
+    assert np.array_equal(pinned.array[:3].view(np.uint8), np.full(36, 0xCD, np.uint8))
+    for got in (pageable, got_pinned):
+        assert np.array_equal(got.view(np.uint8), expect.view(np.uint8))
+    # against the oracle: a record's position in its view gives the pixel its tag named
+    for i in range(len(views)):
+        a, e = int(b.offsets[i]), int(b.offsets[i + 1])
+        g = pageable[a:e]
+        w = v.pack_hits(want[i].reshape(-1))
+        for f in ("voxel", "face", "material", "steps"):
+            assert np.array_equal(g[f], w[f]), f"view {i}: {f} differs"
+        tg, tw = g["t"].astype(np.float64), w["t"].astype(np.float64)
+        fin = np.isfinite(tw)
+        assert np.array_equal(np.isfinite(tg), fin)
+        assert np.all(np.abs(tg[fin] - tw[fin]) <= 1e-6 * np.abs(tw[fin]))
+    pinned.close()
+    b.close()

@@ -17,14 +17,24 @@ import ctypes as C
 import numpy as np
 
 from . import capi
-from .capi import (CAST_GLSL, EDIT_DTYPE, HIT_DTYPE, MISS_FACE, MISS_VOXEL, NO_RAY, RAY_DTYPE, VIEW_GLSL, VIEW_SHADOW,
-                   BatchConfig, Camera,
+from .capi import (CAST_GLSL, EDIT_DTYPE, HIT_DTYPE, MISS_FACE, MISS_VOXEL, NO_RAY, PACKED_DTYPE, PACKED_NO_RAY,
+                   RAY_DTYPE, VIEW_GLSL, VIEW_SHADOW, BatchConfig, Camera,
                    CastParams, View, VrtError, check, check_synth, lib, ptr, synth_lib)
 
 __all__ = ["Server", "PinnedHits", "view_records", "render_path", "render_gbuffer", "cvox_read", "cvox_write", "World", "Camera", "View",
            "make_view", "Batch", "BatchConfig", "VIEW_SHADOW", "VIEW_GLSL", "CAST_GLSL", "look_at", "synth_terrain", "synth_mix", "random_rays", "SectorData", "VrtError",
            "RAY_DTYPE", "HIT_DTYPE", "EDIT_DTYPE", "MISS_VOXEL", "MISS_FACE", "NO_RAY", "unpack_voxel", "sector_index",
-           "lib"]
+           "PACKED_DTYPE", "PACKED_NO_RAY", "pack_hits", "lib"]
+
+
+def pack_hits(hits: np.ndarray) -> np.ndarray:
+    """The 12-byte records (vrt_hit_packed) of 16-byte ones: the tag dropped, and a record of a
+    ray never cast (tag NO_RAY) marked with material PACKED_NO_RAY."""
+    out = np.empty(len(hits), PACKED_DTYPE)
+    for f in PACKED_DTYPE.names:
+        out[f] = hits[f]
+    out["material"][hits["tag"] == NO_RAY] = PACKED_NO_RAY
+    return out
 
 
 def sector_index(x: int, y: int, z: int) -> int:
@@ -348,6 +358,13 @@ class Batch:
         check(lib().vrt_batch_run(self._h, ptr(hits_host), _stream_ptr(stream)))
         return hits_host
 
+    def run_packed(self, records_host=None, stream=None) -> np.ndarray:
+        """vrt_batch_run with 12-byte records (PACKED_DTYPE) delivered to host memory."""
+        if records_host is None:
+            records_host = np.zeros(self.total_records, PACKED_DTYPE)
+        check(lib().vrt_batch_run_packed(self._h, ptr(records_host), _stream_ptr(stream)))
+        return records_host
+
     def update_cameras(self, cams, stream=None) -> None:
         arr = (Camera * len(cams))(*cams)
         check(lib().vrt_batch_update_cameras(self._h, arr, _stream_ptr(stream)))
@@ -369,14 +386,15 @@ class Batch:
 
 
 class PinnedHits:
-    """Pinned host buffer of hit records (vrt_host_alloc), viewed as a numpy array."""
+    """Pinned host buffer of hit records (vrt_host_alloc), viewed as a numpy array
+    (dtype HIT_DTYPE, or PACKED_DTYPE for vrt_batch_run_packed)."""
 
-    def __init__(self, n: int):
+    def __init__(self, n: int, dtype=HIT_DTYPE):
         p = C.c_void_p()
-        check(lib().vrt_host_alloc(max(1, n) * HIT_DTYPE.itemsize, C.byref(p)))
+        check(lib().vrt_host_alloc(max(1, n) * dtype.itemsize, C.byref(p)))
         self._p = p
-        buf = (C.c_uint8 * (max(1, n) * HIT_DTYPE.itemsize)).from_address(p.value)
-        self.array = np.frombuffer(buf, dtype=HIT_DTYPE)[:n]
+        buf = (C.c_uint8 * (max(1, n) * dtype.itemsize)).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=dtype)[:n]
 
     def close(self):
         if self._p:

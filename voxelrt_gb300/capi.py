@@ -27,6 +27,7 @@ VRT_ERR_FORMAT = 9
 MISS_VOXEL = 0xFFFFFFFF
 MISS_FACE = 0xFF
 NO_RAY = 0xFFFFFFFF
+PACKED_NO_RAY = 0xFF  # vrt_hit_packed.material of a record whose ray was never cast
 DEFAULT_MAX_ITERS = 128
 EDIT_FILL = 0
 EDIT_REPLACE = 1
@@ -131,12 +132,15 @@ class SynthTerrain(C.Structure):
 RAY_DTYPE = np.dtype([("origin", "<f4", 3), ("dir", "<f4", 3), ("tag", "<u4"), ("reserved", "<u4")])
 HIT_DTYPE = np.dtype([("voxel", "<u4"), ("face", "u1"), ("material", "u1"), ("steps", "<u2"), ("t", "<f4"),
                       ("tag", "<u4")])
+# vrt_hit_packed: vrt_hit without its tag
+PACKED_DTYPE = np.dtype([("voxel", "<u4"), ("face", "u1"), ("material", "u1"), ("steps", "<u2"), ("t", "<f4")])
 PICK_DTYPE = np.dtype([("distance", "<f8"), ("voxel", "<i4", 3), ("normal", "<f4", 3), ("uv", "<f4", 2),
                        ("iters", "<u4"), ("reserved", "<u4")])
 EDIT_DTYPE = np.dtype([("center", "<i4", 3), ("radius", "<u4"), ("material", "u1"), ("mode", "u1"),
                        ("reserved", "<u2")])
 assert RAY_DTYPE.itemsize == C.sizeof(Ray) == 32
 assert HIT_DTYPE.itemsize == C.sizeof(Hit) == 16
+assert PACKED_DTYPE.itemsize == 12
 assert EDIT_DTYPE.itemsize == C.sizeof(Edit) == 20
 assert PICK_DTYPE.itemsize == 48
 
@@ -182,6 +186,7 @@ PROTOTYPES = {
     "vrt_batch_launch_graph": (_st, [_vp, _vp, _vp]),
     "vrt_batch_launch_per_view": (_st, [_vp, _vp, _vp]),
     "vrt_batch_run": (_st, [_vp, _vp, _vp]),
+    "vrt_batch_run_packed": (_st, [_vp, _vp, _vp]),
     "vrt_batch_update_cameras": (_st, [_vp, C.POINTER(Camera), _vp]),
     "vrt_batch_get_stats": (_st, [_vp, C.POINTER(BatchStats)]),
     "vrt_batch_measure": (_st, [_vp, _vp, _vp, C.POINTER(BatchStats)]),

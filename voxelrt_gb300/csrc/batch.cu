@@ -789,6 +789,24 @@ vrt_status launch_persistent(const BatchParams& p, int blocks, int threads, bool
     return VRT_OK;
 }
 
+namespace {
+
+// vrt_batch_run_packed: records [0, n) of one part as 12-byte vrt_hit_packed, one thread per
+// record (three 4-byte stores: a warp's stores cover 384 contiguous bytes); the 16-byte
+// records are read once, so they are loaded as streaming
+static_assert(sizeof(vrt_hit_packed) == 12 && sizeof(vrt_hit) == 16, "record sizes");
+__global__ void __launch_bounds__(256)
+    pack_records_kernel(const uint4* __restrict__ in, uint32_t* __restrict__ out, uint64_t n) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint4 r = __ldcs(in + i);
+        out[3 * i] = r.x;
+        out[3 * i + 1] = r.w == VRT_NO_RAY ? (r.y & 0xFFFF00FFu) | (VRT_PACKED_NO_RAY << 8) : r.y;
+        out[3 * i + 2] = r.z;
+    }
+}
+
+}  // namespace
 }  // namespace vrt
 
 using namespace vrt;
@@ -807,7 +825,8 @@ struct vrt_batch {
     uint32_t* d_queue = nullptr;  // queue counter followed by 4 u64 counters (16-byte aligned)
     unsigned long long* d_counters = nullptr;
     cudaStream_t last_stream = nullptr;
-    DevBuf d_out;  // record buffer of vrt_batch_run
+    DevBuf d_out;     // record buffer of vrt_batch_run
+    DevBuf d_packed;  // 12-byte records of vrt_batch_run_packed
     // vrt_batch_run: copies of finished parts overlap the traversal of later parts
     cudaStream_t copy_stream = nullptr;
     std::vector<cudaEvent_t> part_done;
@@ -948,6 +967,7 @@ vrt_status vrt_batch_destroy(vrt_batch* b) {
     if (b->d_chunk_base) cudaFree(b->d_chunk_base);
     if (b->d_queue) cudaFree(b->d_queue);
     b->d_out.release();
+    b->d_packed.release();
     delete b;
     return VRT_OK;
 }
@@ -1052,16 +1072,17 @@ vrt_status vrt_batch_launch_per_view(vrt_batch* b, vrt_hit* hits, void* stream_)
     return VRT_OK;
 }
 
-vrt_status vrt_batch_run(vrt_batch* b, vrt_hit* hits_host, void* stream_) {
-    if (!b || !hits_host) {
-        set_error("null argument");
-        return VRT_ERR_INVALID_ARG;
-    }
+}  // extern "C"
+
+namespace {
+
+// vrt_batch_run and vrt_batch_run_packed: trace, (pack,) and copy to `host` part by part.
+vrt_status run_parts(vrt_batch* b, void* host, bool packed, cudaStream_t stream) {
     VRT_CUDA(cudaSetDevice(b->device));
-    cudaStream_t stream = (cudaStream_t)stream_;
     const LaunchPlan& plan = b->plan;
     const size_t nv = plan.views.size();
     VRT_CUDA(b->d_out.reserve(plan.records * sizeof(vrt_hit)));
+    if (packed) VRT_CUDA(b->d_packed.reserve(plan.records * sizeof(vrt_hit_packed)));
     vrt_status st = refresh_worlds(b, stream);
     if (st != VRT_OK) return st;
     // Views are split into parts of about equal record count, at view boundaries.
@@ -1084,6 +1105,8 @@ vrt_status vrt_batch_run(vrt_batch* b, vrt_hit* hits_host, void* stream_) {
         b->part_done.push_back(e);
     }
     auto first_record = [&](size_t v) { return v < nv ? plan.views[v].out_base : plan.records; };
+    const uint4* d_full = (const uint4*)b->d_out.ptr;
+    uint32_t* d_pack = (uint32_t*)b->d_packed.ptr;
     L2Window l2;
     if ((st = l2.enter(b->l2_world, stream)) != VRT_OK) return st;
     for (size_t k = 0; k < parts; k++) {
@@ -1096,13 +1119,21 @@ vrt_status vrt_batch_run(vrt_batch* b, vrt_hit* hits_host, void* stream_) {
         p.chunk_first = plan.chunk_base[a];
         p.total_chunks = plan.chunk_base[e] - plan.chunk_base[a];
         if ((st = launch_persistent(p, b->blocks, b->threads, false, stream, k == 0)) != VRT_OK) return st;
+        const uint64_t r0 = first_record(a), n = first_record(e) - r0;
+        if (packed && n) {
+            const uint32_t blocks = (uint32_t)std::min<uint64_t>((n + 255) / 256, 4096);
+            pack_records_kernel<<<blocks, 256, 0, stream>>>(d_full + r0, d_pack + 3 * r0, n);
+            VRT_CUDA(cudaGetLastError());
+        }
         VRT_CUDA(cudaEventRecord(b->part_done[k], stream));
     }
+    const size_t rec_bytes = packed ? sizeof(vrt_hit_packed) : sizeof(vrt_hit);
+    const uint8_t* src = packed ? (const uint8_t*)d_pack : (const uint8_t*)d_full;
     for (size_t k = 0; k < parts; k++) {
         const uint64_t r0 = first_record(cut[k]), r1 = first_record(cut[k + 1]);
         VRT_CUDA(cudaStreamWaitEvent(b->copy_stream, b->part_done[k], 0));
         if (r1 > r0)
-            VRT_CUDA(cudaMemcpyAsync(hits_host + r0, (const vrt_hit*)b->d_out.ptr + r0, (r1 - r0) * sizeof(vrt_hit),
+            VRT_CUDA(cudaMemcpyAsync((uint8_t*)host + r0 * rec_bytes, src + r0 * rec_bytes, (r1 - r0) * rec_bytes,
                                      cudaMemcpyDeviceToHost, b->copy_stream));
     }
     VRT_CUDA(cudaEventRecord(b->copies_done, b->copy_stream));
@@ -1110,6 +1141,26 @@ vrt_status vrt_batch_run(vrt_batch* b, vrt_hit* hits_host, void* stream_) {
     b->last_stream = stream;
     VRT_CUDA(cudaStreamSynchronize(stream));
     return VRT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+vrt_status vrt_batch_run(vrt_batch* b, vrt_hit* hits_host, void* stream) {
+    if (!b || !hits_host) {
+        set_error("null argument");
+        return VRT_ERR_INVALID_ARG;
+    }
+    return run_parts(b, hits_host, false, (cudaStream_t)stream);
+}
+
+vrt_status vrt_batch_run_packed(vrt_batch* b, vrt_hit_packed* records_host, void* stream) {
+    if (!b || !records_host) {
+        set_error("null argument");
+        return VRT_ERR_INVALID_ARG;
+    }
+    return run_parts(b, records_host, true, (cudaStream_t)stream);
 }
 
 vrt_status vrt_batch_get_stats(vrt_batch* b, vrt_batch_stats* out) {
