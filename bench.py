@@ -559,7 +559,8 @@ def run_ours(args, engine_cls=None, backend: str = "nccl", device: str = "cuda")
     if full:  # the same calls delivering 16-byte records (with tags), this rank's time
         e2e["full_records"] = {"value": eng.rays_per_step / full[0] / 1e9, "unit": "Grays/s",
                                "ms_per_step": full[0] * 1e3, "d2h_bytes_per_step": eng.n_rec * HIT_BYTES,
-                               "api": "vrt_batch_update_cameras + vrt_batch_run (16-byte records)"}
+                               "api": "vrt_batch_update_cameras + vrt_batch_run (16-byte records)",
+                               "calls_ms": [round(c, 3) for c in full[1]]}
     if hasattr(eng, "e2e_packed_exact"):
         e2e["packed_equal_full"] = eng.e2e_packed_exact
     link = eng.d2h_link_gbs()
@@ -569,7 +570,7 @@ def run_ours(args, engine_cls=None, backend: str = "nccl", device: str = "cuda")
     calls = getattr(eng, "e2e_calls_ms", None)
     if calls:  # this rank's calls: a slow mean from a few stalled calls shows here
         e2e["calls_ms"] = {"n": len(calls), "min": min(calls), "median": sorted(calls)[len(calls) // 2],
-                           "max": max(calls)}
+                           "max": max(calls), "each": [round(c, 3) for c in calls]}
     barrier(pg)
 
     if rank == 0:
