@@ -462,7 +462,8 @@ vrt_status vrt_batch_measure(vrt_batch* batch, vrt_hit* hits_device, void* strea
  * table, tile-queue counter) lives in one fixed 152.5 KiB device array that every GPU
  * loading the library holds until the process exits, so a call takes at most 256
  * worlds and 1024 views (VRT_ERR_INVALID_ARG beyond).  The first call on a device
- * looks up that array's address.  All calls share the array: calls whose launches
+ * looks up that array's address and creates the event that guards the host tables;
+ * make that first call before any stream capture begins.  All calls share the array: calls whose launches
  * overlap on the GPU race, so order them on one stream.  The world and view tables are staged in library-owned host tables,
  * so a call first waits on the host until the table copies of the previous call on
  * the same device have run.  The caller's current device is the same when the call
