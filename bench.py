@@ -235,6 +235,13 @@ def peak_hbm():
     return 6800.0, "fallback"
 
 
+# What bounds the persistent kernel on a workload, from the committed ncu summaries.
+LIMITERS = {
+    "uneven_batch": "instruction issue: 73.7 % of issue slots busy, wait (fixed-latency dependency) the first "
+                    "stall (profiles/persistent_kernel_uneven_batch_medium.md)",
+}
+
+
 def traffic_from_profile(workload: str, args=None):
     """DRAM bytes per launch of the persistent kernel from a committed ncu summary, for
     the configuration that summary covers (the workload at its default sizes, default
@@ -440,7 +447,7 @@ class GpuEngine:
         cams = [vw.cam for vw in self.wl.views]
         self.batch.update_cameras(cams, self.stream)
         run(host.array, self.stream)
-        ke = max(1, min(self.args.steps, 5))
+        ke = max(1, min(self.args.steps, 10))
         sync()
         calls = []  # each call returns once its records are in host memory
         t0 = time.perf_counter()
@@ -498,9 +505,15 @@ class GpuEngine:
                              "mean_steps_per_ray": self.meas["step_calls"] / max(self.rays_per_step, 1)}}
         peak, peak_src = peak_hbm()
         achieved = self.alg_bytes / (self.ms * 1e-3) / 1e9
+        traffic = traffic_from_profile(self.wl.name, args)
         out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                           "traffic": traffic_from_profile(self.wl.name, args), "peak_source": peak_src,
+                           "traffic": traffic, "peak_source": peak_src,
                            "algorithmic_bytes_per_launch": self.alg_bytes, "bytes_formula": BYTES_FORMULA}
+        if traffic:
+            # what DRAM actually moved per launch, against the same peak: the brick data stays in
+            # L2/L1, so this fraction is far below the algorithmic one
+            out["roofline"]["dram_frac"] = traffic / (self.ms * 1e-3) / 1e9 / peak
+            out["roofline"]["limiter"] = LIMITERS.get(self.wl.name)
         cpu = None
         if not args.no_cpu:
             cores = host_cores()
