@@ -78,6 +78,7 @@ def parse(argv=None):
                          "over the brick table of a batch's single such world)")
     ap.add_argument("--worlds", type=int, default=128, help="uneven_batch: number of worlds")
     ap.add_argument("--max-views", type=int, default=16, help="uneven_batch: views per world, at most")
+    ap.add_argument("--cameras", type=int, default=64, help="large_world: number of 1080p cameras")
     ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
                     help="N>1: every rank traces its own batch (weak) or a share, by world, of one batch (strong)")
     return ap.parse_args(argv)
@@ -166,7 +167,7 @@ def _build_workload(name: str, rank: int, args=None, world_size: int = 1):
             wl = W.Workload(wl.name, worlds, views, f"{wl.description}, worlds {own} of {world_size} ranks")
         return wl
     if name == "large_world":
-        return W.large_world()
+        return W.large_world(n_cameras=args.cameras if args is not None else 64)
     if name == "incoherent":
         return W.incoherent()
     return W.single_view()
@@ -249,7 +250,8 @@ def traffic_from_profile(workload: str, args=None):
     p = ROOT / "profiles" / "traffic.json"
     if not p.exists():
         return None
-    if args is not None and (args.glsl or args.aniso or args.worlds != 128 or args.max_views != 16):
+    if args is not None and (args.glsl or args.aniso or args.worlds != 128 or args.max_views != 16 or
+                             getattr(args, "cameras", 64) != 64):
         return None
     try:
         return json.loads(p.read_text()).get(workload)
