@@ -426,7 +426,27 @@ class GpuEngine:
             torch.cuda.synchronize()
         sync()
         self.ms = ev0.elapsed_time(ev1) / self.args.steps
+        self.ms_l2_flushed = self._time_l2_flushed()
         return self.ms, clk.summary()
+
+    def _time_l2_flushed(self, flush_bytes=512 << 20):
+        """ms per launch with L2 flushed before each one (a 512 MiB write, four times L2, not
+        timed): the bricks a batch touches fit in L2 across launches, so this shows what the
+        first touch of every line costs."""
+        torch, s = self.torch, self.stream
+        flush = torch.empty(flush_bytes, dtype=torch.uint8, device=self.hits.device)
+        evs = []
+        with torch.cuda.stream(s):
+            for i in range(self.args.steps):
+                flush.fill_(i & 0xFF)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(s)
+                self.batch.launch(self.hits, s, graph=True)
+                e1.record(s)
+                evs.append((e0, e1))
+        s.synchronize()
+        del flush
+        return sum(a.elapsed_time(b) for a, b in evs) / len(evs)
 
     def time_per_view(self):
         """ms per pass of one plain launch per view over the same views."""
@@ -491,7 +511,7 @@ class GpuEngine:
         return {"workload": wl.name, "description": wl.description, "worlds": len(wl.worlds),
                 "views": len(wl.views), "rays_per_step": self.rays_per_step, "records_per_step": self.n_rec,
                 "world_bytes": int(sum(d.n_bricks for d in wl.worlds) * SLOT_BYTES),
-                "l2": "inputs larger than L2 (brick pools of all worlds)",
+                "l2": "inputs larger than L2 (brick pools of all worlds); l2_flushed: the same launches, each after an L2 flush",
                 "batch_config": autotune.describe(self.cfg), "batch_config_source": self.cfg_src,
                 "launch": "persistent kernel + queue reset, CUDA graph replay",
                 "traversal": traversal_name(self.args),
@@ -599,6 +619,10 @@ def run_ours(args, engine_cls=None, backend: str = "nccl", device: str = "cuda")
             "batched_over_per_view": (value / per_view["value"]) if per_view else None,
             "job_rays_per_step": job_rays,
         }
+        fl = getattr(eng, "ms_l2_flushed", None)
+        if fl:  # this rank's launches, each after a 512 MiB write that evicts L2
+            line["l2_flushed"] = {"ms_per_step": fl, "value": eng.rays_per_step / (fl * 1e-3) / 1e9,
+                                  "unit": "Grays/s", "flush_bytes": 512 << 20}
         line.update(extra)
         print(json.dumps(line), flush=True)
     else:
