@@ -29,6 +29,9 @@
  * Every function taking a `stream` takes a cudaStream_t passed as void*
  * (NULL = legacy default stream).  Functions with host buffers synchronise that
  * stream before returning; *_device variants are asynchronous on it.
+ *
+ * A call on a world, batch or server makes that object's device current while it
+ * runs and gives the calling thread's current device back when it returns.
  */
 #ifndef VRT_H_
 #define VRT_H_

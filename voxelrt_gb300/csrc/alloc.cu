@@ -217,14 +217,16 @@ vrt_status ensure_headroom(vrt_world* w, uint64_t need, cudaStream_t stream) {
 using namespace vrt;
 
 extern "C" vrt_status vrt_world_defrag(vrt_world* w, uint32_t capacity, void* stream) {
-    vrt_status st = world_enter(w);
+    DeviceScope ds;
+    vrt_status st = world_enter(w, ds);
     if (st != VRT_OK) return st;
     std::lock_guard<std::mutex> lock(w->mu);
     return world_compact(w, capacity ? capacity : w->capacity, (cudaStream_t)stream);
 }
 
 extern "C" vrt_status vrt_world_wait(vrt_world* w) {
-    vrt_status st = world_enter(w);
+    DeviceScope ds;
+    vrt_status st = world_enter(w, ds);
     if (st != VRT_OK) return st;
     VRT_CUDA(cudaEventSynchronize(w->edited));
     return VRT_OK;

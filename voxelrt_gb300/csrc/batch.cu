@@ -868,7 +868,8 @@ extern "C" {
 uint64_t vrt_view_records(const vrt_view* v) { return check_view(v) == VRT_OK ? view_record_count(*v) : 0; }
 
 vrt_status vrt_render_path_device(vrt_world* w, const vrt_view* view, vrt_hit* hits, void* stream) {
-    vrt_status st = world_enter(w);
+    DeviceScope ds;
+    vrt_status st = world_enter(w, ds);
     if (st != VRT_OK || (st = check_view(view)) != VRT_OK) return st;
     if (!hits) {
         set_error("null hit buffer");
@@ -880,7 +881,8 @@ vrt_status vrt_render_path_device(vrt_world* w, const vrt_view* view, vrt_hit* h
 }
 
 vrt_status vrt_render_path(vrt_world* w, const vrt_view* view, vrt_hit* hits, void* stream_) {
-    vrt_status st = world_enter(w);
+    DeviceScope ds;
+    vrt_status st = world_enter(w, ds);
     if (st != VRT_OK || (st = check_view(view)) != VRT_OK) return st;
     if (!hits) {
         set_error("null hit buffer");
@@ -931,7 +933,8 @@ vrt_status vrt_batch_create(vrt_world* const* worlds, uint32_t n_worlds, const v
         vrt_batch_destroy(b);
         return s;
     };
-    cudaError_t e = cudaSetDevice(b->device);
+    DeviceScope ds;
+    cudaError_t e = ds.enter(b->device);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_worlds, sizeof(DevWorld) * n_worlds);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_views, sizeof(ViewDev) * n_views);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_chunk_base, sizeof(uint32_t) * (n_views + 1));
@@ -956,7 +959,8 @@ vrt_status vrt_batch_create(vrt_world* const* worlds, uint32_t n_worlds, const v
 
 vrt_status vrt_batch_destroy(vrt_batch* b) {
     if (!b) return VRT_OK;
-    cudaSetDevice(b->device);
+    DeviceScope ds;
+    ds.enter(b->device);
     cudaDeviceSynchronize();
     if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
     for (cudaEvent_t e : b->part_done) cudaEventDestroy(e);
@@ -997,7 +1001,8 @@ vrt_status vrt_batch_update_cameras(vrt_batch* b, const vrt_camera* cams, void* 
             return VRT_ERR_INVALID_ARG;
         }
     }
-    VRT_CUDA(cudaSetDevice(b->device));
+    DeviceScope ds;
+    VRT_CUDA(ds.enter(b->device));
     for (size_t i = 0; i < b->plan.views.size(); i++) {
         set_view_camera(b->plan.views[i], cams[i]);
         b->views[i].cam = cams[i];
@@ -1014,7 +1019,8 @@ vrt_status vrt_batch_launch(vrt_batch* b, vrt_hit* hits, void* stream_) {
         set_error("null argument");
         return VRT_ERR_INVALID_ARG;
     }
-    VRT_CUDA(cudaSetDevice(b->device));
+    DeviceScope ds;
+    VRT_CUDA(ds.enter(b->device));
     cudaStream_t stream = (cudaStream_t)stream_;
     vrt_status st = refresh_worlds(b, stream);
     if (st != VRT_OK) return st;
@@ -1027,7 +1033,8 @@ vrt_status vrt_batch_launch_graph(vrt_batch* b, vrt_hit* hits, void* stream_) {
         set_error("null argument");
         return VRT_ERR_INVALID_ARG;
     }
-    VRT_CUDA(cudaSetDevice(b->device));
+    DeviceScope ds;
+    VRT_CUDA(ds.enter(b->device));
     cudaStream_t stream = (cudaStream_t)stream_;
     vrt_status st = refresh_worlds(b, stream);
     if (st != VRT_OK) return st;
@@ -1061,7 +1068,8 @@ vrt_status vrt_batch_launch_per_view(vrt_batch* b, vrt_hit* hits, void* stream_)
         set_error("null argument");
         return VRT_ERR_INVALID_ARG;
     }
-    VRT_CUDA(cudaSetDevice(b->device));
+    DeviceScope ds;
+    VRT_CUDA(ds.enter(b->device));
     cudaStream_t stream = (cudaStream_t)stream_;
     for (size_t i = 0; i < b->plan.views.size(); i++) {
         vrt_status st =
@@ -1078,7 +1086,8 @@ namespace {
 
 // vrt_batch_run and vrt_batch_run_packed: trace, (pack,) and copy to `host` part by part.
 vrt_status run_parts(vrt_batch* b, void* host, bool packed, cudaStream_t stream) {
-    VRT_CUDA(cudaSetDevice(b->device));
+    DeviceScope ds;
+    VRT_CUDA(ds.enter(b->device));
     const LaunchPlan& plan = b->plan;
     const size_t nv = plan.views.size();
     VRT_CUDA(b->d_out.reserve(plan.records * sizeof(vrt_hit)));
@@ -1168,7 +1177,8 @@ vrt_status vrt_batch_get_stats(vrt_batch* b, vrt_batch_stats* out) {
         set_error("null argument");
         return VRT_ERR_INVALID_ARG;
     }
-    VRT_CUDA(cudaSetDevice(b->device));
+    DeviceScope ds;
+    VRT_CUDA(ds.enter(b->device));
     VRT_CUDA(cudaStreamSynchronize(b->last_stream));
     unsigned long long c[4];
     VRT_CUDA(cudaMemcpy(c, b->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
@@ -1184,7 +1194,8 @@ vrt_status vrt_batch_measure(vrt_batch* b, vrt_hit* hits, void* stream_, vrt_bat
         set_error("null argument");
         return VRT_ERR_INVALID_ARG;
     }
-    VRT_CUDA(cudaSetDevice(b->device));
+    DeviceScope ds;
+    VRT_CUDA(ds.enter(b->device));
     cudaStream_t stream = (cudaStream_t)stream_;
     vrt_status st = refresh_worlds(b, stream);
     if (st != VRT_OK || (st = enqueue_batch(b, hits, stream, true)) != VRT_OK) return st;

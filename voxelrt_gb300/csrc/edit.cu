@@ -211,7 +211,8 @@ size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 using namespace vrt;
 
 extern "C" vrt_status vrt_world_edit(vrt_world* w, const vrt_edit* edits, uint32_t n, void* stream_) {
-    vrt_status st = world_enter(w);
+    DeviceScope ds;
+    vrt_status st = world_enter(w, ds);
     if (st != VRT_OK) return st;
     if (n == 0) return VRT_OK;
     if (!edits) {

@@ -105,9 +105,10 @@ vrt_status launch_gbuffer(vrt_world* w, const vrt_view* view, const uint32_t* pa
     return VRT_OK;
 }
 
+// Makes w's device current until `ds` ends.
 vrt_status check_gbuffer_args(vrt_world* w, const vrt_view* view, const uint32_t* palette, const float* proj,
-                              const void* tex, const void* depth) {
-    vrt_status st = world_enter(w);
+                              const void* tex, const void* depth, DeviceScope& ds) {
+    vrt_status st = world_enter(w, ds);
     if (st != VRT_OK || (st = check_view(view)) != VRT_OK) return st;
     if (!palette || !proj || !tex || !depth) {
         set_error("G-buffer needs a palette, a projection and albedo/depth buffers");
@@ -124,14 +125,16 @@ using namespace vrt;
 extern "C" vrt_status vrt_render_gbuffer_device(vrt_world* w, const vrt_view* view, const uint32_t* palette,
                                                 const float* proj, uint32_t* albedo_normal, float* depth,
                                                 vrt_hit* hits, void* stream) {
-    vrt_status st = check_gbuffer_args(w, view, palette, proj, albedo_normal, depth);
+    DeviceScope ds;
+    vrt_status st = check_gbuffer_args(w, view, palette, proj, albedo_normal, depth, ds);
     if (st != VRT_OK) return st;
     return launch_gbuffer(w, view, palette, proj, albedo_normal, depth, hits, (cudaStream_t)stream);
 }
 
 extern "C" vrt_status vrt_render_gbuffer(vrt_world* w, const vrt_view* view, const uint32_t* palette,
                                          const float* proj, uint32_t* albedo_normal, float* depth, void* stream_) {
-    vrt_status st = check_gbuffer_args(w, view, palette, proj, albedo_normal, depth);
+    DeviceScope ds;
+    vrt_status st = check_gbuffer_args(w, view, palette, proj, albedo_normal, depth, ds);
     if (st != VRT_OK) return st;
     std::lock_guard<std::mutex> lock(w->mu);
     cudaStream_t stream = (cudaStream_t)stream_;

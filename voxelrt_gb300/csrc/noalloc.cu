@@ -53,23 +53,6 @@ struct StaticState {
 };
 StaticState g_state;
 
-// Makes `device` current for the call and gives the caller's current device back when
-// the call returns.
-struct DeviceScope {
-    int prev = -1;
-    cudaError_t enter(int device) {
-        cudaError_t e = cudaGetDevice(&prev);
-        if (e != cudaSuccess) {
-            prev = -1;
-            return e;
-        }
-        return prev == device ? cudaSuccess : cudaSetDevice(device);
-    }
-    ~DeviceScope() {
-        if (prev >= 0) cudaSetDevice(prev);
-    }
-};
-
 uint32_t log2u_static(uint32_t v) {
     uint32_t r = 0;
     while ((1u << r) < v) r++;

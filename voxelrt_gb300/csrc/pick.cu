@@ -98,7 +98,8 @@ using namespace vrt;
 
 extern "C" vrt_status vrt_pick(vrt_world* w, const vrt_pick_ray* rays, uint32_t n, uint32_t max_iters,
                                vrt_pick_hit* hits, void* stream_) {
-    vrt_status st = world_enter(w);
+    DeviceScope ds;
+    vrt_status st = world_enter(w, ds);
     if (st != VRT_OK) return st;
     if (n == 0) return VRT_OK;
     if (!rays || !hits) {

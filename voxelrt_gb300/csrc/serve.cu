@@ -764,7 +764,8 @@ vrt_status vrt_server_create(vrt_world* const* worlds, uint32_t n_worlds, const 
         if (st == VRT_OK) set_error("max_inflight must be <= 16");
         return st == VRT_OK ? VRT_ERR_INVALID_ARG : st;
     }
-    cudaError_t e = cudaSetDevice(sv->device);
+    DeviceScope ds;
+    cudaError_t e = ds.enter(sv->device);
     if (e != cudaSuccess) return fail(cuda_fail(e, "set device"));
     if (sv->cfg.hbm_budget_bytes == 0) {
         size_t fr = 0, tot = 0;
@@ -836,7 +837,8 @@ vrt_status vrt_server_destroy(vrt_server* sv, uint32_t timeout_ms) {
         sv->signal();
         sv->worker.join();
     }
-    cudaSetDevice(sv->device);
+    DeviceScope ds;
+    ds.enter(sv->device);
     for (auto& s : sv->slots) {
         if (s->stream) {
             cudaStreamSynchronize(s->stream);

@@ -203,7 +203,8 @@ extern "C" {
 
 vrt_status vrt_cast_device(vrt_world* w, const vrt_ray* rays, uint32_t n, const vrt_cast_params* params,
                            vrt_hit* hits, void* stream) {
-    vrt_status st = world_enter(w);
+    DeviceScope ds;
+    vrt_status st = world_enter(w, ds);
     if (st != VRT_OK || (st = check_params(params)) != VRT_OK) return st;
     if (n && (!rays || !hits)) {
         set_error("null ray or hit buffer");
@@ -214,7 +215,8 @@ vrt_status vrt_cast_device(vrt_world* w, const vrt_ray* rays, uint32_t n, const 
 
 vrt_status vrt_cast(vrt_world* w, const vrt_ray* rays, uint32_t n, const vrt_cast_params* params, vrt_hit* hits,
                     void* stream_) {
-    vrt_status st = world_enter(w);
+    DeviceScope ds;
+    vrt_status st = world_enter(w, ds);
     if (st != VRT_OK || (st = check_params(params)) != VRT_OK) return st;
     if (n == 0) return VRT_OK;
     if (!rays || !hits) {
@@ -236,7 +238,8 @@ vrt_status vrt_cast(vrt_world* w, const vrt_ray* rays, uint32_t n, const vrt_cas
 
 vrt_status vrt_render_view_device(vrt_world* w, const vrt_camera* cam, uint32_t max_iters, vrt_hit* hits,
                                   void* stream) {
-    vrt_status st = world_enter(w);
+    DeviceScope ds;
+    vrt_status st = world_enter(w, ds);
     if (st != VRT_OK || (st = check_camera(cam)) != VRT_OK) return st;
     if (!hits) {
         set_error("null hit buffer");
@@ -246,7 +249,8 @@ vrt_status vrt_render_view_device(vrt_world* w, const vrt_camera* cam, uint32_t 
 }
 
 vrt_status vrt_render_view(vrt_world* w, const vrt_camera* cam, uint32_t max_iters, vrt_hit* hits, void* stream_) {
-    vrt_status st = world_enter(w);
+    DeviceScope ds;
+    vrt_status st = world_enter(w, ds);
     if (st != VRT_OK || (st = check_camera(cam)) != VRT_OK) return st;
     if (!hits) {
         set_error("null hit buffer");

@@ -28,12 +28,12 @@ vrt_status cuda_fail(cudaError_t e, const char* what) {
     return VRT_ERR_DEVICE;
 }
 
-vrt_status world_enter(vrt_world* world) {
+vrt_status world_enter(vrt_world* world, DeviceScope& scope) {
     if (!world) {
         set_error("null world");
         return VRT_ERR_INVALID_ARG;
     }
-    VRT_CUDA(cudaSetDevice(world->device));
+    VRT_CUDA(scope.enter(world->device));
     return VRT_OK;
 }
 
@@ -480,7 +480,8 @@ vrt_status vrt_world_create(const vrt_world_desc* desc, vrt_world** out) {
     w->slots.assign(w->num_sectors(), SectorSlots{});
     w->h_table.assign(w->num_sectors(), SectorRec{0, 0, 0, 0});
     w->arena.reset(0);
-    vrt_status st = world_enter(w);
+    DeviceScope ds;
+    vrt_status st = world_enter(w, ds);
     if (st == VRT_OK) {
         e = cudaMalloc(&w->d_sectors, (size_t)w->num_sectors() * sizeof(SectorRec));
         if (e == cudaSuccess) e = cudaMemset(w->d_sectors, 0, (size_t)w->num_sectors() * sizeof(SectorRec));
@@ -516,7 +517,8 @@ vrt_status vrt_world_create(const vrt_world_desc* desc, vrt_world** out) {
 
 vrt_status vrt_world_destroy(vrt_world* w) {
     if (!w) return VRT_OK;
-    cudaSetDevice(w->device);
+    DeviceScope ds;
+    ds.enter(w->device);
     cudaDeviceSynchronize();
     if (w->d_sectors) cudaFree(w->d_sectors);
     if (w->d_bricks) cudaFree(w->d_bricks);
@@ -546,7 +548,8 @@ vrt_status vrt_world_get_stats(const vrt_world* cw, vrt_world_stats* out) {
     // the host mirror is rebuilt from the device after device edits (a cache of the
     // device's state, not a change to the world)
     vrt_world* w = const_cast<vrt_world*>(cw);
-    vrt_status st = world_enter(w);
+    DeviceScope ds;
+    vrt_status st = world_enter(w, ds);
     if (st != VRT_OK) return st;
     std::lock_guard<std::mutex> lock(w->mu);
     if ((st = refresh_host_mirror(w)) != VRT_OK) return st;
@@ -569,7 +572,8 @@ vrt_status vrt_world_get_stats(const vrt_world* cw, vrt_world_stats* out) {
 
 vrt_status vrt_world_sync_sectors(vrt_world* w, uint32_t n, const int32_t* sector_idx, const uint64_t* alloc_mask,
                                   const uint64_t* dirty_mask, const uint8_t* bricks, void* stream_) {
-    vrt_status st = world_enter(w);
+    DeviceScope ds;
+    vrt_status st = world_enter(w, ds);
     if (st != VRT_OK) return st;
     if (n && (!sector_idx || !alloc_mask)) {
         set_error("null sector arrays");
@@ -614,7 +618,8 @@ vrt_status vrt_world_sync_sectors(vrt_world* w, uint32_t n, const int32_t* secto
 }
 
 vrt_status vrt_world_save_cvox(vrt_world* w, const char* path) {
-    vrt_status st = world_enter(w);
+    DeviceScope ds;
+    vrt_status st = world_enter(w, ds);
     if (st != VRT_OK) return st;
     std::vector<int32_t> idx;
     std::vector<uint64_t> masks;
@@ -650,7 +655,8 @@ vrt_status vrt_world_load_cvox(vrt_world* w, const char* path, void* stream) {
 
 vrt_status vrt_world_read_sector(vrt_world* w, int32_t sector_idx, uint64_t* alloc_mask, uint8_t* bricks,
                                  size_t bricks_capacity, void* stream_) {
-    vrt_status st = world_enter(w);
+    DeviceScope ds;
+    vrt_status st = world_enter(w, ds);
     if (st != VRT_OK) return st;
     int32_t x, y, z;
     sector_index_unpack(sector_idx, x, y, z);

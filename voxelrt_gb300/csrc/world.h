@@ -161,8 +161,29 @@ struct vrt_world {
 };
 
 namespace vrt {
-// Make `world` current on the calling thread.
-vrt_status world_enter(vrt_world* world);
+// Makes a device current for the length of an ABI call and gives the caller's current
+// device back when the call returns, so the library never leaves it switched.
+struct DeviceScope {
+    int prev = -1;
+    bool switched = false;
+    DeviceScope() = default;
+    DeviceScope(const DeviceScope&) = delete;
+    DeviceScope& operator=(const DeviceScope&) = delete;
+    cudaError_t enter(int device) {
+        cudaError_t e = cudaGetDevice(&prev);
+        if (e != cudaSuccess) return e;
+        if (prev == device) return cudaSuccess;
+        e = cudaSetDevice(device);
+        switched = e == cudaSuccess;
+        return e;
+    }
+    ~DeviceScope() {
+        if (switched) cudaSetDevice(prev);
+    }
+};
+
+// Make `world`'s device current on the calling thread until `scope` ends.
+vrt_status world_enter(vrt_world* world, DeviceScope& scope);
 
 // While alive, kernels launched on `stream` carry an L2 access-policy window that keeps the
 // brick table of a VRT_WORLD_L2_PERSIST world persisting in L2 (the table is the mask
