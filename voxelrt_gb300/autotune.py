@@ -89,8 +89,10 @@ def time_config(worlds, views, cfg: BatchConfig, hits, stream, launches: int = 4
     return e0.elapsed_time(e1) / launches
 
 
-def tune(worlds, views, hits, stream, log=print) -> tuple[dict, float, list]:
-    """Staged sweep; returns (best config dict, ms, trials)."""
+def tune(worlds, views, hits, stream, log=print, passes: int = 2) -> tuple[dict, float, list]:
+    """Staged sweep (coordinate descent over the stages, `passes` times, so the tile shape
+    and warps are chosen again under the refill and round length found after them);
+    returns (best config dict, ms, trials)."""
     trials = []
 
     def run(d):
@@ -102,20 +104,27 @@ def tune(worlds, views, hits, stream, log=print) -> tuple[dict, float, list]:
     best = {"tile_w": 8, "tile_h": 8, "morton": 0, "warps_per_block": 4, "blocks_per_sm": 0,
             "refill_threshold": 16, "chunk_tiles": 2, "inner_iters": 4}
     best_ms = run(best)
+    # refill 1 with 128 steps per round is the "no compaction" end: a warp traces its 32
+    # rays until all of them end (up to the iteration cap) before it takes new ones
     stages = [
         [dict(tile_w=tw, tile_h=th, morton=m, warps_per_block=wp)
          for (tw, th, m), wp in itertools.product([(8, 8, 0), (8, 8, 1), (16, 4, 0), (32, 1, 0)], [2, 4, 8])],
-        [dict(refill_threshold=r, inner_iters=i) for r, i in itertools.product([4, 8, 12, 16, 20, 24, 28], [2, 4, 8, 16])],
+        [dict(refill_threshold=r, inner_iters=i)
+         for r, i in itertools.product([1, 2, 4, 8, 12, 16, 20, 24, 28], [4, 8, 16, 32, 64, 128])],
         [dict(chunk_tiles=c) for c in (1, 2, 4, 8, 16, 32, 64)],
     ]
-    for stage in stages:
-        for delta in stage:
-            d = {**best, **delta}
-            if d == best:
-                continue
-            ms = run(d)
-            if ms < best_ms:
-                best, best_ms = d, ms
+    tried = set()
+    for _ in range(passes):
+        for stage in stages:
+            for delta in stage:
+                d = {**best, **delta}
+                key = tuple(sorted(d.items()))
+                if d == best or key in tried:
+                    continue
+                tried.add(key)
+                ms = run(d)
+                if ms < best_ms:
+                    best, best_ms = d, ms
     return best, best_ms, trials
 
 
