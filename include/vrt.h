@@ -415,8 +415,9 @@ typedef struct vrt_batch_config {
     uint32_t warps_per_block;  /* 1..16 (0 = 4) */
     uint32_t blocks_per_sm;    /* 0 = as many as fit */
     uint32_t refill_threshold; /* refill idle lanes when fewer lanes are active (1..32, 0 = 16) */
-    uint32_t chunk_tiles;      /* tiles taken from the device queue per atomic (0 = 2) */
-    uint32_t inner_iters;      /* DDA iterations between refill checks (0 = 4) */
+    uint32_t chunk_tiles;      /* tiles taken from the device queue per atomic (1..64; 0 = chosen
+                                  per launch: about eight fetches per warp, 1..16 tiles) */
+    uint32_t inner_iters;      /* DDA iterations between refill checks (0 = 16) */
 } vrt_batch_config;
 
 typedef struct vrt_batch_stats {

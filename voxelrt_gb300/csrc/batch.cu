@@ -653,8 +653,8 @@ vrt_status normalize_batch_config(const vrt_batch_config* in, vrt_batch_config& 
     }
     if (cfg.warps_per_block == 0) cfg.warps_per_block = 4;
     if (cfg.refill_threshold == 0) cfg.refill_threshold = 16;
-    if (cfg.chunk_tiles == 0) cfg.chunk_tiles = 2;
-    if (cfg.inner_iters == 0) cfg.inner_iters = 4;
+    // chunk_tiles 0 stays 0: the planner picks it per launch (auto_chunk_tiles)
+    if (cfg.inner_iters == 0) cfg.inner_iters = 16;
     if (cfg.warps_per_block > 16 || cfg.refill_threshold > 32 || cfg.chunk_tiles > 64 || cfg.inner_iters > 1024) {
         set_error("batch config out of range");
         return VRT_ERR_INVALID_ARG;
@@ -662,8 +662,13 @@ vrt_status normalize_batch_config(const vrt_batch_config* in, vrt_batch_config& 
     return VRT_OK;
 }
 
-vrt_status plan_views(const vrt_view* views, uint32_t n, uint32_t n_worlds, const vrt_batch_config& cfg,
-                      LaunchPlan& plan) {
+uint32_t auto_chunk_tiles(uint64_t tiles, uint64_t warps) {
+    if (warps == 0) return 1;
+    return (uint32_t)std::min<uint64_t>(16, std::max<uint64_t>(1, tiles / (warps * 8)));
+}
+
+vrt_status plan_views(const vrt_view* views, uint32_t n, uint32_t n_worlds, const vrt_batch_config& cfg_in,
+                      LaunchPlan& plan, uint64_t warps) {
     vrt_status st;
     for (uint32_t i = 0; i < n; i++) {
         if ((st = check_view(&views[i])) != VRT_OK) return st;
@@ -673,6 +678,14 @@ vrt_status plan_views(const vrt_view* views, uint32_t n, uint32_t n_worlds, cons
         }
     }
     if ((st = check_same_mode(views, n)) != VRT_OK) return st;
+    vrt_batch_config cfg = cfg_in;
+    if (cfg.chunk_tiles == 0) {
+        uint64_t tiles = 0;
+        for (uint32_t i = 0; i < n; i++)
+            tiles += (uint64_t)((views[i].cam.width + cfg.tile_w - 1) / cfg.tile_w) *
+                     ((views[i].cam.height + cfg.tile_h - 1) / cfg.tile_h);
+        cfg.chunk_tiles = auto_chunk_tiles(tiles, warps);
+    }
     plan.glsl = n > 0 && view_glsl(views[0]);
     plan.aniso = n > 0 && view_aniso(views[0]);
     plan.full = false;
@@ -914,11 +927,24 @@ vrt_status vrt_batch_create(vrt_world* const* worlds, uint32_t n_worlds, const v
             set_error("worlds must be non-null and on one device");
             return VRT_ERR_INVALID_ARG;
         }
+    DeviceScope ds;
+    VRT_CUDA(ds.enter(worlds[0]->device));
+    // the launch grid first: an auto chunk size depends on the number of warps
+    int grid_blocks = 0, grid_threads = 0;
+    {
+        bool full = false;
+        for (uint32_t i = 0; i < n_views; i++) full |= view_full_path(views[i]);
+        if ((st = persistent_grid(worlds[0]->device, cfg, false, view_glsl(views[0]), view_aniso(views[0]), false,
+                                  full, grid_blocks, grid_threads)) != VRT_OK)
+            return st;
+    }
     auto* b = new vrt_batch;
-    if ((st = plan_views(views, n_views, n_worlds, cfg, b->plan)) != VRT_OK) {
+    if ((st = plan_views(views, n_views, n_worlds, cfg, b->plan, (uint64_t)grid_blocks * (grid_threads / 32))) !=
+        VRT_OK) {
         delete b;
         return st;
     }
+    cfg = b->plan.cfg;
     b->device = worlds[0]->device;
     b->worlds.assign(worlds, worlds + n_worlds);
     uint32_t n_l2 = 0;
@@ -933,9 +959,7 @@ vrt_status vrt_batch_create(vrt_world* const* worlds, uint32_t n_worlds, const v
         vrt_batch_destroy(b);
         return s;
     };
-    DeviceScope ds;
-    cudaError_t e = ds.enter(b->device);
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_worlds, sizeof(DevWorld) * n_worlds);
+    cudaError_t e = cudaMalloc(&b->d_worlds, sizeof(DevWorld) * n_worlds);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_views, sizeof(ViewDev) * n_views);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_chunk_base, sizeof(uint32_t) * (n_views + 1));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_queue, 64);

@@ -112,9 +112,15 @@ uint64_t view_record_count(const vrt_view& v);
 vrt_status check_view(const vrt_view* v);
 // Fill defaults and validate a batch config.
 vrt_status normalize_batch_config(const vrt_batch_config* in, vrt_batch_config& out);
+// Tiles per queue chunk when a config leaves it to the library (chunk_tiles 0): about
+// eight chunks per warp of the launch, 1..16 tiles.  Fixed chunks too large for a small
+// launch leave most warps without work; the tuned table names its chunks explicitly.
+uint32_t auto_chunk_tiles(uint64_t tiles, uint64_t warps);
 // Validate views against n_worlds and lay them out (tiles, queue chunks, record offsets).
+// A config with chunk_tiles 0 gets auto_chunk_tiles for a launch of `warps` warps, and
+// plan.cfg holds the chunk size used.
 vrt_status plan_views(const vrt_view* views, uint32_t n, uint32_t n_worlds, const vrt_batch_config& cfg,
-                      LaunchPlan& plan);
+                      LaunchPlan& plan, uint64_t warps = 0);
 // Grid of the persistent kernel: every SM, as many blocks of the launched instantiation
 // (counting, traversal mode, resident) as fit, or cfg.blocks_per_sm of them.
 vrt_status persistent_grid(int device, const vrt_batch_config& cfg, bool count, bool glsl, bool aniso, bool resident,

@@ -206,7 +206,9 @@ vrt_status launch_slot(vrt_server* sv, Slot& s, std::vector<Request*>& rs) {
     std::vector<vrt_view> views(rs.size());
     for (size_t i = 0; i < rs.size(); i++) views[i] = rs[i]->view;
     LaunchPlan plan;
-    vrt_status st = plan_views(views.data(), (uint32_t)views.size(), (uint32_t)sv->worlds.size(), sv->bcfg, plan);
+    const int* g = sv->grid_of(view_mode(views[0]));
+    vrt_status st = plan_views(views.data(), (uint32_t)views.size(), (uint32_t)sv->worlds.size(), sv->bcfg, plan,
+                               (uint64_t)g[0] * (g[1] / 32));
     if (st != VRT_OK) return st;
     // each request writes into its own arena pages
     for (size_t i = 0; i < rs.size(); i++) plan.views[i].out_base = (uint64_t)(rs[i]->page_base - 1) * kPageRecords;
@@ -230,7 +232,6 @@ vrt_status launch_slot(vrt_server* sv, Slot& s, std::vector<Request*>& rs) {
                              s.stream));
     BatchParams p = make_params(plan, sv->d_worlds, (const ViewDev*)s.views.ptr, (const uint32_t*)s.chunk_base.ptr,
                                 (uint32_t*)s.queue.ptr, (vrt_hit*)sv->arena);
-    const int* g = sv->grid_of(view_mode(views[0]));
     if ((st = launch_persistent(p, g[0], g[1], false, s.stream)) != VRT_OK) return st;
     for (size_t i = 0; i < rs.size(); i++) {
         const Request* r = rs[i];
