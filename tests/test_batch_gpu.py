@@ -90,6 +90,11 @@ CONFIGS = [
     dict(tile_w=8, tile_h=8, morton=1, refill_threshold=32, inner_iters=1),
     dict(tile_w=16, tile_h=4, refill_threshold=1, inner_iters=8, chunk_tiles=1),
     dict(tile_w=32, tile_h=1, warps_per_block=8, refill_threshold=24, chunk_tiles=5, blocks_per_sm=1),
+    # the GB300 table's camera-workload shapes: rounds long enough to trace every ray to its end
+    dict(refill_threshold=28, chunk_tiles=16, inner_iters=128),
+    dict(warps_per_block=2, refill_threshold=1, chunk_tiles=4, inner_iters=128),
+    # chunk size picked per launch, for a grid of one block per SM
+    dict(blocks_per_sm=1, inner_iters=64),
 ]
 
 
