@@ -239,7 +239,7 @@ def peak_hbm():
 
 # What bounds the persistent kernel on a workload, from the committed ncu summaries.
 LIMITERS = {
-    "uneven_batch": "instruction issue: 73.7 % of issue slots busy, wait (fixed-latency dependency) the first "
+    "uneven_batch": "instruction issue: 72.5 % of issue slots busy, wait (fixed-latency dependency) the first "
                     "stall (profiles/persistent_kernel_uneven_batch_medium.md)",
 }
 
