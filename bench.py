@@ -644,9 +644,10 @@ def run_ours(args, engine_cls=None, backend: str = "nccl", device: str = "cuda")
 # ---------------------------------------------------------------------------------------
 # sub-results: the large world (config 1) and the incoherent workload (config 3)
 
-def measure_workload(v, wl, dev, steps, stream, check_views=2, stress=None):
+def measure_workload(v, wl, dev, steps, stream, check_views=2, stress=None, hook=None):
     """Persistent-launch throughput of one workload (CUDA graph replay, inputs resident),
-    its roofline and an oracle check of `check_views` whole views."""
+    its roofline and an oracle check of `check_views` whole views.  hook(v, worlds, wl,
+    stream) -> dict adds further measurements on the same resident worlds."""
     import torch
 
     from voxelrt_gb300 import autotune
@@ -697,6 +698,8 @@ def measure_workload(v, wl, dev, steps, stream, check_views=2, stress=None):
     batch.close()
     if stress is not None:
         out["stress"] = run_stress(v, worlds[0], wl.worlds[0], stress, stream, n=stress.stress_rays)
+    if hook is not None:
+        out.update(hook(v, worlds, wl, stream))
     for w in worlds:
         w.close()
     torch.cuda.synchronize()
@@ -718,8 +721,135 @@ def run_sub_results(args, dev):
             for vw in wl.views:
                 vw.flags |= v.VIEW_GLSL | (v.capi.VIEW_GLSL_ANISO if args.aniso else 0)
         stress = args if (name == "incoherent" and not args.no_stress) else None
-        out[name] = measure_workload(v, wl, dev, args.sub_steps, stream, stress=stress)
+        hook = None
+        if not (args.glsl or args.aniso):
+            hook = renderer_rows if name == "large_world" else cvox_round_trip
+        out[name] = measure_workload(v, wl, dev, args.sub_steps, stream, stress=stress, hook=hook)
     return out
+
+
+def _projection(aspect, near=0.1, far=4000.0, fov=90.0):
+    """A perspective matrix, column-major (glm layout), for the G-buffer's projected depth."""
+    f = 1.0 / np.tan(np.radians(fov) / 2)
+    p = np.zeros((4, 4))
+    p[0, 0], p[1, 1] = f / aspect, f
+    p[2, 2], p[2, 3] = (far + near) / (near - far), 2 * far * near / (near - far)
+    p[3, 2] = -1.0
+    return p.T.astype(np.float32).reshape(16)
+
+
+def _time_ms(stream, fn, reps=5):
+    import torch
+    with torch.cuda.stream(stream):
+        fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def renderer_rows(v, worlds, wl, stream):
+    """On the large world: the G-buffer of a 1080p view (vrt_render_gbuffer_device) and the GPU
+    renderer's whole per-pixel path (primary, sun, 3 bounces with a sun ray after the first two)
+    over 8 1080p views in one persistent launch.  Each is checked against the oracle on a
+    320x180 view of the same camera."""
+    import torch
+
+    from oracle.oracle import OracleWorld
+    w, d = worlds[0], wl.worlds[0]
+    cams = [vw.cam for vw in wl.views[:8]]
+    rng = np.random.default_rng(5)
+    pal = rng.integers(0, 1 << 16, 256, dtype=np.uint32) | rng.integers(0, 1 << 16, 256, dtype=np.uint32) << 16
+    pal[0] = 0
+    proj = _projection(16 / 9)
+    # G-buffer, device buffers, primary records included
+    view = v.make_view(cams[0])
+    n = cams[0].width * cams[0].height
+    d_tex = torch.empty(n, dtype=torch.int32, device="cuda")
+    d_depth = torch.empty(n, dtype=torch.float32, device="cuda")
+    d_hits = torch.empty(n * HIT_BYTES, dtype=torch.uint8, device="cuda")
+    ss = stream.cuda_stream
+
+    def gbuf():
+        v.check(v.lib().vrt_render_gbuffer_device(w.handle, v.capi.C.byref(view), pal.ctypes.data, proj.ctypes.data,
+                                                  d_tex.data_ptr(), d_depth.data_ptr(), d_hits.data_ptr(), ss))
+    g_ms = _time_ms(stream, gbuf)
+    del d_tex, d_depth, d_hits
+    # the renderer's whole path, 8 views in one batch
+    sun = tuple(float(c) for c in wl.views[0].sun_dir)
+    pviews = [v.make_view(c, n_bounces=3, shadow_dir=sun) for c in cams]
+    b = v.Batch(worlds, pviews)
+    ph = torch.empty(b.total_records * HIT_BYTES, dtype=torch.uint8, device="cuda")
+    p_ms = _time_ms(stream, lambda: b.launch(ph, stream, graph=True))
+    st = b.measure(ph, stream)
+    del ph
+    b.close()
+    # oracle checks on a 320x180 view of the first camera
+    o = OracleWorld(d.sectors)
+    o.upload(d)
+    sc = _scaled_camera(v, cams[0], 320, 180)
+    tex, depth = v.render_gbuffer(w, v.make_view(sc), pal, proj)
+    want_tex, want_depth, _ = o.render_gbuffer(sc, pal, proj)
+    g_ok = bool(np.array_equal(tex, want_tex) and np.array_equal(depth.view(np.uint32), want_depth.view(np.uint32)))
+    sb = v.Batch(worlds, [v.make_view(sc, n_bounces=3, shadow_dir=sun)])
+    got = sb.view_hits(sb.run(), 0)
+    sb.close()
+    want = o.render_view_path(sc, np.array(sun, np.float32), 3)
+    p_ok = bool(got.shape == want.shape and all(hits_match(got[k], want[k]) for k in range(got.shape[0])))
+    o.close()
+    return {"gbuffer": {"api": "vrt_render_gbuffer_device", "view": "1920x1080", "ms": g_ms,
+                        "mpix_s": n / (g_ms * 1e-3) / 1e6, "checked": "320x180 view of the same camera",
+                        "bit_exact": g_ok},
+            "renderer_path": {"api": "vrt_batch (persistent launch, graph replay)", "views": "8 x 1920x1080",
+                              "path": "primary, sun, 3 bounces, a sun ray after the first two", "ms": p_ms,
+                              "rays": st["rays_cast"], "value": st["rays_cast"] / (p_ms * 1e-3) / 1e9,
+                              "unit": "Grays/s", "checked": "320x180 view of the first camera", "bit_exact": p_ok}}
+
+
+def _scaled_camera(v, cam, width, height):
+    """The camera `cam` at another resolution: the same eye and image plane (d0 is the plane's
+    corner, du and dv one pixel's step), so the same field of view."""
+    c = v.Camera()
+    C = v.capi.C
+    C.memmove(C.byref(c), C.byref(cam), C.sizeof(c))
+    sx, sy = cam.width / width, cam.height / height
+    for i in range(3):
+        c.du[i] = cam.du[i] * sx
+        c.dv[i] = cam.dv[i] * sy
+    c.width, c.height = width, height
+    return c
+
+
+def cvox_round_trip(v, worlds, wl, stream):
+    """On the 1024^3 world: save to a cvox v4 file (vrt_world_save_cvox) and load it into a new
+    world (vrt_world_load_cvox); the loaded world must cast 64 Ki random rays exactly as the
+    original."""
+    import tempfile
+    import time as _t
+
+    w, d = worlds[0], wl.worlds[0]
+    with tempfile.TemporaryDirectory() as tmp:
+        path = Path(tmp) / "world.cvox"
+        t0 = _t.perf_counter()
+        w.save_cvox(path)
+        t_save = _t.perf_counter() - t0
+        size = path.stat().st_size
+        w2 = v.World(d.sectors, brick_capacity=d.n_bricks + 64)
+        t0 = _t.perf_counter()
+        w2.load_cvox(path)
+        v.check(v.lib().vrt_world_wait(w2.handle))
+        t_load = _t.perf_counter() - t0
+    rays = v.random_rays([c * 32 for c in d.sectors], seed=11, n=1 << 16)
+    same = bool(np.array_equal(w.cast(rays).view(np.uint8), w2.cast(rays).view(np.uint8)))
+    w2.close()
+    bricks_mb = d.n_bricks * 512 / 1e6
+    return {"cvox": {"api": "vrt_world_save_cvox / vrt_world_load_cvox", "file_mb": size / 1e6,
+                     "brick_mb": bricks_mb, "save_s": t_save, "load_s": t_load,
+                     "save_mb_s": bricks_mb / t_save, "load_mb_s": bricks_mb / t_load,
+                     "check": "64 Ki random rays cast on the loaded world equal the original's", "bit_exact": same}}
 
 
 # ---------------------------------------------------------------------------------------
