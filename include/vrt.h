@@ -414,9 +414,11 @@ typedef struct vrt_batch_config {
     uint32_t morton;           /* 1: Z-order inside 8x8 tiles */
     uint32_t warps_per_block;  /* 1..16 (0 = 4) */
     uint32_t blocks_per_sm;    /* 0 = as many as fit */
-    uint32_t refill_threshold; /* refill idle lanes when fewer lanes are active (1..32, 0 = 16) */
-    uint32_t chunk_tiles;      /* tiles taken from the device queue per atomic (1..64; 0 = chosen
-                                  per launch: about eight fetches per warp, 1..16 tiles) */
+    uint32_t refill_threshold; /* refill idle lanes when fewer lanes are active (1..32; 0 = 28 for a
+                                  launch with diffuse bounces, else 16) */
+    uint32_t chunk_tiles;      /* tiles taken from the device queue per atomic (1..64; 0 = 1 for a
+                                  launch with diffuse bounces, else chosen per launch: about
+                                  eight fetches per warp, 1..16 tiles) */
     uint32_t inner_iters;      /* DDA iterations between refill checks (0 = 16) */
 } vrt_batch_config;
 

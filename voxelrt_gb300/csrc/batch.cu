@@ -652,8 +652,8 @@ vrt_status normalize_batch_config(const vrt_batch_config* in, vrt_batch_config& 
         return VRT_ERR_INVALID_ARG;
     }
     if (cfg.warps_per_block == 0) cfg.warps_per_block = 4;
-    if (cfg.refill_threshold == 0) cfg.refill_threshold = 16;
-    // chunk_tiles 0 stays 0: the planner picks it per launch (auto_chunk_tiles)
+    // refill_threshold 0 and chunk_tiles 0 stay 0: resolve_batch_defaults picks them from
+    // the launch's views and grid
     if (cfg.inner_iters == 0) cfg.inner_iters = 16;
     if (cfg.warps_per_block > 16 || cfg.refill_threshold > 32 || cfg.chunk_tiles > 64 || cfg.inner_iters > 1024) {
         set_error("batch config out of range");
@@ -665,6 +665,18 @@ vrt_status normalize_batch_config(const vrt_batch_config* in, vrt_batch_config& 
 uint32_t auto_chunk_tiles(uint64_t tiles, uint64_t warps) {
     if (warps == 0) return 1;
     return (uint32_t)std::min<uint64_t>(16, std::max<uint64_t>(1, tiles / (warps * 8)));
+}
+
+void resolve_batch_defaults(vrt_batch_config& cfg, const vrt_view* views, uint32_t n, uint64_t warps) {
+    bool bounces = false;
+    uint64_t tiles = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        bounces |= views[i].n_bounces > 0;
+        tiles += (uint64_t)((views[i].cam.width + cfg.tile_w - 1) / cfg.tile_w) *
+                 ((views[i].cam.height + cfg.tile_h - 1) / cfg.tile_h);
+    }
+    if (cfg.refill_threshold == 0) cfg.refill_threshold = bounces ? 28 : 16;
+    if (cfg.chunk_tiles == 0) cfg.chunk_tiles = bounces ? 1 : auto_chunk_tiles(tiles, warps);
 }
 
 vrt_status plan_views(const vrt_view* views, uint32_t n, uint32_t n_worlds, const vrt_batch_config& cfg_in,
@@ -679,13 +691,7 @@ vrt_status plan_views(const vrt_view* views, uint32_t n, uint32_t n_worlds, cons
     }
     if ((st = check_same_mode(views, n)) != VRT_OK) return st;
     vrt_batch_config cfg = cfg_in;
-    if (cfg.chunk_tiles == 0) {
-        uint64_t tiles = 0;
-        for (uint32_t i = 0; i < n; i++)
-            tiles += (uint64_t)((views[i].cam.width + cfg.tile_w - 1) / cfg.tile_w) *
-                     ((views[i].cam.height + cfg.tile_h - 1) / cfg.tile_h);
-        cfg.chunk_tiles = auto_chunk_tiles(tiles, warps);
-    }
+    resolve_batch_defaults(cfg, views, n, warps);
     plan.glsl = n > 0 && view_glsl(views[0]);
     plan.aniso = n > 0 && view_aniso(views[0]);
     plan.full = false;
@@ -778,7 +784,9 @@ BatchParams make_params(const LaunchPlan& plan, const DevWorld* worlds, const Vi
     p.tile_size_log2 = plan.tile_size_log2;
     p.morton = plan.cfg.morton;
     p.chunk_rays = plan.cfg.chunk_tiles << plan.tile_size_log2;
-    p.refill = plan.cfg.refill_threshold;
+    // at least 1: a warp whose lanes are all idle must always claim (a resident warp learns
+    // of the mailbox's close only through a claim)
+    p.refill = std::max(1u, plan.cfg.refill_threshold);
     p.inner = plan.cfg.inner_iters;
     p.glsl = plan.glsl ? 1u : 0u;
     p.aniso = plan.aniso ? 1u : 0u;

@@ -116,9 +116,13 @@ vrt_status normalize_batch_config(const vrt_batch_config* in, vrt_batch_config& 
 // eight chunks per warp of the launch, 1..16 tiles.  Fixed chunks too large for a small
 // launch leave most warps without work; the tuned table names its chunks explicitly.
 uint32_t auto_chunk_tiles(uint64_t tiles, uint64_t warps);
+// Fill the fields a config leaves to the library (0): views with diffuse bounces (long,
+// uneven, incoherent paths per pixel) refill below 28 lanes and claim one tile at a time;
+// camera and sun rays refill below 16 and claim auto_chunk_tiles.
+void resolve_batch_defaults(vrt_batch_config& cfg, const vrt_view* views, uint32_t n, uint64_t warps);
 // Validate views against n_worlds and lay them out (tiles, queue chunks, record offsets).
-// A config with chunk_tiles 0 gets auto_chunk_tiles for a launch of `warps` warps, and
-// plan.cfg holds the chunk size used.
+// Fields left to the library are resolved for a launch of `warps` warps
+// (resolve_batch_defaults), and plan.cfg holds the config used.
 vrt_status plan_views(const vrt_view* views, uint32_t n, uint32_t n_worlds, const vrt_batch_config& cfg,
                       LaunchPlan& plan, uint64_t warps = 0);
 // Grid of the persistent kernel: every SM, as many blocks of the launched instantiation

@@ -113,19 +113,13 @@ extern "C" vrt_status vrt_render_views_static(vrt_world* const* worlds, uint32_t
     uint8_t* scratch = g_state.scratch[device];
     // the copies of the last call on this device have read the host tables
     VRT_CUDA(cudaEventSynchronize(g_state.copied[device]));
-    // the launch grid, and the chunk size when the config leaves it to the library
+    // the launch grid, and what the config leaves to the library
     const bool aniso = view_aniso(views[0]);
     bool full = false;
     for (uint32_t i = 0; i < n_views; i++) full |= view_full_path(views[i]);
     int blocks = 0, threads = 0;
     if ((st = persistent_grid(device, cfg, false, glsl, aniso, false, full, blocks, threads)) != VRT_OK) return st;
-    if (cfg.chunk_tiles == 0) {
-        uint64_t tiles = 0;
-        for (uint32_t i = 0; i < n_views; i++)
-            tiles += (uint64_t)((views[i].cam.width + cfg.tile_w - 1) / cfg.tile_w) *
-                     ((views[i].cam.height + cfg.tile_h - 1) / cfg.tile_h);
-        cfg.chunk_tiles = auto_chunk_tiles(tiles, (uint64_t)blocks * (threads / 32));
-    }
+    resolve_batch_defaults(cfg, views, n_views, (uint64_t)blocks * (threads / 32));
     // lay the views out behind one tile queue (same layout as vrt_batch)
     const uint32_t tw_log2 = log2u_static(cfg.tile_w), ts_log2 = log2u_static(cfg.tile_w * cfg.tile_h);
     uint64_t chunks = 0, records = 0;
@@ -173,7 +167,7 @@ extern "C" vrt_status vrt_render_views_static(vrt_world* const* worlds, uint32_t
     p.tile_size_log2 = ts_log2;
     p.morton = cfg.morton;
     p.chunk_rays = cfg.chunk_tiles << ts_log2;
-    p.refill = cfg.refill_threshold;
+    p.refill = std::max(1u, cfg.refill_threshold);
     p.inner = cfg.inner_iters;
     p.glsl = glsl ? 1u : 0u;
     p.aniso = aniso ? 1u : 0u;

@@ -452,6 +452,8 @@ vrt_status resident_start(vrt_server* sv, uint32_t mode, bool full) {
     VRT_CUDA(cudaMemsetAsync(R.queue.ptr, 0, kResidentHintOffset + 8, R.ctl));  // claim counter, counters, hint
     LaunchPlan plan;
     vrt_batch_config cfg = resident_config(sv);
+    // fields the config leaves to the library, for a launch whose views arrive later
+    resolve_batch_defaults(cfg, nullptr, 0, 0);
     plan.cfg = cfg;
     uint32_t r = 0;
     while ((1u << r) < cfg.tile_w) r++;
