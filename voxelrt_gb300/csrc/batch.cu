@@ -787,7 +787,7 @@ BatchParams make_params(const LaunchPlan& plan, const DevWorld* worlds, const Vi
     // at least 1: a warp whose lanes are all idle must always claim (a resident warp learns
     // of the mailbox's close only through a claim)
     p.refill = std::max(1u, plan.cfg.refill_threshold);
-    p.inner = plan.cfg.inner_iters;
+    p.inner = std::max(1u, plan.cfg.inner_iters);  // a round must step, or no ray would progress
     p.glsl = plan.glsl ? 1u : 0u;
     p.aniso = plan.aniso ? 1u : 0u;
     p.full = plan.full ? 1u : 0u;

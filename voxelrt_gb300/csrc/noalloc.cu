@@ -168,7 +168,7 @@ extern "C" vrt_status vrt_render_views_static(vrt_world* const* worlds, uint32_t
     p.morton = cfg.morton;
     p.chunk_rays = cfg.chunk_tiles << ts_log2;
     p.refill = std::max(1u, cfg.refill_threshold);
-    p.inner = cfg.inner_iters;
+    p.inner = std::max(1u, cfg.inner_iters);
     p.glsl = glsl ? 1u : 0u;
     p.aniso = aniso ? 1u : 0u;
     p.full = full ? 1u : 0u;
