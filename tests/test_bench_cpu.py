@@ -38,3 +38,21 @@ def test_reference_arm_loads_no_product_library(tmp_path):
     line = [ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1]
     assert '"impl": "reference"' in line
     assert "MAPS False True True" in r.stdout
+
+
+def test_profiled_traffic_not_for_a_smaller_large_world():
+    assert bench.traffic_from_profile("large_world", bench.parse(["--workload", "large_world", "--cameras", "8"])) is None
+
+
+def test_scaled_camera_keeps_the_image_plane():
+    """The oracle checks of the renderer rows run a smaller view of the same camera: the
+    plane's corner d0 and its far corner d0 + W*du + H*dv stay where they were."""
+    import numpy as np
+    cam = v.look_at((100.5, 80.0, 30.0), (400.0, 60.0, 900.0), 90.0, 1920, 1080)
+    sc = bench._scaled_camera(v, cam, 320, 180)
+    assert (sc.width, sc.height) == (320, 180)
+    assert list(sc.origin) == list(cam.origin) and list(sc.world_origin) == list(cam.world_origin)
+    d0, du, dv = (np.array(getattr(cam, k)[:], np.float64) for k in ("d0", "du", "dv"))
+    s0, su, sv = (np.array(getattr(sc, k)[:], np.float64) for k in ("d0", "du", "dv"))
+    assert np.array_equal(s0, d0)
+    assert np.allclose(s0 + 320 * su + 180 * sv, d0 + 1920 * du + 1080 * dv, rtol=1e-6, atol=1e-6)
