@@ -80,6 +80,9 @@ def parse(argv=None):
     ap.add_argument("--worlds", type=int, default=128, help="uneven_batch: number of worlds")
     ap.add_argument("--max-views", type=int, default=16, help="uneven_batch: views per world, at most")
     ap.add_argument("--cameras", type=int, default=64, help="large_world: number of 1080p cameras")
+    ap.add_argument("--renderer-path", action="store_true",
+                    help="large_world: every view traces the GPU renderer's whole per-pixel path (primary, sun, "
+                         "3 bounces, a sun ray after the first two) instead of primary + shadow")
     ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
                     help="N>1: every rank traces its own batch (weak) or a share, by world, of one batch (strong)")
     return ap.parse_args(argv)
@@ -168,7 +171,14 @@ def _build_workload(name: str, rank: int, args=None, world_size: int = 1):
             wl = W.Workload(wl.name, worlds, views, f"{wl.description}, worlds {own} of {world_size} ranks")
         return wl
     if name == "large_world":
-        return W.large_world(n_cameras=args.cameras if args is not None else 64)
+        wl = W.large_world(n_cameras=args.cameras if args is not None else 64)
+        if args is not None and getattr(args, "renderer_path", False):
+            from voxelrt_gb300 import make_view
+            sun = tuple(float(c) for c in wl.views[0].sun_dir)
+            wl.views = [make_view(vw.cam, n_bounces=3, shadow_dir=sun) for vw in wl.views]
+            wl.description = (f"2048x256x2048 terrain+caves, {len(wl.views)} cameras 1920x1080, the GPU renderer's "
+                              "whole path (primary, sun, 3 bounces, a sun ray after the first two)")
+        return wl
     if name == "incoherent":
         return W.incoherent()
     return W.single_view()
@@ -252,7 +262,7 @@ def traffic_from_profile(workload: str, args=None):
     if not p.exists():
         return None
     if args is not None and (args.glsl or args.aniso or args.worlds != 128 or args.max_views != 16 or
-                             getattr(args, "cameras", 64) != 64):
+                             getattr(args, "cameras", 64) != 64 or getattr(args, "renderer_path", False)):
         return None
     try:
         return json.loads(p.read_text()).get(workload)
