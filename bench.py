@@ -178,6 +178,8 @@ def _build_workload(name: str, rank: int, args=None, world_size: int = 1):
             wl.views = [make_view(vw.cam, n_bounces=3, shadow_dir=sun) for vw in wl.views]
             wl.description = (f"2048x256x2048 terrain+caves, {len(wl.views)} cameras 1920x1080, the GPU renderer's "
                               "whole path (primary, sun, 3 bounces, a sun ray after the first two)")
+            # no tuned entry: the library's defaults for views with bounces, not the camera-ray table entry
+            wl.name = "large_world_renderer_path"
         return wl
     if name == "incoherent":
         return W.incoherent()
