@@ -363,6 +363,11 @@ __global__ void __maxnreg__(72) persistent_kernel(BatchParams p) {
                 }
             }
         }
+        // Compaction and regeneration: once fewer than p.refill lanes trace, the idle ones
+        // take new rays from the warp's chunk.  With rounds as long as the iteration cap
+        // (p.inner >= max_iters) a round ends only when every lane has finished, so the
+        // warp takes 32 new rays of one tile together, which keeps camera rays coherent;
+        // bounce rays, incoherent anyway, gain from refills in the middle of a path.
         const uint32_t act = __ballot_sync(0xffffffffu, active);
         bool q_wait = false;  // resident: nothing published right now
         if ((uint32_t)__popc(act) < p.refill && !q_empty) {
