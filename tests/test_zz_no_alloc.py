@@ -82,9 +82,11 @@ def test_static_scratch_matches_oracle_and_batch(scene):
     for vs, want in zip(sets, wants):
         assert_hits_equal(v.Batch(worlds, vs).run(), want)
     outs = [torch.empty(len(w) * 16, dtype=torch.uint8, device="cuda") for w in wants]
-    # the first call of each mode loads that kernel's module; the device memory that
+    # the first call of each mode loads that kernel's module, and the first fill loads
+    # torch's fill kernel (modules load lazily, at first use); the device memory that
     # takes is in place before the checked calls below
     for vs, out in zip(sets, outs):
+        out.fill_(0xAB)
         v.check(call_static(worlds, vs, out.data_ptr()))
     torch.cuda.synchronize()
     before = device_memory(torch)
