@@ -10,6 +10,7 @@
 // BinaryIO.cpp framing, compiled in place with the system's libzstd.
 #include "CpuRenderer.cpp"
 #include "VoxelMap.cpp"
+#include "BrickSlotAllocator.cpp"
 
 #include <algorithm>
 #include <stdexcept>
@@ -174,6 +175,62 @@ int ref_pick(void* p, uint64_t n, const double* rays, uint32_t max_iters, double
         uv[i * 2 + 1] = h.UV.y;
     }
     return 0;
+}
+
+// BrickSlotAllocator (BrickSlotAllocator.cpp:5-94, .h:6-65) over a run of sector edits:
+// op i adds the bricks add[i] to sector sector[i] (Alloc), then drops remove[i] (Free).
+// After each op the sector's BaseSlot and AllocMask are recorded; at the end the free
+// ranges (start, length), up to max_ranges of them.  The reference throws when no range
+// fits, after freeing the sector's old range, so the run stops before such an op.
+// Returns the number of ops run; *n_ranges receives the number of free ranges.
+uint32_t ref_alloc_run(uint32_t bounds_xz, uint32_t bounds_y, uint32_t n, const uint32_t* sector, const uint64_t* add,
+                       const uint64_t* remove, uint32_t* base_out, uint64_t* mask_out, uint32_t* ranges_out,
+                       uint32_t max_ranges, uint32_t* n_ranges) {
+    BrickSlotAllocator alloc(glm::uvec2(bounds_xz, bounds_y));
+    const uint32_t n_sectors = alloc.Arena.Capacity / 64;
+    uint32_t i = 0;
+    for (; i < n; i++) {
+        if (sector[i] >= n_sectors) break;
+        BrickSlotAllocator::SectorInfo* s = &alloc.Sectors[sector[i]];
+        // would Alloc find room? (the same test as FreeList::Realloc, without its side effects)
+        const uint64_t nm = s->AllocMask | add[i];
+        if (nm != s->AllocMask) {
+            const uint32_t cur = (uint32_t)std::popcount(s->AllocMask), want = (uint32_t)std::popcount(nm);
+            bool fits = false;
+            if (s->BaseSlot != 0) {
+                auto it = alloc.Arena.FreeRanges.lower_bound(s->BaseSlot);
+                fits = it != alloc.Arena.FreeRanges.end() && it->first == s->BaseSlot + cur &&
+                       s->BaseSlot + want < it->first + it->second;
+            }
+            uint32_t largest = 0;
+            for (const auto& r : alloc.Arena.FreeRanges) largest = std::max(largest, r.second);
+            // freeing the old range first can merge it with its neighbours
+            if (!fits) {
+                BrickSlotAllocator trial = BrickSlotAllocator(glm::uvec2(bounds_xz, bounds_y));
+                trial.Arena.FreeRanges = alloc.Arena.FreeRanges;
+                trial.Arena.NumAllocated = alloc.Arena.NumAllocated;
+                if (s->BaseSlot != 0) trial.Arena.Free(s->BaseSlot, cur);
+                largest = 0;
+                for (const auto& r : trial.Arena.FreeRanges) largest = std::max(largest, r.second);
+                fits = largest >= want;
+            }
+            if (!fits) break;
+            alloc.Alloc(s, add[i]);
+        }
+        alloc.Free(s, remove[i]);
+        base_out[i] = s->BaseSlot;
+        mask_out[i] = s->AllocMask;
+    }
+    uint32_t k = 0;
+    for (const auto& r : alloc.Arena.FreeRanges) {
+        if (k < max_ranges) {
+            ranges_out[2 * k] = r.first;
+            ranges_out[2 * k + 1] = r.second;
+        }
+        k++;
+    }
+    *n_ranges = k;
+    return i;
 }
 
 }  // extern "C"
