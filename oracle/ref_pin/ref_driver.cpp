@@ -177,6 +177,31 @@ int ref_pick(void* p, uint64_t n, const double* rays, uint32_t max_iters, double
     return 0;
 }
 
+// Sphere edits through the reference's own region dispatch and brick GC:
+// VoxelMap::RegionDispatchSIMD (VoxelMap.h:222-263) called as BrushSession::Dispatch calls
+// it (Brush.cpp:10-31): region center -/+ radius, bricks created unless the edit erases,
+// Replace restricted to non-empty voxels, set_if + any.  The capsule SDF of the brush is
+// replaced by the library's exact integer sphere |v - center|^2 <= radius^2 (vrt_edit).
+int ref_world_edit_spheres(void* p, uint32_t n, const int32_t* centers, const uint32_t* radii,
+                           const uint8_t* materials, const uint8_t* modes) {
+    auto* w = static_cast<RefWorld*>(p);
+    for (uint32_t k = 0; k < n; k++) {
+        const glm::ivec3 c(centers[3 * k], centers[3 * k + 1], centers[3 * k + 2]);
+        const int32_t r = (int32_t)radii[k];
+        const int32_t r2 = r * r;
+        const uint8_t material = materials[k];
+        const bool replace = modes[k] == 1;
+        w->map->RegionDispatchSIMD(c - r, c + r, material != 0, [&](VoxelDispatchInvocationPars& invoc) {
+            VInt dx = invoc.X - c.x, dy = invoc.Y - c.y, dz = invoc.Z - c.z;
+            VMask mask = (dx * dx + dy * dy + dz * dz) <= r2;
+            if (replace) mask &= invoc.VoxelIds != 0;
+            invoc.VoxelIds.set_if(mask, (int32_t)material);
+            return simd::any(mask);
+        });
+    }
+    return 0;
+}
+
 // BrickSlotAllocator (BrickSlotAllocator.cpp:5-94, .h:6-65) over a run of sector edits:
 // op i adds the bricks add[i] to sector sector[i] (Alloc), then drops remove[i] (Free).
 // After each op the sector's BaseSlot and AllocMask are recorded; at the end the free
