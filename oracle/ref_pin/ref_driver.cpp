@@ -177,6 +177,25 @@ int ref_pick(void* p, uint64_t n, const double* rays, uint32_t max_iters, double
     return 0;
 }
 
+// The 4^3-cell occupancy masks FlatVoxelStorage::UpdateOccupancy (CpuRenderer.cpp:63-83)
+// derived for the bricks at the given brick positions (x, y, z), 8 masks each in
+// BrickMaskIndexer order; bricks outside the storage's view get zeros.
+void ref_world_occupancy(void* p, uint32_t n, const int32_t* brick_pos, uint64_t* out) {
+    auto* w = static_cast<RefWorld*>(p);
+    for (uint32_t i = 0; i < n; i++) {
+        const glm::ivec3 bp(brick_pos[3 * i], brick_pos[3 * i + 1], brick_pos[3 * i + 2]);
+        const glm::ivec3 sp = bp >> glm::ivec3(MaskIndexer::ShiftXZ, MaskIndexer::ShiftY, MaskIndexer::ShiftXZ);
+        uint64_t* o = out + 8 * (size_t)i;
+        if (!ViewSectorIndexer::CheckInBounds(sp)) {
+            for (int c = 0; c < 8; c++) o[c] = 0;
+            continue;
+        }
+        const uint32_t view_idx = ViewSectorIndexer::GetIndex(sp);
+        const uint32_t offset = view_idx * (sizeof(Brick) * 64) + MaskIndexer::GetIndex(bp) * sizeof(Brick);
+        for (int c = 0; c < 8; c++) o[c] = w->storage->OccupancyStorage[offset / 64 + c];
+    }
+}
+
 // Sphere edits through the reference's own region dispatch and brick GC:
 // VoxelMap::RegionDispatchSIMD (VoxelMap.h:222-263) called as BrushSession::Dispatch calls
 // it (Brush.cpp:10-31): region center -/+ radius, bricks created unless the edit erases,
@@ -199,6 +218,8 @@ int ref_world_edit_spheres(void* p, uint32_t n, const int32_t* centers, const ui
             return simd::any(mask);
         });
     }
+    // the edited bricks reach the flat storage and their cell masks, as a frame's sync does
+    w->storage->SyncBuffers(*w->map);
     return 0;
 }
 

@@ -40,6 +40,18 @@ def world() -> v.SectorData:
     return v.synth_terrain(size=(EDGE, EDGE, EDGE), base=48, amplitude=24, seed=SEED)
 
 
+def brick_positions(sector_idx, masks) -> np.ndarray:
+    """(x, y, z) brick positions of the allocated bricks, sector by sector in mask-bit order
+    (WorldSectorIndexer packing: x in bits 0-11, z in 12-23, y in 24-31, non-negative here)."""
+    out = []
+    for idx, m in zip(sector_idx, masks):
+        sx, sz, sy = int(idx) & 4095, (int(idx) >> 12) & 4095, (int(idx) >> 24) & 255
+        for b in range(64):
+            if (int(m) >> b) & 1:
+                out.append((sx * 4 + (b & 3), sy * 4 + (b >> 4), sz * 4 + ((b >> 2) & 3)))
+    return np.array(out, np.int32).reshape(-1, 3)
+
+
 def edits(rng) -> np.ndarray:
     """Sphere edits inside the world: fills, carves (material 0) and replaces."""
     e = np.zeros(N_EDITS, v.EDIT_DTYPE)
@@ -66,6 +78,7 @@ def main(argv):
     L.ref_world_sector_count.restype = C.c_uint32
     L.ref_world_sector_count.argtypes = [C.c_void_p, C.c_void_p]
     L.ref_world_export.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.ref_world_occupancy.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
     d = world()
     e = edits(np.random.default_rng(20261205))
     w = L.ref_world_create()
@@ -81,9 +94,12 @@ def main(argv):
     masks = np.zeros(ns, np.uint64)
     bricks = np.zeros((nb.value, 512), np.uint8)
     L.ref_world_export(w, idx.ctypes.data, masks.ctypes.data, bricks.ctypes.data)
+    pos = brick_positions(idx, masks)
+    occ = np.zeros((len(pos), 8), np.uint64)
+    L.ref_world_occupancy(w, len(pos), np.ascontiguousarray(pos, np.int32).ctypes.data, occ.ctypes.data)
     L.ref_world_destroy(w)
     np.savez_compressed(OUT, edge=np.array([EDGE, SEED], np.int32), edits=e, sector_idx=idx, alloc_mask=masks,
-                        bricks=bricks)
+                        bricks=bricks, occupancy=occ)
     print(f"{len(e)} edits -> {ns} sectors, {nb.value} bricks (before: {len(d.sector_idx)} sectors, "
           f"{d.n_bricks} bricks): {OUT}")
 

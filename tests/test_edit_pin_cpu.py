@@ -66,3 +66,22 @@ def test_the_edits_create_and_free_bricks():
     modes = g["edits"]["mode"]
     mats = g["edits"]["material"]
     assert (mats == 0).sum() > 40 and (modes == 1).sum() > 20 and ((mats != 0) & (modes == 0)).sum() > 80
+
+
+def test_cell_masks_match_the_reference():
+    """The 4^3-cell occupancy masks of every brick of the edited world equal those the
+    reference's FlatVoxelStorage::UpdateOccupancy (CpuRenderer.cpp:63-83) derived for it."""
+    from tests.golden.make_golden_edit import brick_positions
+    g = np.load(GOLDEN)
+    d = world()
+    o = OracleWorld(d.sectors)
+    o.upload(d)
+    o.edit(g["edits"])
+    pos = brick_positions(g["sector_idx"], g["alloc_mask"])
+    want = g["occupancy"]
+    assert len(pos) == len(want) == len(g["bricks"])
+    got = np.stack([o.brick_occupancy(int(x), int(y), int(z)) for x, y, z in pos])
+    assert np.array_equal(got, want)
+    full = np.uint64(0xFFFFFFFFFFFFFFFF)
+    assert (want == 0).any() and (want == full).any() and ((want != 0) & (want != full)).mean() > 0.1
+    o.close()
